@@ -1,0 +1,93 @@
+"""ctypes binding of libchollagb (include/cholla_gb300.h).
+
+The library is the only compute path: if it is missing or cannot load, every call raises.
+There is no host fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+from .build import LIB, build
+
+_lib = None
+
+CGB_OK = 0
+CGB_ERR_CUDA = 1
+CGB_ERR_ARGS = 2
+CGB_ERR_NOMEM = 3
+CGB_ERR_NONFINITE = 4
+CGB_ERR_TIMEOUT = 5
+CGB_ERR_UNSUPPORTED = 6
+
+PCM, PLMC, PPMC = 0, 1, 2
+HLLC, ROE, HLLD = 0, 1, 2
+FP64, MIXED = 0, 1
+
+
+class CgbError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"libchollagb error {code}: {msg}")
+        self.code = code
+
+
+class cgb_scheme(C.Structure):
+    _fields_ = [
+        ("reconstruction", C.c_int),
+        ("riemann_solver", C.c_int),
+        ("dual_energy", C.c_int),
+        ("mhd", C.c_int),
+        ("n_scalars", C.c_int),
+        ("density_floor", C.c_int),
+        ("temperature_floor", C.c_int),
+        ("precision", C.c_int),
+        ("gamma", C.c_double),
+        ("U_floor", C.c_double),
+    ]
+
+
+_D = C.c_double
+_I = C.c_int
+_P = C.c_void_p
+
+# name -> (restype, argtypes); every declaration of include/cholla_gb300.h
+SIGNATURES = {
+    "cgb_set_scheme": (_I, [C.POINTER(cgb_scheme)]),
+    "cgb_get_scheme": (_I, [C.POINTER(cgb_scheme)]),
+    "cgb_set_stream": (_I, [_P]),
+    "cgb_last_error": (C.c_char_p, []),
+    "cgb_version": (C.c_char_p, []),
+    "cgb_vl_algorithm_3d": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _D, _D, _D, _D, _I, _I, _D, _P]),
+    "cgb_vl_algorithm_1d": (_I, [_P, _I, _I, _I, _D, _D, _D, _I, _I]),
+    "cgb_free_memory_vl_3d": (_I, []),
+    "cgb_calc_dt_gpu": (_I, [_P, _I, _I, _I, _I, _I, _D, _D, _D, _D, C.POINTER(_D)]),
+    "cgb_apply_temperature_floor": (_I, [_P, _I, _I, _I, _I, _I, _D]),
+    "cgb_set_boundaries": (_I, [_P, _I, _I, _I, _I, _I, C.POINTER(_I)]),
+    "cgb_max_magnetic_divergence": (_I, [_P, _I, _I, _I, _I, _I, _D, _D, _D, C.POINTER(_D)]),
+}
+
+
+def lib(auto_build: bool = True) -> C.CDLL:
+    """Load libchollagb (building it first if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = Path(os.environ.get("CHOLLA_GB300_LIB", LIB))
+    if not path.exists():
+        if not auto_build:
+            raise CgbError(CGB_ERR_ARGS, f"{path} not built")
+        build()
+    handle = C.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(handle, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = handle
+    return handle
+
+
+def check(rc: int) -> None:
+    if rc != CGB_OK:
+        msg = lib().cgb_last_error()
+        raise CgbError(rc, msg.decode() if msg else "")

@@ -1,0 +1,278 @@
+// capi.cu -- the C ABI of libchollagb (declared in include/cholla_gb300.h).
+//
+// Host-side bookkeeping only: argument checks, the run-time scheme, per-shape scratch and
+// kernel dispatch.  No entry point falls back to host computation: if a kernel cannot run
+// the call returns an error.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/cholla_gb300.h"
+#include "common.cuh"
+#include "kernels.h"
+
+namespace
+{
+std::mutex g_mu;
+cgb_scheme g_scheme = {CGB_PPMC, CGB_HLLC, 1, 0, 0, 1, 1, CGB_FP64, 5.0 / 3.0, 0.0};
+cudaStream_t g_stream = nullptr;
+thread_local std::string g_err;
+
+struct ScratchSlot {
+  int nx = 0, ny = 0, nz = 0, nf = 0, mhd = -1;
+  cgb::Scratch s{};
+  bool live = false;
+};
+ScratchSlot g_slot;
+unsigned long long *g_dti_host = nullptr;  // pinned result of the CFL reduction
+
+int fail(int code, const std::string &msg)
+{
+  g_err = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char *where)
+{
+  return fail(CGB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+void free_slot(ScratchSlot &sl)
+{
+  if (!sl.live) return;
+  cudaFree(sl.s.Uh);
+  cudaFree(sl.s.GEp);
+  cudaFree(sl.s.Epre);
+  cudaFree(sl.s.emf);
+  cudaFree(sl.s.Fx);
+  cudaFree(sl.s.Fy);
+  cudaFree(sl.s.Fz);
+  cudaFree(sl.s.dti);
+  cudaFree(sl.s.status);
+  sl   = ScratchSlot{};
+}
+
+int ensure_slot(int nx, int ny, int nz, int nf, int mhd)
+{
+  if (g_slot.live && g_slot.nx == nx && g_slot.ny == ny && g_slot.nz == nz && g_slot.nf == nf && g_slot.mhd == mhd)
+    return CGB_OK;
+  free_slot(g_slot);
+  size_t const n = (size_t)nx * ny * nz;
+  cgb::Scratch s{};
+  auto alloc = [&](void **p, size_t bytes) -> bool {
+    if (bytes == 0) {
+      *p = nullptr;
+      return true;
+    }
+    if (cudaMalloc(p, bytes) != cudaSuccess) return false;
+    return cudaMemset(*p, 0, bytes) == cudaSuccess;
+  };
+  bool ok = alloc((void **)&s.Uh, n * nf * sizeof(double)) && alloc((void **)&s.GEp, n * sizeof(double)) &&
+            alloc((void **)&s.Epre, n * sizeof(double)) && alloc((void **)&s.dti, sizeof(unsigned long long)) &&
+            alloc((void **)&s.status, sizeof(int));
+  if (ok && mhd) {
+    ok = alloc((void **)&s.emf, 3 * n * sizeof(double)) && alloc((void **)&s.Fx, n * (nf - 1) * sizeof(double)) &&
+         alloc((void **)&s.Fy, n * (nf - 1) * sizeof(double)) && alloc((void **)&s.Fz, n * (nf - 1) * sizeof(double));
+  }
+  g_slot.s    = s;
+  g_slot.live = true;
+  if (!ok) {
+    cudaGetLastError();
+    free_slot(g_slot);
+    return fail(CGB_ERR_NOMEM, "scratch allocation failed");
+  }
+  g_slot.nx = nx, g_slot.ny = ny, g_slot.nz = nz, g_slot.nf = nf, g_slot.mhd = mhd;
+  return CGB_OK;
+}
+
+int check_scheme(const cgb_scheme &s)
+{
+  if (s.reconstruction < CGB_PCM || s.reconstruction > CGB_PPMC) return fail(CGB_ERR_ARGS, "bad reconstruction");
+  if (s.riemann_solver < CGB_HLLC || s.riemann_solver > CGB_HLLD) return fail(CGB_ERR_ARGS, "bad riemann solver");
+  if (s.n_scalars < 0 || s.n_scalars > cgb::NS_MAX) return fail(CGB_ERR_ARGS, "n_scalars must be 0..2");
+  if (!(s.gamma > 1.0)) return fail(CGB_ERR_ARGS, "gamma must exceed 1");
+  if (s.mhd && s.riemann_solver != CGB_HLLD) return fail(CGB_ERR_ARGS, "MHD needs the HLLD solver");
+  if (!s.mhd && s.riemann_solver == CGB_HLLD) return fail(CGB_ERR_ARGS, "HLLD needs MHD");
+  if (s.mhd && s.dual_energy)
+    return fail(CGB_ERR_UNSUPPORTED, "MHD with dual energy is not supported (the reference indexes past its flux arrays)");
+  if (s.precision != CGB_FP64 && s.precision != CGB_MIXED) return fail(CGB_ERR_ARGS, "bad precision");
+  return CGB_OK;
+}
+
+int expected_fields(const cgb_scheme &s) { return 5 + s.n_scalars + (s.mhd ? 3 : 0) + (s.dual_energy ? 1 : 0); }
+
+int make_box(cgb::Box &b, int nx, int ny, int nz, int ng, int nf, double dx, double dy, double dz,
+             double density_floor, const cgb_scheme &s)
+{
+  if (nx < 1 || ny < 1 || nz < 1 || ng < 1) return fail(CGB_ERR_ARGS, "bad grid size");
+  if (nf != expected_fields(s)) return fail(CGB_ERR_ARGS, "n_fields does not match the scheme");
+  if (!(dx > 0) || !(dy > 0) || !(dz > 0)) return fail(CGB_ERR_ARGS, "cell sizes must be positive");
+  b.nx = nx, b.ny = ny, b.nz = nz, b.ng = ng, b.nf = nf, b.ns = s.n_scalars;
+  b.de = s.dual_energy ? 1 : 0;
+  b.mhd = s.mhd ? 1 : 0;
+  b.floor_on = s.density_floor ? 1 : 0;
+  b.n = (long long)nx * ny * nz;
+  b.gamma = s.gamma;
+  b.dx = dx, b.dy = dy, b.dz = dz;
+  b.density_floor = density_floor;
+  return CGB_OK;
+}
+}  // namespace
+
+extern "C" {
+
+const char *cgb_last_error(void) { return g_err.c_str(); }
+const char *cgb_version(void) { return "cholla_gb300 0.1 (sm_103a)"; }
+
+int cgb_set_scheme(const cgb_scheme *scheme)
+{
+  if (!scheme) return fail(CGB_ERR_ARGS, "null scheme");
+  int const rc = check_scheme(*scheme);
+  if (rc != CGB_OK) return rc;
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_scheme = *scheme;
+  return CGB_OK;
+}
+
+int cgb_get_scheme(cgb_scheme *scheme)
+{
+  if (!scheme) return fail(CGB_ERR_ARGS, "null scheme");
+  std::lock_guard<std::mutex> lk(g_mu);
+  *scheme = g_scheme;
+  return CGB_OK;
+}
+
+int cgb_set_stream(void *stream)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  g_stream = (cudaStream_t)stream;
+  return CGB_OK;
+}
+
+int cgb_vl_algorithm_3d(double *d_conserved, double *d_grav_potential, int nx, int ny, int nz, int x_off, int y_off,
+                        int z_off, int n_ghost, double dx, double dy, double dz, double xbound, double ybound,
+                        double zbound, double dt, int n_fields, int custom_grav, double density_floor,
+                        double *host_grav_potential)
+{
+  (void)x_off, (void)y_off, (void)z_off, (void)xbound, (void)ybound, (void)zbound;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!d_conserved) return fail(CGB_ERR_ARGS, "null d_conserved");
+  if (d_grav_potential || host_grav_potential || custom_grav)
+    return fail(CGB_ERR_UNSUPPORTED, "gravity source terms are not part of this library");
+  if (ny < 2 * n_ghost + 1 || nz < 2 * n_ghost + 1 || nx < 2 * n_ghost + 1)
+    return fail(CGB_ERR_ARGS, "3D step needs at least one real cell per dimension");
+  cgb::Box b;
+  int rc = make_box(b, nx, ny, nz, n_ghost, n_fields, dx, dy, dz, density_floor, g_scheme);
+  if (rc != CGB_OK) return rc;
+  int const H = g_scheme.reconstruction == CGB_PPMC ? 4 : g_scheme.reconstruction == CGB_PLMC ? 3 : 2;
+  if (n_ghost < H) return fail(CGB_ERR_ARGS, "n_ghost too small for the reconstruction");
+  if (g_scheme.mhd) return fail(CGB_ERR_UNSUPPORTED, "MHD step not built in this version");
+  if (g_scheme.precision != CGB_FP64) return fail(CGB_ERR_UNSUPPORTED, "mixed precision not built in this version");
+  rc = ensure_slot(nx, ny, nz, n_fields, g_scheme.mhd);
+  if (rc != CGB_OK) return rc;
+  cudaError_t e = cgb::hydro_exact_step(b, g_scheme.reconstruction, g_scheme.riemann_solver, d_conserved, g_slot.s,
+                                        dt, 0.0, 0, 0, g_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "vl_algorithm_3d");
+  return CGB_OK;
+}
+
+int cgb_vl_algorithm_1d(double *d_conserved, int nx, int x_off, int n_ghost, double dx, double xbound, double dt,
+                        int n_fields, int custom_grav)
+{
+  (void)x_off, (void)xbound;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!d_conserved) return fail(CGB_ERR_ARGS, "null d_conserved");
+  if (custom_grav) return fail(CGB_ERR_UNSUPPORTED, "gravity source terms are not part of this library");
+  if (g_scheme.mhd) return fail(CGB_ERR_UNSUPPORTED, "the 1D integrator is hydro only");
+  if (nx < 2 * n_ghost + 1) return fail(CGB_ERR_ARGS, "1D step needs at least one real cell");
+  cgb::Box b;
+  int rc = make_box(b, nx, 1, 1, n_ghost, n_fields, dx, dx, dx, 0.0, g_scheme);
+  if (rc != CGB_OK) return rc;
+  b.floor_on = 0;  // the 1D updates apply no density floor (hydro_cuda.cu:20-82, VL_1D_cuda.cu:158-215)
+  if (g_scheme.precision != CGB_FP64) return fail(CGB_ERR_UNSUPPORTED, "mixed precision not built in this version");
+  rc = ensure_slot(nx, 1, 1, n_fields, 0);
+  if (rc != CGB_OK) return rc;
+  cudaError_t e = cgb::hydro_exact_step(b, g_scheme.reconstruction, g_scheme.riemann_solver, d_conserved, g_slot.s,
+                                        dt, 0.0, 0, 0, g_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "vl_algorithm_1d");
+  return CGB_OK;
+}
+
+int cgb_free_memory_vl_3d(void)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  free_slot(g_slot);
+  return CGB_OK;
+}
+
+int cgb_calc_dt_gpu(const double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields, double dx,
+                    double dy, double dz, double gamma, double *max_dti)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!d_conserved || !max_dti) return fail(CGB_ERR_ARGS, "null pointer");
+  (void)n_fields;  // as in the reference (the caller passes n_cells here, grid3D.cpp:119)
+  cgb_scheme s = g_scheme;
+  s.gamma      = gamma;
+  cgb::Box b;
+  b.nx = nx, b.ny = ny, b.nz = nz, b.ng = n_ghost, b.nf = expected_fields(s), b.ns = s.n_scalars;
+  b.de = s.dual_energy, b.mhd = s.mhd, b.floor_on = 0, b.n = (long long)nx * ny * nz, b.gamma = gamma;
+  b.dx = dx, b.dy = dy, b.dz = dz, b.density_floor = 0;
+  if (b.mhd) return fail(CGB_ERR_UNSUPPORTED, "MHD CFL not built in this version");
+  if (!(nx > 1 && ((ny == 1 && nz == 1) || (ny > 1 && nz > 1)))) return fail(CGB_ERR_ARGS, "1D or 3D boxes only");
+  static unsigned long long *d_dti = nullptr;
+  if (!d_dti && cudaMalloc(&d_dti, sizeof(unsigned long long)) != cudaSuccess)
+    return fail(CGB_ERR_NOMEM, "dt buffer");
+  if (!g_dti_host && cudaMallocHost(&g_dti_host, sizeof(unsigned long long)) != cudaSuccess)
+    return fail(CGB_ERR_NOMEM, "pinned dt buffer");
+  cudaError_t e = cgb::hydro_calc_dt(b, d_conserved, d_dti, g_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "calc_dt");
+  e = cudaMemcpyAsync(g_dti_host, d_dti, sizeof(unsigned long long), cudaMemcpyDeviceToHost, g_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "calc_dt readback");
+  unsigned long long const bits = *g_dti_host;
+  double v;
+  std::memcpy(&v, &bits, sizeof(v));
+  *max_dti = bits == 0 ? 0.0 : v;
+  return CGB_OK;
+}
+
+int cgb_apply_temperature_floor(double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields,
+                                double U_floor)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!d_conserved) return fail(CGB_ERR_ARGS, "null d_conserved");
+  cgb::Box b;
+  int rc = make_box(b, nx, ny, nz, n_ghost, n_fields, 1.0, 1.0, 1.0, 0.0, g_scheme);
+  if (rc != CGB_OK) return rc;
+  cudaError_t e = cgb::hydro_temperature_floor(b, d_conserved, U_floor, g_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "temperature floor");
+  return CGB_OK;
+}
+
+int cgb_set_boundaries(double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields, const int flags[6])
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!d_conserved || !flags) return fail(CGB_ERR_ARGS, "null pointer");
+  for (int i = 0; i < 6; i++)
+    if (flags[i] < 0 || flags[i] > 5) return fail(CGB_ERR_ARGS, "boundary flags must be 0..5");
+  cgb::Box b;
+  b.nx = nx, b.ny = ny, b.nz = nz, b.ng = n_ghost, b.nf = n_fields, b.ns = g_scheme.n_scalars;
+  b.de = g_scheme.dual_energy, b.mhd = g_scheme.mhd, b.floor_on = 0, b.n = (long long)nx * ny * nz;
+  b.gamma = g_scheme.gamma, b.dx = b.dy = b.dz = 1.0, b.density_floor = 0;
+  if (nx < 1 || ny < 1 || nz < 1 || n_ghost < 1 || n_fields < 5) return fail(CGB_ERR_ARGS, "bad grid");
+  cudaError_t e = cgb::set_boundaries(b, d_conserved, flags, g_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "set_boundaries");
+  return CGB_OK;
+}
+
+int cgb_max_magnetic_divergence(const double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields,
+                                double dx, double dy, double dz, double *max_divb)
+{
+  (void)d_conserved, (void)nx, (void)ny, (void)nz, (void)n_ghost, (void)n_fields, (void)dx, (void)dy, (void)dz;
+  (void)max_divb;
+  return fail(CGB_ERR_UNSUPPORTED, "MHD not built in this version");
+}
+
+}  // extern "C"

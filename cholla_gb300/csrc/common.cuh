@@ -1,0 +1,56 @@
+// common.cuh -- shared types for the GB300 VL hydro/MHD step.
+//
+// State layout (the reference's, src/grid/grid_enum.h:18-111): field-major doubles
+//   U[f * n_cells + x + y*nx + z*nx*ny], fields d, mx, my, mz, E, [scalars], [Bx, By, Bz], [GasEnergy].
+// Magnetic fields are face-centred at the +1/2 face of their cell.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cgb
+{
+
+constexpr double TINY  = 1.0e-20;  // src/global/global.h:25
+constexpr double ETA_1 = 0.001;    // src/global/global.h:62-73 (non-cosmology)
+constexpr double ETA_2 = 0.035;
+constexpr int NS_MAX   = 2;        // passive scalars supported by the fused kernels
+constexpr int NQ_MAX   = 5 + NS_MAX + 1;
+
+enum Recon { RECON_PCM = 0, RECON_PLMC = 1, RECON_PPMC = 2 };
+enum Solver { SOLVER_HLLC = 0, SOLVER_ROE = 1, SOLVER_HLLD = 2 };
+
+// Everything a kernel needs to know about one padded box.  Passed by value.
+struct Box {
+  int nx, ny, nz;   // padded extents
+  int ng;           // ghost layers
+  int nf;           // fields in the state array
+  int ns;           // passive scalars (fields 5 .. 5+ns-1)
+  int de;           // dual energy: GasEnergy is field nf-1
+  int mhd;          // face-centred B at fields 5+ns .. 7+ns
+  int floor_on;     // DENSITY_FLOOR behaviour
+  long long n;      // nx*ny*nz
+  double gamma;
+  double dx, dy, dz;
+  double density_floor;
+  __host__ __device__ long long id(int x, int y, int z) const
+  {
+    return (long long)x + (long long)y * nx + (long long)z * nx * ny;
+  }
+  __host__ __device__ int fGE() const { return nf - 1; }
+  __host__ __device__ int fB() const { return 5 + ns; }
+  // number of fields carried by reconstruction / Riemann: d, m(3), E, scalars, [ge]
+  __host__ __device__ int nq() const { return 5 + ns + (de ? 1 : 0); }
+};
+
+// Device scratch of one box, owned by the library (allocated once per box shape).
+struct Scratch {
+  double *Uh;      // half-step state, nf fields
+  double *GEp;     // GasEnergy after the pdV partial update (DE)
+  double *Epre;    // total energy after the full update, before the DE sync (DE)
+  double *emf;     // 3 edge-EMF fields (MHD)
+  double *Fx, *Fy, *Fz;  // face fluxes (MHD path only)
+  unsigned long long *dti;  // encoded max inverse time step (one per box)
+  int *status;              // device status word (bad cells seen, ...)
+};
+
+}  // namespace cgb

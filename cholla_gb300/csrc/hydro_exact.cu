@@ -1,0 +1,754 @@
+// hydro_exact.cu -- fused FP64 VL hydro step (PCM/PLMC/PPMC x HLLC/Roe, dual energy, floors).
+//
+// Built with -fmad=false: every kernel keeps the reference's operation order, so the
+// result equals the reference's FP64 build bit for bit.  The step is three kernels:
+//
+//   predictor  Uⁿ  -> U½     PCM + Riemann + half update, per 3D tile; the 3 face fluxes
+//                            of every cell live in shared memory (VL_3D_cuda.cu:138-212)
+//                            + the full-dt pdV partial update of GasEnergy (hydro_cuda.cu:754-833)
+//   corrector  U½ -> Uⁿ⁺¹    per tile: x, y, z sweeps of reconstruction + Riemann into
+//                            register accumulators, then the conserved update in place
+//                            (VL_3D_cuda.cu:224-339, hydro_cuda.cu:172-402)
+//   finalize   Uⁿ⁺¹          dual-energy selection + sync, temperature floor and the CFL
+//                            reduction on the new state (hydro_cuda.cu:949-1099, 1117-1153, 514-597)
+//
+// Interface states and fluxes never leave the SM.
+#include "common.cuh"
+#include "hydro_math.cuh"
+#include "kernels.h"
+
+namespace cgb
+{
+
+namespace
+{
+
+__device__ __forceinline__ int field_of_q(int q, const Box &b)
+{
+  return (q < 5 + b.ns) ? q : b.nf - 1;  // the last carried quantity is GasEnergy
+}
+
+// rotation of the three momenta for a sweep direction: (o1, o2, o3) of hllc_cuda.cu:54-70
+__device__ __forceinline__ void rot(int dir, int &o1, int &o2, int &o3)
+{
+  o1 = dir + 1;
+  o2 = (dir + 1) % 3 + 1;
+  o3 = (dir + 2) % 3 + 1;
+}
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// ------------------------------------------------------------------------------------------
+// predictor
+// ------------------------------------------------------------------------------------------
+template <int TX, int TY, int TZ, int SOLVER>
+__global__ void __launch_bounds__(TX *TY *TZ) k_predictor(Box b, const double *__restrict__ U, double *__restrict__ Uh,
+                                                          double *__restrict__ GEp, double dt)
+{
+  constexpr int HY = TY > 1 ? 1 : 0, HZ = TZ > 1 ? 1 : 0;
+  constexpr int BX = TX + 2, BY = TY + 2 * HY, BZ = TZ + 2 * HZ;
+  constexpr int NB  = BX * BY * BZ;
+  constexpr int NFX = (TX + 1) * TY * TZ;
+  constexpr int NFY = HY ? TX * (TY + 1) * TZ : 0;
+  constexpr int NFZ = HZ ? TX * TY * (TZ + 1) : 0;
+  constexpr int NT  = TX * TY * TZ;
+  extern __shared__ double smem[];
+  int const nq = b.nq();
+  double *Us   = smem;            // [nq][NB] canonical fields
+  double *Fxs  = Us + nq * NB;    // [nq][NFX]
+  double *Fys  = Fxs + nq * NFX;  // [nq][NFY]
+  double *Fzs  = Fys + nq * NFY;  // [nq][NFZ]
+
+  int const x0 = 1 + blockIdx.x * TX;
+  int const y0 = HY ? 1 + blockIdx.y * TY : 0;
+  int const z0 = HZ ? 1 + blockIdx.z * TZ : 0;
+
+  for (int t = threadIdx.x; t < NB; t += NT) {
+    int const bx = t % BX, by = (t / BX) % BY, bz = t / (BX * BY);
+    int const gx = clampi(x0 - 1 + bx, 0, b.nx - 1);
+    int const gy = clampi(y0 - HY + by, 0, b.ny - 1);
+    int const gz = clampi(z0 - HZ + bz, 0, b.nz - 1);
+    long long const gid = b.id(gx, gy, gz);
+    for (int q = 0; q < nq; q++) Us[q * NB + t] = U[(long long)field_of_q(q, b) * b.n + gid];
+  }
+  __syncthreads();
+
+  // face fluxes: x faces first, then y, then z (each thread takes a strided share)
+  int const nfaces = NFX + NFY + NFZ;
+  for (int t = threadIdx.x; t < nfaces; t += NT) {
+    int dir, i, j, k, nfd;
+    double *Fd;
+    if (t < NFX) {
+      dir = 0, nfd = NFX, Fd = Fxs;
+      int const u = t;
+      i = u % (TX + 1), j = (u / (TX + 1)) % TY, k = u / ((TX + 1) * TY);
+    } else if (t < NFX + NFY) {
+      dir = 1, nfd = NFY, Fd = Fys;
+      int const u = t - NFX;
+      i = u % TX, j = (u / TX) % (TY + 1), k = u / (TX * (TY + 1));
+    } else {
+      dir = 2, nfd = NFZ, Fd = Fzs;
+      int const u = t - NFX - NFY;
+      i = u % TX, j = (u / TX) % TY, k = u / (TX * TY);
+    }
+    // left and right box cells of this face
+    int lx = i + 1, ly = j + HY, lz = k + HZ;
+    if (dir == 0) lx = i;
+    if (dir == 1) ly = j;
+    if (dir == 2) lz = k;
+    int const rx = lx + (dir == 0), ry = ly + (dir == 1), rz = lz + (dir == 2);
+    int const cl = lx + BX * (ly + BY * lz), cr = rx + BX * (ry + BY * rz);
+    int o1, o2, o3;
+    rot(dir, o1, o2, o3);
+    double qL[NQ_MAX], qR[NQ_MAX], f[NQ_MAX];
+#pragma unroll
+    for (int q = 0; q < NQ_MAX; q++) {
+      if (q < nq) {
+        int const src = (q == 1) ? o1 : (q == 2) ? o2 : (q == 3) ? o3 : q;
+        qL[q]         = Us[src * NB + cl];
+        qR[q]         = Us[src * NB + cr];
+      }
+    }
+    if (SOLVER == SOLVER_ROE) {
+      hx::roe(qL, qR, f, b.ns, b.de, b.gamma);
+    } else {
+      hx::hllc(qL, qR, f, b.ns, b.de, b.gamma);
+    }
+    int const fidx = t - (dir == 0 ? 0 : dir == 1 ? NFX : NFX + NFY);
+#pragma unroll
+    for (int q = 0; q < NQ_MAX; q++) {
+      if (q < nq) {
+        int const dst        = (q == 1) ? o1 : (q == 2) ? o2 : (q == 3) ? o3 : q;
+        Fd[dst * nfd + fidx] = f[q];
+      }
+    }
+  }
+  __syncthreads();
+
+  // half update (VL_3D_cuda.cu:379-495; VL_1D_cuda.cu:158-215 when ny = nz = 1)
+  int const t = threadIdx.x;
+  int const i = t % TX, j = (t / TX) % TY, k = t / (TX * TY);
+  int const gx = x0 + i, gy = y0 + j, gz = z0 + k;
+  bool const one_d = (b.ny == 1 && b.nz == 1);
+  bool valid = gx > 0 && gx < b.nx - 1;
+  if (!one_d) valid = valid && gy > 0 && gy < b.ny - 1 && gz > 0 && gz < b.nz - 1;
+  if (!valid) return;
+  long long const gid = b.id(gx, gy, gz);
+  int const c  = (i + 1) + BX * ((j + HY) + BY * (k + HZ));
+  int const fx = i + (TX + 1) * (j + TY * k);
+  int const fy = i + TX * (j + (TY + 1) * k);
+  int const fz = i + TX * (j + TY * k);
+  double const dth   = 0.5 * dt;
+  double const dtodx = dth / b.dx, dtody = dth / b.dy, dtodz = dth / b.dz;
+  int const fge      = b.nf - 1;
+
+  double P = 0.0, Pp = 0.0, vx_imo = 0, vx_ipo = 0, vy_jmo = 0, vy_jpo = 0, vz_kmo = 0, vz_kpo = 0;
+  int const qge = 5 + b.ns;
+  if (b.de) {
+    double const d = Us[c], d_inv = 1.0 / d;
+    double const vx = Us[NB + c] * d_inv, vy = Us[2 * NB + c] * d_inv, vz = Us[3 * NB + c] * d_inv;
+    double const E = Us[4 * NB + c], GE = Us[qge * NB + c];
+    if (one_d) {
+      // VL_1D_cuda.cu:180-187: plain total-minus-kinetic pressure, no floor
+      P = (E - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (b.gamma - 1.0);
+      // hydro_cuda.cu:705-752 (1D partial update) uses the dual-energy pressure
+      double const E_kin = 0.5 * d * (vx * vx + vy * vy + vz * vz);
+      Pp                 = fmax(hx::pressure_de(E, E - E_kin, GE, b.gamma), TINY);
+    } else {
+      double const E_kin = 0.5 * d * hx::sqmag(vx, vy, vz);
+      P                  = hx::pressure_de(E, E - E_kin, GE, b.gamma);
+      P                  = fmax(P, TINY);
+      Pp                 = P;
+    }
+    vx_imo = Us[NB + c - 1] / Us[c - 1];
+    vx_ipo = Us[NB + c + 1] / Us[c + 1];
+    if (!one_d) {
+      vy_jmo = Us[2 * NB + c - BX] / Us[c - BX];
+      vy_jpo = Us[2 * NB + c + BX] / Us[c + BX];
+      vz_kmo = Us[3 * NB + c - BX * BY] / Us[c - BX * BY];
+      vz_kpo = Us[3 * NB + c + BX * BY] / Us[c + BX * BY];
+    }
+  }
+  double out[NQ_MAX];
+#pragma unroll
+  for (int q = 0; q < NQ_MAX; q++) {
+    if (q < nq) {
+      double v = Us[q * NB + c] + dtodx * (Fxs[q * NFX + fx] - Fxs[q * NFX + fx + 1]);
+      if (!one_d) {
+        v = v + dtody * (Fys[q * NFY + fy] - Fys[q * NFY + fy + TX]);
+        v = v + dtodz * (Fzs[q * NFZ + fz] - Fzs[q * NFZ + fz + TX * TY]);
+      }
+      out[q] = v;
+    }
+  }
+  if (b.de) {
+    double const pdv = one_d ? 0.5 * P * (dtodx * (vx_imo - vx_ipo))
+                             : 0.5 * P * (dtodx * (vx_imo - vx_ipo) + dtody * (vy_jmo - vy_jpo) +
+                                          dtodz * (vz_kmo - vz_kpo));
+    out[qge] = out[qge] + pdv;
+  }
+  if (b.floor_on && !one_d) {
+    double const floor = b.density_floor;
+    if (out[0] < floor) {
+      double const dens_0 = out[0];
+      out[0]              = floor;
+      out[1] *= (floor / dens_0);
+      out[2] *= (floor / dens_0);
+      out[3] *= (floor / dens_0);
+      out[4] *= (floor / dens_0);
+      if (b.de) out[qge] *= (floor / dens_0);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NQ_MAX; q++)
+    if (q < nq) Uh[(long long)field_of_q(q, b) * b.n + gid] = out[q];
+
+  // pdV partial update of GasEnergy with the full dt, on real cells (hydro_cuda.cu:754-833)
+  if (b.de) {
+    int const ng = b.ng;
+    bool real    = gx >= ng && gx < b.nx - ng;
+    if (!one_d) real = real && gy >= ng && gy < b.ny - ng && gz >= ng && gz < b.nz - ng;
+    if (real) {
+      double const fdx = dt / b.dx, fdy = dt / b.dy, fdz = dt / b.dz;
+      double const GE  = Us[qge * NB + c];
+      double const term =
+          one_d ? 0.5 * Pp * (fdx * (vx_imo - vx_ipo))
+                : 0.5 * Pp * (fdx * (vx_imo - vx_ipo) + fdy * (vy_jmo - vy_jpo) + fdz * (vz_kmo - vz_kpo));
+      GEp[gid] = GE + term;
+    }
+  }
+  (void)fge;
+}
+
+// ------------------------------------------------------------------------------------------
+// corrector
+// ------------------------------------------------------------------------------------------
+template <int RECON>
+struct Halo {
+  static constexpr int H = RECON == RECON_PPMC ? 3 : (RECON == RECON_PLMC ? 2 : 1);
+};
+
+template <int TX, int TY, int TZ, int RECON>
+struct CorrSizes {
+  static constexpr int H   = Halo<RECON>::H;
+  static constexpr int HY  = TY > 1, HZ = TZ > 1;
+  static constexpr int PX  = (TX + 2 * H) * TY * TZ;
+  static constexpr int PY  = HY ? TX * (TY + 2 * H) * TZ : 0;
+  static constexpr int PZ  = HZ ? TX * TY * (TZ + 2 * H) : 0;
+  static constexpr int PM  = PX > PY ? (PX > PZ ? PX : PZ) : (PY > PZ ? PY : PZ);
+  static constexpr int RX  = (TX + 2) * TY * TZ;
+  static constexpr int RY  = HY ? TX * (TY + 2) * TZ : 0;
+  static constexpr int RZ  = HZ ? TX * TY * (TZ + 2) : 0;
+  static constexpr int RM  = RX > RY ? (RX > RZ ? RX : RZ) : (RY > RZ ? RY : RZ);
+  static constexpr int FX  = (TX + 1) * TY * TZ;
+  static constexpr int FY  = HY ? TX * (TY + 1) * TZ : 0;
+  static constexpr int FZ  = HZ ? TX * TY * (TZ + 1) : 0;
+  static constexpr int FM  = FX > FY ? (FX > FZ ? FX : FZ) : (FY > FZ ? FY : FZ);
+  // shared doubles per carried quantity: pencil (primitives / conserved), QL, QR, F
+  static constexpr int PER_Q = PM + (RECON == RECON_PCM ? 0 : 2 * RM) + FM;
+};
+
+template <int TX, int TY, int TZ, int RECON, int SOLVER>
+__global__ void __launch_bounds__(TX *TY *TZ) k_corrector(Box b, const double *__restrict__ Uh, double *__restrict__ U,
+                                                          const double *__restrict__ GEp, double *__restrict__ Epre,
+                                                          int *__restrict__ status, double dt)
+{
+  using S         = CorrSizes<TX, TY, TZ, RECON>;
+  constexpr int H = S::H;
+  constexpr int NT = TX * TY * TZ;
+  extern __shared__ double smem[];
+  int const nq = b.nq();
+  double *Ps   = smem;             // [nq][PM]  primitives in rotated order (conserved for PCM)
+  double *QLs  = Ps + nq * S::PM;  // [nq][RM]
+  double *QRs  = (RECON == RECON_PCM) ? QLs : QLs + nq * S::RM;
+  double *Fs   = (RECON == RECON_PCM) ? QLs : QRs + nq * S::RM;  // [nq][FM]
+
+  int const ng = b.ng;
+  int const x0 = ng + blockIdx.x * TX;
+  int const y0 = S::HY ? ng + blockIdx.y * TY : 0;
+  int const z0 = S::HZ ? ng + blockIdx.z * TZ : 0;
+  bool const one_d = (b.ny == 1 && b.nz == 1);
+
+  int const t  = threadIdx.x;
+  int const ti = t % TX, tj = (t / TX) % TY, tk = t / (TX * TY);
+  double acc[NQ_MAX];
+#pragma unroll
+  for (int q = 0; q < NQ_MAX; q++) acc[q] = 0.0;
+
+  int const ndir = one_d ? 1 : 3;
+  for (int dir = 0; dir < ndir; dir++) {
+    int o1, o2, o3;
+    rot(dir, o1, o2, o3);
+    // extents of the pencil along (a = sweep axis, u, w = the other two tile axes)
+    int const TA = dir == 0 ? TX : dir == 1 ? TY : TZ;
+    int const TU = dir == 0 ? TY : dir == 1 ? TZ : TX;  // (y,z), (z,x), (x,y) ordering for u,w
+    int const TW = dir == 0 ? TZ : dir == 1 ? TX : TY;
+    int const LA = TA + 2 * H;
+    int const np = LA * TU * TW;
+    // 1. pencil of U½ -> primitives (Load_Data) for this direction
+    for (int p = t; p < np; p += NT) {
+      int const a = p % LA - H, u = (p / LA) % TU, w = p / (LA * TU);
+      int gx, gy, gz;
+      if (dir == 0) {
+        gx = x0 + a, gy = y0 + u, gz = z0 + w;
+      } else if (dir == 1) {
+        gy = y0 + a, gz = z0 + u, gx = x0 + w;
+      } else {
+        gz = z0 + a, gx = x0 + u, gy = y0 + w;
+      }
+      gx = clampi(gx, 0, b.nx - 1);
+      gy = clampi(gy, 0, b.ny - 1);
+      gz = clampi(gz, 0, b.nz - 1);
+      long long const gid = b.id(gx, gy, gz);
+      double q[NQ_MAX];
+#pragma unroll
+      for (int qq = 0; qq < NQ_MAX; qq++) {
+        if (qq < nq) {
+          int const src = (qq == 1) ? o1 : (qq == 2) ? o2 : (qq == 3) ? o3 : field_of_q(qq, b);
+          q[qq]         = Uh[(long long)src * b.n + gid];
+        }
+      }
+      if (RECON == RECON_PCM) {
+#pragma unroll
+        for (int qq = 0; qq < NQ_MAX; qq++)
+          if (qq < nq) Ps[qq * S::PM + p] = q[qq];
+      } else {
+        hx::Prim const P = hx::load_prim(q, b.ns, b.de, b.gamma);
+        Ps[0 * S::PM + p] = P.d;
+        Ps[1 * S::PM + p] = P.vn;
+        Ps[2 * S::PM + p] = P.vt1;
+        Ps[3 * S::PM + p] = P.vt2;
+        Ps[4 * S::PM + p] = P.p;
+#pragma unroll
+        for (int k = 0; k < NS_MAX; k++)
+          if (k < b.ns) Ps[(5 + k) * S::PM + p] = P.sc[k];
+        if (b.de) Ps[(5 + b.ns) * S::PM + p] = P.ge;
+      }
+    }
+    __syncthreads();
+    // 2. reconstruct cells a = -1 .. TA along the sweep -> QL (at a+1/2), QR (at a-1/2)
+    int const LR = TA + 2;
+    if (RECON != RECON_PCM) {
+      int const nr = LR * TU * TW;
+      for (int r = t; r < nr; r += NT) {
+        int const a = r % LR - 1, uw = r / LR;
+        int const base = (a + H) + LA * uw;  // pencil index of the centre cell
+        auto prim_at = [&](int off) {
+          hx::Prim P;
+          int const pi = base + off;
+          P.d   = Ps[0 * S::PM + pi];
+          P.vn  = Ps[1 * S::PM + pi];
+          P.vt1 = Ps[2 * S::PM + pi];
+          P.vt2 = Ps[3 * S::PM + pi];
+          P.p   = Ps[4 * S::PM + pi];
+#pragma unroll
+          for (int k = 0; k < NS_MAX; k++) P.sc[k] = (k < b.ns) ? Ps[(5 + k) * S::PM + pi] : 0.0;
+          P.ge = b.de ? Ps[(5 + b.ns) * S::PM + pi] : 0.0;
+          return P;
+        };
+        hx::Prim L, R;
+        if (RECON == RECON_PPMC) {
+          hx::ppmc_cell(prim_at(-2), prim_at(-1), prim_at(0), prim_at(1), prim_at(2), b.ns, b.de, b.gamma, L, R);
+        } else {
+          hx::plmc_cell(prim_at(-1), prim_at(0), prim_at(1), b.ns, b.de, b.gamma, L, R);
+        }
+        double qLv[NQ_MAX], qRv[NQ_MAX];
+        hx::prim_to_q(L, qLv, b.ns, b.de, b.gamma);
+        hx::prim_to_q(R, qRv, b.ns, b.de, b.gamma);
+#pragma unroll
+        for (int qq = 0; qq < NQ_MAX; qq++) {
+          if (qq < nq) {
+            QLs[qq * S::RM + r] = qLv[qq];
+            QRs[qq * S::RM + r] = qRv[qq];
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // 3. Riemann problems at faces between a and a+1, a = -1 .. TA-1 (face index a+1)
+    int const LF = TA + 1;
+    int const nfc = LF * TU * TW;
+    // PCM keeps the conserved pencil in Ps; fluxes go to a separate slice to avoid aliasing
+    double *Fd = (RECON == RECON_PCM) ? QLs : Fs;
+    for (int fi = t; fi < nfc; fi += NT) {
+      int const a = fi % LF - 1, uw = fi / LF;
+      double qL[NQ_MAX], qR[NQ_MAX], f[NQ_MAX];
+      if (RECON == RECON_PCM) {
+        int const pl = (a + H) + LA * uw, pr = pl + 1;
+#pragma unroll
+        for (int qq = 0; qq < NQ_MAX; qq++) {
+          if (qq < nq) {
+            qL[qq] = Ps[qq * S::PM + pl];
+            qR[qq] = Ps[qq * S::PM + pr];
+          }
+        }
+      } else {
+        int const rl = (a + 1) + LR * uw, rr = rl + 1;
+#pragma unroll
+        for (int qq = 0; qq < NQ_MAX; qq++) {
+          if (qq < nq) {
+            qL[qq] = QLs[qq * S::RM + rl];
+            qR[qq] = QRs[qq * S::RM + rr];
+          }
+        }
+      }
+      if (SOLVER == SOLVER_ROE) {
+        hx::roe(qL, qR, f, b.ns, b.de, b.gamma);
+      } else {
+        hx::hllc(qL, qR, f, b.ns, b.de, b.gamma);
+      }
+#pragma unroll
+      for (int qq = 0; qq < NQ_MAX; qq++)
+        if (qq < nq) Fd[qq * S::FM + fi] = f[qq];
+    }
+    __syncthreads();
+    // 4. flux difference for this thread's cell, back in canonical field order
+    {
+      int a, u, w;
+      if (dir == 0) {
+        a = ti, u = tj, w = tk;
+      } else if (dir == 1) {
+        a = tj, u = tk, w = ti;
+      } else {
+        a = tk, u = ti, w = tj;
+      }
+      int const fm = a + LF * (u + TU * w);  // face a-1/2
+      double const dtod = dt / (dir == 0 ? b.dx : dir == 1 ? b.dy : b.dz);
+#pragma unroll
+      for (int qq = 0; qq < NQ_MAX; qq++) {
+        if (qq < nq) {
+          int const dst  = (qq == 1) ? o1 : (qq == 2) ? o2 : (qq == 3) ? o3 : qq;
+          double const d = dtod * (Fd[qq * S::FM + fm] - Fd[qq * S::FM + fm + 1]);
+          // acc[dst] += d, written without a runtime-indexed register array
+#pragma unroll
+          for (int c = 0; c < NQ_MAX; c++)
+            if (c == dst) acc[c] = (dir == 0) ? d : acc[c] + d;
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // conserved update of real cells (hydro_cuda.cu:172-402; 1D: :20-82), in place
+  int const gx = x0 + ti, gy = y0 + tj, gz = z0 + tk;
+  bool real = gx < b.nx - ng;
+  if (!one_d) real = real && gy < b.ny - ng && gz < b.nz - ng;
+  if (!real) return;
+  long long const gid = b.id(gx, gy, gz);
+  double v[NQ_MAX];
+#pragma unroll
+  for (int qq = 0; qq < NQ_MAX; qq++) {
+    if (qq < nq) {
+      int const f     = field_of_q(qq, b);
+      double const u0 = (b.de && qq == nq - 1) ? GEp[gid] : U[(long long)f * b.n + gid];
+      v[qq]           = u0 + acc[qq];
+    }
+  }
+  if (b.floor_on && !one_d) {
+    double const floor = b.density_floor;
+    if (v[0] < floor) {
+      if (v[0] > 0) {
+        double const dens_0 = v[0];
+        v[0]                = floor;
+        v[1] *= (floor / dens_0);
+        v[2] *= (floor / dens_0);
+        v[3] *= (floor / dens_0);
+        v[4] *= (floor / dens_0);
+        if (b.de) v[nq - 1] *= (floor / dens_0);
+      } else {
+        atomicOr(status, 1);  // negative density: averaged by the finalize kernel
+      }
+    }
+  }
+#pragma unroll
+  for (int qq = 0; qq < NQ_MAX; qq++)
+    if (qq < nq) U[(long long)field_of_q(qq, b) * b.n + gid] = v[qq];
+  if (b.de) Epre[gid] = v[4];
+}
+
+// ------------------------------------------------------------------------------------------
+// finalize: negative-density average, DE select + sync, temperature floor, CFL reduction
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ double hydro_inverse_crossing_time(double E, double d, double d_inv, double vx, double vy,
+                                                              double vz, double dx, double dy, double dz,
+                                                              double gamma)
+{
+  // hydro_cuda.cu:404-419 hydroInverseCrossingTime
+  double const P  = (E - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (gamma - 1.0);
+  double const cs = sqrt(d_inv * gamma * P);
+  double m        = fmax((fabs(vx) + cs) / dx, (fabs(vy) + cs) / dy);
+  m               = fmax(m, (fabs(vz) + cs) / dz);
+  m               = fmax(m, 0.0);
+  return m;
+}
+
+__device__ __forceinline__ void block_max_to(double v, unsigned long long *dst)
+{
+  // values are >= 0 (or -DBL_MAX for threads without a cell): compare as ordered bit patterns
+  __shared__ double red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    int const nw = (blockDim.x + 31) >> 5;
+    v            = (lane < nw) ? red[lane] : -1.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0 && v >= 0.0) atomicMax(dst, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
+__global__ void __launch_bounds__(256) k_finalize(Box b, double *__restrict__ U, const double *__restrict__ Epre,
+                                                  unsigned long long *__restrict__ dti, double U_floor, int temp_floor,
+                                                  int do_dt)
+{
+  int const ng = b.ng;
+  bool const one_d = (b.ny == 1 && b.nz == 1);
+  int const rx = b.nx - 2 * ng, ry = one_d ? 1 : b.ny - 2 * ng, rz = one_d ? 1 : b.nz - 2 * ng;
+  long long const nreal = (long long)rx * ry * rz;
+  long long const r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double m = -1.0;
+  if (r < nreal) {
+    int const x = (int)(r % rx) + ng;
+    int const y = one_d ? 0 : (int)((r / rx) % ry) + ng;
+    int const z = one_d ? 0 : (int)(r / ((long long)rx * ry)) + ng;
+    long long const n = b.n, id = b.id(x, y, z);
+    double const d = U[id], d_inv = 1.0 / d;
+    double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+    double E = U[4 * n + id];
+    if (b.de) {
+      // hydro_cuda.cu:949-1016 Select_Internal_Energy_3D, then :1070-1099 Sync_Energies_3D
+      long long const fge = (long long)(b.nf - 1) * n;
+      double Emax;
+      if (one_d) {
+        int const imo = max(x - 1, ng), ipo = min(x + 1, b.nx - ng - 1);
+        Emax = fmax(Epre[imo], E);
+        Emax = fmax(Emax, Epre[ipo]);
+      } else {
+        Emax = fmax(Epre[b.id(max(x - 1, ng), y, z)], E);
+        Emax = fmax(Emax, Epre[b.id(min(x + 1, b.nx - ng - 1), y, z)]);
+        Emax = fmax(Emax, Epre[b.id(x, max(y - 1, ng), z)]);
+        Emax = fmax(Emax, Epre[b.id(x, min(y + 1, b.ny - ng - 1), z)]);
+        Emax = fmax(Emax, Epre[b.id(x, y, max(z - 1, ng))]);
+        Emax = fmax(Emax, Epre[b.id(x, y, min(z + 1, b.nz - ng - 1))]);
+      }
+      double const U_adv   = U[fge + id];
+      double const U_total = E - 0.5 * d * (vx * vx + vy * vy + vz * vz);
+      double Ui            = ((U_total / E > ETA_1) or (U_total / Emax > ETA_2)) ? U_total : U_adv;
+      Ui                   = fmax(Ui, TINY);
+      U[fge + id]          = Ui;
+      E                    = 0.5 * d * (vx * vx + vy * vy + vz * vz) + Ui;
+      U[4 * n + id]        = E;
+    }
+    if (temp_floor) {
+      // hydro_cuda.cu:1117-1153 Temperature_Floor_Kernel
+      double const Ekin = 0.5 * d * (vx * vx + vy * vy + vz * vz);
+      double Ui         = (E - Ekin) / d;
+      if (Ui < U_floor) {
+        E             = Ekin + d * U_floor;
+        U[4 * n + id] = E;
+      }
+      if (b.de) {
+        long long const fge = (long long)(b.nf - 1) * n;
+        Ui                  = U[fge + id] / d;
+        if (Ui < U_floor) U[fge + id] = d * U_floor;
+      }
+    }
+    if (do_dt) {
+      if (one_d) {
+        // hydro_cuda.cu:437-471 Calc_dt_1D
+        double P = (E - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (b.gamma - 1.0);
+        P        = fmax(P, TINY);
+        double const cs = sqrt(d_inv * b.gamma * P);
+        m               = fmax(-1.0, (fabs(vx) + cs) / b.dx);
+      } else {
+        m = hydro_inverse_crossing_time(E, d, d_inv, vx, vy, vz, b.dx, b.dy, b.dz, b.gamma);
+      }
+    }
+  }
+  if (do_dt) block_max_to(m, dti);
+}
+
+// Average_Cell_Single_Field for cells the corrector found with negative density
+__global__ void k_negative_density_average(Box b, double *__restrict__ U)
+{
+  int const ng = b.ng;
+  int const rx = b.nx - 2 * ng, ry = b.ny - 2 * ng, rz = b.nz - 2 * ng;
+  long long const nreal = (long long)rx * ry * rz;
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < nreal;
+       r += (long long)gridDim.x * blockDim.x) {
+    int const x = (int)(r % rx) + ng, y = (int)((r / rx) % ry) + ng, z = (int)(r / ((long long)rx * ry)) + ng;
+    long long const id = b.id(x, y, z);
+    if (U[id] < b.density_floor && !(U[id] > 0)) {
+      U[id] = (U[b.id(x - 1, y, z)] + U[b.id(x + 1, y, z)] + U[b.id(x, y - 1, z)] + U[b.id(x, y + 1, z)] +
+               U[b.id(x, y, z - 1)] + U[b.id(x, y, z + 1)]) /
+              6;
+    }
+  }
+}
+
+// standalone CFL reduction over the real cells (hydro_cuda.cu:514-597 Calc_dt_3D / Calc_dt_1D)
+__global__ void __launch_bounds__(256) k_calc_dt(Box b, const double *__restrict__ U, unsigned long long *__restrict__ dti)
+{
+  int const ng = b.ng;
+  bool const one_d = (b.ny == 1 && b.nz == 1);
+  int const rx = b.nx - 2 * ng, ry = one_d ? 1 : b.ny - 2 * ng, rz = one_d ? 1 : b.nz - 2 * ng;
+  long long const nreal = (long long)rx * ry * rz;
+  double m = -1.0;
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < nreal;
+       r += (long long)gridDim.x * blockDim.x) {
+    int const x = (int)(r % rx) + ng;
+    int const y = one_d ? 0 : (int)((r / rx) % ry) + ng;
+    int const z = one_d ? 0 : (int)(r / ((long long)rx * ry)) + ng;
+    long long const n = b.n, id = b.id(x, y, z);
+    double const d = U[id], d_inv = 1.0 / d;
+    double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+    double const E = U[4 * n + id];
+    if (one_d) {
+      double P = (E - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (b.gamma - 1.0);
+      P        = fmax(P, TINY);
+      double const cs = sqrt(d_inv * b.gamma * P);
+      m               = fmax(m, (fabs(vx) + cs) / b.dx);
+    } else {
+      m = fmax(m, hydro_inverse_crossing_time(E, d, d_inv, vx, vy, vz, b.dx, b.dy, b.dz, b.gamma));
+    }
+  }
+  block_max_to(m, dti);
+}
+
+__global__ void k_temperature_floor(Box b, double *__restrict__ U, double U_floor)
+{
+  int const ng = b.ng;
+  bool const one_d = (b.ny == 1 && b.nz == 1);
+  int const rx = b.nx - 2 * ng, ry = one_d ? 1 : b.ny - 2 * ng, rz = one_d ? 1 : b.nz - 2 * ng;
+  long long const nreal = (long long)rx * ry * rz;
+  for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < nreal;
+       r += (long long)gridDim.x * blockDim.x) {
+    int const x = (int)(r % rx) + ng;
+    int const y = one_d ? 0 : (int)((r / rx) % ry) + ng;
+    int const z = one_d ? 0 : (int)(r / ((long long)rx * ry)) + ng;
+    long long const n = b.n, id = b.id(x, y, z);
+    double const d = U[id], d_inv = 1.0 / d;
+    double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+    double const E    = U[4 * n + id];
+    double const Ekin = 0.5 * d * (vx * vx + vy * vy + vz * vz);
+    double Ui         = (E - Ekin) / d;
+    if (Ui < U_floor) U[4 * n + id] = Ekin + d * U_floor;
+    if (b.de) {
+      long long const fge = (long long)(b.nf - 1) * n;
+      Ui                  = U[fge + id] / d;
+      if (Ui < U_floor) U[fge + id] = d * U_floor;
+    }
+  }
+}
+
+template <int TX, int TY, int TZ, int SOLVER>
+size_t predictor_smem(const Box &b)
+{
+  constexpr int HY = TY > 1 ? 1 : 0, HZ = TZ > 1 ? 1 : 0;
+  constexpr int NB  = (TX + 2) * (TY + 2 * HY) * (TZ + 2 * HZ);
+  constexpr int NFX = (TX + 1) * TY * TZ;
+  constexpr int NFY = HY ? TX * (TY + 1) * TZ : 0;
+  constexpr int NFZ = HZ ? TX * TY * (TZ + 1) : 0;
+  return sizeof(double) * (size_t)b.nq() * (NB + NFX + NFY + NFZ);
+}
+
+template <int TX, int TY, int TZ, int RECON, int SOLVER>
+size_t corrector_smem(const Box &b)
+{
+  return sizeof(double) * (size_t)b.nq() * CorrSizes<TX, TY, TZ, RECON>::PER_Q;
+}
+
+template <int TX, int TY, int TZ, int SOLVER>
+cudaError_t launch_predictor(const Box &b, const double *U, double *Uh, double *GEp, double dt, cudaStream_t s)
+{
+  size_t const sm = predictor_smem<TX, TY, TZ, SOLVER>(b);
+  auto k          = k_predictor<TX, TY, TZ, SOLVER>;
+  cudaError_t e   = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  dim3 grid((b.nx - 2 + TX - 1) / TX, TY > 1 ? (b.ny - 2 + TY - 1) / TY : 1, TZ > 1 ? (b.nz - 2 + TZ - 1) / TZ : 1);
+  k<<<grid, TX * TY * TZ, sm, s>>>(b, U, Uh, GEp, dt);
+  return cudaGetLastError();
+}
+
+template <int TX, int TY, int TZ, int RECON, int SOLVER>
+cudaError_t launch_corrector(const Box &b, const double *Uh, double *U, const double *GEp, double *Epre, int *status,
+                             double dt, cudaStream_t s)
+{
+  size_t const sm = corrector_smem<TX, TY, TZ, RECON, SOLVER>(b);
+  auto k          = k_corrector<TX, TY, TZ, RECON, SOLVER>;
+  cudaError_t e   = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  int const rx = b.nx - 2 * b.ng, ry = b.ny - 2 * b.ng, rz = b.nz - 2 * b.ng;
+  dim3 grid((rx + TX - 1) / TX, TY > 1 ? (ry + TY - 1) / TY : 1, TZ > 1 ? (rz + TZ - 1) / TZ : 1);
+  k<<<grid, TX * TY * TZ, sm, s>>>(b, Uh, U, GEp, Epre, status, dt);
+  return cudaGetLastError();
+}
+
+template <int TX, int TY, int TZ>
+cudaError_t dispatch_step(const Box &b, int recon, int solver, double *U, const Scratch &sc, double dt,
+                          cudaStream_t s)
+{
+  cudaError_t e;
+  if (solver == SOLVER_ROE) {
+    e = launch_predictor<TX, TY, TZ, SOLVER_ROE>(b, U, sc.Uh, sc.GEp, dt, s);
+  } else {
+    e = launch_predictor<TX, TY, TZ, SOLVER_HLLC>(b, U, sc.Uh, sc.GEp, dt, s);
+  }
+  if (e != cudaSuccess) return e;
+#define CGB_CORR(R, SV) launch_corrector<TX, TY, TZ, R, SV>(b, sc.Uh, U, sc.GEp, sc.Epre, sc.status, dt, s)
+  if (recon == RECON_PPMC) {
+    e = (solver == SOLVER_ROE) ? CGB_CORR(RECON_PPMC, SOLVER_ROE) : CGB_CORR(RECON_PPMC, SOLVER_HLLC);
+  } else if (recon == RECON_PLMC) {
+    e = (solver == SOLVER_ROE) ? CGB_CORR(RECON_PLMC, SOLVER_ROE) : CGB_CORR(RECON_PLMC, SOLVER_HLLC);
+  } else {
+    e = (solver == SOLVER_ROE) ? CGB_CORR(RECON_PCM, SOLVER_ROE) : CGB_CORR(RECON_PCM, SOLVER_HLLC);
+  }
+#undef CGB_CORR
+  return e;
+}
+
+}  // namespace
+
+cudaError_t hydro_exact_step(const Box &b, int recon, int solver, double *U, const Scratch &sc, double dt,
+                             double U_floor, int temp_floor, int do_dt, cudaStream_t s)
+{
+  bool const one_d = (b.ny == 1 && b.nz == 1);
+  cudaError_t e    = one_d ? dispatch_step<128, 1, 1>(b, recon, solver, U, sc, dt, s)
+                           : dispatch_step<8, 8, 4>(b, recon, solver, U, sc, dt, s);
+  if (e != cudaSuccess) return e;
+  if (b.floor_on && !one_d) {
+    k_negative_density_average<<<152 * 4, 256, 0, s>>>(b, U);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  if (b.de || temp_floor || do_dt) {
+    if (do_dt) {
+      e = cudaMemsetAsync(sc.dti, 0, sizeof(unsigned long long), s);
+      if (e != cudaSuccess) return e;
+    }
+    int const ng = b.ng;
+    long long const nreal =
+        (long long)(b.nx - 2 * ng) * (one_d ? 1 : b.ny - 2 * ng) * (one_d ? 1 : b.nz - 2 * ng);
+    k_finalize<<<(unsigned)((nreal + 255) / 256), 256, 0, s>>>(b, U, sc.Epre, sc.dti, U_floor, temp_floor, do_dt);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
+cudaError_t hydro_calc_dt(const Box &b, const double *U, unsigned long long *dti, cudaStream_t s)
+{
+  cudaError_t e = cudaMemsetAsync(dti, 0, sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return e;
+  k_calc_dt<<<152 * 8, 256, 0, s>>>(b, U, dti);
+  return cudaGetLastError();
+}
+
+cudaError_t hydro_temperature_floor(const Box &b, double *U, double U_floor, cudaStream_t s)
+{
+  k_temperature_floor<<<152 * 8, 256, 0, s>>>(b, U, U_floor);
+  return cudaGetLastError();
+}
+
+}  // namespace cgb

@@ -1,0 +1,113 @@
+/*
+ * cholla_gb300.h -- C ABI of libchollagb, the GB300 (sm_103a) replacement for Cholla's
+ * single-GPU VL hydro/MHD step.
+ *
+ * The entry points mirror the reference interface of the path they replace (cited per
+ * function, paths relative to the cholla-hydro/cholla source tree).  Differences from the
+ * reference, all at the boundary:
+ *   - every function returns an int status (CGB_OK or an error code; cgb_last_error()
+ *     gives the message) instead of aborting the process through GPU_Error_Check/chexit;
+ *   - the scheme (reconstruction, Riemann solver, dual energy, floors, adiabatic index),
+ *     which the reference fixes with compile-time macros and the global `gama`, is set at
+ *     run time with cgb_set_scheme();
+ *   - work is queued on the stream given to cgb_set_stream() (default: the legacy stream 0,
+ *     as in the reference) and the step itself never synchronises with the host.
+ * Pointers named d_* are device pointers; the state is updated in place in the
+ * reference's field-major layout U[f*n_cells + i + j*nx + k*nx*ny].
+ */
+#ifndef CHOLLA_GB300_H
+#define CHOLLA_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define CGB_OK              0
+#define CGB_ERR_CUDA        1  /* a CUDA call failed (message from cudaGetErrorString) */
+#define CGB_ERR_ARGS        2  /* invalid sizes, pointers or options */
+#define CGB_ERR_NOMEM       3  /* device allocation of scratch failed */
+#define CGB_ERR_NONFINITE   4  /* the step produced non-finite or negative density */
+#define CGB_ERR_TIMEOUT     5  /* a bounded device wait ran out */
+#define CGB_ERR_UNSUPPORTED 6  /* option combination not built */
+
+/* reconstruction (builds/make.type.*: -DPCM / -DPLMC / -DPPMC) */
+#define CGB_PCM  0
+#define CGB_PLMC 1
+#define CGB_PPMC 2
+/* Riemann solver (-DHLLC / -DROE / -DHLLD) */
+#define CGB_HLLC 0
+#define CGB_ROE  1
+#define CGB_HLLD 2
+/* arithmetic */
+#define CGB_FP64  0 /* FP64 in the reference's operation order: bit-exact with its -fmad=false build */
+#define CGB_MIXED 1 /* FP32 reconstruction and fluxes, FP64 state accumulation, energy recovery and dt */
+
+typedef struct {
+  int reconstruction;    /* CGB_PCM / CGB_PLMC / CGB_PPMC */
+  int riemann_solver;    /* CGB_HLLC / CGB_ROE / CGB_HLLD */
+  int dual_energy;       /* -DDE: GasEnergy is the last field */
+  int mhd;               /* -DMHD: face-centred Bx, By, Bz follow the scalars; needs CGB_HLLD */
+  int n_scalars;         /* -DSCALAR: passive scalars after Energy (0..2) */
+  int density_floor;     /* -DDENSITY_FLOOR */
+  int temperature_floor; /* -DTEMPERATURE_FLOOR: applied after the step, before the CFL reduction */
+  int precision;         /* CGB_FP64 or CGB_MIXED */
+  double gamma;          /* adiabatic index: the reference's global `gama` (global.h:147) */
+  double U_floor;        /* specific internal-energy floor used by the temperature floor */
+} cgb_scheme;
+
+/* Scheme for the drop-in entry points below (replaces the make.type macros and `gama`). */
+int cgb_set_scheme(const cgb_scheme *scheme);
+int cgb_get_scheme(cgb_scheme *scheme);
+/* Stream for subsequent calls (a cudaStream_t; NULL = legacy default stream). */
+int cgb_set_stream(void *stream);
+const char *cgb_last_error(void);
+/* Library version string. */
+const char *cgb_version(void);
+
+/* One VL step of the padded box in place.
+ * Replaces VL_Algorithm_3D_CUDA (src/integrators/VL_3D_cuda.h:9-11, VL_3D_cuda.cu:38-360).
+ * Same arguments and meaning; d_grav_potential, x/y/z_off, x/y/zbound, custom_grav and
+ * host_grav_potential belong to the gravity build (out of scope) and must be NULL / 0
+ * (non-zero custom_grav or a non-NULL potential returns CGB_ERR_UNSUPPORTED).
+ * Scratch is allocated on the first call for a box shape and kept until
+ * cgb_free_memory_vl_3d(); a call with a new shape reallocates it. */
+int cgb_vl_algorithm_3d(double *d_conserved, double *d_grav_potential, int nx, int ny, int nz, int x_off, int y_off,
+                        int z_off, int n_ghost, double dx, double dy, double dz, double xbound, double ybound,
+                        double zbound, double dt, int n_fields, int custom_grav, double density_floor,
+                        double *host_grav_potential);
+
+/* Replaces VL_Algorithm_1D_CUDA (src/integrators/VL_1D_cuda.h, VL_1D_cuda.cu:30-146). */
+int cgb_vl_algorithm_1d(double *d_conserved, int nx, int x_off, int n_ghost, double dx, double xbound, double dt,
+                        int n_fields, int custom_grav);
+
+/* Replaces Free_Memory_VL_3D (VL_3D_cuda.cu:362-377).  Frees the library's scratch only:
+ * unlike the reference it does not free the caller's d_conserved. */
+int cgb_free_memory_vl_3d(void);
+
+/* Replaces Calc_dt_GPU (src/hydro/hydro_cuda.h:69-70, hydro_cuda.cu:562-597): writes the
+ * maximum inverse crossing time over the real cells to *max_dti (host).  As in the
+ * reference this synchronises the stream; dt = C_cfl / max_dti. */
+int cgb_calc_dt_gpu(const double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields, double dx,
+                    double dy, double dz, double gamma, double *max_dti);
+
+/* Replaces Apply_Temperature_Floor (src/hydro/hydro_cuda.cu:1103-1115). */
+int cgb_apply_temperature_floor(double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields,
+                                double U_floor);
+
+/* Ghost-cell fill of all faces of a single-GPU machine.  Replaces Grid3D::Set_Boundaries for
+ * flags 1 periodic, 2 reflective, 3 transmissive (with the hydro inflow diode), 4 custom
+ * (left untouched) (src/grid/boundary_conditions.cpp:165-417, cuda_boundaries.cu:71-300).
+ * flags[6] = {x-lower, x-upper, y-lower, y-upper, z-lower, z-upper}. */
+int cgb_set_boundaries(double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields, const int flags[6]);
+
+/* Maximum |div B| over the real cells (MHD).  Replaces calculateMagneticDivergence
+ * (src/mhd/magnetic_divergence.cu:33-76); writes the value to *max_divb (host). */
+int cgb_max_magnetic_divergence(const double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields,
+                                double dx, double dy, double dz, double *max_divb);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CHOLLA_GB300_H */

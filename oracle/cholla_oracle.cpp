@@ -1,0 +1,1790 @@
+/*
+ * cholla_oracle.cpp -- FP64 CPU restatement of Cholla's VL hydro/MHD step.
+ *
+ * TEST INFRASTRUCTURE ONLY (parity checker and CPU baseline); see cholla_oracle.h.
+ * Compiled with -O2 -ffp-contract=off so that no multiply-add is fused, matching the
+ * reference's -fmad=false build (Makefile:148).  Every arithmetic expression keeps the
+ * reference's evaluation order: that is what makes the oracle reproduce the reference
+ * to the last bit, so the order is part of the specification being restated.
+ *
+ * Paths below are relative to the cholla-hydro/cholla source tree.
+ */
+#include "cholla_oracle.h"
+
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <vector>
+#ifdef _OPENMP
+  #include <omp.h>
+#endif
+
+namespace
+{
+// src/global/global.h:25, 62-73
+constexpr double TINY  = 1.0e-20;
+constexpr double ETA_1 = 0.001;
+constexpr double ETA_2 = 0.035;
+// src/riemann_solvers/hlld_cuda.h:56
+constexpr double HLLD_SMALL = 1.0e-8;
+constexpr int MAXS          = 8;
+
+int g_threads = 0;
+
+inline double SIGN(double a) { return (a < 0.) ? -1. : 1.; }  // global.h:144
+inline int sgn_int(double x) { return (x < 0) ? -1 : 1; }     // global_cuda.h:41-48
+
+// math_utilities.h: dotProduct = a1*b1 + ((a2*b2) + (a3*b3))
+inline double dot3(double a1, double a2, double a3, double b1, double b2, double b3)
+{
+  return a1 * b1 + ((a2 * b2) + (a3 * b3));
+}
+inline double sqmag(double a, double b, double c) { return dot3(a, b, c, a, b, c); }
+
+// hydro_utilities.h:136-151
+inline double pressure_from_de(double E, double U_total, double U_advected, double gamma)
+{
+  double U;
+  if (U_total / E > ETA_1) {
+    U = U_total;
+  } else {
+    U = U_advected;
+  }
+  double P = U * (gamma - 1.0);
+  return fmax(P, TINY);
+}
+
+// Geometry and field bookkeeping for one padded grid.
+struct Grid {
+  int nx, ny, nz;
+  size_t n;  // n_cells
+  int ng, nf, ns;
+  bool de, mhd;
+  int fB;    // index of magnetic_x (mhd)
+  int fGE;   // index of GasEnergy (de)
+  int nif;   // number of fields in interface / flux arrays
+  double gamma;
+  explicit Grid(const orc_config *c)
+  {
+    nx    = c->nx;
+    ny    = c->ny;
+    nz    = c->nz;
+    n     = (size_t)nx * ny * nz;
+    ng    = c->n_ghost;
+    nf    = c->n_fields;
+    ns    = c->n_scalars;
+    de    = c->de != 0;
+    mhd   = c->mhd != 0;
+    fB    = 5 + ns;
+    fGE   = nf - 1;
+    nif   = mhd ? nf - 1 : nf;
+    gamma = c->gamma;
+  }
+  size_t id(int x, int y, int z) const { return (size_t)x + (size_t)y * nx + (size_t)z * nx * ny; }
+  void xyz(size_t i, int &x, int &y, int &z) const
+  {
+    z = (int)(i / ((size_t)nx * ny));
+    y = (int)((i - (size_t)z * nx * ny) / nx);
+    x = (int)(i - (size_t)z * nx * ny - (size_t)y * nx);
+  }
+};
+
+inline void perm(int dir, int &o1, int &o2, int &o3)
+{
+  if (dir == 0) {
+    o1 = 1, o2 = 2, o3 = 3;
+  } else if (dir == 1) {
+    o1 = 2, o2 = 3, o3 = 1;
+  } else {
+    o1 = 3, o2 = 1, o3 = 2;
+  }
+}
+
+// mhd_utilities.h:205-237 cellCenteredMagneticFields
+inline void cc_b(const Grid &g, const double *U, int x, int y, int z, double &bx, double &by, double &bz)
+{
+  size_t const id = g.id(x, y, z);
+  const double *Bx = U + (size_t)g.fB * g.n, *By = U + (size_t)(g.fB + 1) * g.n, *Bz = U + (size_t)(g.fB + 2) * g.n;
+  bx = (x > 0) ? 0.5 * (Bx[id] + Bx[g.id(x - 1, y, z)]) : Bx[id];
+  by = (y > 0) ? 0.5 * (By[id] + By[g.id(x, y - 1, z)]) : By[id];
+  bz = (z > 0) ? 0.5 * (Bz[id] + Bz[g.id(x, y, z - 1)]) : Bz[id];
+}
+
+// mhd_utilities.h:38-59 _magnetosonicSpeed
+inline double magnetosonic(double d, double p, double bx, double by, double bz, double gamma, double choice)
+{
+  double bXSquared = bx * bx;
+  double bSquared  = bXSquared + ((by * by) + (bz * bz));
+  double term1     = gamma * p + bSquared;
+  double term2     = (term1 * term1) - 4. * gamma * p * bXSquared;
+  term2            = sqrt(term2);
+  return sqrt((term1 + choice * term2) / (2.0 * fmax(d, TINY)));
+}
+inline double cfast(double d, double p, double bx, double by, double bz, double gamma)
+{
+  return magnetosonic(d, p, bx, by, bz, gamma, 1.0);
+}
+inline double cslow(double d, double p, double bx, double by, double bz, double gamma)
+{
+  return magnetosonic(d, p, bx, by, bz, gamma, -1.0);
+}
+inline double magE(double bx, double by, double bz) { return 0.5 * sqmag(bx, by, bz); }  // mhd_utilities.h:84
+
+// ============================================================================================
+// Reconstruction (src/reconstruction/reconstruction.h)
+// ============================================================================================
+struct Prim {
+  double d, vx, vy, vz, p, bx, by, bz, ge;
+  double sc[MAXS];
+};
+struct Chr {
+  double a[7];
+};
+struct Eig {
+  double cf, cs, cf2, cs2, af, as, by, bz, nfs, sign, qf, qs, Af, As, qpf, qps, Apf, Aps;
+};
+
+// reconstruction.h:139-212 Load_Data
+Prim load_data(const Grid &g, const double *U, int x, int y, int z, int o1, int o2, int o3)
+{
+  size_t const id = g.id(x, y, z);
+  size_t const n  = g.n;
+  Prim P;
+  P.d  = U[id];
+  P.vx = U[o1 * n + id] / P.d;
+  P.vy = U[o2 * n + id] / P.d;
+  P.vz = U[o3 * n + id] / P.d;
+  double cbx = 0, cby = 0, cbz = 0;
+  P.bx = P.by = P.bz = 0;
+  if (g.mhd) {
+    cc_b(g, U, x, y, z, cbx, cby, cbz);
+    if (o1 == 1) {
+      P.bx = cbx, P.by = cby, P.bz = cbz;
+    } else if (o1 == 2) {
+      P.bx = cby, P.by = cbz, P.bz = cbx;
+    } else {
+      P.bx = cbz, P.by = cbx, P.bz = cby;
+    }
+  }
+  P.ge = 0;
+  if (g.de) {
+    double const E  = U[4 * n + id];
+    double const GE = U[(size_t)g.fGE * n + id];
+    double Ent      = 0.5 * P.d * sqmag(P.vx, P.vy, P.vz);
+    if (g.mhd) Ent += magE(cbx, cby, cbz);
+    P.p  = pressure_from_de(E, E - Ent, GE, g.gamma);
+    P.ge = GE / P.d;
+  } else {
+    // hydro_utilities.h:34-45 Calc_Pressure_Primitive
+    double pressure = U[4 * n + id] - 0.5 * P.d * sqmag(P.vx, P.vy, P.vz);
+    if (g.mhd) pressure -= magE(P.bx, P.by, P.bz);
+    P.p = fmax((g.gamma - 1.) * pressure, TINY);
+  }
+  for (int s = 0; s < g.ns; s++) P.sc[s] = U[(size_t)(5 + s) * n + id] / P.d;
+  return P;
+}
+
+// reconstruction.h:310-361 Compute_Eigenvectors (MHD)
+Eig eigenvectors(const Prim &p, double cs, double cs2, double gamma)
+{
+  Eig e;
+  e.cf  = cfast(p.d, p.p, p.bx, p.by, p.bz, gamma);
+  e.cs  = cslow(p.d, p.p, p.bx, p.by, p.bz, gamma);
+  e.cf2 = e.cf * e.cf;
+  e.cs2 = e.cs * e.cs;
+  double const denom = (e.cf2 - e.cs2), num2 = (e.cf2 - cs2);
+  if (denom <= 0.0 or num2 <= 0.0) {
+    e.af = 1.0;
+    e.as = 0.0;
+  } else if (double const num1 = (cs2 - e.cs2); num1 <= 0.0) {
+    e.af = 0.0;
+    e.as = 1.0;
+  } else {
+    e.af = sqrt(num1 / denom);
+    e.as = sqrt(num2 / denom);
+  }
+  double const bd = 1.0 / hypot(p.by, p.bz);  // rhypot
+  e.by            = std::isfinite(bd) ? p.by * bd : 1.0;
+  e.bz            = std::isfinite(bd) ? p.bz * bd : 0.0;
+  e.sign          = copysign(1.0, p.bx);
+  e.nfs           = 0.5 / cs2;
+  e.qpf           = e.sign * e.nfs * e.af * e.cf;
+  e.qps           = e.sign * e.nfs * e.as * e.cs;
+  e.qf            = e.sign * e.af * e.cf;
+  e.qs            = e.sign * e.as * e.cs;
+  e.Af            = e.af * cs * sqrt(p.d);
+  e.As            = e.as * cs * sqrt(p.d);
+  e.Apf           = 0.5 * e.af / (cs * sqrt(p.d));
+  e.Aps           = 0.5 * e.as / (cs * sqrt(p.d));
+  return e;
+}
+
+// reconstruction.h:378-437 Primitive_To_Characteristic
+Chr prim_to_char(bool mhd, const Prim &p, const Prim &s, const Eig &e, double cs, double cs2)
+{
+  Chr o;
+  if (mhd) {
+    double const isd = 1.0 / sqrt(p.d);  // rsqrt
+    o.a[0] = e.nfs * e.af * (s.p / p.d - e.cf * s.vx) + e.qps * (e.by * s.vy + e.bz * s.vz) +
+             e.Aps * (e.by * s.by + e.bz * s.bz);
+    o.a[1] = 0.5 * (e.by * (s.bz * e.sign * isd + s.vz) - e.bz * (s.by * e.sign * isd + s.vy));
+    o.a[2] = e.nfs * e.as * (s.p / p.d - e.cs * s.vx) - e.qpf * (e.by * s.vy + e.bz * s.vz) -
+             e.Apf * (e.by * s.by + e.bz * s.bz);
+    o.a[3] = s.d - s.p / cs2;
+    o.a[4] = e.nfs * e.as * (s.p / p.d + e.cs * s.vx) + e.qpf * (e.by * s.vy + e.bz * s.vz) -
+             e.Apf * (e.by * s.by + e.bz * s.bz);
+    o.a[5] = 0.5 * (e.by * (s.bz * e.sign * isd - s.vz) - e.bz * (s.by * e.sign * isd - s.vy));
+    o.a[6] = e.nfs * e.af * (s.p / p.d + e.cf * s.vx) - e.qps * (e.by * s.vy + e.bz * s.vz) +
+             e.Aps * (e.by * s.by + e.bz * s.bz);
+  } else {
+    o.a[0] = -p.d * s.vx / (2.0 * cs) + s.p / (2.0 * cs2);
+    o.a[1] = s.d - s.p / (cs2);
+    o.a[2] = s.vy;
+    o.a[3] = s.vz;
+    o.a[4] = p.d * s.vx / (2.0 * cs) + s.p / (2.0 * cs2);
+    o.a[5] = o.a[6] = 0.0;
+  }
+  return o;
+}
+
+// reconstruction.h:453-491 Characteristic_To_Primitive
+Prim char_to_prim(bool mhd, const Prim &p, const Chr &c, const Eig &e, double cs, double cs2)
+{
+  Prim o;
+  std::memset(&o, 0, sizeof(o));
+  const double *a = c.a;
+  if (mhd) {
+    o.d  = p.d * (e.af * (a[0] + a[6]) + e.as * (a[2] + a[4])) + a[3];
+    o.vx = e.cf * e.af * (a[6] - a[0]) + e.cs * e.as * (a[4] - a[2]);
+    o.vy = e.by * (e.qs * (a[0] - a[6]) + e.qf * (a[4] - a[2])) + e.bz * (a[5] - a[1]);
+    o.vz = e.bz * (e.qs * (a[0] - a[6]) + e.qf * (a[4] - a[2])) + e.by * (a[1] - a[5]);
+    o.p  = p.d * cs2 * (e.af * (a[0] + a[6]) + e.as * (a[2] + a[4]));
+    o.by = e.by * (e.As * (a[0] + a[6]) - e.Af * (a[2] + a[4])) - e.bz * e.sign * sqrt(p.d) * (a[5] + a[1]);
+    o.bz = e.bz * (e.As * (a[0] + a[6]) - e.Af * (a[2] + a[4])) + e.by * e.sign * sqrt(p.d) * (a[5] + a[1]);
+  } else {
+    o.d  = a[0] + a[1] + a[4];
+    o.vx = cs / p.d * (a[4] - a[0]);
+    o.vy = a[2];
+    o.vz = a[3];
+    o.p  = cs2 * (a[0] + a[4]);
+  }
+  return o;
+}
+
+// reconstruction.h:794-901 PPM_Single_Variable
+void ppm1(double im2, double im1, double i, double ip1, double ip2, double &L_iph, double &R_imh)
+{
+  double const C2 = 1.25;
+  auto limit      = [&C2](double const &ci, double const &cim1, double const &iface, double const &s2i,
+                     double const &s2im1) -> double {
+    double s2c = 3.0 * (cim1 + ci - 2.0 * iface);
+    double lim = 0.0;
+    if (SIGN(s2c) == SIGN(s2im1) and SIGN(s2c) == SIGN(s2i)) {
+      lim = SIGN(s2c) * fmin(C2 * fabs(s2im1), fmin(C2 * fabs(s2i), fabs(s2c)));
+    }
+    double const dl = iface - cim1;
+    double const dr = ci - iface;
+    if (dl * dr < 0.0) {
+      return 0.5 * (cim1 + ci) - lim / 6.0;
+    } else {
+      return iface;
+    }
+  };
+  double const sl   = (i - im1);
+  double const sr   = (ip1 - i);
+  double const sim1 = 0.5 * sl + 0.5 * (im1 - im2);
+  double const si   = 0.5 * sr + 0.5 * sl;
+  double const sip1 = 0.5 * (ip2 - ip1) + 0.5 * sr;
+  R_imh             = 0.5 * (im1 + i) + (sim1 - si) / 6.0;
+  L_iph             = 0.5 * (i + ip1) + (si - sip1) / 6.0;
+  double const d2im1 = im2 + i - 2.0 * im1;
+  double const d2i   = im1 + ip1 - 2.0 * i;
+  double const d2ip1 = i + ip2 - 2.0 * ip1;
+  R_imh              = limit(i, im1, R_imh, d2i, d2im1);
+  L_iph              = limit(ip1, i, L_iph, d2ip1, d2i);
+  double d2f         = 6.0 * (R_imh + L_iph - 2.0 * i);
+  double d2lim       = 0.0;
+  if (SIGN(d2im1) == SIGN(d2i) and SIGN(d2im1) == SIGN(d2ip1) and SIGN(d2im1) == SIGN(d2f)) {
+    d2lim = SIGN(d2f) * fmin(fmin(C2 * fabs(d2im1), C2 * fabs(d2i)), fmin(C2 * fabs(d2ip1), fabs(d2f)));
+  }
+  double cmax       = fmax(fabs(im2), fabs(im1));
+  cmax              = fmax(cmax, fabs(i));
+  cmax              = fmax(cmax, fabs(ip1));
+  cmax              = fmax(cmax, fabs(ip2));
+  double const rho  = (fabs(d2f) > (1.0e-12) * cmax) ? d2lim / d2f : 0.0;
+  double const sfl  = i - R_imh;
+  double const sfr  = L_iph - i;
+  if ((sfl * sfr) <= 0.0 or ((ip1 - i) * (i - im1)) <= 0.0) {
+    if (rho <= (1.0 - (1.0e-12))) {
+      R_imh = i - rho * sfl;
+      L_iph = i + rho * sfr;
+    }
+  } else {
+    if (fabs(sfl) >= 2.0 * fabs(sfr)) R_imh = i - 2.0 * sfr;
+    if (fabs(sfr) >= 2.0 * fabs(sfl)) L_iph = i + 2.0 * sfl;
+  }
+}
+
+// reconstruction.h:918-968 Write_Data
+void write_data(const Grid &g, const Prim &s, double *Q, const double *U, size_t id, int o1, int o2, int o3)
+{
+  size_t const n = g.n;
+  Q[id]          = s.d;
+  Q[o1 * n + id] = s.d * s.vx;
+  Q[o2 * n + id] = s.d * s.vy;
+  Q[o3 * n + id] = s.d * s.vz;
+  if (g.mhd) {
+    double bx;
+    Q[(size_t)g.fB * n + id]       = s.by;
+    Q[(size_t)(g.fB + 1) * n + id] = s.bz;
+    bx                             = U[(size_t)(g.fB + (o1 - 1)) * n + id];
+    // hydro_utilities.h:106-118 Calc_Energy_Primitive
+    double energy = (fmax(s.p, TINY) / (g.gamma - 1.)) + 0.5 * s.d * sqmag(s.vx, s.vy, s.vz);
+    energy += magE(bx, s.by, s.bz);
+    Q[4 * n + id] = energy;
+  } else {
+    Q[4 * n + id] = (fmax(s.p, TINY) / (g.gamma - 1.)) + 0.5 * s.d * sqmag(s.vx, s.vy, s.vz);
+  }
+  if (g.de) Q[(size_t)g.fGE * n + id] = s.d * s.ge;
+  for (int k = 0; k < g.ns; k++) Q[(size_t)(5 + k) * n + id] = s.d * s.sc[k];
+}
+
+// reconstruction.h:95-119 Thread_Guard (true = skip)
+template <int order>
+bool guard(const Grid &g, int x, int y, int z)
+{
+  bool out = x < order - 1 or x >= g.nx - order;
+  if (g.ny > 1) out = y < order - 1 or y >= g.ny - order or out;
+  if (g.nz > 1) {
+    out = z < order - 1 or z >= g.nz - order or out;
+  } else {
+    out = z >= g.nz or out;
+  }
+  return out;
+}
+
+template <typename F>
+void par_cells(const Grid &g, F f)
+{
+  long long const n = (long long)g.n;
+#pragma omp parallel for schedule(static) num_threads(g_threads > 0 ? g_threads : omp_get_max_threads())
+  for (long long i = 0; i < n; i++) f((size_t)i);
+}
+
+}  // namespace
+
+#ifndef _OPENMP
+static int omp_get_max_threads() { return 1; }
+#endif
+
+extern "C" {
+
+void orc_set_threads(int n) { g_threads = n; }
+
+void orc_mt19937_uniform(unsigned long long seed, double a, double b, size_t n, double *out)
+{
+  std::mt19937_64 prng(seed);
+  std::uniform_real_distribution<double> dist(a, b);
+  for (size_t i = 0; i < n; i++) out[i] = dist(prng);
+}
+int orc_get_threads(void) { return g_threads > 0 ? g_threads : omp_get_max_threads(); }
+
+void orc_ppm_single_variable(double im2, double im1, double i, double ip1, double ip2, double *L_iph, double *R_imh)
+{
+  ppm1(im2, im1, i, ip1, ip2, *L_iph, *R_imh);
+}
+
+// src/reconstruction/pcm_cuda.cu:256-424 PCM_Reconstruction_3D (and :13-121 for 1D)
+void orc_pcm_3d(const orc_config *c, const double *U, double *QLx, double *QRx, double *QLy, double *QRy, double *QLz,
+                double *QRz)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  par_cells(g, [&](size_t id) {
+    int x, y, z;
+    g.xyz(id, x, y, z);
+    double v[16];
+    int nv = 0;
+    double const d = U[id], mx = U[n + id], my = U[2 * n + id], mz = U[3 * n + id], E = U[4 * n + id];
+    double cbx = 0, cby = 0, cbz = 0;
+    if (g.mhd) cc_b(g, U, x, y, z, cbx, cby, cbz);
+    (void)v;
+    (void)nv;
+    auto put = [&](double *Q, size_t at, int dir) {
+      Q[at]         = d;
+      Q[n + at]     = mx;
+      Q[2 * n + at] = my;
+      Q[3 * n + at] = mz;
+      Q[4 * n + at] = E;
+      for (int s = 0; s < g.ns; s++) Q[(size_t)(5 + s) * n + at] = U[(size_t)(5 + s) * n + id];
+      if (g.mhd) {
+        double const b[3] = {cbx, cby, cbz};
+        Q[(size_t)g.fB * n + at]       = b[(dir + 1) % 3];
+        Q[(size_t)(g.fB + 1) * n + at] = b[(dir + 2) % 3];
+      }
+      if (g.de) Q[(size_t)g.fGE * n + at] = U[(size_t)g.fGE * n + id];
+    };
+    put(QLx, id, 0);
+    put(QLy, id, 1);
+    put(QLz, id, 2);
+    if (x > 0) put(QRx, g.id(x - 1, y, z), 0);
+    if (y > 0) put(QRy, g.id(x, y - 1, z), 1);
+    if (z > 0) put(QRz, g.id(x, y, z - 1), 2);
+  });
+}
+
+// src/reconstruction/ppmc_cuda.cu:540-695 PPMC_VL
+void orc_ppmc_vl(const orc_config *c, const double *U, double *QL, double *QR, int dir)
+{
+  Grid g(c);
+  int o1, o2, o3;
+  perm(dir, o1, o2, o3);
+  int const sx = dir == 0, sy = dir == 1, sz = dir == 2;
+  par_cells(g, [&](size_t id) {
+    int x, y, z;
+    g.xyz(id, x, y, z);
+    if (guard<3>(g, x, y, z)) return;
+    Prim const ci   = load_data(g, U, x, y, z, o1, o2, o3);
+    Prim const cim1 = load_data(g, U, x - sx, y - sy, z - sz, o1, o2, o3);
+    Prim const cip1 = load_data(g, U, x + sx, y + sy, z + sz, o1, o2, o3);
+    Prim const cim2 = load_data(g, U, x - 2 * sx, y - 2 * sy, z - 2 * sz, o1, o2, o3);
+    Prim const cip2 = load_data(g, U, x + 2 * sx, y + 2 * sy, z + 2 * sz, o1, o2, o3);
+    double const cs  = sqrt(g.gamma * ci.p / ci.d);  // hydro_utilities.h:209 Calc_Sound_Speed
+    double const cs2 = cs * cs;
+    Eig e;
+    std::memset(&e, 0, sizeof(e));
+    if (g.mhd) e = eigenvectors(ci, cs, cs2, g.gamma);
+    Chr const ai   = prim_to_char(g.mhd, ci, ci, e, cs, cs2);
+    Chr const aim1 = prim_to_char(g.mhd, ci, cim1, e, cs, cs2);
+    Chr const aim2 = prim_to_char(g.mhd, ci, cim2, e, cs, cs2);
+    Chr const aip1 = prim_to_char(g.mhd, ci, cip1, e, cs, cs2);
+    Chr const aip2 = prim_to_char(g.mhd, ci, cip2, e, cs, cs2);
+    Chr aR, aL;
+    int const nchar = g.mhd ? 7 : 5;
+    for (int k = 0; k < 7; k++) aR.a[k] = aL.a[k] = 0.0;
+    for (int k = 0; k < nchar; k++) ppm1(aim2.a[k], aim1.a[k], ai.a[k], aip1.a[k], aip2.a[k], aL.a[k], aR.a[k]);
+    Prim L = char_to_prim(g.mhd, ci, aL, e, cs, cs2);
+    Prim R = char_to_prim(g.mhd, ci, aR, e, cs, cs2);
+    if (g.de) ppm1(cim2.ge, cim1.ge, ci.ge, cip1.ge, cip2.ge, L.ge, R.ge);
+    for (int s = 0; s < g.ns; s++) ppm1(cim2.sc[s], cim1.sc[s], ci.sc[s], cip1.sc[s], cip2.sc[s], L.sc[s], R.sc[s]);
+    R.d = fmax(R.d, TINY);
+    L.d = fmax(L.d, TINY);
+    R.p = fmax(R.p, TINY);
+    L.p = fmax(L.p, TINY);
+    write_data(g, L, QL, U, id, o1, o2, o3);
+    write_data(g, R, QR, U, g.id(x - sx, y - sy, z - sz), o1, o2, o3);
+  });
+}
+
+// src/reconstruction/plmc_cuda.cu:24-300 PLMC_cuda (VL: no characteristic tracing)
+void orc_plmc(const orc_config *c, const double *U, double *QL, double *QR, int dir)
+{
+  Grid g(c);
+  int o1, o2, o3;
+  perm(dir, o1, o2, o3);
+  int const sx = dir == 0, sy = dir == 1, sz = dir == 2;
+  par_cells(g, [&](size_t id) {
+    int x, y, z;
+    g.xyz(id, x, y, z);
+    if (guard<2>(g, x, y, z)) return;
+    Prim const ci   = load_data(g, U, x, y, z, o1, o2, o3);
+    Prim const cimo = load_data(g, U, x - sx, y - sy, z - sz, o1, o2, o3);
+    Prim const cipo = load_data(g, U, x + sx, y + sy, z + sz, o1, o2, o3);
+    double const cs  = sqrt(g.gamma * ci.p / ci.d);
+    double const cs2 = cs * cs;
+    Eig e;
+    std::memset(&e, 0, sizeof(e));
+    if (g.mhd) e = eigenvectors(ci, cs, cs2, g.gamma);
+    // reconstruction.h:224-296 Compute_Slope / Van_Leer_Slope
+    auto slope = [&](const Prim &l, const Prim &r, double coef) {
+      Prim s;
+      std::memset(&s, 0, sizeof(s));
+      s.d  = coef * (r.d - l.d);
+      s.vx = coef * (r.vx - l.vx);
+      s.vy = coef * (r.vy - l.vy);
+      s.vz = coef * (r.vz - l.vz);
+      s.p  = coef * (r.p - l.p);
+      if (g.mhd) {
+        s.by = coef * (r.by - l.by);
+        s.bz = coef * (r.bz - l.bz);
+      }
+      if (g.de) s.ge = coef * (r.ge - l.ge);
+      for (int k = 0; k < g.ns; k++) s.sc[k] = coef * (r.sc[k] - l.sc[k]);
+      return s;
+    };
+    auto vl = [](double l, double r) -> double {
+      if (l * r > 0.0) {
+        return 2.0 * l * r / (l + r);
+      } else {
+        return 0.0;
+      }
+    };
+    Prim const dL = slope(cimo, ci, 1.0);
+    Prim const dR = slope(ci, cipo, 1.0);
+    Prim const dC = slope(cimo, cipo, 0.5);
+    Prim dG;
+    std::memset(&dG, 0, sizeof(dG));
+    dG.d  = vl(dL.d, dR.d);
+    dG.vx = vl(dL.vx, dR.vx);
+    dG.vy = vl(dL.vy, dR.vy);
+    dG.vz = vl(dL.vz, dR.vz);
+    dG.p  = vl(dL.p, dR.p);
+    if (g.mhd) {
+      dG.by = vl(dL.by, dR.by);
+      dG.bz = vl(dL.bz, dR.bz);
+    }
+    if (g.de) dG.ge = vl(dL.ge, dR.ge);
+    for (int k = 0; k < g.ns; k++) dG.sc[k] = vl(dL.sc[k], dR.sc[k]);
+    Chr const aL = prim_to_char(g.mhd, ci, dL, e, cs, cs2);
+    Chr const aR = prim_to_char(g.mhd, ci, dR, e, cs, cs2);
+    Chr const aC = prim_to_char(g.mhd, ci, dC, e, cs, cs2);
+    Chr const aG = prim_to_char(g.mhd, ci, dG, e, cs, cs2);
+    // reconstruction.h:512-559 Monotonize_Characteristic_Return_Primitive
+    auto mono = [](double l, double r, double cc, double vg) -> double {
+      if (l * r > 0.0) {
+        double const la = 2.0 * fmin(fabs(l), fabs(r));
+        double const lb = fmin(fabs(cc), fabs(vg));
+        return copysign(fmin(la, lb), cc);
+      } else {
+        return 0.0;
+      }
+    };
+    Chr am;
+    int const nchar = g.mhd ? 7 : 5;
+    for (int k = 0; k < 7; k++) am.a[k] = 0.0;
+    for (int k = 0; k < nchar; k++) am.a[k] = mono(aL.a[k], aR.a[k], aC.a[k], aG.a[k]);
+    Prim dm = char_to_prim(g.mhd, ci, am, e, cs, cs2);
+    if (g.de) dm.ge = mono(dL.ge, dR.ge, dC.ge, dG.ge);
+    for (int k = 0; k < g.ns; k++) dm.sc[k] = mono(dL.sc[k], dR.sc[k], dC.sc[k], dG.sc[k]);
+    // reconstruction.h:645-673 Calc_Interface_Linear
+    auto lin = [&](double sign) {
+      Prim o;
+      std::memset(&o, 0, sizeof(o));
+      auto f = [&sign](double st, double sl) -> double { return st + sign * 0.5 * sl; };
+      o.d  = f(ci.d, dm.d);
+      o.vx = f(ci.vx, dm.vx);
+      o.vy = f(ci.vy, dm.vy);
+      o.vz = f(ci.vz, dm.vz);
+      o.p  = f(ci.p, dm.p);
+      if (g.mhd) {
+        o.by = f(ci.by, dm.by);
+        o.bz = f(ci.bz, dm.bz);
+      }
+      if (g.de) o.ge = f(ci.ge, dm.ge);
+      for (int k = 0; k < g.ns; k++) o.sc[k] = f(ci.sc[k], dm.sc[k]);
+      return o;
+    };
+    Prim L = lin(1.0);
+    Prim R = lin(-1.0);
+    // reconstruction.h:686-723 Plm_Limit_Interfaces
+    auto lim = [](double &l, double &r, double vm, double vi, double vp) {
+      r = fmax(fmin(vi, vm), r);
+      r = fmin(fmax(vi, vm), r);
+      l = fmax(fmin(vi, vp), l);
+      l = fmin(fmax(vi, vp), l);
+    };
+    lim(L.d, R.d, cimo.d, ci.d, cipo.d);
+    lim(L.vx, R.vx, cimo.vx, ci.vx, cipo.vx);
+    lim(L.vy, R.vy, cimo.vy, ci.vy, cipo.vy);
+    lim(L.vz, R.vz, cimo.vz, ci.vz, cipo.vz);
+    lim(L.p, R.p, cimo.p, ci.p, cipo.p);
+    if (g.mhd) {
+      lim(L.by, R.by, cimo.by, ci.by, cipo.by);
+      lim(L.bz, R.bz, cimo.bz, ci.bz, cipo.bz);
+    }
+    if (g.de) lim(L.ge, R.ge, cimo.ge, ci.ge, cipo.ge);
+    for (int k = 0; k < g.ns; k++) lim(L.sc[k], R.sc[k], cimo.sc[k], ci.sc[k], cipo.sc[k]);
+    R.d = fmax(R.d, TINY);
+    L.d = fmax(L.d, TINY);
+    R.p = fmax(R.p, TINY);
+    L.p = fmax(L.p, TINY);
+    write_data(g, L, QL, U, id, o1, o2, o3);
+    write_data(g, R, QR, U, g.id(x - sx, y - sy, z - sz), o1, o2, o3);
+  });
+}
+
+// src/riemann_solvers/hllc_cuda.cu:19-307 Calculate_HLLC_Fluxes_CUDA
+void orc_hllc(const orc_config *c, const double *QL, const double *QR, double *F, int dir)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int o1, o2, o3;
+  perm(dir, o1, o2, o3);
+  double const gamma = g.gamma;
+  par_cells(g, [&](size_t tid) {
+    double const g1 = gamma - 1.0;
+    double const etah = 0;
+    double dl = QL[tid], mxl = QL[o1 * n + tid], myl = QL[o2 * n + tid], mzl = QL[o3 * n + tid], El = QL[4 * n + tid];
+    double dr = QR[tid], mxr = QR[o1 * n + tid], myr = QR[o2 * n + tid], mzr = QR[o3 * n + tid], Er = QR[4 * n + tid];
+    double dscl[MAXS], dscr[MAXS], scl[MAXS], scr[MAXS];
+    for (int s = 0; s < g.ns; s++) {
+      dscl[s] = QL[(size_t)(5 + s) * n + tid];
+      dscr[s] = QR[(size_t)(5 + s) * n + tid];
+    }
+    double dgel = 0, dger = 0, gel = 0, ger = 0;
+    if (g.de) {
+      dgel = QL[(size_t)g.fGE * n + tid];
+      dger = QR[(size_t)g.fGE * n + tid];
+    }
+    double vxl = mxl / dl, vyl = myl / dl, vzl = mzl / dl, pl;
+    if (g.de) {
+      double const E_kin = 0.5 * dl * (vxl * vxl + vyl * vyl + vzl * vzl);
+      pl                 = pressure_from_de(El, El - E_kin, dgel, gamma);
+    } else {
+      pl = (El - 0.5 * dl * (vxl * vxl + vyl * vyl + vzl * vzl)) * (gamma - 1.0);
+    }
+    pl = fmax(pl, TINY);
+    for (int s = 0; s < g.ns; s++) scl[s] = dscl[s] / dl;
+    if (g.de) gel = dgel / dl;
+    double vxr = mxr / dr, vyr = myr / dr, vzr = mzr / dr, pr;
+    if (g.de) {
+      double const E_kin = 0.5 * dr * (vxr * vxr + vyr * vyr + vzr * vzr);
+      pr                 = pressure_from_de(Er, Er - E_kin, dger, gamma);
+    } else {
+      pr = (Er - 0.5 * dr * (vxr * vxr + vyr * vyr + vzr * vzr)) * (gamma - 1.0);
+    }
+    pr = fmax(pr, TINY);
+    for (int s = 0; s < g.ns; s++) scr[s] = dscr[s] / dr;
+    if (g.de) ger = dger / dr;
+    double const Hl = (El + pl) / dl;
+    double const Hr = (Er + pr) / dr;
+    double const sqrtdl = sqrt(dl);
+    double const sqrtdr = sqrt(dr);
+    double const vx     = (sqrtdl * vxl + sqrtdr * vxr) / (sqrtdl + sqrtdr);
+    double const vy     = (sqrtdl * vyl + sqrtdr * vyr) / (sqrtdl + sqrtdr);
+    double const vz     = (sqrtdl * vzl + sqrtdr * vzr) / (sqrtdl + sqrtdr);
+    double const H      = (sqrtdl * Hl + sqrtdr * Hr) / (sqrtdl + sqrtdr);
+    double const vsq    = (vx * vx + vy * vy + vz * vz);
+    double const asq    = g1 * (H - 0.5 * vsq);
+    double const a      = sqrt(asq);
+    double const lambda_m = vx - a;
+    double const lambda_p = vx + a;
+    double const cfl      = sqrt(gamma * pl / dl);
+    double const cfr      = sqrt(gamma * pr / dr);
+    double Sl             = fmin(lambda_m, vxl - cfl);
+    double Sr             = fmax(lambda_p, vxr + cfr);
+    Sl                    = sgn_int(Sl) * fmax(fabs(Sl), etah);
+    Sr                    = sgn_int(Sr) * fmax(fabs(Sr), etah);
+    double const f_d_l = mxl, f_mx_l = mxl * vxl + pl, f_my_l = myl * vxl, f_mz_l = mzl * vxl,
+                 f_E_l = (El + pl) * vxl;
+    double const f_d_r = mxr, f_mx_r = mxr * vxr + pr, f_my_r = myr * vxr, f_mz_r = mzr * vxr,
+                 f_E_r = (Er + pr) * vxr;
+    double const f_ge_l = dgel * vxl, f_ge_r = dger * vxr;
+    auto out = [&](double fd, double fmx, double fmy, double fmz, double fE) {
+      F[tid]          = fd;
+      F[o1 * n + tid] = fmx;
+      F[o2 * n + tid] = fmy;
+      F[o3 * n + tid] = fmz;
+      F[4 * n + tid]  = fE;
+    };
+    if (Sl > 0.0) {
+      out(f_d_l, f_mx_l, f_my_l, f_mz_l, f_E_l);
+      for (int s = 0; s < g.ns; s++) F[(size_t)(5 + s) * n + tid] = dscl[s] * vxl;
+      if (g.de) F[(size_t)g.fGE * n + tid] = f_ge_l;
+      return;
+    } else if (Sr < 0.0) {
+      out(f_d_r, f_mx_r, f_my_r, f_mz_r, f_E_r);
+      for (int s = 0; s < g.ns; s++) F[(size_t)(5 + s) * n + tid] = dscr[s] * vxr;
+      if (g.de) F[(size_t)g.fGE * n + tid] = f_ge_r;
+      return;
+    }
+    double const Sm = (dr * vxr * (Sr - vxr) - dl * vxl * (Sl - vxl) + pl - pr) / (dr * (Sr - vxr) - dl * (Sl - vxl));
+    double const ps = dl * (vxl - Sl) * (vxl - Sm) + pl;
+    double const dls  = dl * (Sl - vxl) / (Sl - Sm);
+    double const mxls = (mxl * (Sl - vxl) + ps - pl) / (Sl - Sm);
+    double const myls = dls * vyl;
+    double const mzls = dls * vzl;
+    double const Els  = (El * (Sl - vxl) - pl * vxl + ps * Sm) / (Sl - Sm);
+    double const gels = dls * gel;
+    double const drs  = dr * (Sr - vxr) / (Sr - Sm);
+    double const mxrs = (mxr * (Sr - vxr) + ps - pr) / (Sr - Sm);
+    double const myrs = drs * vyr;
+    double const mzrs = drs * vzr;
+    double const Ers  = (Er * (Sr - vxr) - pr * vxr + ps * Sm) / (Sr - Sm);
+    double const gers = drs * ger;
+    double const f_d  = 0.5 * (f_d_l + f_d_r + (Sr - fabs(Sm)) * drs + (Sl + fabs(Sm)) * dls - Sl * dl - Sr * dr);
+    double const f_mx =
+        0.5 * (f_mx_l + f_mx_r + (Sr - fabs(Sm)) * mxrs + (Sl + fabs(Sm)) * mxls - Sl * mxl - Sr * mxr);
+    double const f_my =
+        0.5 * (f_my_l + f_my_r + (Sr - fabs(Sm)) * myrs + (Sl + fabs(Sm)) * myls - Sl * myl - Sr * myr);
+    double const f_mz =
+        0.5 * (f_mz_l + f_mz_r + (Sr - fabs(Sm)) * mzrs + (Sl + fabs(Sm)) * mzls - Sl * mzl - Sr * mzr);
+    double const f_E = 0.5 * (f_E_l + f_E_r + (Sr - fabs(Sm)) * Ers + (Sl + fabs(Sm)) * Els - Sl * El - Sr * Er);
+    out(f_d, f_mx, f_my, f_mz, f_E);
+    for (int s = 0; s < g.ns; s++) {
+      double const scls = dls * scl[s], scrs = drs * scr[s];
+      double const fl = dscl[s] * vxl, fr = dscr[s] * vxr;
+      F[(size_t)(5 + s) * n + tid] =
+          0.5 * (fl + fr + (Sr - fabs(Sm)) * scrs + (Sl + fabs(Sm)) * scls - Sl * dscl[s] - Sr * dscr[s]);
+    }
+    if (g.de) {
+      F[(size_t)g.fGE * n + tid] =
+          0.5 * (f_ge_l + f_ge_r + (Sr - fabs(Sm)) * gers + (Sl + fabs(Sm)) * gels - Sl * dgel - Sr * dger);
+    }
+  });
+}
+
+// src/riemann_solvers/roe_cuda.cu:19-400 Calculate_Roe_Fluxes_CUDA
+void orc_roe(const orc_config *c, const double *QL, const double *QR, double *F, int dir)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int o1, o2, o3;
+  perm(dir, o1, o2, o3);
+  double const gamma = g.gamma;
+  par_cells(g, [&](size_t tid) {
+    double const etah = 0.0;
+    double const g1   = gamma - 1.0;
+    double dl = QL[tid], mxl = QL[o1 * n + tid], myl = QL[o2 * n + tid], mzl = QL[o3 * n + tid], El = QL[4 * n + tid];
+    double dr = QR[tid], mxr = QR[o1 * n + tid], myr = QR[o2 * n + tid], mzr = QR[o3 * n + tid], Er = QR[4 * n + tid];
+    double dscl[MAXS], dscr[MAXS], scl[MAXS], scr[MAXS], fscl[MAXS], fscr[MAXS];
+    for (int s = 0; s < g.ns; s++) {
+      dscl[s] = QL[(size_t)(5 + s) * n + tid];
+      dscr[s] = QR[(size_t)(5 + s) * n + tid];
+    }
+    double dgel = 0, dger = 0, gel = 0, ger = 0, f_ge_l = 0, f_ge_r = 0;
+    if (g.de) {
+      dgel = QL[(size_t)g.fGE * n + tid];
+      dger = QR[(size_t)g.fGE * n + tid];
+    }
+    double vxl = mxl / dl, vyl = myl / dl, vzl = mzl / dl, pl;
+    if (g.de) {
+      double const E_kin = 0.5 * dl * (vxl * vxl + vyl * vyl + vzl * vzl);
+      pl                 = pressure_from_de(El, El - E_kin, dgel, gamma);
+    } else {
+      pl = (El - 0.5 * dl * (vxl * vxl + vyl * vyl + vzl * vzl)) * (gamma - 1.0);
+    }
+    pl = fmax(pl, TINY);
+    for (int s = 0; s < g.ns; s++) scl[s] = dscl[s] / dl;
+    if (g.de) gel = dgel / dl;
+    double vxr = mxr / dr, vyr = myr / dr, vzr = mzr / dr, pr;
+    if (g.de) {
+      double const E_kin = 0.5 * dr * (vxr * vxr + vyr * vyr + vzr * vzr);
+      pr                 = pressure_from_de(Er, Er - E_kin, dger, gamma);
+    } else {
+      pr = (Er - 0.5 * dr * (vxr * vxr + vyr * vyr + vzr * vzr)) * (gamma - 1.0);
+    }
+    pr = fmax(pr, TINY);
+    for (int s = 0; s < g.ns; s++) scr[s] = dscr[s] / dr;
+    if (g.de) ger = dger / dr;
+    double const Hl = (El + pl) / dl, Hr = (Er + pr) / dr;
+    double const sqrtdl = sqrt(dl), sqrtdr = sqrt(dr);
+    double const vx  = (sqrtdl * vxl + sqrtdr * vxr) / (sqrtdl + sqrtdr);
+    double const vy  = (sqrtdl * vyl + sqrtdr * vyr) / (sqrtdl + sqrtdr);
+    double const vz  = (sqrtdl * vzl + sqrtdr * vzr) / (sqrtdl + sqrtdr);
+    double const H   = (sqrtdl * Hl + sqrtdr * Hr) / (sqrtdl + sqrtdr);
+    double const vsq = (vx * vx + vy * vy + vz * vz);
+    double const asq = g1 * fmax((H - 0.5 * vsq), TINY);
+    double const a   = sqrt(asq);
+    double const lambda_m = vx - a, lambda_0 = vx, lambda_p = vx + a;
+    double f_d_l = mxl, f_mx_l = mxl * vxl + pl, f_my_l = mxl * vyl, f_mz_l = mxl * vzl, f_E_l = (El + pl) * vxl;
+    double f_d_r = mxr, f_mx_r = mxr * vxr + pr, f_my_r = mxr * vyr, f_mz_r = mxr * vzr, f_E_r = (Er + pr) * vxr;
+    if (g.de) {
+      f_ge_l = mxl * gel;
+      f_ge_r = mxr * ger;
+    }
+    for (int s = 0; s < g.ns; s++) {
+      fscl[s] = mxl * scl[s];
+      fscr[s] = mxr * scr[s];
+    }
+    auto out = [&](double fd, double fmx, double fmy, double fmz, double fE) {
+      F[tid]          = fd;
+      F[o1 * n + tid] = fmx;
+      F[o2 * n + tid] = fmy;
+      F[o3 * n + tid] = fmz;
+      F[4 * n + tid]  = fE;
+    };
+    if (lambda_m >= 0.0) {
+      out(f_d_l, f_mx_l, f_my_l, f_mz_l, f_E_l);
+      for (int s = 0; s < g.ns; s++) F[(size_t)(5 + s) * n + tid] = fscl[s];
+      if (g.de) F[(size_t)g.fGE * n + tid] = f_ge_l;
+      return;
+    } else if (lambda_p <= 0.0) {
+      out(f_d_r, f_mx_r, f_my_r, f_mz_r, f_E_r);
+      for (int s = 0; s < g.ns; s++) F[(size_t)(5 + s) * n + tid] = fscr[s];
+      if (g.de) F[(size_t)g.fGE * n + tid] = f_ge_r;
+      return;
+    }
+    double sum_0 = 0, sum_1 = 0, sum_2 = 0, sum_3 = 0, sum_4 = 0;
+    double const del_d = dr - dl, del_mx = mxr - mxl, del_my = myr - myl, del_mz = mzr - mzl, del_E = Er - El;
+    double const Na = 0.5 / asq;
+    double coeff    = 0.0;
+    double const a0 = del_d * Na * (0.5 * g1 * vsq + vx * a) - del_mx * Na * (g1 * vx + a) - del_my * Na * g1 * vy -
+                      del_mz * Na * g1 * vz + del_E * Na * g1;
+    coeff = a0 * fmax(fabs(lambda_m), etah);
+    sum_0 += coeff;
+    sum_1 += coeff * (vx - a);
+    sum_2 += coeff * vy;
+    sum_3 += coeff * vz;
+    sum_4 += coeff * (H - vx * a);
+    double const a1 = -del_d * vy + del_my;
+    coeff           = a1 * fmax(fabs(lambda_0), etah);
+    sum_2 += coeff;
+    sum_4 += coeff * vy;
+    double const a2 = -del_d * vz + del_mz;
+    coeff           = a2 * fmax(fabs(lambda_0), etah);
+    sum_3 += coeff;
+    sum_4 += coeff * vz;
+    double const a3 = del_d * (1.0 - Na * g1 * vsq) + del_mx * g1 * vx / asq + del_my * g1 * vy / asq +
+                      del_mz * g1 * vz / asq - del_E * g1 / asq;
+    coeff = a3 * fmax(fabs(lambda_0), etah);
+    sum_0 += coeff;
+    sum_1 += coeff * vx;
+    sum_2 += coeff * vy;
+    sum_3 += coeff * vz;
+    sum_4 += coeff * 0.5 * vsq;
+    double const a4 = del_d * Na * (0.5 * g1 * vsq - vx * a) - del_mx * Na * (g1 * vx - a) - del_my * Na * g1 * vy -
+                      del_mz * Na * g1 * vz + del_E * Na * g1;
+    coeff = a4 * fmax(fabs(lambda_p), etah);
+    sum_0 += coeff;
+    sum_1 += coeff * (vx + a);
+    sum_2 += coeff * vy;
+    sum_3 += coeff * vz;
+    sum_4 += coeff * (H + vx * a);
+    int hlle_flag = 0;
+    double test0 = dl + a0, test1 = mxl + a0 * (vx - a), test2 = myl + a0 * vy, test3 = mzl + a0 * vz,
+           test4 = El + a0 * (H - vx * a);
+    if (lambda_0 > lambda_m) {
+      if (test0 <= 0.0) hlle_flag = 1;
+      if (test4 - 0.5 * (test1 * test1 + test2 * test2 + test3 * test3) / test0 < 0.0) hlle_flag = 2;
+    }
+    test0 += a3 + a4;
+    test1 += a3 * vx;
+    test2 += a1 + a3 * vy;
+    test3 += a2 + a3 * vz;
+    test4 += a1 * vy + a2 * vz + a3 * 0.5 * vsq;
+    if (lambda_p > lambda_0) {
+      if (test0 <= 0.0) hlle_flag = 1;
+      if (test4 - 0.5 * (test1 * test1 + test2 * test2 + test3 * test3) / test0 < 0.0) hlle_flag = 2;
+    }
+    if (hlle_flag != 0) {
+      double const cfl = sqrt(gamma * pl / dl);
+      double const cfr = sqrt(gamma * pr / dr);
+      double const bm  = fmin(fmin(lambda_m, vxl - cfl), 0.0);
+      double const bp  = fmax(fmax(lambda_p, vxr + cfr), 0.0);
+      f_d_l            = mxl - bm * dl;
+      f_d_r            = mxr - bp * dr;
+      f_mx_l           = mxl * (vxl - bm) + pl;
+      f_mx_r           = mxr * (vxr - bp) + pr;
+      f_my_l           = myl * (vxl - bm);
+      f_my_r           = myr * (vxr - bp);
+      f_mz_l           = mzl * (vxl - bm);
+      f_mz_r           = mzr * (vxr - bp);
+      f_E_l            = El * (vxl - bm) + pl * vxl;
+      f_E_r            = Er * (vxr - bp) + pr * vxr;
+      if (g.de) {
+        f_ge_l = dgel * (vxl - bm);
+        f_ge_r = dger * (vxr - bp);
+      }
+      for (int s = 0; s < g.ns; s++) {
+        fscl[s] = dscl[s] * (vxl - bm);
+        fscr[s] = dscr[s] * (vxr - bp);
+      }
+      double const tmp = 0.5 * (bp + bm) / (bp - bm);
+      out(0.5 * (f_d_l + f_d_r) + (f_d_l - f_d_r) * tmp, 0.5 * (f_mx_l + f_mx_r) + (f_mx_l - f_mx_r) * tmp,
+          0.5 * (f_my_l + f_my_r) + (f_my_l - f_my_r) * tmp, 0.5 * (f_mz_l + f_mz_r) + (f_mz_l - f_mz_r) * tmp,
+          0.5 * (f_E_l + f_E_r) + (f_E_l - f_E_r) * tmp);
+      for (int s = 0; s < g.ns; s++)
+        F[(size_t)(5 + s) * n + tid] = 0.5 * (fscl[s] + fscr[s]) + (fscl[s] - fscr[s]) * tmp;
+      if (g.de) F[(size_t)g.fGE * n + tid] = 0.5 * (f_ge_l + f_ge_r) + (f_ge_l - f_ge_r) * tmp;
+      return;
+    }
+    out(0.5 * (f_d_l + f_d_r - sum_0), 0.5 * (f_mx_l + f_mx_r - sum_1), 0.5 * (f_my_l + f_my_r - sum_2),
+        0.5 * (f_mz_l + f_mz_r - sum_3), 0.5 * (f_E_l + f_E_r - sum_4));
+    for (int s = 0; s < g.ns; s++)
+      F[(size_t)(5 + s) * n + tid] = (F[tid] >= 0.0) ? F[tid] * scl[s] : F[tid] * scr[s];
+    if (g.de) F[(size_t)g.fGE * n + tid] = (F[tid] >= 0.0) ? F[tid] * gel : F[tid] * ger;
+  });
+}
+
+// src/riemann_solvers/hlld_cuda.cu:31-508 (mhd::Calculate_HLLD_Fluxes_CUDA and mhd::internal)
+namespace
+{
+struct HState {
+  double d, vx, vy, vz, E, by, bz, p, pt;
+  double sc[MAXS];
+  double ge;
+};
+struct HStar {
+  double d, vy, vz, E, by, bz;
+};
+struct HDStar {
+  double vy, vz, by, bz, EL = 0.0, ER = 0.0;
+};
+struct HFlux {
+  double d, mx, my, mz, E, by, bz;
+};
+struct HSpeeds {
+  double L, LStar, M, RStar, R;
+};
+
+HState hlld_load(const Grid &g, const double *Q, double bx, size_t t, int o1, int o2, int o3)
+{
+  size_t const n = g.n;
+  HState s;
+  s.d  = Q[t];
+  s.d  = fmax(s.d, TINY);
+  s.vx = Q[t + n * o1] / s.d;
+  s.vy = Q[t + n * o2] / s.d;
+  s.vz = Q[t + n * o3] / s.d;
+  s.E  = Q[t + n * 4];
+  s.E  = fmax(s.E, TINY);
+  s.by = Q[t + n * g.fB];
+  s.bz = Q[t + n * (g.fB + 1)];
+  for (int k = 0; k < g.ns; k++) s.sc[k] = Q[t + n * (5 + k)] / s.d;
+  s.ge = 0;
+  if (g.de) {
+    s.ge         = Q[t + n * g.fGE] / s.d;
+    double const Ent = 0.5 * s.d * sqmag(s.vx, s.vy, s.vz) + magE(bx, s.by, s.bz);
+    s.p          = fmax(pressure_from_de(s.E, s.E - Ent, s.ge * s.d, g.gamma), TINY);
+  } else {
+    double pressure = s.E - 0.5 * s.d * sqmag(s.vx, s.vy, s.vz);
+    pressure -= magE(bx, s.by, s.bz);
+    s.p = fmax((g.gamma - 1.) * pressure, TINY);
+  }
+  double pt = s.p + magE(bx, s.by, s.bz);  // mhd_utilities.h computeTotalPressure
+  s.pt      = fmax(pt, TINY);
+  return s;
+}
+HFlux hlld_nonstar(const HState &s, double bx)
+{
+  HFlux f;
+  f.d  = s.d * s.vx;
+  f.mx = f.d * s.vx + s.pt - bx * bx;
+  f.my = f.d * s.vy - bx * s.by;
+  f.mz = f.d * s.vz - bx * s.bz;
+  f.by = s.by * s.vx - bx * s.vy;
+  f.bz = s.bz * s.vx - bx * s.vz;
+  f.E  = s.vx * (s.E + s.pt) - bx * (s.vx * bx + ((s.vy * s.by) + (s.vz * s.bz)));
+  return f;
+}
+HStar hlld_star(const HState &s, const HSpeeds &sp, double S, double bx, double ptStar)
+{
+  HStar st;
+  st.d = s.d * (S - s.vx) / (S - sp.M);
+  if (fabs(s.d * (S - s.vx) * (S - sp.M) - (bx * bx)) < ptStar * HLLD_SMALL) {
+    st.vy = s.vy;
+    st.vz = s.vz;
+    st.by = s.by;
+    st.bz = s.bz;
+  } else {
+    double const denom = s.d * (S - s.vx) * (S - sp.M) - (bx * bx);
+    double coef        = bx * (sp.M - s.vx) / denom;
+    st.vy              = s.vy - s.by * coef;
+    st.vz              = s.vz - s.bz * coef;
+    double tp          = (S - s.vx);
+    tp                 = tp * tp;
+    coef               = (s.d * tp - (bx * bx)) / denom;
+    st.by              = s.by * coef;
+    st.bz              = s.bz * coef;
+  }
+  st.E = (s.E * (S - s.vx) - s.pt * s.vx + ptStar * sp.M +
+          bx * (dot3(s.vx, s.vy, s.vz, bx, s.by, s.bz) - dot3(sp.M, st.vy, st.vz, bx, st.by, st.bz))) /
+         (S - sp.M);
+  return st;
+}
+HFlux hlld_starflux(const HStar &st, const HState &s, const HFlux &f, const HSpeeds &sp, double S)
+{
+  HFlux o;
+  o.d  = f.d + S * (st.d - s.d);
+  o.mx = f.mx + S * (st.d * sp.M - s.d * s.vx);
+  o.my = f.my + S * (st.d * st.vy - s.d * s.vy);
+  o.mz = f.mz + S * (st.d * st.vz - s.d * s.vz);
+  o.E  = f.E + S * (st.E - s.E);
+  o.by = f.by + S * (st.by - s.by);
+  o.bz = f.bz + S * (st.bz - s.bz);
+  return o;
+}
+HDStar hlld_dstar(const HStar &L, const HStar &R, double bx, double ptStar, const HSpeeds &sp)
+{
+  HDStar o;
+  if (0.5 * (bx * bx) < HLLD_SMALL * ptStar) {
+    if (sp.M >= 0.0) {
+      o.vy = L.vy, o.vz = L.vz, o.by = L.by, o.bz = L.bz, o.EL = L.E;
+    } else {
+      o.vy = R.vy, o.vz = R.vz, o.by = R.by, o.bz = R.bz, o.ER = R.E;
+    }
+  } else {
+    double const sqrtDL = sqrt(L.d), sqrtDR = sqrt(R.d);
+    double const inv    = 1.0 / (sqrtDL + sqrtDR);
+    double const sgnb   = copysign(1.0, bx);
+    o.vy = inv * (sqrtDL * L.vy + sqrtDR * R.vy + sgnb * (R.by - L.by));
+    o.vz = inv * (sqrtDL * L.vz + sqrtDR * R.vz + sgnb * (R.bz - L.bz));
+    o.by = inv * (sqrtDL * R.by + sqrtDR * L.by + sgnb * (sqrtDL * sqrtDR) * (R.vy - L.vy));
+    o.bz = inv * (sqrtDL * R.bz + sqrtDR * L.bz + sgnb * (sqrtDL * sqrtDR) * (R.vz - L.vz));
+    double const vdb = dot3(sp.M, o.vy, o.vz, bx, o.by, o.bz);
+    o.EL = L.E - sqrtDL * sgnb * (dot3(sp.M, L.vy, L.vz, bx, L.by, L.bz) - vdb);
+    o.ER = R.E + sqrtDR * sgnb * (dot3(sp.M, R.vy, R.vz, bx, R.by, R.bz) - vdb);
+  }
+  return o;
+}
+HFlux hlld_dstarflux(const HDStar &ds, double dsE, const HStar &st, const HState &s, const HFlux &f,
+                     const HSpeeds &sp, double S, double SStar)
+{
+  HFlux o;
+  double const sd = SStar - S;
+  o.d  = f.d - S * s.d - sd * st.d + SStar * st.d;
+  o.mx = f.mx - S * (s.d * s.vx) - sd * (st.d * sp.M) + SStar * (st.d * sp.M);
+  o.my = f.my - S * (s.d * s.vy) - sd * (st.d * st.vy) + SStar * (st.d * ds.vy);
+  o.mz = f.mz - S * (s.d * s.vz) - sd * (st.d * st.vz) + SStar * (st.d * ds.vz);
+  o.E  = f.E - S * s.E - sd * st.E + SStar * dsE;
+  o.by = f.by - S * s.by - sd * st.by + SStar * ds.by;
+  o.bz = f.bz - S * s.bz - sd * st.bz + SStar * ds.bz;
+  return o;
+}
+}  // namespace
+
+void orc_hlld(const orc_config *c, const double *QL, const double *QR, const double *Bface, double *F, int dir)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int o1, o2, o3;
+  perm(dir, o1, o2, o3);
+  par_cells(g, [&](size_t t) {
+    double const bx   = Bface[t];
+    HState const sL   = hlld_load(g, QL, bx, t, o1, o2, o3);
+    HState const sR   = hlld_load(g, QR, bx, t, o1, o2, o3);
+    auto ret = [&](const HFlux &f, const HState &s) {
+      F[t]                = f.d;
+      F[t + n * o1]       = f.mx;
+      F[t + n * o2]       = f.my;
+      F[t + n * o3]       = f.mz;
+      F[t + n * 4]        = f.E;
+      F[t + n * g.fB]     = f.by;
+      F[t + n * (g.fB + 1)] = f.bz;
+      for (int k = 0; k < g.ns; k++) F[t + n * (5 + k)] = s.sc[k] * f.d;
+      if (g.de) F[t + n * g.fGE] = s.ge * f.d;
+    };
+    double const cL = cfast(sL.d, sL.p, bx, sL.by, sL.bz, g.gamma);
+    double const cR = cfast(sR.d, sR.p, bx, sR.by, sR.bz, g.gamma);
+    double const cmax = fmax(cL, cR);
+    HSpeeds sp;
+    sp.L  = fmin(sL.vx, sR.vx) - cmax;
+    sp.R  = fmax(sL.vx, sR.vx) + cmax;
+    HFlux fL = hlld_nonstar(sL, bx);
+    if (sp.L > 0.0) {
+      ret(fL, sL);
+      return;
+    }
+    HFlux fR = hlld_nonstar(sR, bx);
+    if (sp.R < 0.0) {
+      ret(fR, sR);
+      return;
+    }
+    {
+      double const rd = sp.R - sR.vx, ld = sp.L - sL.vx;
+      sp.M = (rd * sR.d * sR.vx - ld * sL.d * sL.vx - sR.pt + sL.pt) / (rd * sR.d - ld * sL.d);
+    }
+    double const ptStar = (sR.d * sL.pt * (sp.R - sR.vx) - sL.d * sR.pt * (sp.L - sL.vx) +
+                           sL.d * sR.d * (sp.R - sR.vx) * (sp.L - sL.vx) * (sR.vx - sL.vx)) /
+                          (sR.d * (sp.R - sR.vx) - sL.d * (sp.L - sL.vx));
+    HStar const stL = hlld_star(sL, sp, sp.L, bx, ptStar);
+    sp.LStar        = sp.M + -1 * (fabs(bx) / sqrt(fmax(stL.d, TINY)));
+    if (sp.LStar > 0.0 and sp.L <= 0.0) {
+      ret(hlld_starflux(stL, sL, fL, sp, sp.L), sL);
+      return;
+    }
+    HStar const stR = hlld_star(sR, sp, sp.R, bx, ptStar);
+    sp.RStar        = sp.M + 1 * (fabs(bx) / sqrt(fmax(stR.d, TINY)));
+    if (sp.RStar <= 0.0 and sp.R >= 0.0) {
+      ret(hlld_starflux(stR, sR, fR, sp, sp.R), sR);
+      return;
+    }
+    HDStar const ds = hlld_dstar(stL, stR, bx, ptStar, sp);
+    if (sp.M > 0.0 and sp.LStar <= 0.0) {
+      ret(hlld_dstarflux(ds, ds.EL, stL, sL, fL, sp, sp.L, sp.LStar), sL);
+      return;
+    }
+    if (sp.RStar > 0.0 and sp.M <= 0.0) {
+      ret(hlld_dstarflux(ds, ds.ER, stR, sR, fR, sp, sp.R, sp.RStar), sR);
+      return;
+    }
+  });
+}
+
+// src/mhd/ct_electric_fields.h:66-118 _ctSlope and ct_electric_fields.cu:20-279
+namespace
+{
+inline double ct_slope(const Grid &g, const double *flux, const double *U, double fluxSign, int ctDir, int cq1,
+                       int cq2, int fq1, int fq2, int x, int y, int z)
+{
+  size_t const n = g.n;
+  int const m1   = (ctDir + 1) % 3;
+  int const m2   = (ctDir + 2) % 3;
+  int const xc   = x - int(cq1 == 0) - int(cq2 == 0);
+  int const yc   = y - int(cq1 == 1) - int(cq2 == 1);
+  int const zc   = z - int(cq1 == 2) - int(cq2 == 2);
+  size_t const ic = g.id(xc, yc, zc);
+  size_t const iflux = g.id(x - int(fq1 == 0) - int(fq2 == 0), y - int(fq1 == 1) - int(fq2 == 1),
+                            z - int(fq1 == 2) - int(fq2 == 2));
+  size_t const iB2 = g.id(xc - int(m1 == 0), yc - int(m1 == 1), zc - int(m1 == 2));
+  size_t const iB3 = g.id(xc - int(m2 == 0), yc - int(m2 == 1), zc - int(m2 == 2));
+  double const density = U[ic];
+  double const M2      = U[ic + (size_t)(m1 + 1) * n];
+  double const M3      = U[ic + (size_t)(m2 + 1) * n];
+  double const B2c     = 0.5 * (U[ic + (size_t)(m1 + g.fB) * n] + U[iB2 + (size_t)(m1 + g.fB) * n]);
+  double const B3c     = 0.5 * (U[ic + (size_t)(m2 + g.fB) * n] + U[iB3 + (size_t)(m2 + g.fB) * n]);
+  double const ec      = (M3 * B2c - M2 * B3c) / density;
+  double const ef      = fluxSign * flux[iflux + (size_t)(int(fluxSign == 1) + g.fB) * n];
+  return ef - ec;
+}
+}  // namespace
+
+void orc_ct_electric_fields(const orc_config *c, const double *Fx, const double *Fy, const double *Fz,
+                            const double *U, double *emf)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int const fB   = g.fB;
+  // flux field positions of the magnetic fluxes (grid_enum.h:95-100)
+  int const fxBz = fB, fxBy = fB + 1, fyBx = fB, fyBz = fB + 1, fzBy = fB, fzBx = fB + 1;
+  par_cells(g, [&](size_t t) {
+    int x, y, z;
+    g.xyz(t, x, y, z);
+    if (!(x > 0 and y > 0 and z > 0 and x < g.nx and y < g.ny and z < g.nz)) return;
+    auto S = [&](const double *fl, double sgn, int cd, int a, int b, int cc, int d) {
+      return ct_slope(g, fl, U, sgn, cd, a, b, cc, d, x, y, z);
+    };
+    auto pick = [](double sgnUp, double pos, double neg) {
+      if (sgnUp > 0.0) return pos;
+      if (sgnUp < 0.0) return neg;
+      return 0.5 * (pos + neg);
+    };
+    double syp, syn, szp, szn, sxp, sxn, fyp, fyn, fzp, fzn, fxp, fxn;
+    // X electric field
+    syp = pick(Fz[g.id(x, y, z - 1)], S(Fy, -1, 0, 2, -1, 1, 2), S(Fy, -1, 0, -1, -1, 1, -1));
+    syn = pick(Fz[g.id(x, y - 1, z - 1)], S(Fy, -1, 0, 1, 2, 1, 2), S(Fy, -1, 0, 1, -1, 1, -1));
+    szp = pick(Fy[g.id(x, y - 1, z)], S(Fz, 1, 0, 1, -1, 1, 2), S(Fz, 1, 0, -1, -1, 2, -1));
+    szn = pick(Fy[g.id(x, y - 1, z - 1)], S(Fz, 1, 0, 1, 2, 1, 2), S(Fz, 1, 0, 2, -1, -1, 2));
+    fyp = +Fz[g.id(x, y, z - 1) + (size_t)fzBx * n];
+    fyn = +Fz[g.id(x, y - 1, z - 1) + (size_t)fzBx * n];
+    fzp = -Fy[g.id(x, y - 1, z) + (size_t)fyBx * n];
+    fzn = -Fy[g.id(x, y - 1, z - 1) + (size_t)fyBx * n];
+    emf[t + 0 * n] = 0.25 * (+fyp + fyn + fzp + fzn + syp + syn + szp + szn);
+    // Y electric field
+    sxp = pick(Fz[g.id(x, y, z - 1)], S(Fx, 1, 1, 2, -1, 0, 2), S(Fx, 1, 1, -1, -1, 0, -1));
+    sxn = pick(Fz[g.id(x - 1, y, z - 1)], S(Fx, 1, 1, 0, 2, 0, 2), S(Fx, 1, 1, 0, -1, 0, -1));
+    szp = pick(Fx[g.id(x - 1, y, z)], S(Fz, -1, 1, 0, -1, 0, 2), S(Fz, -1, 1, -1, -1, 2, -1));
+    szn = pick(Fx[g.id(x - 1, y, z - 1)], S(Fz, -1, 1, 0, 2, 0, 2), S(Fz, -1, 1, 2, -1, 2, -1));
+    fxp = -Fz[g.id(x, y, z - 1) + (size_t)fzBy * n];
+    fxn = -Fz[g.id(x - 1, y, z - 1) + (size_t)fzBy * n];
+    fzp = +Fx[g.id(x - 1, y, z) + (size_t)fxBy * n];
+    fzn = +Fx[g.id(x - 1, y, z - 1) + (size_t)fxBy * n];
+    emf[t + 1 * n] = 0.25 * (+fxp + fxn + fzp + fzn + sxp + sxn + szp + szn);
+    // Z electric field
+    syp = pick(Fx[g.id(x - 1, y, z)], S(Fy, 1, 2, 0, -1, 0, 1), S(Fy, 1, 2, -1, -1, 1, -1));
+    syn = pick(Fx[g.id(x - 1, y - 1, z)], S(Fy, 1, 2, 0, 1, 0, 1), S(Fy, 1, 2, 1, -1, 1, -1));
+    sxp = pick(Fy[g.id(x, y - 1, z)], S(Fx, -1, 2, 1, -1, 0, 1), S(Fx, -1, 2, -1, -1, 0, -1));
+    sxn = pick(Fy[g.id(x - 1, y - 1, z)], S(Fx, -1, 2, 0, 1, 0, 1), S(Fx, -1, 2, 0, -1, 0, -1));
+    fxp = +Fy[g.id(x, y - 1, z) + (size_t)fyBz * n];
+    fxn = +Fy[g.id(x - 1, y - 1, z) + (size_t)fyBz * n];
+    fyp = -Fx[g.id(x - 1, y, z) + (size_t)fxBz * n];
+    fyn = -Fx[g.id(x - 1, y - 1, z) + (size_t)fxBz * n];
+    emf[t + 2 * n] = 0.25 * (+fxp + fxn + fyp + fyn + sxp + sxn + syp + syn);
+  });
+}
+
+// src/mhd/magnetic_update.cu:21-81 Update_Magnetic_Field_3D
+void orc_update_magnetic(const orc_config *c, const double *src, double *dst, const double *emf, double dt)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  double const dtodx = dt / c->dx, dtody = dt / c->dy, dtodz = dt / c->dz;
+  par_cells(g, [&](size_t t) {
+    int x, y, z;
+    g.xyz(t, x, y, z);
+    if (!(x > 0 and y > 0 and z > 0 and x < g.nx - 1 and y < g.ny - 1 and z < g.nz - 1)) return;
+    double const ex1 = emf[g.id(x, y + 1, z) + 0 * n], ex2 = emf[g.id(x, y, z + 1) + 0 * n],
+                 ex3 = emf[g.id(x, y + 1, z + 1) + 0 * n];
+    double const ey1 = emf[g.id(x + 1, y, z) + 1 * n], ey2 = emf[g.id(x, y, z + 1) + 1 * n],
+                 ey3 = emf[g.id(x + 1, y, z + 1) + 1 * n];
+    double const ez1 = emf[g.id(x + 1, y, z) + 2 * n], ez2 = emf[g.id(x, y + 1, z) + 2 * n],
+                 ez3 = emf[g.id(x + 1, y + 1, z) + 2 * n];
+    size_t const bx = t + (size_t)g.fB * n, by = t + (size_t)(g.fB + 1) * n, bz = t + (size_t)(g.fB + 2) * n;
+    dst[bx] = src[bx] + dtodz * (ey3 - ey1) + dtody * (ez1 - ez3);
+    dst[by] = src[by] + dtodx * (ez3 - ez2) + dtodz * (ex1 - ex3);
+    dst[bz] = src[bz] + dtody * (ex3 - ex2) + dtodx * (ey2 - ey3);
+  });
+}
+
+// src/integrators/VL_3D_cuda.cu:379-495 Update_Conserved_Variables_3D_half
+void orc_update_half(const orc_config *c, const double *U, double *Uh, const double *Fx, const double *Fy,
+                     const double *Fz, double dt)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  double const dtodx = dt / c->dx, dtody = dt / c->dy, dtodz = dt / c->dz;
+  double const gamma = g.gamma, floor = c->density_floor;
+  par_cells(g, [&](size_t id) {
+    int x, y, z;
+    g.xyz(id, x, y, z);
+    if (!(x > 0 && x < g.nx - 1 && y > 0 && y < g.ny - 1 && z > 0 && z < g.nz - 1)) return;
+    size_t const imo = g.id(x - 1, y, z), jmo = g.id(x, y - 1, z), kmo = g.id(x, y, z - 1);
+    double P = 0, vx_imo = 0, vx_ipo = 0, vy_jmo = 0, vy_jpo = 0, vz_kmo = 0, vz_kpo = 0;
+    if (g.de) {
+      double const d = U[id], d_inv = 1.0 / d;
+      double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+      double const E = U[4 * n + id], GE = U[(size_t)g.fGE * n + id];
+      double E_kin   = 0.5 * d * sqmag(vx, vy, vz);
+      if (g.mhd) {
+        double bx, by, bz;
+        cc_b(g, U, x, y, z, bx, by, bz);
+        E_kin += magE(bx, by, bz);
+      }
+      P = pressure_from_de(E, E - E_kin, GE, gamma);
+      P = fmax(P, TINY);
+      size_t const ipo = g.id(x + 1, y, z), jpo = g.id(x, y + 1, z), kpo = g.id(x, y, z + 1);
+      vx_imo = U[n + imo] / U[imo];
+      vx_ipo = U[n + ipo] / U[ipo];
+      vy_jmo = U[2 * n + jmo] / U[jmo];
+      vy_jpo = U[2 * n + jpo] / U[jpo];
+      vz_kmo = U[3 * n + kmo] / U[kmo];
+      vz_kpo = U[3 * n + kpo] / U[kpo];
+    }
+    auto upd = [&](int f) {
+      size_t const o = (size_t)f * n;
+      return U[o + id] + dtodx * (Fx[o + imo] - Fx[o + id]) + dtody * (Fy[o + jmo] - Fy[o + id]) +
+             dtodz * (Fz[o + kmo] - Fz[o + id]);
+    };
+    for (int f = 0; f < 5; f++) Uh[(size_t)f * n + id] = upd(f);
+    for (int s = 0; s < g.ns; s++) Uh[(size_t)(5 + s) * n + id] = upd(5 + s);
+    if (g.de) {
+      size_t const o = (size_t)g.fGE * n;
+      Uh[o + id] = U[o + id] + dtodx * (Fx[o + imo] - Fx[o + id]) + dtody * (Fy[o + jmo] - Fy[o + id]) +
+                   dtodz * (Fz[o + kmo] - Fz[o + id]) +
+                   0.5 * P * (dtodx * (vx_imo - vx_ipo) + dtody * (vy_jmo - vy_jpo) + dtodz * (vz_kmo - vz_kpo));
+    }
+    if (c->density_floor_on) {
+      if (Uh[id] < floor) {
+        double const dens_0 = Uh[id];
+        Uh[id]              = floor;
+        Uh[1 * n + id] *= (floor / dens_0);
+        Uh[2 * n + id] *= (floor / dens_0);
+        Uh[3 * n + id] *= (floor / dens_0);
+        Uh[4 * n + id] *= (floor / dens_0);
+        if (g.de) Uh[(size_t)g.fGE * n + id] *= (floor / dens_0);
+      }
+    }
+  });
+}
+
+// src/hydro/hydro_cuda.cu:754-833 Partial_Update_Advected_Internal_Energy_3D (and :705-752 for 1D)
+void orc_de_partial_update(const orc_config *c, double *U, double dt)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int const ng   = g.ng;
+  double const dtodx = dt / c->dx, dtody = dt / c->dy, dtodz = dt / c->dz;
+  bool const one_d = g.ny == 1 && g.nz == 1;
+  par_cells(g, [&](size_t id) {
+    int x, y, z;
+    g.xyz(id, x, y, z);
+    if (one_d) {
+      if (!(x > ng - 1 && x < g.nx - ng)) return;
+      double const d = U[id], d_inv = 1.0 / d;
+      double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+      double const E = U[4 * n + id], GE = U[(size_t)g.fGE * n + id];
+      double const E_kin = 0.5 * d * (vx * vx + vy * vy + vz * vz);
+      double P           = pressure_from_de(E, E - E_kin, GE, g.gamma);
+      P                  = fmax(P, TINY);
+      double const vx_imo = U[n + id - 1] / U[id - 1], vx_ipo = U[n + id + 1] / U[id + 1];
+      U[(size_t)g.fGE * n + id] += 0.5 * P * (dtodx * (vx_imo - vx_ipo));
+      return;
+    }
+    if (!(x > ng - 1 && x < g.nx - ng && y > ng - 1 && y < g.ny - ng && z > ng - 1 && z < g.nz - ng)) return;
+    double const d = U[id], d_inv = 1.0 / d;
+    double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+    double const E = U[4 * n + id], GE = U[(size_t)g.fGE * n + id];
+    double E_kin   = 0.5 * d * sqmag(vx, vy, vz);
+    if (g.mhd) {
+      double bx, by, bz;
+      cc_b(g, U, x, y, z, bx, by, bz);
+      E_kin += magE(bx, by, bz);
+    }
+    double P = pressure_from_de(E, E - E_kin, GE, g.gamma);
+    P        = fmax(P, TINY);
+    size_t const imo = g.id(x - 1, y, z), jmo = g.id(x, y - 1, z), kmo = g.id(x, y, z - 1);
+    size_t const ipo = g.id(x + 1, y, z), jpo = g.id(x, y + 1, z), kpo = g.id(x, y, z + 1);
+    double const vx_imo = U[n + imo] / U[imo], vx_ipo = U[n + ipo] / U[ipo];
+    double const vy_jmo = U[2 * n + jmo] / U[jmo], vy_jpo = U[2 * n + jpo] / U[jpo];
+    double const vz_kmo = U[3 * n + kmo] / U[kmo], vz_kpo = U[3 * n + kpo] / U[kpo];
+    U[(size_t)g.fGE * n + id] +=
+        0.5 * P * (dtodx * (vx_imo - vx_ipo) + dtody * (vy_jmo - vy_jpo) + dtodz * (vz_kmo - vz_kpo));
+  });
+}
+
+// src/hydro/hydro_cuda.cu:172-402 Update_Conserved_Variables_3D (DENSITY_FLOOR and TEMPERATURE_FLOOR on)
+void orc_update_full(const orc_config *c, double *U, const double *Fx, const double *Fy, const double *Fz, double dt)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int const ng   = g.ng;
+  double const dtodx = dt / c->dx, dtody = dt / c->dy, dtodz = dt / c->dz;
+  double const floor = c->density_floor;
+  std::vector<unsigned char> negative(c->density_floor_on ? g.n : 0, 0);
+  par_cells(g, [&](size_t id) {
+    int x, y, z;
+    g.xyz(id, x, y, z);
+    if (!(x > ng - 1 && x < g.nx - ng && y > ng - 1 && y < g.ny - ng && z > ng - 1 && z < g.nz - ng)) return;
+    size_t const imo = g.id(x - 1, y, z), jmo = g.id(x, y - 1, z), kmo = g.id(x, y, z - 1);
+    auto upd = [&](int f) {
+      size_t const o = (size_t)f * n;
+      U[o + id] += dtodx * (Fx[o + imo] - Fx[o + id]) + dtody * (Fy[o + jmo] - Fy[o + id]) +
+                   dtodz * (Fz[o + kmo] - Fz[o + id]);
+    };
+    for (int f = 0; f < 5; f++) upd(f);
+    for (int s = 0; s < g.ns; s++) upd(5 + s);
+    if (g.de) upd(g.fGE);
+    if (c->density_floor_on) {
+      if (U[id] < floor) {
+        if (U[id] > 0) {
+          double const dens_0 = U[id];
+          U[id]               = floor;
+          U[1 * n + id] *= (floor / dens_0);
+          U[2 * n + id] *= (floor / dens_0);
+          U[3 * n + id] *= (floor / dens_0);
+          U[4 * n + id] *= (floor / dens_0);
+          if (g.de) U[(size_t)g.fGE * n + id] *= (floor / dens_0);
+        } else {
+          negative[id] = 1;
+        }
+      }
+    }
+  });
+  // hydro_cuda.cu:1155-1177 Average_Cell_Single_Field(density).  The reference averages the six
+  // neighbours while they are being updated by other threads; here the average is taken over the
+  // updated neighbours, after the whole update, which is the outcome once every thread has finished.
+  if (c->density_floor_on) {
+    for (size_t id = 0; id < g.n; id++) {
+      if (!negative[id]) continue;
+      int x, y, z;
+      g.xyz(id, x, y, z);
+      double const v = (U[g.id(x - 1, y, z)] + U[g.id(x + 1, y, z)] + U[g.id(x, y - 1, z)] + U[g.id(x, y + 1, z)] +
+                        U[g.id(x, y, z - 1)] + U[g.id(x, y, z + 1)]) /
+                       6;
+      U[id] = v;
+    }
+  }
+}
+
+// src/hydro/hydro_cuda.cu:20-82 Update_Conserved_Variables_1D
+static void update_full_1d(const Grid &g, double *U, const double *F, double dx, double dt)
+{
+  size_t const n     = g.n;
+  double const dtodx = dt / dx;
+  for (size_t id = g.ng; id < n - g.ng; id++) {
+    for (int f = 0; f < 5; f++) U[(size_t)f * n + id] += dtodx * (F[(size_t)f * n + id - 1] - F[(size_t)f * n + id]);
+    for (int s = 0; s < g.ns; s++)
+      U[(size_t)(5 + s) * n + id] += dtodx * (F[(size_t)(5 + s) * n + id - 1] - F[(size_t)(5 + s) * n + id]);
+    if (g.de) U[(size_t)g.fGE * n + id] += dtodx * (F[(size_t)g.fGE * n + id - 1] - F[(size_t)g.fGE * n + id]);
+  }
+}
+
+// src/hydro/hydro_cuda.cu:949-1016 Select_Internal_Energy_3D (and :835-885 for 1D)
+void orc_de_select(const orc_config *c, double *U)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int const ng   = g.ng;
+  bool const one_d = g.ny == 1 && g.nz == 1;
+  // every read is of E or of the cell's own fields, and only GasEnergy is written
+  par_cells(g, [&](size_t id) {
+    int x, y, z;
+    g.xyz(id, x, y, z);
+    double Emax;
+    double const d = U[id], d_inv = 1.0 / d;
+    if (one_d) {
+      if (!(x > ng - 1 && x < g.nx - ng)) return;
+      int const imo = std::max(x - 1, ng), ipo = std::min(x + 1, g.nx - ng - 1);
+      double const E = U[4 * n + id];
+      Emax           = fmax(U[4 * n + imo], E);
+      Emax           = fmax(Emax, U[4 * n + ipo]);
+    } else {
+      if (!(x > ng - 1 && x < g.nx - ng && y > ng - 1 && y < g.ny - ng && z > ng - 1 && z < g.nz - ng)) return;
+      size_t const imo = g.id(std::max(x - 1, ng), y, z), ipo = g.id(std::min(x + 1, g.nx - ng - 1), y, z);
+      size_t const jmo = g.id(x, std::max(y - 1, ng), z), jpo = g.id(x, std::min(y + 1, g.ny - ng - 1), z);
+      size_t const kmo = g.id(x, y, std::max(z - 1, ng)), kpo = g.id(x, y, std::min(z + 1, g.nz - ng - 1));
+      double const E = U[4 * n + id];
+      Emax           = fmax(U[4 * n + imo], E);
+      Emax           = fmax(Emax, U[4 * n + ipo]);
+      Emax           = fmax(Emax, U[4 * n + jmo]);
+      Emax           = fmax(Emax, U[4 * n + jpo]);
+      Emax           = fmax(Emax, U[4 * n + kmo]);
+      Emax           = fmax(Emax, U[4 * n + kpo]);
+    }
+    double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+    double const E          = U[4 * n + id];
+    double const U_advected = U[(size_t)g.fGE * n + id];
+    double const U_total    = E - 0.5 * d * (vx * vx + vy * vy + vz * vz);
+    double Ui;
+    if ((U_total / E > ETA_1) or (U_total / Emax > ETA_2)) {
+      Ui = U_total;
+    } else {
+      Ui = U_advected;
+    }
+    Ui                        = fmax(Ui, TINY);
+    U[(size_t)g.fGE * n + id] = Ui;
+  });
+}
+
+// src/hydro/hydro_cuda.cu:1070-1099 Sync_Energies_3D (and :1018-1041 for 1D)
+void orc_de_sync(const orc_config *c, double *U)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int const ng   = g.ng;
+  bool const one_d = g.ny == 1 && g.nz == 1;
+  par_cells(g, [&](size_t id) {
+    int x, y, z;
+    g.xyz(id, x, y, z);
+    if (one_d) {
+      if (!(x > ng - 1 && x < g.nx - ng)) return;
+    } else if (!(x > ng - 1 && x < g.nx - ng && y > ng - 1 && y < g.ny - ng && z > ng - 1 && z < g.nz - ng)) {
+      return;
+    }
+    double const d = U[id], d_inv = 1.0 / d;
+    double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+    double const Ui = U[(size_t)g.fGE * n + id];
+    U[4 * n + id]   = 0.5 * d * (vx * vx + vy * vy + vz * vz) + Ui;
+  });
+}
+
+// src/hydro/hydro_cuda.cu:1117-1153 Temperature_Floor_Kernel
+void orc_temperature_floor(const orc_config *c, double *U, double U_floor)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int const ng   = g.ng;
+  par_cells(g, [&](size_t id) {
+    int x, y, z;
+    g.xyz(id, x, y, z);
+    if (!(x > ng - 1 && x < g.nx - ng && y > ng - 1 && y < g.ny - ng && z > ng - 1 && z < g.nz - ng)) return;
+    double const d = U[id], d_inv = 1.0 / d;
+    double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+    double const E = U[4 * n + id];
+    double const Ekin = 0.5 * d * (vx * vx + vy * vy + vz * vz);
+    double Ui = (E - Ekin) / d;
+    if (Ui < U_floor) U[4 * n + id] = Ekin + d * U_floor;
+    if (g.de) {
+      Ui = U[(size_t)g.fGE * n + id] / d;
+      if (Ui < U_floor) U[(size_t)g.fGE * n + id] = d * U_floor;
+    }
+  });
+}
+
+// src/hydro/hydro_cuda.cu:404-435, 437-471, 514-560: Calc_dt_{1D,3D}; returns max inverse time step
+double orc_calc_dt(const orc_config *c, const double *U)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int const ng   = g.ng;
+  double const gamma = g.gamma, dx = c->dx, dy = c->dy, dz = c->dz;
+  bool const one_d = g.ny == 1 && g.nz == 1;
+  double result = -DBL_MAX;
+  long long const N = (long long)n;
+#pragma omp parallel for reduction(max : result) num_threads(g_threads > 0 ? g_threads : omp_get_max_threads())
+  for (long long ii = 0; ii < N; ii++) {
+    size_t const id = (size_t)ii;
+    int x, y, z;
+    g.xyz(id, x, y, z);
+    double m = -DBL_MAX;
+    if (one_d) {
+      if (!(id > (size_t)ng - 1 && id < n - ng)) continue;
+      double const d = U[id], d_inv = 1.0 / d;
+      double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+      double P = (U[4 * n + id] - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (gamma - 1.0);
+      P        = fmax(P, TINY);
+      double const cs = sqrt(d_inv * gamma * P);
+      m               = fmax(m, (fabs(vx) + cs) / dx);
+    } else {
+      if (!(x > ng - 1 && x < g.nx - ng && y > ng - 1 && y < g.ny - ng && z > ng - 1 && z < g.nz - ng)) continue;
+      double const d = U[id], d_inv = 1.0 / d;
+      double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+      double const E = U[4 * n + id];
+      double cm;
+      if (g.mhd) {
+        double bx, by, bz;
+        cc_b(g, U, x, y, z, bx, by, bz);
+        double pressure = E - 0.5 * d * sqmag(vx, vy, vz);
+        pressure -= magE(bx, by, bz);
+        double const gasP = fmax((gamma - 1.) * pressure, TINY);
+        double const cf   = cfast(d, gasP, bx, by, bz, gamma);
+        cm = fmax((fabs(vx) + cf) / dx, (fabs(vy) + cf) / dy);
+        cm = fmax(cm, (fabs(vz) + cf) / dz);
+        cm = fmax(cm, 0.0);
+      } else {
+        double const P  = (E - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (gamma - 1.0);
+        double const cs = sqrt(d_inv * gamma * P);
+        cm = fmax((fabs(vx) + cs) / dx, (fabs(vy) + cs) / dy);
+        cm = fmax(cm, (fabs(vz) + cs) / dz);
+        cm = fmax(cm, 0.0);
+      }
+      m = fmax(m, cm);
+    }
+    result = fmax(result, m);
+  }
+  return result;
+}
+
+// src/mhd/magnetic_divergence.cu:33-76 calculateMagneticDivergence: max |div B| over real cells
+double orc_max_divB(const orc_config *c, const double *U)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int const ng   = g.ng;
+  double const dx = c->dx, dy = c->dy, dz = c->dz;
+  double result = 0.0;
+  for (int z = ng; z < g.nz - ng; z++)
+    for (int y = ng; y < g.ny - ng; y++)
+      for (int x = ng; x < g.nx - ng; x++) {
+        size_t const id = g.id(x, y, z);
+        double const div =
+            fabs((U[(size_t)g.fB * n + id] - U[(size_t)g.fB * n + g.id(x - 1, y, z)]) / dx +
+                 (U[(size_t)(g.fB + 1) * n + id] - U[(size_t)(g.fB + 1) * n + g.id(x, y - 1, z)]) / dy +
+                 (U[(size_t)(g.fB + 2) * n + id] - U[(size_t)(g.fB + 2) * n + g.id(x, y, z - 1)]) / dz);
+        result = fmax(result, div);
+      }
+  return result;
+}
+
+// src/grid/cuda_boundaries.cu:71-300 SetGhostCellsKernel / SetBoundaryMapping / FindIndex and
+// src/grid/boundary_conditions.cpp:54-131, 412-500 (the six faces, in order, with their extents)
+namespace
+{
+int find_index(int ig, int nx, int flag, int face, int ng, double *a)
+{
+  if (face == 0) {
+    switch (flag) {
+      case 1: return ig + nx - 2 * ng;
+      case 2: *a = -1.0; return 2 * ng - ig - 1;
+      case 3: return ng;
+      case 4: return -1;
+      case 5: return ig;
+      default: return ig + nx - 2 * ng;
+    }
+  } else {
+    switch (flag) {
+      case 1: return ig - nx + 2 * ng;
+      case 2: *a = -1.0; return 2 * (nx - ng) - ig - 1;
+      case 3: return nx - ng - 1;
+      case 4: return -1;
+      case 5: return ig;
+      default: return ig - nx + 2 * ng;
+    }
+  }
+}
+long long boundary_mapping(int ig, int jg, int kg, double *a, const int *flags, int nx, int ny, int nz, int ng)
+{
+  long long idx = 0;
+  int ir = 0, jr = 0, kr = 0;
+  if (nx > 1) {
+    if (ig < ng) {
+      ir = find_index(ig, nx, flags[0], 0, ng, &a[0]);
+    } else if (ig >= nx - ng) {
+      ir = find_index(ig, nx, flags[1], 1, ng, &a[0]);
+    } else {
+      ir = ig;
+    }
+    if (ir < 0) return -1;
+    idx += ir;
+  }
+  if (ny > 1) {
+    if (jg < ng) {
+      jr = find_index(jg, ny, flags[2], 0, ng, &a[1]);
+    } else if (jg >= ny - ng) {
+      jr = find_index(jg, ny, flags[3], 1, ng, &a[1]);
+    } else {
+      jr = jg;
+    }
+    if (jr < 0) return -1;
+    idx += (long long)nx * jr;
+  }
+  if (nz > 1) {
+    if (kg < ng) {
+      kr = find_index(kg, nz, flags[4], 0, ng, &a[2]);
+    } else if (kg >= nz - ng) {
+      kr = find_index(kg, nz, flags[5], 1, ng, &a[2]);
+    } else {
+      kr = kg;
+    }
+    if (kr < 0) return -1;
+    idx += (long long)nx * ny * kr;
+  }
+  return idx;
+}
+}  // namespace
+
+void orc_set_boundaries(const orc_config *c, double *U, const int flags_in[6])
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int const ng   = g.ng;
+  int flags[6]   = {0, 0, 0, 0, 0, 0};
+  if (g.nx > 1) flags[0] = flags_in[0], flags[1] = flags_in[1];
+  if (g.ny > 1) flags[2] = flags_in[2], flags[3] = flags_in[3];
+  if (g.nz > 1) flags[4] = flags_in[4], flags[5] = flags_in[5];
+  for (int dir = 0; dir < 6; dir++) {
+    if ((dir < 2 && g.nx <= 1) || (dir >= 2 && dir < 4 && g.ny <= 1) || (dir >= 4 && g.nz <= 1)) continue;
+    if (flags[dir] == 4 || flags[dir] == 5) continue;
+    // boundary_conditions.cpp Set_Boundary_Extents
+    int imin[3], imax[3];
+    int jl = 0, ju = g.ny, kl = 0, ku = g.nz;
+    if (g.ny > 1) jl = ng, ju = g.ny - ng;
+    if (g.nz > 1) kl = ng, ku = g.nz - ng;
+    if (dir == 0) imin[0] = 0, imax[0] = ng, imin[1] = jl, imax[1] = ju, imin[2] = kl, imax[2] = ku;
+    if (dir == 1) imin[0] = g.nx - ng, imax[0] = g.nx, imin[1] = jl, imax[1] = ju, imin[2] = kl, imax[2] = ku;
+    if (dir == 2) imin[0] = 0, imax[0] = g.nx, imin[1] = 0, imax[1] = ng, imin[2] = kl, imax[2] = ku;
+    if (dir == 3) imin[0] = 0, imax[0] = g.nx, imin[1] = g.ny - ng, imax[1] = g.ny, imin[2] = kl, imax[2] = ku;
+    if (dir == 4) imin[0] = 0, imax[0] = g.nx, imin[1] = 0, imax[1] = g.ny, imin[2] = 0, imax[2] = ng;
+    if (dir == 5) imin[0] = 0, imax[0] = g.nx, imin[1] = 0, imax[1] = g.ny, imin[2] = g.nz - ng, imax[2] = g.nz;
+    for (int k = imin[2]; k < imax[2]; k++)
+      for (int j = imin[1]; j < imax[1]; j++)
+        for (int i = imin[0]; i < imax[0]; i++) {
+          size_t const gidx = g.id(i, j, k);
+          double a[3]       = {1., 1., 1.};
+          long long const idx = boundary_mapping(i, j, k, a, flags, g.nx, g.ny, g.nz, ng);
+          if (idx < 0) continue;
+          for (int f = 0; f < g.nf; f++) U[gidx + (size_t)f * n] = U[(size_t)idx + (size_t)f * n];
+          if (flags[0] == 2 || flags[1] == 2) U[gidx + n] *= a[0];
+          if (flags[2] == 2 || flags[3] == 2) U[gidx + 2 * n] *= a[1];
+          if (flags[4] == 2 || flags[5] == 2) U[gidx + 3 * n] *= a[2];
+          if (!g.mhd && flags[dir] == 3) {
+            size_t const momdex = gidx + (size_t)(dir / 2 + 1) * n;
+            if (dir % 2 == 0) {
+              if (U[momdex] > 0.0) {
+                U[gidx + 4 * n] -= 0.5 * (U[momdex] * U[momdex]) / U[gidx];
+                U[momdex] = 0.0;
+              }
+            } else {
+              if (U[momdex] < 0.0) {
+                U[gidx + 4 * n] -= 0.5 * (U[momdex] * U[momdex]) / U[gidx];
+                U[momdex] = 0.0;
+              }
+            }
+          }
+        }
+  }
+}
+
+// src/integrators/VL_3D_cuda.cu:38-360 VL_Algorithm_3D_CUDA
+int orc_vl_step_3d(const orc_config *c, double *U, double dt)
+{
+  Grid g(c);
+  if (g.mhd && g.de) return -1;  // the reference's MHD+DE flux indexing is out of bounds
+  if (g.mhd && c->solver != ORC_HLLD) return -1;
+  if (!g.mhd && c->solver == ORC_HLLD) return -1;
+  if (g.ns > MAXS) return -1;
+  size_t const n = g.n;
+  std::vector<double> Uh((size_t)g.nf * n, 0.0);
+  std::vector<double> QLx((size_t)g.nf * n, 0.0), QRx((size_t)g.nf * n, 0.0), QLy((size_t)g.nf * n, 0.0),
+      QRy((size_t)g.nf * n, 0.0), QLz((size_t)g.nf * n, 0.0), QRz((size_t)g.nf * n, 0.0);
+  std::vector<double> Fx((size_t)g.nf * n, 0.0), Fy((size_t)g.nf * n, 0.0), Fz((size_t)g.nf * n, 0.0);
+  std::vector<double> emf(g.mhd ? 3 * n : 0, 0.0);
+  auto riemann = [&](const double *Ub) {
+    if (c->solver == ORC_HLLC) {
+      orc_hllc(c, QLx.data(), QRx.data(), Fx.data(), 0);
+      orc_hllc(c, QLy.data(), QRy.data(), Fy.data(), 1);
+      orc_hllc(c, QLz.data(), QRz.data(), Fz.data(), 2);
+    } else if (c->solver == ORC_ROE) {
+      orc_roe(c, QLx.data(), QRx.data(), Fx.data(), 0);
+      orc_roe(c, QLy.data(), QRy.data(), Fy.data(), 1);
+      orc_roe(c, QLz.data(), QRz.data(), Fz.data(), 2);
+    } else {
+      orc_hlld(c, QLx.data(), QRx.data(), Ub + (size_t)g.fB * n, Fx.data(), 0);
+      orc_hlld(c, QLy.data(), QRy.data(), Ub + (size_t)(g.fB + 1) * n, Fy.data(), 1);
+      orc_hlld(c, QLz.data(), QRz.data(), Ub + (size_t)(g.fB + 2) * n, Fz.data(), 2);
+    }
+  };
+  // predictor
+  orc_pcm_3d(c, U, QLx.data(), QRx.data(), QLy.data(), QRy.data(), QLz.data(), QRz.data());
+  riemann(U);
+  if (g.mhd) orc_ct_electric_fields(c, Fx.data(), Fy.data(), Fz.data(), U, emf.data());
+  orc_update_half(c, U, Uh.data(), Fx.data(), Fy.data(), Fz.data(), 0.5 * dt);
+  if (g.mhd) orc_update_magnetic(c, U, Uh.data(), emf.data(), 0.5 * dt);
+  // corrector
+  if (c->recon == ORC_PCM) {
+    orc_pcm_3d(c, Uh.data(), QLx.data(), QRx.data(), QLy.data(), QRy.data(), QLz.data(), QRz.data());
+  } else if (c->recon == ORC_PLMC) {
+    orc_plmc(c, Uh.data(), QLx.data(), QRx.data(), 0);
+    orc_plmc(c, Uh.data(), QLy.data(), QRy.data(), 1);
+    orc_plmc(c, Uh.data(), QLz.data(), QRz.data(), 2);
+  } else {
+    orc_ppmc_vl(c, Uh.data(), QLx.data(), QRx.data(), 0);
+    orc_ppmc_vl(c, Uh.data(), QLy.data(), QRy.data(), 1);
+    orc_ppmc_vl(c, Uh.data(), QLz.data(), QRz.data(), 2);
+  }
+  riemann(Uh.data());
+  if (g.de) orc_de_partial_update(c, U, dt);
+  if (g.mhd) orc_ct_electric_fields(c, Fx.data(), Fy.data(), Fz.data(), Uh.data(), emf.data());
+  orc_update_full(c, U, Fx.data(), Fy.data(), Fz.data(), dt);
+  if (g.mhd) orc_update_magnetic(c, U, U, emf.data(), dt);
+  if (g.de) {
+    orc_de_select(c, U);
+    orc_de_sync(c, U);
+  }
+  return 0;
+}
+
+// src/integrators/VL_1D_cuda.cu:30-146 VL_Algorithm_1D_CUDA and :158-215 Update_Conserved_Variables_1D_half
+int orc_vl_step_1d(const orc_config *c, double *U, double dt)
+{
+  Grid g(c);
+  if (g.mhd || g.ny != 1 || g.nz != 1 || c->solver == ORC_HLLD) return -1;
+  size_t const n = g.n;
+  std::vector<double> Uh((size_t)g.nf * n, 0.0), QL((size_t)g.nf * n, 0.0), QR((size_t)g.nf * n, 0.0),
+      F((size_t)g.nf * n, 0.0);
+  auto pcm1 = [&](const double *Ub) {  // pcm_cuda.cu:13-121 PCM_Reconstruction_1D
+    for (size_t x = 0; x + 1 < n; x++)
+      for (int f = 0; f < g.nf; f++) {
+        QL[(size_t)f * n + x] = Ub[(size_t)f * n + x];
+        QR[(size_t)f * n + x] = Ub[(size_t)f * n + x + 1];
+      }
+  };
+  auto riemann = [&]() {
+    if (c->solver == ORC_ROE) {
+      orc_roe(c, QL.data(), QR.data(), F.data(), 0);
+    } else {
+      orc_hllc(c, QL.data(), QR.data(), F.data(), 0);
+    }
+  };
+  pcm1(U);
+  riemann();
+  {
+    double const dtodx = (0.5 * dt) / c->dx;
+    for (size_t id = 1; id + 1 < n; id++) {
+      size_t const imo = id - 1;
+      double P = 0, vx_imo = 0, vx_ipo = 0;
+      if (g.de) {
+        double const d = U[id], d_inv = 1.0 / d;
+        double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+        P      = (U[4 * n + id] - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (g.gamma - 1.0);
+        vx_imo = U[n + imo] / U[imo];
+        vx_ipo = U[n + id + 1] / U[id + 1];
+      }
+      for (int f = 0; f < 5 + g.ns; f++)
+        Uh[(size_t)f * n + id] = U[(size_t)f * n + id] + dtodx * (F[(size_t)f * n + imo] - F[(size_t)f * n + id]);
+      if (g.de) {
+        size_t const o = (size_t)g.fGE * n;
+        Uh[o + id]     = U[o + id] + dtodx * (F[o + imo] - F[o + id]) + 0.5 * P * (dtodx * (vx_imo - vx_ipo));
+      }
+    }
+  }
+  if (c->recon == ORC_PCM) {
+    pcm1(Uh.data());
+  } else if (c->recon == ORC_PLMC) {
+    orc_plmc(c, Uh.data(), QL.data(), QR.data(), 0);
+  } else {
+    orc_ppmc_vl(c, Uh.data(), QL.data(), QR.data(), 0);
+  }
+  riemann();
+  if (g.de) orc_de_partial_update(c, U, dt);
+  update_full_1d(g, U, F.data(), c->dx, dt);
+  if (g.de) {
+    orc_de_select(c, U);
+    orc_de_sync(c, U);
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,83 @@
+/*
+ * cholla_oracle.h -- FP64 CPU restatement of Cholla's single-GPU VL hydro/MHD step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity checker and the CPU
+ * baseline.  Nothing in the cholla_gb300 product links, loads or calls it; only
+ * tests/, __graft_entry__.smoke() and bench.py (cpu_baseline / --impl reference)
+ * may use it.
+ *
+ * Each function restates one kernel of the reference (cholla-hydro/cholla) over
+ * the full padded grid, in the reference's operation order, so that this code
+ * compiled with -ffp-contract=off reproduces the reference's -fmad=false build.
+ * The file:line of the reference kernel each function follows is given beside it.
+ *
+ * Layout (src/grid/grid_enum.h:18-111): field-major U[f*n_cells + i + j*nx + k*nx*ny],
+ * fields d, mx, my, mz, E, [scalars], [Bx, By, Bz], [GasEnergy (last)].
+ */
+#pragma once
+#include <cstddef>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_PCM = 0, ORC_PLMC = 1, ORC_PPMC = 2 };
+enum { ORC_HLLC = 0, ORC_ROE = 1, ORC_HLLD = 2 };
+
+typedef struct {
+  int nx, ny, nz;     /* padded sizes (ghosts included) */
+  int n_ghost;
+  int n_fields;
+  int n_scalars;
+  int de;             /* dual energy on */
+  int mhd;            /* MHD (face-centred B, CT) */
+  int recon;          /* ORC_PCM / ORC_PLMC / ORC_PPMC */
+  int solver;         /* ORC_HLLC / ORC_ROE / ORC_HLLD */
+  int density_floor_on;
+  double gamma;
+  double dx, dy, dz;
+  double density_floor;
+} orc_config;
+
+/* ---- kernel-level restatements (write into caller-owned full-grid arrays) ---- */
+void orc_pcm_3d(const orc_config *c, const double *U, double *QLx, double *QRx, double *QLy, double *QRy,
+                double *QLz, double *QRz);
+void orc_ppmc_vl(const orc_config *c, const double *U, double *QL, double *QR, int dir);
+void orc_plmc(const orc_config *c, const double *U, double *QL, double *QR, int dir);
+void orc_hllc(const orc_config *c, const double *QL, const double *QR, double *F, int dir);
+void orc_roe(const orc_config *c, const double *QL, const double *QR, double *F, int dir);
+void orc_hlld(const orc_config *c, const double *QL, const double *QR, const double *Bface, double *F, int dir);
+void orc_ct_electric_fields(const orc_config *c, const double *Fx, const double *Fy, const double *Fz,
+                            const double *U, double *emf);
+void orc_update_magnetic(const orc_config *c, const double *src, double *dst, const double *emf, double dt);
+void orc_update_half(const orc_config *c, const double *U, double *Uh, const double *Fx, const double *Fy,
+                     const double *Fz, double dt_half);
+void orc_de_partial_update(const orc_config *c, double *U, double dt);
+void orc_update_full(const orc_config *c, double *U, const double *Fx, const double *Fy, const double *Fz,
+                     double dt);
+void orc_de_select(const orc_config *c, double *U);
+void orc_de_sync(const orc_config *c, double *U);
+void orc_temperature_floor(const orc_config *c, double *U, double U_floor);
+double orc_calc_dt(const orc_config *c, const double *U);
+double orc_max_divB(const orc_config *c, const double *U);
+void orc_set_boundaries(const orc_config *c, double *U, const int flags[6]);
+
+/* PPM single-variable reconstruction (reconstruction.h:794-901) */
+void orc_ppm_single_variable(double im2, double im1, double i, double ip1, double ip2, double *L_iph,
+                             double *R_imh);
+
+/* ---- the step: VL_Algorithm_3D_CUDA / VL_Algorithm_1D_CUDA ---- */
+int orc_vl_step_3d(const orc_config *c, double *U, double dt);
+int orc_vl_step_1d(const orc_config *c, double *U, double dt);
+
+/* std::mt19937_64(seed) + std::uniform_real_distribution<double>(a, b), n draws: the input
+ * generator of the reference's unit tests (e.g. src/reconstruction/ppmc_cuda_tests.cu:131-132) */
+void orc_mt19937_uniform(unsigned long long seed, double a, double b, size_t n, double *out);
+
+/* threads used by the OpenMP loops (0 = library default) */
+void orc_set_threads(int n);
+int orc_get_threads(void);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,134 @@
+"""Extract the golden vectors of the reference's unit tests into reference_fiducials.json.
+
+Run in a container where the reference source tree is mounted (default /root/reference):
+
+    python tests/golden/extract_reference_fiducials.py [/path/to/cholla]
+
+Only numbers are taken from the reference's test files (fiducial outputs and the literal
+inputs of the small known-answer tests); the inputs of the randomised tests are regenerated
+by the oracle's std::mt19937_64 helper with the seed and ranges recorded here.
+"""
+from __future__ import annotations
+
+import json
+import re
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+
+
+def braces_to_json(text: str):
+    t = re.sub(r"//[^\n]*", "", text)
+    t = t.replace("{", "[").replace("}", "]")
+    t = re.sub(r",\s*]", "]", t)
+    return json.loads(t)
+
+
+def initializer(src: str, name: str, start: int = 0) -> tuple[object, int]:
+    """JSON value of `<type> name = {...};` (or `name{...};`) found at or after `start`."""
+    m = re.compile(re.escape(name) + r"\s*(=\s*)?\{").search(src, start)
+    if not m:
+        raise KeyError(name)
+    i = src.index("{", m.start())
+    depth = 0
+    for j in range(i, len(src)):
+        if src[j] == "{":
+            depth += 1
+        elif src[j] == "}":
+            depth -= 1
+            if depth == 0:
+                return braces_to_json(src[i:j + 1]), j
+    raise ValueError(name)
+
+
+def split_mhd(block: str) -> tuple[str, str]:
+    """(MHD branch, hydro branch) of an `#ifdef MHD ... #else ... #endif` region."""
+    m = re.search(r"#ifdef MHD(.*?)#else[^\n]*\n(.*?)#endif", block, re.S)
+    return m.group(1), m.group(2)
+
+
+def maps(lst) -> list[dict]:
+    return [{str(int(k)): float(v) for k, v in d} for d in lst]
+
+
+def ppmc_vl(src_dir: Path) -> dict:
+    s = (src_dir / "reconstruction/ppmc_cuda_tests.cu").read_text()
+    t0 = s.index("TEST(tALLPpmcVLReconstructor")
+    body = s[t0:s.index("// Loop over different directions", t0)]
+    mhd, hydro = split_mhd(body[body.index("// Fiducial Data"):])
+    out = {}
+    for tag, b in (("mhd", mhd), ("hydro", hydro)):
+        left, _ = initializer(b, "fiducial_interface_left")
+        right, _ = initializer(b, "fiducial_interface_right")
+        out[tag] = {"left": maps(left), "right": maps(right)}
+    out["setup"] = {"seed": 42, "range": [0.1, 5.0], "nx": 6, "ny": 6, "nz": 6, "gamma": 5.0 / 3.0,
+                    "n_fields": {"hydro": 5, "mhd": 8}, "source": "src/reconstruction/ppmc_cuda_tests.cu:121-259"}
+    return out
+
+
+def plmc(src_dir: Path) -> dict:
+    s = (src_dir / "reconstruction/plmc_cuda_tests.cu").read_text()
+    out = {}
+    for test, tag in (("TEST(tHYDROPlmcReconstructor", "hydro"), ("TEST(tMHDPlmcReconstructor", "mhd")):
+        if test not in s:
+            continue
+        t0 = s.index(test)
+        left, j = initializer(s, "fiducial_interface_left", t0)
+        right, _ = initializer(s, "fiducial_interface_right", j)
+        head = s[t0:s.index("fiducial_interface_left", t0)]
+        dims = {}
+        for k in ("nx", "ny", "nz", "n_fields"):
+            m = re.search(rf"\b{k}\s*=\s*(\w+)", head)
+            v = m.group(1)
+            dims[k] = int(v) if v.isdigit() else dims[v]
+        out[tag] = {"left": maps(left), "right": maps(right), **dims}
+    out["setup"] = {"seed": 42, "range": [0.1, 5.0], "gamma": 5.0 / 3.0, "draws_before_grid": 2,
+                    "source": "src/reconstruction/plmc_cuda_tests.cu:26-293"}
+    return out
+
+
+def ppm_single_variable(src_dir: Path) -> dict:
+    s = (src_dir / "reconstruction/reconstruction_tests.cu").read_text()
+    t0 = s.index("TEST(tALLReconstructionPPMSingleVariable")
+    left, j = initializer(s, "fiducial_left_interface", t0)
+    right, _ = initializer(s, "fiducial_right_interface", j)
+    return {"seed": 42, "range": [-100.0, 100.0], "n_tests": 100, "left": left, "right": right,
+            "source": "src/reconstruction/reconstruction_tests.cu:501-572"}
+
+
+def dt_tests(src_dir: Path) -> dict:
+    s = (src_dir / "hydro/hydro_cuda_tests.cu").read_text()
+    t0 = s.index("TEST(tHYDROCalcDt3D")
+    blk = s[t0:s.index("TEST(", t0 + 10)]
+    vals = [float(v) for v in re.findall(r"host_conserved\.at\(\d\)\s*=\s*([-0-9.eE]+)", blk)]
+    calc = {"conserved": vals, "gamma": 5.0 / 3.0, "dx": 1.0, "dy": 1.0, "dz": 1.0,
+            "fiducial": float(re.search(r"fiducialDt\s*=\s*([-0-9.eE]+)", blk).group(1)),
+            "source": "src/hydro/hydro_cuda_tests.cu:29-82"}
+    t1 = s.index("TEST(tHYDROHydroInverseCrossingTime")
+    blk = s[t1:s.index("TEST(", t1 + 10)]
+    names = ["energy", "density", "velocityX", "velocityY", "velocityZ", "cellSizeX", "cellSizeY", "cellSizeZ"]
+    ict = {n: float(re.search(rf"double const {n}\s*=\s*([-0-9.eE]+)", blk).group(1)) for n in names}
+    ict["fiducial"] = float(re.search(r"fiducialInverseCrossingTime\s*=\s*([-0-9.eE]+)", blk).group(1))
+    ict["gamma"] = 5.0 / 3.0
+    ict["source"] = "src/hydro/hydro_cuda_tests.cu:89-110"
+    return {"calc_dt_3d": calc, "hydro_inverse_crossing_time": ict}
+
+
+def main() -> None:
+    root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    src = root / "src"
+    data = {
+        "note": "golden vectors read from the reference's unit tests by extract_reference_fiducials.py",
+        "ppmc_vl": ppmc_vl(src),
+        "plmc": plmc(src),
+        "ppm_single_variable": ppm_single_variable(src),
+        "dt": dt_tests(src),
+    }
+    out = HERE / "reference_fiducials.json"
+    out.write_text(json.dumps(data, indent=1))
+    print(f"wrote {out}")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,116 @@
+"""The oracle against the golden vectors of the reference's own unit tests (CPU only).
+
+Inputs are regenerated with std::mt19937_64(42) + uniform_real_distribution, exactly as the
+reference tests draw them; expected outputs come from tests/golden/reference_fiducials.json
+(extracted from the reference's test sources by tests/golden/extract_reference_fiducials.py).
+Comparison rule: |diff| <= 1e-14 or <= 4 ULP (testing_utilities::nearlyEqualDbl).
+"""
+import ctypes as C
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from helpers import nearly_equal
+
+GOLD = json.loads((Path(__file__).parent / "golden" / "reference_fiducials.json").read_text())
+
+
+def _check_interfaces(QL, QR, fid_left, fid_right, n_check):
+    for name, arr, fid in (("left", QL, fid_left), ("right", QR, fid_right)):
+        expect = np.zeros(n_check)
+        for k, v in fid.items():
+            expect[int(k)] = v
+        got = arr[:n_check]
+        ok = nearly_equal(expect, got)
+        bad = np.nonzero(~ok)[0]
+        assert ok.all(), f"{name} interface mismatch at {bad[:10]}: expect {expect[bad[:5]]} got {got[bad[:5]]}"
+
+
+@pytest.mark.parametrize("kind", ["hydro", "mhd"])
+def test_ppmc_vl_reference_fiducials(oracle_lib, kind):
+    o = oracle_lib
+    g = GOLD["ppmc_vl"]
+    st = g["setup"]
+    nx, ny, nz = st["nx"], st["ny"], st["nz"]
+    nf = st["n_fields"][kind]
+    n = nx * ny * nz
+    grid = o.mt_uniform(st["seed"], *st["range"], n * nf)
+    cfg = o.config(nx, ny, nz, 4, nf, mhd=(kind == "mhd"), recon=o.PPMC, gamma=st["gamma"])
+    n_if = n * (nf - 1)
+    for d in range(3):
+        QL = np.zeros(n * nf)
+        QR = np.zeros(n * nf)
+        o.lib().orc_ppmc_vl(C.byref(cfg), grid, QL, QR, d)
+        right = QR[:n_if].copy()
+        if kind == "hydro":
+            # The reference test sizes its hydro interface buffers with n_fields-1 fields, so the
+            # kernel's Energy store lands past the end of the left buffer, inside the right buffer
+            # that cudaMalloc placed after it (512-byte granularity).  Its fiducials record that
+            # store; model it to compare like for like.
+            pad = -(-n_if * 8 // 512) * 512 // 8
+            for j in range(n_if, n * nf):
+                if QL[j] != 0.0 and 0 <= j - pad < n_if:
+                    right[j - pad] = QL[j]
+        _check_interfaces(QL, right, g[kind]["left"][d], g[kind]["right"][d], n_if)
+
+
+@pytest.mark.parametrize("kind", ["hydro", "mhd"])
+def test_plmc_reference_fiducials(oracle_lib, kind):
+    o = oracle_lib
+    g = GOLD["plmc"]
+    st, tk = g["setup"], g[kind]
+    nx, ny, nz, nf = tk["nx"], tk["ny"], tk["nz"], tk["n_fields"]
+    n = nx * ny * nz
+    draws = o.mt_uniform(st["seed"], *st["range"], st["draws_before_grid"] + n * nf)
+    grid = np.ascontiguousarray(draws[st["draws_before_grid"]:])
+    for d in range(3):
+        # the reference test hands the kernel the grid shape rotated with the direction
+        # (plmc_cuda_tests.cu:125-144)
+        rx, ry, rz = [(nx, ny, nz), (ny, nz, nx), (nz, nx, ny)][d]
+        cfg = o.config(rx, ry, rz, 3, nf, mhd=(kind == "mhd"), recon=o.PLMC, gamma=st["gamma"])
+        QL = np.zeros(n * nf)
+        QR = np.zeros(n * nf)
+        o.lib().orc_plmc(C.byref(cfg), grid, QL, QR, d)
+        _check_interfaces(QL, QR, tk["left"][d], tk["right"][d], n * nf)
+
+
+def test_ppm_single_variable_reference_fiducials(oracle_lib):
+    o = oracle_lib
+    g = GOLD["ppm_single_variable"]
+    data = o.mt_uniform(g["seed"], *g["range"], 5 * g["n_tests"])
+    L = C.c_double()
+    R = C.c_double()
+    gotL, gotR = [], []
+    for i in range(g["n_tests"]):
+        o.lib().orc_ppm_single_variable(*data[5 * i:5 * i + 5], C.byref(L), C.byref(R))
+        gotL.append(L.value)
+        gotR.append(R.value)
+    assert nearly_equal(g["left"], gotL).all()
+    assert nearly_equal(g["right"], gotR).all()
+
+
+def test_calc_dt_reference_fiducial(oracle_lib):
+    """Calc_dt_3D on a one-cell state (hydro_cuda_tests.cu:29-82), here the centre of a 3^3 box."""
+    o = oracle_lib
+    g = GOLD["dt"]["calc_dt_3d"]
+    U = np.zeros((5, 3, 3, 3))
+    for f, v in enumerate(g["conserved"]):
+        U[f] = v
+    cfg = o.config(3, 3, 3, 1, 5, gamma=g["gamma"], dx=g["dx"], dy=g["dy"], dz=g["dz"])
+    got = o.calc_dt(cfg, np.ascontiguousarray(U.ravel()))
+    assert nearly_equal(g["fiducial"], got)
+
+
+def test_hydro_inverse_crossing_time_reference_fiducial(oracle_lib):
+    o = oracle_lib
+    g = GOLD["dt"]["hydro_inverse_crossing_time"]
+    d = g["density"]
+    U = np.zeros((5, 3, 3, 3))
+    U[0], U[1], U[2], U[3] = d, d * g["velocityX"], d * g["velocityY"], d * g["velocityZ"]
+    U[4] = g["energy"]
+    cfg = o.config(3, 3, 3, 1, 5, gamma=g["gamma"], dx=g["cellSizeX"], dy=g["cellSizeY"], dz=g["cellSizeZ"])
+    got = o.calc_dt(cfg, np.ascontiguousarray(U.ravel()))
+    # the oracle recomputes v = m * (1/d), the reference test passes v directly: allow a few ULP
+    assert abs(got - g["fiducial"]) <= 1e-15 * abs(g["fiducial"]) * 8
