@@ -1,0 +1,417 @@
+"""Benchmark: cell updates/s of the VL hydro step on one GB300 (and N replicas under torchrun).
+
+Workload (N=1 line): the 3D adiabatic hydro box -- 256^3 real cells (+4 ghosts), periodic,
+gamma 5/3, PPMC + HLLC + VL, dual energy, density and temperature floors, CFL 0.3; seeded
+lognormal density (sigma 0.5) and k^-2 velocities at rms Mach 2, uniform pressure.  A step
+is one full VL step of the box through the library: ghost fill, dt from the device-side CFL
+reduction, predictor, corrector, finalize (DE select/sync, temperature floor, CFL reduction).
+
+    python bench.py [--steps K] [--warmup W] [--gpus N] [--n 256] [--impl ours|reference]
+
+--impl reference times the reference's CPU path: the FP64 host restatement of the same scheme
+(oracle/, OpenMP over every host core), on a bounded 128^3 sample of the same workload.
+Multi-GPU (torchrun): every rank steps its own independent box (replicas; there is no
+collective on this path); value = all cells updated / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+L2_BYTES = 129 * 2 ** 20
+
+
+def hbm_peak():
+    try:
+        return float(json.loads(PEAKS.read_text())["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        dist.init_process_group(backend=backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(world, value, device=None):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------------------------------------
+# CPU path (the oracle): cpu_baseline and --impl reference
+# ------------------------------------------------------------------------------------------
+def cpu_sample(n_sample: int, min_seconds: float, max_steps: int, threads: int):
+    import oracle
+    from cholla_gb300 import ics
+
+    ng, gamma = 4, 5.0 / 3.0
+    U = ics.turbulence_box(n_sample, ng, gamma, seed=0)
+    nf, N = U.shape[0], U.shape[1]
+    dx = 1.0 / n_sample
+    oracle.set_threads(threads)
+    cfg = oracle.config(N, N, N, ng, nf, de=True, recon=oracle.PPMC, solver=oracle.HLLC, gamma=gamma, dx=dx, dy=dx,
+                        dz=dx)
+    flat = U.reshape(-1)
+    steps, t0 = 0, time.perf_counter()
+    while True:
+        oracle.set_boundaries(cfg, flat, (1,) * 6)
+        dt = 0.3 / oracle.calc_dt(cfg, flat)
+        oracle.vl_step_3d(cfg, flat, dt)
+        oracle.temperature_floor(cfg, flat, 0.0)
+        steps += 1
+        el = time.perf_counter() - t0
+        if steps >= max_steps or (min_seconds > 0 and el >= min_seconds):
+            break
+    return n_sample ** 3 * steps / el, steps, el
+
+
+def run_reference(args, world, rank):
+    """The reference's CPU implementation of the path: the FP64 host restatement (oracle)."""
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n_sample = 128
+    cpu_sample(n_sample, 0.0, args.warmup, threads)  # warm-up
+    cu_s, steps, el = cpu_sample(n_sample, 0.0, args.steps, threads)
+    sample = (f"{steps} steps of a {n_sample}^3 box of the same workload (seed 0), exact FP64 oracle, "
+              f"{threads} OpenMP threads")
+    line = {
+        "metric": "cell updates/s", "value": cu_s, "unit": "cell-updates/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": cu_s, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": cu_s, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(args, n_override=None):
+    n = n_override or args.n
+    return {"workload": f"3D adiabatic hydro {n}^3 periodic turbulence-like box, PPMC+HLLC+VL, dual energy, "
+                        f"density+temperature floors, CFL 0.3",
+            "n": n, "n_ghost": 4, "fields": 6, "gamma": 5.0 / 3.0, "reconstruction": "PPMC",
+            "riemann": "HLLC", "precision": getattr(args, "precision", "fp64_fast"),
+            "l2": f"state {6 * (n + 8) ** 3 * 8 / 1e6:.0f} MB > L2 129 MB (inputs larger than L2)"}
+
+
+# ------------------------------------------------------------------------------------------
+# GPU path
+# ------------------------------------------------------------------------------------------
+def time_box(box, U, steps, stream, torch):
+    """CUDA-event time of `steps` device-resident steps on `stream` (graph replay, dt on device)."""
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    box.advance(U, steps, 0.3, stream)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def kernel_breakdown(box, U, steps, stream):
+    box.enable_timing(True)
+    box.advance(U, steps, 0.3, stream)
+    kt = box.kernel_times()
+    box.enable_timing(False)
+    k = max(kt["steps"], 1)
+    return {name: kt[name] / k for name in ("predictor", "corrector", "finalize")}
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    from cholla_gb300 import ics
+    from cholla_gb300 import integrator as I
+    from cholla_gb300.engine import Box
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n, ng, gamma = args.n, 4, 5.0 / 3.0
+    N = n + 2 * ng
+    dx = 1.0 / n
+
+    def scheme(prec):
+        return I.Scheme(reconstruction="PPMC", riemann_solver="HLLC", dual_energy=True, density_floor=True,
+                        temperature_floor=True, gamma=gamma, precision=prec)
+
+    U0 = ics.turbulence_box(n, ng, gamma, seed=rank)
+    nf = U0.shape[0]
+    state_bytes = U0.nbytes
+    stream = torch.cuda.Stream(device=dev)
+    U = torch.from_numpy(U0).to(dev)
+    box = Box(N, N, N, ng, dx, dx, dx, scheme(args.precision))
+    box.use_graph(True)
+    box.advance(U, args.warmup, 0.3, stream)
+    stream.synchronize()
+
+    # ---- timed region: the headline arithmetic, device-resident, graph replay, dt on device ----
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ms = time_box(box, U, args.steps, stream, torch)
+    torch.cuda.synchronize()
+    barrier(world)
+    ms_max = max_over_ranks(world, ms, dev)
+    value = n ** 3 * args.steps * world / (ms_max / 1e3)
+
+    # ---- per-kernel times over a second timed region (events on the launching stream) ----
+    kt = kernel_breakdown(box, U, args.steps, stream)
+    box.close()
+    corr_ms = kt["corrector"]
+    # algorithmic bytes of one corrector launch: half-step primitives in (6 fields, compute type),
+    # U^n in and U^{n+1} out (6 fields FP64), GasEnergy partial update in, pre-sync energy out
+    wbytes = 4 if args.precision == "mixed" else 8
+    corr_bytes = n ** 3 * (nf * wbytes + 2 * nf * 8 + 2 * 8)
+    peak, peak_kind = hbm_peak()
+    achieved = corr_bytes / (corr_ms / 1e3) / 1e9
+
+    # ---- the other arithmetic forms of the same step, for comparison (rank 0) ----
+    others = {}
+    if rank == 0 and not args.no_variants:
+        for prec, k in (("fp64", 2), ("mixed", 20), ("fp64_fast", 5)):
+            if prec == args.precision:
+                continue
+            Uv = torch.from_numpy(U0).to(dev)
+            bv = Box(N, N, N, ng, dx, dx, dx, scheme(prec))
+            bv.use_graph(True)
+            bv.advance(Uv, 1, 0.3, stream)
+            stream.synchronize()
+            vms = time_box(bv, Uv, k, stream, torch) / k
+            others[prec] = {"value": n ** 3 / (vms / 1e3), "ms_per_step": vms, "steps": k,
+                            "kernels_ms": kernel_breakdown(bv, Uv, 2, stream)}
+            bv.close()
+            del Uv
+
+    # ---- end to end through the drop-in C ABI with host buffers ----
+    e2e = None
+    if rank == 0 and not args.no_e2e:
+        host = torch.from_numpy(ics.turbulence_box(n, ng, gamma, seed=rank)).pin_memory()
+        out = torch.empty_like(host).pin_memory()
+        Ud = torch.empty_like(host, device=dev)
+        I.set_scheme(scheme(args.precision))
+        I.set_stream(stream)
+        k = max(3, min(args.steps, 5))
+
+        def e2e_step():
+            Ud.copy_(host, non_blocking=True)
+            I.Set_Boundaries(Ud, N, N, N, ng, nf, (1,) * 6)
+            dti = I.Calc_dt_GPU(Ud, N, N, N, ng, nf, dx, dx, dx, gamma)
+            I.VL_Algorithm_3D_CUDA(Ud, None, N, N, N, 0, 0, 0, ng, dx, dx, dx, 0, 0, 0, 0.3 / dti, nf, 0, 0.0)
+            I.Apply_Temperature_Floor(Ud, N, N, N, ng, nf, 0.0)
+            out.copy_(Ud, non_blocking=True)
+
+        with torch.cuda.stream(stream):
+            e2e_step()
+            stream.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(k):
+                e2e_step()
+            stream.synchronize()
+            el = time.perf_counter() - t0
+        I.set_stream(None)
+        e2e = {"value": n ** 3 * k / el, "unit": "cell-updates/s", "h2d_bytes_per_step": state_bytes,
+               "d2h_bytes_per_step": state_bytes, "steps": k,
+               "path": "cgb_set_boundaries + cgb_calc_dt_gpu + cgb_vl_algorithm_3d + cgb_apply_temperature_floor, "
+                       "pinned host state copied in and out every step"}
+        del Ud
+
+    # ---- the reference's own CUDA build on the same GPU (cubins compiled from its source) ----
+    ref_gpu = None
+    if rank == 0 and not args.no_reference_gpu:
+        try:
+            from oracle import reference_gpu as R
+
+            if R.available():
+                R.init("hydro_ppmc_hllc_de")
+                R.set_stream(stream)
+                Ur = torch.from_numpy(ics.turbulence_box(n, ng, gamma, seed=0)).to(dev)
+                kr = 3
+
+                def ref_step():
+                    R.set_boundaries(Ur, N, N, N, ng, nf, (1,) * 6)
+                    dti = R.calc_dt(Ur, N, N, N, ng, nf, dx, dx, dx, gamma)
+                    R.vl_step_3d(Ur, N, N, N, ng, dx, dx, dx, 0.3 / dti, nf, gamma, 0.0)
+                    R.temperature_floor(Ur, N, N, N, ng, nf, 0.0)
+
+                ref_step()
+                stream.synchronize()
+                f0 = torch.cuda.Event(enable_timing=True)
+                f1 = torch.cuda.Event(enable_timing=True)
+                f0.record(stream)
+                for _ in range(kr):
+                    ref_step()
+                f1.record(stream)
+                f1.synchronize()
+                rms = f0.elapsed_time(f1) / kr
+                rv = n ** 3 / (rms / 1e3)
+                ref_gpu = {"value": rv, "unit": "cell-updates/s", "ms_per_step": rms, "steps": kr,
+                           "speedup_vs_reference_build": {"headline": (value / world) / rv,
+                                                          **{p: o["value"] / rv for p, o in others.items()}},
+                           "build": "reference hot-path .cu files compiled unchanged for sm_103a with its Makefile "
+                                    "flags (-O3 -fmad=false), launched kernel by kernel as VL_Algorithm_3D_CUDA does"}
+                del Ur
+        except Exception as ex:  # the reference build is a comparison, not part of the product
+            ref_gpu = {"unavailable": str(ex)[:200]}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        cu_s, steps, el = cpu_sample(96, 12.0, 400, threads)
+        cpu = {"value": cu_s, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+               "sample": f"{steps} steps of a 96^3 box of the same workload in {el:.1f} s (FP64 oracle, OpenMP)"}
+
+    if rank == 0:
+        clocks = clk.summary()
+        line = {
+            "metric": "cell updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if args.precision == "mixed" else "f64",
+            "data": "synthetic (seeded turbulence-like initial state, generated on the host)",
+            "config": {**workload_config(args), "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": load_traffic(n, args.precision),
+                         "kernel": "corrector", "kernel_ms": corr_ms, "kernels_ms": kt,
+                         "algorithmic_bytes_per_launch": corr_bytes,
+                         "peak_source": f"{peak_kind} (MEASURED_PEAKS.json)",
+                         "binding_ceiling": "FP64 pipe: GB300 FP64 FMA measured 1.19 TFLOP/s, divide 60 G/s"},
+            "variants": others,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "reference_gpu": ref_gpu,
+            "gpu_launches": 6 * args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def load_traffic(n, precision):
+    """DRAM bytes per corrector launch from the committed ncu summary (profiles/traffic.json),
+    scaled from the captured box to n^3 real cells (traffic grows with the number of cells)."""
+    f = ROOT / "profiles" / "traffic.json"
+    try:
+        d = json.loads(f.read_text())
+        return d["corrector"][precision]["dram_bytes_per_real_cell"] * n ** 3
+    except Exception:
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--precision", choices=["fp64_fast", "fp64", "mixed"], default="fp64_fast")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -23,7 +23,7 @@ CGB_ERR_UNSUPPORTED = 6
 
 PCM, PLMC, PPMC = 0, 1, 2
 HLLC, ROE, HLLD = 0, 1, 2
-FP64, MIXED = 0, 1
+FP64, MIXED, FP64_FAST = 0, 1, 2
 
 
 class CgbError(RuntimeError):
@@ -65,6 +65,16 @@ SIGNATURES = {
     "cgb_apply_temperature_floor": (_I, [_P, _I, _I, _I, _I, _I, _D]),
     "cgb_set_boundaries": (_I, [_P, _I, _I, _I, _I, _I, C.POINTER(_I)]),
     "cgb_max_magnetic_divergence": (_I, [_P, _I, _I, _I, _I, _I, _D, _D, _D, C.POINTER(_D)]),
+    "cgb_box_create": (_I, [C.POINTER(_P), _I, _I, _I, _I, _D, _D, _D, C.POINTER(cgb_scheme), C.POINTER(_I)]),
+    "cgb_box_destroy": (_I, [_P]),
+    "cgb_box_n_fields": (_I, [_P]),
+    "cgb_box_set_time": (_I, [_P, _D, _D]),
+    "cgb_box_use_graph": (_I, [_P, _I]),
+    "cgb_box_enable_timing": (_I, [_P, _I]),
+    "cgb_box_kernel_times": (_I, [_P, C.POINTER(_D), C.POINTER(C.c_longlong)]),
+    "cgb_box_advance": (_I, [_P, _P, _I, _D, _P]),
+    "cgb_box_get_time": (_I, [_P, C.POINTER(_D), C.POINTER(_D)]),
+    "cgb_box_last_error": (C.c_char_p, []),
 }
 
 

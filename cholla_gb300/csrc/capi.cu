@@ -51,6 +51,7 @@ void free_slot(ScratchSlot &sl)
   cudaFree(sl.s.Fz);
   cudaFree(sl.s.dti);
   cudaFree(sl.s.status);
+  cudaFree(sl.s.W);
   sl   = ScratchSlot{};
 }
 
@@ -71,7 +72,7 @@ int ensure_slot(int nx, int ny, int nz, int nf, int mhd)
   };
   bool ok = alloc((void **)&s.Uh, n * nf * sizeof(double)) && alloc((void **)&s.GEp, n * sizeof(double)) &&
             alloc((void **)&s.Epre, n * sizeof(double)) && alloc((void **)&s.dti, sizeof(unsigned long long)) &&
-            alloc((void **)&s.status, sizeof(int));
+            alloc((void **)&s.status, sizeof(int)) && alloc((void **)&s.W, 2 * (nf + 1) * n * sizeof(double));
   if (ok && mhd) {
     ok = alloc((void **)&s.emf, 3 * n * sizeof(double)) && alloc((void **)&s.Fx, n * (nf - 1) * sizeof(double)) &&
          alloc((void **)&s.Fy, n * (nf - 1) * sizeof(double)) && alloc((void **)&s.Fz, n * (nf - 1) * sizeof(double));
@@ -97,7 +98,7 @@ int check_scheme(const cgb_scheme &s)
   if (!s.mhd && s.riemann_solver == CGB_HLLD) return fail(CGB_ERR_ARGS, "HLLD needs MHD");
   if (s.mhd && s.dual_energy)
     return fail(CGB_ERR_UNSUPPORTED, "MHD with dual energy is not supported (the reference indexes past its flux arrays)");
-  if (s.precision != CGB_FP64 && s.precision != CGB_MIXED) return fail(CGB_ERR_ARGS, "bad precision");
+  if (s.precision < CGB_FP64 || s.precision > CGB_FP64_FAST) return fail(CGB_ERR_ARGS, "bad precision");
   return CGB_OK;
 }
 
@@ -169,11 +170,10 @@ int cgb_vl_algorithm_3d(double *d_conserved, double *d_grav_potential, int nx, i
   int const H = g_scheme.reconstruction == CGB_PPMC ? 4 : g_scheme.reconstruction == CGB_PLMC ? 3 : 2;
   if (n_ghost < H) return fail(CGB_ERR_ARGS, "n_ghost too small for the reconstruction");
   if (g_scheme.mhd) return fail(CGB_ERR_UNSUPPORTED, "MHD step not built in this version");
-  if (g_scheme.precision != CGB_FP64) return fail(CGB_ERR_UNSUPPORTED, "mixed precision not built in this version");
   rc = ensure_slot(nx, ny, nz, n_fields, g_scheme.mhd);
   if (rc != CGB_OK) return rc;
-  cudaError_t e = cgb::hydro_exact_step(b, g_scheme.reconstruction, g_scheme.riemann_solver, d_conserved, g_slot.s,
-                                        dt, 0.0, 0, 0, g_stream);
+  cudaError_t e = cgb::hydro_step(b, g_scheme.reconstruction, g_scheme.riemann_solver, g_scheme.precision,
+                                  d_conserved, g_slot.s, dt, nullptr, 0.0, 0, 0, g_stream);
   if (e != cudaSuccess) return cuda_fail(e, "vl_algorithm_3d");
   return CGB_OK;
 }
@@ -191,11 +191,10 @@ int cgb_vl_algorithm_1d(double *d_conserved, int nx, int x_off, int n_ghost, dou
   int rc = make_box(b, nx, 1, 1, n_ghost, n_fields, dx, dx, dx, 0.0, g_scheme);
   if (rc != CGB_OK) return rc;
   b.floor_on = 0;  // the 1D updates apply no density floor (hydro_cuda.cu:20-82, VL_1D_cuda.cu:158-215)
-  if (g_scheme.precision != CGB_FP64) return fail(CGB_ERR_UNSUPPORTED, "mixed precision not built in this version");
   rc = ensure_slot(nx, 1, 1, n_fields, 0);
   if (rc != CGB_OK) return rc;
-  cudaError_t e = cgb::hydro_exact_step(b, g_scheme.reconstruction, g_scheme.riemann_solver, d_conserved, g_slot.s,
-                                        dt, 0.0, 0, 0, g_stream);
+  cudaError_t e = cgb::hydro_step(b, g_scheme.reconstruction, g_scheme.riemann_solver, g_scheme.precision,
+                                  d_conserved, g_slot.s, dt, nullptr, 0.0, 0, 0, g_stream);
   if (e != cudaSuccess) return cuda_fail(e, "vl_algorithm_1d");
   return CGB_OK;
 }

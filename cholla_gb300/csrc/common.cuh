@@ -49,6 +49,7 @@ struct Scratch {
   double *Epre;    // total energy after the full update, before the DE sync (DE)
   double *emf;     // 3 edge-EMF fields (MHD)
   double *Fx, *Fy, *Fz;  // face fluxes (MHD path only)
+  void *W;               // half-step primitives of the fast / mixed paths (nq fields, 8 bytes each)
   unsigned long long *dti;  // encoded max inverse time step (one per box)
   int *status;              // device status word (bad cells seen, ...)
 };

@@ -43,8 +43,10 @@ __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? l
 // ------------------------------------------------------------------------------------------
 template <int TX, int TY, int TZ, int SOLVER>
 __global__ void __launch_bounds__(TX *TY *TZ) k_predictor(Box b, const double *__restrict__ U, double *__restrict__ Uh,
-                                                          double *__restrict__ GEp, double dt)
+                                                          double *__restrict__ GEp, double dt,
+                                                          const double *__restrict__ dtp)
 {
+  if (dtp) dt = *dtp;  // time step kept on the device (engine path)
   constexpr int HY = TY > 1 ? 1 : 0, HZ = TZ > 1 ? 1 : 0;
   constexpr int BX = TX + 2, BY = TY + 2 * HY, BZ = TZ + 2 * HZ;
   constexpr int NB  = BX * BY * BZ;
@@ -251,8 +253,10 @@ struct CorrSizes {
 template <int TX, int TY, int TZ, int RECON, int SOLVER>
 __global__ void __launch_bounds__(TX *TY *TZ) k_corrector(Box b, const double *__restrict__ Uh, double *__restrict__ U,
                                                           const double *__restrict__ GEp, double *__restrict__ Epre,
-                                                          int *__restrict__ status, double dt)
+                                                          int *__restrict__ status, double dt,
+                                                          const double *__restrict__ dtp)
 {
+  if (dtp) dt = *dtp;
   using S         = CorrSizes<TX, TY, TZ, RECON>;
   constexpr int H = S::H;
   constexpr int NT = TX * TY * TZ;
@@ -662,20 +666,21 @@ size_t corrector_smem(const Box &b)
 }
 
 template <int TX, int TY, int TZ, int SOLVER>
-cudaError_t launch_predictor(const Box &b, const double *U, double *Uh, double *GEp, double dt, cudaStream_t s)
+cudaError_t launch_predictor(const Box &b, const double *U, double *Uh, double *GEp, double dt, const double *dtp,
+                             cudaStream_t s)
 {
   size_t const sm = predictor_smem<TX, TY, TZ, SOLVER>(b);
   auto k          = k_predictor<TX, TY, TZ, SOLVER>;
   cudaError_t e   = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   dim3 grid((b.nx - 2 + TX - 1) / TX, TY > 1 ? (b.ny - 2 + TY - 1) / TY : 1, TZ > 1 ? (b.nz - 2 + TZ - 1) / TZ : 1);
-  k<<<grid, TX * TY * TZ, sm, s>>>(b, U, Uh, GEp, dt);
+  k<<<grid, TX * TY * TZ, sm, s>>>(b, U, Uh, GEp, dt, dtp);
   return cudaGetLastError();
 }
 
 template <int TX, int TY, int TZ, int RECON, int SOLVER>
 cudaError_t launch_corrector(const Box &b, const double *Uh, double *U, const double *GEp, double *Epre, int *status,
-                             double dt, cudaStream_t s)
+                             double dt, const double *dtp, cudaStream_t s)
 {
   size_t const sm = corrector_smem<TX, TY, TZ, RECON, SOLVER>(b);
   auto k          = k_corrector<TX, TY, TZ, RECON, SOLVER>;
@@ -683,22 +688,24 @@ cudaError_t launch_corrector(const Box &b, const double *Uh, double *U, const do
   if (e != cudaSuccess) return e;
   int const rx = b.nx - 2 * b.ng, ry = b.ny - 2 * b.ng, rz = b.nz - 2 * b.ng;
   dim3 grid((rx + TX - 1) / TX, TY > 1 ? (ry + TY - 1) / TY : 1, TZ > 1 ? (rz + TZ - 1) / TZ : 1);
-  k<<<grid, TX * TY * TZ, sm, s>>>(b, Uh, U, GEp, Epre, status, dt);
+  k<<<grid, TX * TY * TZ, sm, s>>>(b, Uh, U, GEp, Epre, status, dt, dtp);
   return cudaGetLastError();
 }
 
 template <int TX, int TY, int TZ>
 cudaError_t dispatch_step(const Box &b, int recon, int solver, double *U, const Scratch &sc, double dt,
-                          cudaStream_t s)
+                          const double *dtp, cudaStream_t s, cudaEvent_t *marks)
 {
   cudaError_t e;
+  if (marks) cudaEventRecord(marks[0], s);
   if (solver == SOLVER_ROE) {
-    e = launch_predictor<TX, TY, TZ, SOLVER_ROE>(b, U, sc.Uh, sc.GEp, dt, s);
+    e = launch_predictor<TX, TY, TZ, SOLVER_ROE>(b, U, sc.Uh, sc.GEp, dt, dtp, s);
   } else {
-    e = launch_predictor<TX, TY, TZ, SOLVER_HLLC>(b, U, sc.Uh, sc.GEp, dt, s);
+    e = launch_predictor<TX, TY, TZ, SOLVER_HLLC>(b, U, sc.Uh, sc.GEp, dt, dtp, s);
   }
   if (e != cudaSuccess) return e;
-#define CGB_CORR(R, SV) launch_corrector<TX, TY, TZ, R, SV>(b, sc.Uh, U, sc.GEp, sc.Epre, sc.status, dt, s)
+  if (marks) cudaEventRecord(marks[1], s);
+#define CGB_CORR(R, SV) launch_corrector<TX, TY, TZ, R, SV>(b, sc.Uh, U, sc.GEp, sc.Epre, sc.status, dt, dtp, s)
   if (recon == RECON_PPMC) {
     e = (solver == SOLVER_ROE) ? CGB_CORR(RECON_PPMC, SOLVER_ROE) : CGB_CORR(RECON_PPMC, SOLVER_HLLC);
   } else if (recon == RECON_PLMC) {
@@ -707,17 +714,19 @@ cudaError_t dispatch_step(const Box &b, int recon, int solver, double *U, const 
     e = (solver == SOLVER_ROE) ? CGB_CORR(RECON_PCM, SOLVER_ROE) : CGB_CORR(RECON_PCM, SOLVER_HLLC);
   }
 #undef CGB_CORR
+  if (marks) cudaEventRecord(marks[2], s);
   return e;
 }
 
 }  // namespace
 
 cudaError_t hydro_exact_step(const Box &b, int recon, int solver, double *U, const Scratch &sc, double dt,
-                             double U_floor, int temp_floor, int do_dt, cudaStream_t s)
+                             const double *dt_dev, double U_floor, int temp_floor, int do_dt, cudaStream_t s,
+                             cudaEvent_t *marks)
 {
   bool const one_d = (b.ny == 1 && b.nz == 1);
-  cudaError_t e    = one_d ? dispatch_step<128, 1, 1>(b, recon, solver, U, sc, dt, s)
-                           : dispatch_step<8, 8, 4>(b, recon, solver, U, sc, dt, s);
+  cudaError_t e    = one_d ? dispatch_step<128, 1, 1>(b, recon, solver, U, sc, dt, dt_dev, s, marks)
+                           : dispatch_step<8, 8, 4>(b, recon, solver, U, sc, dt, dt_dev, s, marks);
   if (e != cudaSuccess) return e;
   if (b.floor_on && !one_d) {
     k_negative_density_average<<<152 * 4, 256, 0, s>>>(b, U);
@@ -734,7 +743,26 @@ cudaError_t hydro_exact_step(const Box &b, int recon, int solver, double *U, con
     k_finalize<<<(unsigned)((nreal + 255) / 256), 256, 0, s>>>(b, U, sc.Epre, sc.dti, U_floor, temp_floor, do_dt);
     e = cudaGetLastError();
   }
+  if (marks) cudaEventRecord(marks[3], s);
   return e;
+}
+
+// dt = C_cfl / max_dti, clamped to t_end (main.cpp:258-261, grid3D.cpp:397); t advances by dt.
+__global__ void k_cfl_dt(const unsigned long long *__restrict__ dti, double *__restrict__ dt_t, double c_cfl,
+                         double t_end)
+{
+  double const m  = __longlong_as_double((long long)*dti);
+  double dt       = c_cfl / m;
+  double const t  = dt_t[1];
+  if (t_end > 0.0 && t + dt > t_end) dt = t_end - t;
+  dt_t[0] = dt;
+  dt_t[1] = t + dt;
+}
+
+cudaError_t cfl_dt(const unsigned long long *dti, double *dt_t, double c_cfl, double t_end, cudaStream_t s)
+{
+  k_cfl_dt<<<1, 1, 0, s>>>(dti, dt_t, c_cfl, t_end);
+  return cudaGetLastError();
 }
 
 cudaError_t hydro_calc_dt(const Box &b, const double *U, unsigned long long *dti, cudaStream_t s)
@@ -742,6 +770,12 @@ cudaError_t hydro_calc_dt(const Box &b, const double *U, unsigned long long *dti
   cudaError_t e = cudaMemsetAsync(dti, 0, sizeof(unsigned long long), s);
   if (e != cudaSuccess) return e;
   k_calc_dt<<<152 * 8, 256, 0, s>>>(b, U, dti);
+  return cudaGetLastError();
+}
+
+cudaError_t negative_density_average(const Box &b, double *U, cudaStream_t s)
+{
+  k_negative_density_average<<<152 * 4, 256, 0, s>>>(b, U);
   return cudaGetLastError();
 }
 

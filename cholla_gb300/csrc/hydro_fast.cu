@@ -1,0 +1,630 @@
+// hydro_fast.cu -- throughput forms of the fused VL hydro step: fast FP64 (T = double) and
+// mixed precision (T = float: reconstruction and fluxes in FP32; conserved accumulation,
+// total-minus-kinetic energy, dual-energy selection and the CFL reduction in FP64).
+//
+//   prims      Uⁿ (FP64) -> Wⁿ: primitives in T, once per cell, pressure recovered in FP64
+//   predictor  Wⁿ tile -> PCM + Riemann (T) -> half update in FP64 -> primitives of U½ (T)
+//              written as W½; GasEnergy pdV partial update (FP64)
+//   corrector  W½ -> x, y, z sweeps of reconstruction + Riemann (T) into register
+//              accumulators -> Uⁿ⁺¹ = Uⁿ + ΔU in FP64, in place
+//   finalize   dual-energy select/sync, temperature floor, CFL reduction (FP64)
+//
+// Quantities travel in fixed slots: 0 d, 1-3 velocity / momentum, 4 p / E, 5 GasEnergy,
+// 6.. passive scalars, so every register-array index is a compile-time constant.
+#include <type_traits>
+
+#include "common.cuh"
+#include "hydro_fast.cuh"
+#include "kernels.h"
+
+namespace cgb
+{
+namespace
+{
+
+constexpr int NSLOT = 6 + NS_MAX;
+
+__device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// number of slots a box carries and which of them are live
+__host__ __device__ __forceinline__ int nslot(const Box &b) { return b.ns > 0 ? 6 + b.ns : 5 + b.de; }
+__device__ __forceinline__ bool live(int s, const Box &b)
+{
+  return s < 5 || (s == 5 && b.de) || (s >= 6 && s - 6 < b.ns);
+}
+// state field of slot s (unrotated)
+__device__ __forceinline__ long long field(int s, const Box &b) { return s < 5 ? s : s == 5 ? b.nf - 1 : s - 1; }
+// slot of the rotated quantity q for a sweep with momenta (o1, o2, o3)
+__device__ __forceinline__ int rot(int q, int o1, int o2, int o3)
+{
+  return q == 1 ? o1 : q == 2 ? o2 : q == 3 ? o3 : q;
+}
+
+// 1/d in FP64 from an FP32 estimate and `steps` Newton steps (2 FP64 FMAs each)
+template <int steps>
+__device__ __forceinline__ double rcp_nr(double d)
+{
+  double r = (double)__frcp_rn((float)d);
+#pragma unroll
+  for (int i = 0; i < steps; i++) r = fma(r, fma(-d, r, 1.0), r);
+  return r;
+}
+
+// Primitives (T) of one cell from its FP64 conserved state q (slots), pressure recovered in
+// FP64 (Load_Data, reconstruction.h:139-212; Get_Pressure_From_DE, hydro_utilities.h:136-151).
+template <typename T>
+__device__ __forceinline__ void prim_from_cons(const double *q, const Box &b, T *w)
+{
+  bool const mix  = std::is_same<T, float>::value;
+  double const d  = q[0];
+  double const id = mix ? rcp_nr<1>(d) : 1.0 / d;
+  double const ke  = 0.5 * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) * id;
+  double const eth = q[4] - ke;
+  double p;
+  if (b.de) {
+    p    = hf::ratio_gt(eth, q[4], ETA_1) ? eth : q[5];
+    p    = fmax(p * (b.gamma - 1.0), TINY);
+    w[5] = (T)(q[5] * id);
+  } else {
+    p    = fmax((b.gamma - 1.0) * eth, TINY);
+    w[5] = T(0);
+  }
+  w[0] = (T)d;
+  if (mix) {
+    float const idf = (float)id;
+    w[1] = (T)((float)q[1] * idf);
+    w[2] = (T)((float)q[2] * idf);
+    w[3] = (T)((float)q[3] * idf);
+  } else {
+    w[1] = (T)(q[1] * id);
+    w[2] = (T)(q[2] * id);
+    w[3] = (T)(q[3] * id);
+  }
+  w[4] = (T)p;
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++) w[6 + k] = (k < b.ns) ? (T)(mix ? (float)q[6 + k] * (float)id : q[6 + k] * id) : T(0);
+}
+
+template <typename T>
+__device__ __forceinline__ hf::Prim<T> prim_at(const T *P, int stride, int i, const Box &b)
+{
+  hf::Prim<T> s;
+  s.d   = P[0 * stride + i];
+  s.vn  = P[1 * stride + i];
+  s.vt1 = P[2 * stride + i];
+  s.vt2 = P[3 * stride + i];
+  s.p   = P[4 * stride + i];
+  s.ge  = b.de ? P[5 * stride + i] : T(0);
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++) s.sc[k] = (k < b.ns) ? P[(6 + k) * stride + i] : T(0);
+  return s;
+}
+
+template <typename T>
+__device__ __forceinline__ void prim_put(T *P, int stride, int i, const hf::Prim<T> &s, const Box &b)
+{
+  P[0 * stride + i] = s.d;
+  P[1 * stride + i] = s.vn;
+  P[2 * stride + i] = s.vt1;
+  P[3 * stride + i] = s.vt2;
+  P[4 * stride + i] = s.p;
+  if (b.de) P[5 * stride + i] = s.ge;
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++)
+    if (k < b.ns) P[(6 + k) * stride + i] = s.sc[k];
+}
+
+template <typename T, int SOLVER>
+__device__ __forceinline__ void riemann(const hf::Prim<T> &L, const hf::Prim<T> &R, T *f, const Box &b)
+{
+  if (SOLVER == SOLVER_ROE) {
+    hf::roe(L, R, f, b.ns, b.de, (T)b.gamma);
+  } else {
+    hf::hllc(L, R, f, b.ns, b.de, (T)b.gamma);
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// primitives of every cell of the padded box
+template <typename T>
+__global__ void __launch_bounds__(256) k_fprims(Box b, const double *__restrict__ U, T *__restrict__ Wn)
+{
+  long long const n = b.n;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double q[NSLOT];
+#pragma unroll
+    for (int s = 0; s < NSLOT; s++) q[s] = live(s, b) ? U[field(s, b) * n + i] : 0.0;
+    T w[NSLOT];
+    prim_from_cons<T>(q, b, w);
+#pragma unroll
+    for (int s = 0; s < NSLOT; s++)
+      if (live(s, b)) Wn[(long long)s * n + i] = w[s];
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+template <typename T, int TX, int TY, int TZ, int SOLVER>
+__global__ void __launch_bounds__(TX *TY *TZ, 2)
+    k_fpred(Box b, const double *__restrict__ U, const T *__restrict__ Wn, T *__restrict__ W, double *__restrict__ GEp,
+            double dt, const double *__restrict__ dtp)
+{
+  if (dtp) dt = *dtp;
+  constexpr int HY = TY > 1 ? 1 : 0, HZ = TZ > 1 ? 1 : 0;
+  constexpr int BX = TX + 2, BY = TY + 2 * HY, BZ = TZ + 2 * HZ;
+  constexpr int NB  = BX * BY * BZ;
+  constexpr int NFX = (TX + 1) * TY * TZ;
+  constexpr int NFY = HY ? TX * (TY + 1) * TZ : 0;
+  constexpr int NFZ = HZ ? TX * TY * (TZ + 1) : 0;
+  constexpr int NT  = TX * TY * TZ;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int const ns_ = nslot(b);
+  T *Ps  = reinterpret_cast<T *>(smem_raw);  // [slot][NB] primitives of the box
+  T *Fxs = Ps + ns_ * NB;                    // [slot][faces] fluxes, conserved orientation
+  T *Fys = Fxs + ns_ * NFX;
+  T *Fzs = Fys + ns_ * NFY;
+
+  int const x0 = 1 + blockIdx.x * TX;
+  int const y0 = HY ? 1 + blockIdx.y * TY : 0;
+  int const z0 = HZ ? 1 + blockIdx.z * TZ : 0;
+  long long const n = b.n;
+
+  for (int t = threadIdx.x; t < NB; t += NT) {
+    int const bx = t % BX, by = (t / BX) % BY, bz = t / (BX * BY);
+    long long const gid =
+        b.id(clampi(x0 - 1 + bx, 0, b.nx - 1), clampi(y0 - HY + by, 0, b.ny - 1), clampi(z0 - HZ + bz, 0, b.nz - 1));
+    for (int s = 0; s < ns_; s++) Ps[s * NB + t] = Wn[(long long)s * n + gid];
+  }
+  __syncthreads();
+
+  int const nfaces = NFX + NFY + NFZ;
+  for (int t = threadIdx.x; t < nfaces; t += NT) {
+    int dir, i, j, k, nfd, fidx;
+    T *Fd;
+    if (t < NFX) {
+      dir = 0, nfd = NFX, Fd = Fxs, fidx = t;
+      i = t % (TX + 1), j = (t / (TX + 1)) % TY, k = t / ((TX + 1) * TY);
+    } else if (t < NFX + NFY) {
+      dir = 1, nfd = NFY, Fd = Fys, fidx = t - NFX;
+      i = fidx % TX, j = (fidx / TX) % (TY + 1), k = fidx / (TX * (TY + 1));
+    } else {
+      dir = 2, nfd = NFZ, Fd = Fzs, fidx = t - NFX - NFY;
+      i = fidx % TX, j = (fidx / TX) % TY, k = fidx / (TX * TY);
+    }
+    int const lx = (dir == 0) ? i : i + 1, ly = (dir == 1) ? j : j + HY, lz = (dir == 2) ? k : k + HZ;
+    int const cl = lx + BX * (ly + BY * lz);
+    int const cr = cl + (dir == 0 ? 1 : dir == 1 ? BX : BX * BY);
+    int const o1 = dir + 1, o2 = (dir + 1) % 3 + 1, o3 = (dir + 2) % 3 + 1;
+    hf::Prim<T> L = prim_at(Ps, NB, cl, b), R = prim_at(Ps, NB, cr, b);
+    // rotate the velocities into (normal, t1, t2)
+    T const lv[3] = {L.vn, L.vt1, L.vt2}, rv[3] = {R.vn, R.vt1, R.vt2};
+    L.vn = lv[o1 - 1], L.vt1 = lv[o2 - 1], L.vt2 = lv[o3 - 1];
+    R.vn = rv[o1 - 1], R.vt1 = rv[o2 - 1], R.vt2 = rv[o3 - 1];
+    T f[NSLOT];
+    riemann<T, SOLVER>(L, R, f, b);
+#pragma unroll
+    for (int q = 0; q < NSLOT; q++)
+      if (live(q, b)) Fd[rot(q, o1, o2, o3) * nfd + fidx] = f[q];
+  }
+  __syncthreads();
+
+  int const t = threadIdx.x;
+  int const i = t % TX, j = (t / TX) % TY, k = t / (TX * TY);
+  int const gx = x0 + i, gy = y0 + j, gz = z0 + k;
+  bool const one_d = (b.ny == 1 && b.nz == 1);
+  bool valid = gx > 0 && gx < b.nx - 1;
+  if (!one_d) valid = valid && gy > 0 && gy < b.ny - 1 && gz > 0 && gz < b.nz - 1;
+  if (!valid) return;
+  long long const gid = b.id(gx, gy, gz);
+  int const c  = (i + 1) + BX * ((j + HY) + BY * (k + HZ));
+  int const fx = i + (TX + 1) * (j + TY * k);
+  int const fy = i + TX * (j + (TY + 1) * k);
+  int const fz = i + TX * (j + TY * k);
+  T const dtodx = (T)(0.5 * dt / b.dx), dtody = (T)(0.5 * dt / b.dy), dtodz = (T)(0.5 * dt / b.dz);
+  double q[NSLOT];
+#pragma unroll
+  for (int s = 0; s < NSLOT; s++) {
+    q[s] = 0.0;
+    if (live(s, b)) {
+      T a = dtodx * (Fxs[s * NFX + fx] - Fxs[s * NFX + fx + 1]);
+      if (!one_d) {
+        a += dtody * (Fys[s * NFY + fy] - Fys[s * NFY + fy + TX]);
+        a += dtodz * (Fzs[s * NFZ + fz] - Fzs[s * NFZ + fz + TX * TY]);
+      }
+      q[s] = U[field(s, b) * n + gid] + (double)a;
+    }
+  }
+  if (b.de) {
+    // pdV source from the neighbours' cell-centred velocities of Uⁿ (hydro_cuda.cu:178-202);
+    // the 1D half step takes the plain total-minus-kinetic pressure (VL_1D_cuda.cu:180-187)
+    T const P = Ps[4 * NB + c];
+    T Ph      = P;
+    if (one_d) {
+      double const d = U[gid], id = 1.0 / d;
+      double const mx = U[n + gid], my = U[2 * n + gid], mz = U[3 * n + gid];
+      Ph = (T)((U[4 * n + gid] - 0.5 * (mx * mx + my * my + mz * mz) * id) * (b.gamma - 1.0));
+    }
+    T div = dtodx * (Ps[NB + c - 1] - Ps[NB + c + 1]);
+    if (!one_d)
+      div += dtody * (Ps[2 * NB + c - BX] - Ps[2 * NB + c + BX]) +
+             dtodz * (Ps[3 * NB + c - BX * BY] - Ps[3 * NB + c + BX * BY]);
+    q[5] += (double)(T(0.5) * Ph * div);
+    int const ng = b.ng;
+    bool real    = gx >= ng && gx < b.nx - ng;
+    if (!one_d) real = real && gy >= ng && gy < b.ny - ng && gz >= ng && gz < b.nz - ng;
+    // full-dt partial update (hydro_cuda.cu:754-833): twice the half-step pdV term
+    if (real) GEp[gid] = U[(long long)(b.nf - 1) * n + gid] + (double)(P * div);
+  }
+  if (b.floor_on && !one_d && q[0] < b.density_floor) {
+    double const s = b.density_floor / q[0];
+    q[0]           = b.density_floor;
+    q[1] *= s, q[2] *= s, q[3] *= s, q[4] *= s;
+    if (b.de) q[5] *= s;
+  }
+  T w[NSLOT];
+  prim_from_cons<T>(q, b, w);
+#pragma unroll
+  for (int s = 0; s < NSLOT; s++)
+    if (live(s, b)) W[(long long)s * n + gid] = w[s];
+}
+
+// ------------------------------------------------------------------------------------------
+template <int RECON>
+struct FHalo {
+  static constexpr int H = RECON == RECON_PPMC ? 3 : (RECON == RECON_PLMC ? 2 : 1);
+};
+
+template <int TX, int TY, int TZ, int RECON>
+struct FSizes {
+  static constexpr int H  = FHalo<RECON>::H;
+  static constexpr int HY = TY > 1, HZ = TZ > 1;
+  static constexpr int PX = (TX + 2 * H) * TY * TZ;
+  static constexpr int PY = HY ? TX * (TY + 2 * H) * TZ : 0;
+  static constexpr int PZ = HZ ? TX * TY * (TZ + 2 * H) : 0;
+  static constexpr int PM = PX > PY ? (PX > PZ ? PX : PZ) : (PY > PZ ? PY : PZ);
+  static constexpr int RX = (TX + 2) * TY * TZ;
+  static constexpr int RY = HY ? TX * (TY + 2) * TZ : 0;
+  static constexpr int RZ = HZ ? TX * TY * (TZ + 2) : 0;
+  static constexpr int RM = RX > RY ? (RX > RZ ? RX : RZ) : (RY > RZ ? RY : RZ);
+  static constexpr int FX = (TX + 1) * TY * TZ;
+  static constexpr int FY = HY ? TX * (TY + 1) * TZ : 0;
+  static constexpr int FZ = HZ ? TX * TY * (TZ + 1) : 0;
+  static constexpr int FM = FX > FY ? (FX > FZ ? FX : FZ) : (FY > FZ ? FY : FZ);
+  static constexpr int PER_Q = PM + (RECON == RECON_PCM ? 0 : 2 * RM) + FM;
+};
+
+template <typename T, int TX, int TY, int TZ, int RECON, int SOLVER>
+__global__ void __launch_bounds__(TX *TY *TZ, 2)
+    k_fcorr(Box b, const T *__restrict__ W, double *__restrict__ U, const double *__restrict__ GEp,
+            double *__restrict__ Epre, int *__restrict__ status, double dt, const double *__restrict__ dtp)
+{
+  if (dtp) dt = *dtp;
+  using S          = FSizes<TX, TY, TZ, RECON>;
+  constexpr int H  = S::H;
+  constexpr int NT = TX * TY * TZ;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int const ns_ = nslot(b);
+  T *Ps  = reinterpret_cast<T *>(smem_raw);
+  T *QLs = Ps + ns_ * S::PM;
+  T *QRs = (RECON == RECON_PCM) ? QLs : QLs + ns_ * S::RM;
+  T *Fs  = (RECON == RECON_PCM) ? QLs : QRs + ns_ * S::RM;
+
+  int const ng = b.ng;
+  int const x0 = ng + blockIdx.x * TX;
+  int const y0 = S::HY ? ng + blockIdx.y * TY : 0;
+  int const z0 = S::HZ ? ng + blockIdx.z * TZ : 0;
+  bool const one_d = (b.ny == 1 && b.nz == 1);
+  long long const n = b.n;
+
+  int const t  = threadIdx.x;
+  int const ti = t % TX, tj = (t / TX) % TY, tk = t / (TX * TY);
+  T acc[NSLOT];
+#pragma unroll
+  for (int q = 0; q < NSLOT; q++) acc[q] = T(0);
+
+  int const ndir = one_d ? 1 : 3;
+  for (int dir = 0; dir < ndir; dir++) {
+    int const o1 = dir + 1, o2 = (dir + 1) % 3 + 1, o3 = (dir + 2) % 3 + 1;
+    int const TA = dir == 0 ? TX : dir == 1 ? TY : TZ;
+    int const TU = dir == 0 ? TY : dir == 1 ? TZ : TX;
+    int const TW = dir == 0 ? TZ : dir == 1 ? TX : TY;
+    int const LA = TA + 2 * H;
+    int const np = LA * TU * TW;
+    for (int p = t; p < np; p += NT) {
+      int const a = p % LA - H, u = (p / LA) % TU, w = p / (LA * TU);
+      int gx, gy, gz;
+      if (dir == 0) {
+        gx = x0 + a, gy = y0 + u, gz = z0 + w;
+      } else if (dir == 1) {
+        gy = y0 + a, gz = z0 + u, gx = x0 + w;
+      } else {
+        gz = z0 + a, gx = x0 + u, gy = y0 + w;
+      }
+      long long const gid = b.id(clampi(gx, 0, b.nx - 1), clampi(gy, 0, b.ny - 1), clampi(gz, 0, b.nz - 1));
+      for (int q = 0; q < ns_; q++) Ps[q * S::PM + p] = W[(long long)rot(q, o1, o2, o3) * n + gid];
+    }
+    __syncthreads();
+    int const LR = TA + 2;
+    if (RECON != RECON_PCM) {
+      int const nr = LR * TU * TW;
+      for (int r = t; r < nr; r += NT) {
+        int const a = r % LR - 1, uw = r / LR;
+        int const base = (a + H) + LA * uw;
+        hf::Prim<T> L, R;
+        if (RECON == RECON_PPMC) {
+          hf::ppmc_cell(prim_at(Ps, S::PM, base - 2, b), prim_at(Ps, S::PM, base - 1, b), prim_at(Ps, S::PM, base, b),
+                        prim_at(Ps, S::PM, base + 1, b), prim_at(Ps, S::PM, base + 2, b), b.ns, b.de, (T)b.gamma, L,
+                        R);
+        } else {
+          hf::plmc_cell(prim_at(Ps, S::PM, base - 1, b), prim_at(Ps, S::PM, base, b), prim_at(Ps, S::PM, base + 1, b),
+                        b.ns, b.de, (T)b.gamma, L, R);
+        }
+        prim_put(QLs, S::RM, r, L, b);
+        prim_put(QRs, S::RM, r, R, b);
+      }
+      __syncthreads();
+    }
+    int const LF  = TA + 1;
+    int const nfc = LF * TU * TW;
+    T *Fd         = (RECON == RECON_PCM) ? QLs : Fs;
+    for (int fi = t; fi < nfc; fi += NT) {
+      int const a = fi % LF - 1, uw = fi / LF;
+      hf::Prim<T> L, R;
+      if (RECON == RECON_PCM) {
+        int const pl = (a + H) + LA * uw;
+        L = prim_at(Ps, S::PM, pl, b);
+        R = prim_at(Ps, S::PM, pl + 1, b);
+      } else {
+        int const rl = (a + 1) + LR * uw;
+        L = prim_at(QLs, S::RM, rl, b);
+        R = prim_at(QRs, S::RM, rl + 1, b);
+      }
+      T f[NSLOT];
+      riemann<T, SOLVER>(L, R, f, b);
+#pragma unroll
+      for (int q = 0; q < NSLOT; q++)
+        if (live(q, b)) Fd[q * S::FM + fi] = f[q];
+    }
+    __syncthreads();
+    {
+      int a, u, w;
+      if (dir == 0) {
+        a = ti, u = tj, w = tk;
+      } else if (dir == 1) {
+        a = tj, u = tk, w = ti;
+      } else {
+        a = tk, u = ti, w = tj;
+      }
+      int const fm = a + LF * (u + TU * w);
+      T const dtod = (T)(dt / (dir == 0 ? b.dx : dir == 1 ? b.dy : b.dz));
+      T d[NSLOT];
+#pragma unroll
+      for (int q = 0; q < NSLOT; q++) d[q] = live(q, b) ? dtod * (Fd[q * S::FM + fm] - Fd[q * S::FM + fm + 1]) : T(0);
+      // rotated momentum components back to x, y, z
+      T const dm[3] = {d[1], d[2], d[3]};
+      acc[0] += d[0];
+      acc[o1] += dm[0];
+      acc[o2] += dm[1];
+      acc[o3] += dm[2];
+#pragma unroll
+      for (int q = 4; q < NSLOT; q++) acc[q] += d[q];
+    }
+    __syncthreads();
+  }
+
+  int const gx = x0 + ti, gy = y0 + tj, gz = z0 + tk;
+  bool real = gx < b.nx - ng;
+  if (!one_d) real = real && gy < b.ny - ng && gz < b.nz - ng;
+  if (!real) return;
+  long long const gid = b.id(gx, gy, gz);
+  double v[NSLOT];
+#pragma unroll
+  for (int q = 0; q < NSLOT; q++) {
+    v[q] = 0.0;
+    if (live(q, b)) v[q] = (q == 5 ? GEp[gid] : U[field(q, b) * n + gid]) + (double)acc[q];
+  }
+  if (b.floor_on && !one_d && v[0] < b.density_floor) {
+    if (v[0] > 0) {
+      double const s = b.density_floor / v[0];
+      v[0]           = b.density_floor;
+      v[1] *= s, v[2] *= s, v[3] *= s, v[4] *= s;
+      if (b.de) v[5] *= s;
+    } else {
+      atomicOr(status, 1);
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < NSLOT; q++)
+    if (live(q, b)) U[field(q, b) * n + gid] = v[q];
+  if (b.de) Epre[gid] = v[4];
+}
+
+// ------------------------------------------------------------------------------------------
+// finalize (FP64): DE select/sync, temperature floor, CFL reduction
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ void block_max_to(double v, unsigned long long *dst)
+{
+  __shared__ double red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    int const nw = (blockDim.x + 31) >> 5;
+    v            = (lane < nw) ? red[lane] : -1.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (lane == 0 && v >= 0.0) atomicMax(dst, (unsigned long long)__double_as_longlong(v));
+  }
+}
+
+// MIX: the mixed-precision form takes the sound speed's square root in FP32 and the
+// reciprocal of the density with one Newton step; the selection, sync, floor and the
+// maximum stay FP64.
+template <bool MIX>
+__global__ void __launch_bounds__(256) k_ffinalize(Box b, double *__restrict__ U, const double *__restrict__ Epre,
+                                                   unsigned long long *__restrict__ dti, double U_floor,
+                                                   int temp_floor, int do_dt, double idx, double idy, double idz)
+{
+  int const ng = b.ng;
+  bool const one_d = (b.ny == 1 && b.nz == 1);
+  int const rx = b.nx - 2 * ng, ry = one_d ? 1 : b.ny - 2 * ng, rz = one_d ? 1 : b.nz - 2 * ng;
+  long long const nreal = (long long)rx * ry * rz;
+  long long const r     = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  double m = -1.0;
+  if (r < nreal) {
+    int const x = (int)(r % rx) + ng;
+    int const y = one_d ? 0 : (int)((r / rx) % ry) + ng;
+    int const z = one_d ? 0 : (int)(r / ((long long)rx * ry)) + ng;
+    long long const n = b.n, id = b.id(x, y, z);
+    double const d = U[id], d_inv = MIX ? rcp_nr<1>(d) : hf::rcp(d);
+    double const mx = U[n + id], my = U[2 * n + id], mz = U[3 * n + id];
+    double const ke = 0.5 * (mx * mx + my * my + mz * mz) * d_inv;
+    double E        = U[4 * n + id];
+    if (b.de) {
+      long long const fge = (long long)(b.nf - 1) * n;
+      double Emax;
+      if (one_d) {
+        Emax = fmax(fmax(Epre[max(x - 1, ng)], E), Epre[min(x + 1, b.nx - ng - 1)]);
+      } else {
+        Emax = fmax(Epre[b.id(max(x - 1, ng), y, z)], E);
+        Emax = fmax(Emax, Epre[b.id(min(x + 1, b.nx - ng - 1), y, z)]);
+        Emax = fmax(Emax, Epre[b.id(x, max(y - 1, ng), z)]);
+        Emax = fmax(Emax, Epre[b.id(x, min(y + 1, b.ny - ng - 1), z)]);
+        Emax = fmax(Emax, Epre[b.id(x, y, max(z - 1, ng))]);
+        Emax = fmax(Emax, Epre[b.id(x, y, min(z + 1, b.nz - ng - 1))]);
+      }
+      double const ut = E - ke;
+      // Select_Internal_Energy_3D (hydro_cuda.cu:949-1016): U/E > eta1 or U/Emax > eta2
+      double Ui   = (hf::ratio_gt(ut, E, ETA_1) || hf::ratio_gt(ut, Emax, ETA_2)) ? ut : U[fge + id];
+      Ui          = fmax(Ui, TINY);
+      U[fge + id] = Ui;
+      E           = ke + Ui;  // Sync_Energies_3D (hydro_cuda.cu:1070-1099)
+      U[4 * n + id] = E;
+    }
+    if (temp_floor) {  // Temperature_Floor_Kernel (hydro_cuda.cu:1117-1153)
+      if (E - ke < U_floor * d) {
+        E             = ke + d * U_floor;
+        U[4 * n + id] = E;
+      }
+      if (b.de) {
+        long long const fge = (long long)(b.nf - 1) * n;
+        if (U[fge + id] < U_floor * d) U[fge + id] = d * U_floor;
+      }
+    }
+    if (do_dt) {  // hydroInverseCrossingTime (hydro_cuda.cu:404-419)
+      double const c2 = b.gamma * (E - ke) * (b.gamma - 1.0) * d_inv;
+      double const cs = MIX ? (double)sqrtf((float)fmax(c2, 0.0)) : hf::sqrtT(fmax(c2, 0.0));
+      double const ax = fabs(mx * d_inv) + cs;
+      if (one_d) {
+        m = ax * idx;
+      } else {
+        double const ay = fabs(my * d_inv) + cs, az = fabs(mz * d_inv) + cs;
+        m = fmax(fmax(ax * idx, ay * idy), fmax(az * idz, 0.0));
+      }
+    }
+  }
+  if (do_dt) block_max_to(m, dti);
+}
+
+// ------------------------------------------------------------------------------------------
+template <typename T, int TX, int TY, int TZ>
+size_t fpred_smem(const Box &b)
+{
+  constexpr int HY = TY > 1, HZ = TZ > 1;
+  constexpr int NB = (TX + 2) * (TY + 2 * HY) * (TZ + 2 * HZ);
+  constexpr int NF = (TX + 1) * TY * TZ + (HY ? TX * (TY + 1) * TZ : 0) + (HZ ? TX * TY * (TZ + 1) : 0);
+  return sizeof(T) * (size_t)nslot(b) * (NB + NF);
+}
+
+template <typename T, int TX, int TY, int TZ>
+cudaError_t launch_fast(const Box &b, int recon, int solver, double *U, const Scratch &sc, double dt,
+                        const double *dtp, cudaStream_t s, cudaEvent_t *marks)
+{
+  T *Wn = (T *)sc.W;
+  T *Wh = Wn + (size_t)nslot(b) * (size_t)b.n;
+  cudaError_t e;
+  if (marks) cudaEventRecord(marks[0], s);
+  {
+    long long blocks = (b.n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    k_fprims<T><<<(unsigned)blocks, 256, 0, s>>>(b, U, Wn);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  {
+    size_t const sm = fpred_smem<T, TX, TY, TZ>(b);
+    dim3 grid((b.nx - 2 + TX - 1) / TX, TY > 1 ? (b.ny - 2 + TY - 1) / TY : 1, TZ > 1 ? (b.nz - 2 + TZ - 1) / TZ : 1);
+    auto k = (solver == SOLVER_ROE) ? k_fpred<T, TX, TY, TZ, SOLVER_ROE> : k_fpred<T, TX, TY, TZ, SOLVER_HLLC>;
+    if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess) return e;
+    k<<<grid, TX * TY * TZ, sm, s>>>(b, U, Wn, Wh, sc.GEp, dt, dtp);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  if (marks) cudaEventRecord(marks[1], s);
+  {
+    int const rx = b.nx - 2 * b.ng, ry = b.ny - 2 * b.ng, rz = b.nz - 2 * b.ng;
+    dim3 grid((rx + TX - 1) / TX, TY > 1 ? (ry + TY - 1) / TY : 1, TZ > 1 ? (rz + TZ - 1) / TZ : 1);
+    void (*k)(Box, const T *, double *, const double *, double *, int *, double, const double *);
+    size_t per_q;
+#define CGB_PICK(R)                                                                                      \
+  per_q = FSizes<TX, TY, TZ, R>::PER_Q;                                                                 \
+  k     = (solver == SOLVER_ROE) ? k_fcorr<T, TX, TY, TZ, R, SOLVER_ROE> : k_fcorr<T, TX, TY, TZ, R, SOLVER_HLLC>;
+    if (recon == RECON_PPMC) {
+      CGB_PICK(RECON_PPMC)
+    } else if (recon == RECON_PLMC) {
+      CGB_PICK(RECON_PLMC)
+    } else {
+      CGB_PICK(RECON_PCM)
+    }
+#undef CGB_PICK
+    size_t const sm = sizeof(T) * (size_t)nslot(b) * per_q;
+    if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess) return e;
+    k<<<grid, TX * TY * TZ, sm, s>>>(b, Wh, U, sc.GEp, sc.Epre, sc.status, dt, dtp);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  if (marks) cudaEventRecord(marks[2], s);
+  return cudaSuccess;
+}
+
+}  // namespace
+
+// bytes of W scratch the fast paths need: primitives of Uⁿ and of U½ (8 bytes covers both types)
+size_t fast_scratch_bytes(const Box &b) { return 2 * (size_t)nslot(b) * (size_t)b.n * sizeof(double); }
+
+cudaError_t hydro_fast_step(const Box &b, int recon, int solver, int mixed, double *U, const Scratch &sc, void *W,
+                            double dt, const double *dt_dev, double U_floor, int temp_floor, int do_dt,
+                            cudaStream_t s, cudaEvent_t *marks)
+{
+  (void)W;
+  bool const one_d = (b.ny == 1 && b.nz == 1);
+  cudaError_t e;
+  if (mixed) {
+    e = one_d ? launch_fast<float, 128, 1, 1>(b, recon, solver, U, sc, dt, dt_dev, s, marks)
+              : launch_fast<float, 8, 8, 4>(b, recon, solver, U, sc, dt, dt_dev, s, marks);
+  } else {
+    e = one_d ? launch_fast<double, 128, 1, 1>(b, recon, solver, U, sc, dt, dt_dev, s, marks)
+              : launch_fast<double, 8, 8, 4>(b, recon, solver, U, sc, dt, dt_dev, s, marks);
+  }
+  if (e != cudaSuccess) return e;
+  if (b.floor_on && !one_d) {
+    if ((e = negative_density_average(b, U, s)) != cudaSuccess) return e;
+  }
+  if (b.de || temp_floor || do_dt) {
+    if (do_dt && (e = cudaMemsetAsync(sc.dti, 0, sizeof(unsigned long long), s)) != cudaSuccess) return e;
+    int const ng = b.ng;
+    long long const nreal =
+        (long long)(b.nx - 2 * ng) * (one_d ? 1 : b.ny - 2 * ng) * (one_d ? 1 : b.nz - 2 * ng);
+    unsigned const grid = (unsigned)((nreal + 255) / 256);
+    if (mixed) {
+      k_ffinalize<true><<<grid, 256, 0, s>>>(b, U, sc.Epre, sc.dti, U_floor, temp_floor, do_dt, 1.0 / b.dx,
+                                              1.0 / b.dy, 1.0 / b.dz);
+    } else {
+      k_ffinalize<false><<<grid, 256, 0, s>>>(b, U, sc.Epre, sc.dti, U_floor, temp_floor, do_dt, 1.0 / b.dx,
+                                               1.0 / b.dy, 1.0 / b.dz);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  if (marks) cudaEventRecord(marks[3], s);
+  return cudaSuccess;
+}
+
+}  // namespace cgb

@@ -1,0 +1,431 @@
+// hydro_fast.cuh -- the VL hydro arithmetic reformulated for GB300's ALU balance.
+//
+// Same scheme as hydro_math.cuh (PPMC / PLMC / PCM, HLLC / Roe, dual energy), same limiter
+// decisions, but written for throughput: every quotient by a shared denominator becomes one
+// reciprocal and multiplies, primitives are computed once per cell instead of once per
+// stencil use, constant divisions are multiplications, the Riemann solvers take primitive
+// interface states directly (no round trip through conserved variables), and fused
+// multiply-adds are allowed.  T is the compute type: double for the fast FP64 path (agrees
+// with the reference to ~1e-14 relative per step), float for the mixed-precision path.
+#pragma once
+#include "common.cuh"
+
+namespace cgb
+{
+namespace hf
+{
+
+template <typename T>
+struct Prim {
+  T d, vn, vt1, vt2, p, ge;
+  T sc[NS_MAX];
+};
+
+template <typename T>
+__device__ __forceinline__ T sgnT(T a)
+{
+  return (a < T(0)) ? T(-1) : T(1);
+}
+
+template <typename T>
+struct Eps;
+template <>
+struct Eps<double> {
+  static constexpr double roundoff = 1.0e-12;  // reconstruction.h:869-879 thresholds
+};
+template <>
+struct Eps<float> {
+  static constexpr float roundoff = 1.0e-6f;  // same test scaled to single precision
+};
+
+// Reciprocal and square root.  FP64: an FP32 estimate refined by two Newton steps (4 and 5
+// FP64 FMAs instead of a ~12-instruction divide or square-root sequence); the result is within
+// an ulp or two of the correctly rounded value.  Outside the FP32 exponent range a true
+// divide / square root is used.  FP32: the hardware approximations (about 1 ulp).
+__device__ __forceinline__ double rcp(double d)
+{
+  float const f = (float)d;
+  if (!(fabsf(f) > 1e-30f && fabsf(f) < 1e30f)) return 1.0 / d;
+  double r = (double)__frcp_rn(f);
+  r        = fma(r, fma(-d, r, 1.0), r);
+  return fma(r, fma(-d, r, 1.0), r);
+}
+__device__ __forceinline__ float rcp(float d) { return __frcp_rn(d); }
+
+__device__ __forceinline__ double sqrtT(double x)
+{
+  float const f = (float)x;
+  if (!(f > 1e-30f && f < 1e30f)) return sqrt(x);
+  double y       = (double)rsqrtf(f);
+  double const h = 0.5 * x;
+  y              = y * fma(-h * y, y, 1.5);
+  y              = y * fma(-h * y, y, 1.5);
+  double const s = x * y;
+  return fma(fma(-s, s, x), 0.5 * y, s);  // final correction of the square root itself
+}
+__device__ __forceinline__ float sqrtT(float x) { return __fsqrt_rn(x); }
+
+// PPM_Single_Variable (reconstruction.h:794-901), reciprocal-multiply form.
+template <typename T>
+__device__ __forceinline__ void ppm1(T im2, T im1, T i, T ip1, T ip2, T &L_iph, T &R_imh)
+{
+  T const C2    = T(1.25);
+  T const sixth = T(1.0 / 6.0);
+  auto limit    = [&](T ci, T cim1, T iface, T s2i, T s2im1) -> T {
+    T const s2c = T(3) * (cim1 + ci - T(2) * iface);
+    T lim       = T(0);
+    if (sgnT(s2c) == sgnT(s2im1) && sgnT(s2c) == sgnT(s2i))
+      lim = sgnT(s2c) * fmin(C2 * fabs(s2im1), fmin(C2 * fabs(s2i), fabs(s2c)));
+    T const dl = iface - cim1, dr = ci - iface;
+    return (dl * dr < T(0)) ? T(0.5) * (cim1 + ci) - lim * sixth : iface;
+  };
+  T const sl    = i - im1;
+  T const sr    = ip1 - i;
+  T const sim1  = T(0.5) * (sl + (im1 - im2));
+  T const si    = T(0.5) * (sr + sl);
+  T const sip1  = T(0.5) * ((ip2 - ip1) + sr);
+  T R           = T(0.5) * (im1 + i) + (sim1 - si) * sixth;
+  T L           = T(0.5) * (i + ip1) + (si - sip1) * sixth;
+  T const d2im1 = im2 + i - T(2) * im1;
+  T const d2i   = im1 + ip1 - T(2) * i;
+  T const d2ip1 = i + ip2 - T(2) * ip1;
+  R             = limit(i, im1, R, d2i, d2im1);
+  L             = limit(ip1, i, L, d2ip1, d2i);
+  T const sfl   = i - R;
+  T const sfr   = L - i;
+  if ((sfl * sfr) <= T(0) || ((ip1 - i) * (i - im1)) <= T(0)) {
+    T const d2f = T(6) * (R + L - T(2) * i);
+    T cmax      = fmax(fmax(fmax(fabs(im2), fabs(im1)), fmax(fabs(i), fabs(ip1))), fabs(ip2));
+    T rho       = T(0);
+    if (fabs(d2f) > Eps<T>::roundoff * cmax) {
+      T d2lim = T(0);
+      if (sgnT(d2im1) == sgnT(d2i) && sgnT(d2im1) == sgnT(d2ip1) && sgnT(d2im1) == sgnT(d2f))
+        d2lim = sgnT(d2f) * fmin(fmin(C2 * fabs(d2im1), C2 * fabs(d2i)), fmin(C2 * fabs(d2ip1), fabs(d2f)));
+      rho = d2lim * rcp(d2f);
+    }
+    if (rho <= T(1) - Eps<T>::roundoff) {
+      R = i - rho * sfl;
+      L = i + rho * sfr;
+    }
+  } else {
+    if (fabs(sfl) >= T(2) * fabs(sfr)) R = i - T(2) * sfr;
+    if (fabs(sfr) >= T(2) * fabs(sfl)) L = i + T(2) * sfl;
+  }
+  L_iph = L;
+  R_imh = R;
+}
+
+// PPMC_VL for one cell (ppmc_cuda.cu:540-695), hydro characteristic projection.
+template <typename T>
+__device__ __forceinline__ void ppmc_cell(const Prim<T> &cm2, const Prim<T> &cm1, const Prim<T> &c, const Prim<T> &cp1,
+                                          const Prim<T> &cp2, int ns, int de, T gamma, Prim<T> &L, Prim<T> &R)
+{
+  T const id   = rcp(c.d);
+  T const cs   = sqrtT(gamma * c.p * id);
+  T const cs2  = cs * cs;
+  T const rcs  = rcp(cs);
+  T const h2c  = T(0.5) * rcs;        // 1 / (2 cs)
+  T const h2c2 = T(0.5) * rcs * rcs;  // 1 / (2 cs^2)
+  T const dh2c = c.d * h2c;
+  auto a0 = [&](const Prim<T> &s) { return s.p * h2c2 - dh2c * s.vn; };
+  auto a1 = [&](const Prim<T> &s) { return s.d - T(2) * s.p * h2c2; };
+  auto a4 = [&](const Prim<T> &s) { return s.p * h2c2 + dh2c * s.vn; };
+  T l0, r0, l1, r1, l2, r2, l3, r3, l4, r4;
+  ppm1(a0(cm2), a0(cm1), a0(c), a0(cp1), a0(cp2), l0, r0);
+  ppm1(a1(cm2), a1(cm1), a1(c), a1(cp1), a1(cp2), l1, r1);
+  ppm1(cm2.vt1, cm1.vt1, c.vt1, cp1.vt1, cp2.vt1, l2, r2);
+  ppm1(cm2.vt2, cm1.vt2, c.vt2, cp1.vt2, cp2.vt2, l3, r3);
+  ppm1(a4(cm2), a4(cm1), a4(c), a4(cp1), a4(cp2), l4, r4);
+  T const csid = cs * id;
+  L.d   = l0 + l1 + l4;
+  L.vn  = csid * (l4 - l0);
+  L.vt1 = l2;
+  L.vt2 = l3;
+  L.p   = cs2 * (l0 + l4);
+  R.d   = r0 + r1 + r4;
+  R.vn  = csid * (r4 - r0);
+  R.vt1 = r2;
+  R.vt2 = r3;
+  R.p   = cs2 * (r0 + r4);
+  L.ge = R.ge = T(0);
+  if (de) ppm1(cm2.ge, cm1.ge, c.ge, cp1.ge, cp2.ge, L.ge, R.ge);
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++) {
+    L.sc[k] = R.sc[k] = T(0);
+    if (k < ns) ppm1(cm2.sc[k], cm1.sc[k], c.sc[k], cp1.sc[k], cp2.sc[k], L.sc[k], R.sc[k]);
+  }
+  T const tiny = T(TINY);
+  R.d = fmax(R.d, tiny);
+  L.d = fmax(L.d, tiny);
+  R.p = fmax(R.p, tiny);
+  L.p = fmax(L.p, tiny);
+}
+
+// PLMC_cuda for one cell (plmc_cuda.cu:24-300; VL, no characteristic tracing).
+template <typename T>
+__device__ __forceinline__ void plmc_cell(const Prim<T> &cm, const Prim<T> &c, const Prim<T> &cp, int ns, int de,
+                                          T gamma, Prim<T> &L, Prim<T> &R)
+{
+  T const id   = rcp(c.d);
+  T const cs   = sqrtT(gamma * c.p * id);
+  T const cs2  = cs * cs;
+  T const rcs  = rcp(cs);
+  T const h2c  = T(0.5) * rcs;
+  T const h2c2 = T(0.5) * rcs * rcs;
+  T const dh2c = c.d * h2c;
+  auto vl      = [](T l, T r) -> T { return (l * r > T(0)) ? T(2) * l * r / (l + r) : T(0); };
+  auto mono    = [](T l, T r, T cc, T vg) -> T {
+    if (l * r > T(0)) return copysign(fmin(T(2) * fmin(fabs(l), fabs(r)), fmin(fabs(cc), fabs(vg))), cc);
+    return T(0);
+  };
+  auto chr = [&](T sd, T sn, T sp, T &b0, T &b1, T &b4) {
+    b0 = sp * h2c2 - dh2c * sn;
+    b1 = sd - T(2) * sp * h2c2;
+    b4 = sp * h2c2 + dh2c * sn;
+  };
+  T const dLd = c.d - cm.d, dRd = cp.d - c.d, dCd = T(0.5) * (cp.d - cm.d);
+  T const dLn = c.vn - cm.vn, dRn = cp.vn - c.vn, dCn = T(0.5) * (cp.vn - cm.vn);
+  T const dL1 = c.vt1 - cm.vt1, dR1 = cp.vt1 - c.vt1, dC1 = T(0.5) * (cp.vt1 - cm.vt1);
+  T const dL2 = c.vt2 - cm.vt2, dR2 = cp.vt2 - c.vt2, dC2 = T(0.5) * (cp.vt2 - cm.vt2);
+  T const dLp = c.p - cm.p, dRp = cp.p - c.p, dCp = T(0.5) * (cp.p - cm.p);
+  T L0, L1, L4, R0, R1, R4, C0, C1, C4, G0, G1, G4;
+  chr(dLd, dLn, dLp, L0, L1, L4);
+  chr(dRd, dRn, dRp, R0, R1, R4);
+  chr(dCd, dCn, dCp, C0, C1, C4);
+  chr(vl(dLd, dRd), vl(dLn, dRn), vl(dLp, dRp), G0, G1, G4);
+  T const m0 = mono(L0, R0, C0, G0), m1 = mono(L1, R1, C1, G1), m4 = mono(L4, R4, C4, G4);
+  T const m2 = mono(dL1, dR1, dC1, vl(dL1, dR1)), m3 = mono(dL2, dR2, dC2, vl(dL2, dR2));
+  T const hd = T(0.5) * (m0 + m1 + m4), hn = T(0.5) * cs * id * (m4 - m0), hp = T(0.5) * cs2 * (m0 + m4);
+  L.d = c.d + hd, R.d = c.d - hd;
+  L.vn = c.vn + hn, R.vn = c.vn - hn;
+  L.vt1 = c.vt1 + T(0.5) * m2, R.vt1 = c.vt1 - T(0.5) * m2;
+  L.vt2 = c.vt2 + T(0.5) * m3, R.vt2 = c.vt2 - T(0.5) * m3;
+  L.p = c.p + hp, R.p = c.p - hp;
+  auto lim = [](T &l, T &r, T vm, T vi, T vp) {
+    r = fmin(fmax(vi, vm), fmax(fmin(vi, vm), r));
+    l = fmin(fmax(vi, vp), fmax(fmin(vi, vp), l));
+  };
+  lim(L.d, R.d, cm.d, c.d, cp.d);
+  lim(L.vn, R.vn, cm.vn, c.vn, cp.vn);
+  lim(L.vt1, R.vt1, cm.vt1, c.vt1, cp.vt1);
+  lim(L.vt2, R.vt2, cm.vt2, c.vt2, cp.vt2);
+  lim(L.p, R.p, cm.p, c.p, cp.p);
+  L.ge = R.ge = T(0);
+  if (de) {
+    T const dL = c.ge - cm.ge, dR = cp.ge - c.ge;
+    T const h  = T(0.5) * mono(dL, dR, T(0.5) * (cp.ge - cm.ge), vl(dL, dR));
+    L.ge = c.ge + h, R.ge = c.ge - h;
+    lim(L.ge, R.ge, cm.ge, c.ge, cp.ge);
+  }
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++) {
+    L.sc[k] = R.sc[k] = T(0);
+    if (k < ns) {
+      T const dL = c.sc[k] - cm.sc[k], dR = cp.sc[k] - c.sc[k];
+      T const h  = T(0.5) * mono(dL, dR, T(0.5) * (cp.sc[k] - cm.sc[k]), vl(dL, dR));
+      L.sc[k] = c.sc[k] + h, R.sc[k] = c.sc[k] - h;
+      lim(L.sc[k], R.sc[k], cm.sc[k], c.sc[k], cp.sc[k]);
+    }
+  }
+  T const tiny = T(TINY);
+  R.d = fmax(R.d, tiny);
+  L.d = fmax(L.d, tiny);
+  R.p = fmax(R.p, tiny);
+  L.p = fmax(L.p, tiny);
+}
+
+// u / e > eta without the division, keeping the quotient's sign behaviour: the total energy
+// e of an updated cell can be negative, and then the reference's ratio test selects u when
+// u < eta * e.  e == 0 gives +inf (u > 0) or NaN (u == 0) in the quotient.
+template <typename T>
+__device__ __forceinline__ bool ratio_gt(T u, T e, T eta)
+{
+  return e > T(0) ? u > eta * e : (e < T(0) ? u < eta * e : u > T(0));
+}
+
+// Pressure a Riemann solver uses for an interface state: with dual energy the reference
+// recomputes it from the interface's conserved E and GasEnergy with Get_Pressure_From_DE
+// (hydro_utilities.h:136-151): the total-minus-kinetic pressure unless the thermal fraction
+// of E is below eta_1, then (gamma-1) * GasEnergy.
+template <typename T>
+__device__ __forceinline__ T pressure_used(const Prim<T> &s, T E, T ig1, T g1, int de)
+{
+  if (!de) return fmax(s.p, T(TINY));
+  T const eth = s.p * ig1;
+  T const p   = ratio_gt(eth, E, T(ETA_1)) ? s.p : s.d * s.ge * g1;
+  return fmax(p, T(TINY));
+}
+
+// HLLC flux (hllc_cuda.cu:19-307) from primitive interface states; f in rotated order
+// in fixed slots: 0 d, 1 m_n, 2 m_t1, 3 m_t2, 4 E, 5 GasEnergy, 6.. scalars.  Fixed slots keep
+// every register-array index a compile-time constant (no local memory).
+template <typename T>
+__device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, int ns, int de, T gamma)
+{
+  T const g1  = gamma - T(1);
+  T const ig1 = T(1) / g1;
+  T const mxl = l.d * l.vn, myl = l.d * l.vt1, mzl = l.d * l.vt2;
+  T const mxr = r.d * r.vn, myr = r.d * r.vt1, mzr = r.d * r.vt2;
+  T const El  = l.p * ig1 + T(0.5) * l.d * (l.vn * l.vn + l.vt1 * l.vt1 + l.vt2 * l.vt2);
+  T const Er  = r.p * ig1 + T(0.5) * r.d * (r.vn * r.vn + r.vt1 * r.vt1 + r.vt2 * r.vt2);
+  T const pl  = pressure_used(l, El, ig1, g1, de);
+  T const pr  = pressure_used(r, Er, ig1, g1, de);
+  T const idl = rcp(l.d), idr = rcp(r.d);
+  T const sqrtdl = sqrtT(l.d), sqrtdr = sqrtT(r.d);
+  T const isum   = rcp(sqrtdl + sqrtdr);
+  T const wl = sqrtdl * isum, wr = sqrtdr * isum;
+  T const vx  = wl * l.vn + wr * r.vn;
+  T const vy  = wl * l.vt1 + wr * r.vt1;
+  T const vz  = wl * l.vt2 + wr * r.vt2;
+  T const H   = wl * ((El + pl) * idl) + wr * ((Er + pr) * idr);
+  T const asq = g1 * (H - T(0.5) * (vx * vx + vy * vy + vz * vz));
+  T const a   = sqrtT(asq);
+  T const cfl = sqrtT(gamma * pl * idl);
+  T const cfr = sqrtT(gamma * pr * idr);
+  T const Sl  = fmin(vx - a, l.vn - cfl);
+  T const Sr  = fmax(vx + a, r.vn + cfr);
+  T const gel = l.ge, ger = r.ge;  // specific
+  if (Sl > T(0)) {
+    f[0] = mxl, f[1] = mxl * l.vn + pl, f[2] = myl * l.vn, f[3] = mzl * l.vn, f[4] = (El + pl) * l.vn;
+#pragma unroll
+    for (int k = 0; k < NS_MAX; k++)
+      if (k < ns) f[6 + k] = mxl * l.sc[k];
+    if (de) f[5] = mxl * gel;
+    return;
+  }
+  if (Sr < T(0)) {
+    f[0] = mxr, f[1] = mxr * r.vn + pr, f[2] = myr * r.vn, f[3] = mzr * r.vn, f[4] = (Er + pr) * r.vn;
+#pragma unroll
+    for (int k = 0; k < NS_MAX; k++)
+      if (k < ns) f[6 + k] = mxr * r.sc[k];
+    if (de) f[5] = mxr * ger;
+    return;
+  }
+  T const ql = l.d * (Sl - l.vn), qr = r.d * (Sr - r.vn);  // mass fluxes relative to the outer waves
+  T const Sm  = (qr * r.vn - ql * l.vn + pl - pr) * rcp(qr - ql);
+  T const ps  = ql * (Sm - l.vn) + pl;
+  T const isl = rcp(Sl - Sm), isr = rcp(Sr - Sm);
+  T const dls = ql * isl, drs = qr * isr;
+  T const mxls = (mxl * (Sl - l.vn) + ps - pl) * isl;
+  T const mxrs = (mxr * (Sr - r.vn) + ps - pr) * isr;
+  T const Els  = (El * (Sl - l.vn) - pl * l.vn + ps * Sm) * isl;
+  T const Ers  = (Er * (Sr - r.vn) - pr * r.vn + ps * Sm) * isr;
+  T const aSm = fabs(Sm);
+  T const cr = Sr - aSm, cl = Sl + aSm;
+  // f = 0.5 * (F_L + F_R + (Sr-|Sm|) U*_R + (Sl+|Sm|) U*_L - Sl U_L - Sr U_R)  (Batten eq. 27)
+  f[0] = T(0.5) * (mxl + mxr + cr * drs + cl * dls - Sl * l.d - Sr * r.d);
+  f[1] = T(0.5) * (mxl * l.vn + pl + mxr * r.vn + pr + cr * mxrs + cl * mxls - Sl * mxl - Sr * mxr);
+  f[2] = T(0.5) * (myl * l.vn + myr * r.vn + cr * drs * r.vt1 + cl * dls * l.vt1 - Sl * myl - Sr * myr);
+  f[3] = T(0.5) * (mzl * l.vn + mzr * r.vn + cr * drs * r.vt2 + cl * dls * l.vt2 - Sl * mzl - Sr * mzr);
+  f[4] = T(0.5) * ((El + pl) * l.vn + (Er + pr) * r.vn + cr * Ers + cl * Els - Sl * El - Sr * Er);
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++) {
+    if (k < ns) {
+      T const ul = l.d * l.sc[k], ur = r.d * r.sc[k];
+      f[6 + k]   = T(0.5) * (ul * l.vn + ur * r.vn + cr * drs * r.sc[k] + cl * dls * l.sc[k] - Sl * ul - Sr * ur);
+    }
+  }
+  if (de) {
+    T const ul = l.d * gel, ur = r.d * ger;
+    f[5]  = T(0.5) * (ul * l.vn + ur * r.vn + cr * drs * ger + cl * dls * gel - Sl * ul - Sr * ur);
+  }
+}
+
+// Roe flux with the HLLE fallback (roe_cuda.cu:19-400) from primitive interface states.
+template <typename T>
+__device__ __forceinline__ void roe(const Prim<T> &l, const Prim<T> &r, T *f, int ns, int de, T gamma)
+{
+  T const g1  = gamma - T(1);
+  T const ig1 = T(1) / g1;
+  T const dl = l.d, dr = r.d, vxl = l.vn, vyl = l.vt1, vzl = l.vt2, vxr = r.vn, vyr = r.vt1, vzr = r.vt2;
+  T const mxl = dl * vxl, myl = dl * vyl, mzl = dl * vzl, mxr = dr * vxr, myr = dr * vyr, mzr = dr * vzr;
+  T const El  = l.p * ig1 + T(0.5) * dl * (vxl * vxl + vyl * vyl + vzl * vzl);
+  T const Er  = r.p * ig1 + T(0.5) * dr * (vxr * vxr + vyr * vyr + vzr * vzr);
+  T const pl  = pressure_used(l, El, ig1, g1, de);
+  T const pr  = pressure_used(r, Er, ig1, g1, de);
+  T const idl = rcp(dl), idr = rcp(dr);
+  T const sqrtdl = sqrtT(dl), sqrtdr = sqrtT(dr);
+  T const isum   = rcp(sqrtdl + sqrtdr);
+  T const wl = sqrtdl * isum, wr = sqrtdr * isum;
+  T const vx = wl * vxl + wr * vxr, vy = wl * vyl + wr * vyr, vz = wl * vzl + wr * vzr;
+  T const H   = wl * ((El + pl) * idl) + wr * ((Er + pr) * idr);
+  T const vsq = vx * vx + vy * vy + vz * vz;
+  T const asq = g1 * fmax(H - T(0.5) * vsq, T(TINY));
+  T const a   = sqrtT(asq);
+  T const lm = vx - a, l0 = vx, lp = vx + a;
+  T fdl = mxl, fmxl = mxl * vxl + pl, fmyl = mxl * vyl, fmzl = mxl * vzl, fEl = (El + pl) * vxl;
+  T fdr = mxr, fmxr = mxr * vxr + pr, fmyr = mxr * vyr, fmzr = mxr * vzr, fEr = (Er + pr) * vxr;
+  if (lm >= T(0)) {
+    f[0] = fdl, f[1] = fmxl, f[2] = fmyl, f[3] = fmzl, f[4] = fEl;
+#pragma unroll
+    for (int k = 0; k < NS_MAX; k++)
+      if (k < ns) f[6 + k] = mxl * l.sc[k];
+    if (de) f[5] = mxl * l.ge;
+    return;
+  }
+  if (lp <= T(0)) {
+    f[0] = fdr, f[1] = fmxr, f[2] = fmyr, f[3] = fmzr, f[4] = fEr;
+#pragma unroll
+    for (int k = 0; k < NS_MAX; k++)
+      if (k < ns) f[6 + k] = mxr * r.sc[k];
+    if (de) f[5] = mxr * r.ge;
+    return;
+  }
+  T const dd = dr - dl, dmx = mxr - mxl, dmy = myr - myl, dmz = mzr - mzl, dE = Er - El;
+  T const iasq = rcp(asq);
+  T const Na   = T(0.5) * iasq;
+  T const a0 = Na * (dd * (T(0.5) * g1 * vsq + vx * a) - dmx * (g1 * vx + a) - g1 * (dmy * vy + dmz * vz) + dE * g1);
+  T const a1 = dmy - dd * vy;
+  T const a2 = dmz - dd * vz;
+  T const a3 = dd * (T(1) - Na * g1 * vsq) + g1 * iasq * (dmx * vx + dmy * vy + dmz * vz - dE);
+  T const a4 = Na * (dd * (T(0.5) * g1 * vsq - vx * a) - dmx * (g1 * vx - a) - g1 * (dmy * vy + dmz * vz) + dE * g1);
+  T const c0 = a0 * fabs(lm), c1 = a1 * fabs(l0), c2 = a2 * fabs(l0), c3 = a3 * fabs(l0), c4 = a4 * fabs(lp);
+  T const s0 = c0 + c3 + c4;
+  T const s1 = c0 * (vx - a) + c3 * vx + c4 * (vx + a);
+  T const s2 = c0 * vy + c1 + c3 * vy + c4 * vy;
+  T const s3 = c0 * vz + c2 + c3 * vz + c4 * vz;
+  T const s4 = c0 * (H - vx * a) + c1 * vy + c2 * vz + c3 * T(0.5) * vsq + c4 * (H + vx * a);
+  bool hlle = false;
+  T t0 = dl + a0, t1 = mxl + a0 * (vx - a), t2 = myl + a0 * vy, t3 = mzl + a0 * vz, t4 = El + a0 * (H - vx * a);
+  if (l0 > lm) {
+    if (t0 <= T(0)) hlle = true;
+    if (t4 - T(0.5) * (t1 * t1 + t2 * t2 + t3 * t3) / t0 < T(0)) hlle = true;
+  }
+  t0 += a3 + a4;
+  t1 += a3 * vx;
+  t2 += a1 + a3 * vy;
+  t3 += a2 + a3 * vz;
+  t4 += a1 * vy + a2 * vz + a3 * T(0.5) * vsq;
+  if (lp > l0) {
+    if (t0 <= T(0)) hlle = true;
+    if (t4 - T(0.5) * (t1 * t1 + t2 * t2 + t3 * t3) / t0 < T(0)) hlle = true;
+  }
+  if (hlle) {
+    T const cfl = sqrtT(gamma * pl * idl), cfr = sqrtT(gamma * pr * idr);
+    T const bm = fmin(fmin(lm, vxl - cfl), T(0)), bp = fmax(fmax(lp, vxr + cfr), T(0));
+    T const tmp = T(0.5) * (bp + bm) / (bp - bm);
+    auto hl = [&](T fl, T fr) { return T(0.5) * (fl + fr) + (fl - fr) * tmp; };
+    f[0] = hl(mxl - bm * dl, mxr - bp * dr);
+    f[1] = hl(mxl * (vxl - bm) + pl, mxr * (vxr - bp) + pr);
+    f[2] = hl(myl * (vxl - bm), myr * (vxr - bp));
+    f[3] = hl(mzl * (vxl - bm), mzr * (vxr - bp));
+    f[4] = hl(El * (vxl - bm) + pl * vxl, Er * (vxr - bp) + pr * vxr);
+#pragma unroll
+    for (int k = 0; k < NS_MAX; k++)
+      if (k < ns) f[6 + k] = hl(dl * l.sc[k] * (vxl - bm), dr * r.sc[k] * (vxr - bp));
+    if (de) f[5] = hl(dl * l.ge * (vxl - bm), dr * r.ge * (vxr - bp));
+    return;
+  }
+  f[0] = T(0.5) * (fdl + fdr - s0);
+  f[1] = T(0.5) * (fmxl + fmxr - s1);
+  f[2] = T(0.5) * (fmyl + fmyr - s2);
+  f[3] = T(0.5) * (fmzl + fmzr - s3);
+  f[4] = T(0.5) * (fEl + fEr - s4);
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++)
+    if (k < ns) f[6 + k] = f[0] * ((f[0] >= T(0)) ? l.sc[k] : r.sc[k]);
+  if (de) f[5] = f[0] * ((f[0] >= T(0)) ? l.ge : r.ge);
+}
+
+}  // namespace hf
+}  // namespace cgb

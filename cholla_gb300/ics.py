@@ -26,7 +26,7 @@ def gaussian_random_field(n: int, slope: float, rng: np.random.Generator) -> np.
     nz = kk > 0
     amp[nz] = kk[nz] ** (slope / 2.0)
     noise = rng.standard_normal((n, n, n))
-    f = np.fft.irfftn(np.fft.rfftn(noise) * amp, s=(n, n, n))
+    f = np.fft.irfftn(np.fft.rfftn(noise) * amp, s=(n, n, n), axes=(0, 1, 2))
     f -= f.mean()
     f /= f.std()
     return f

@@ -31,7 +31,7 @@ def _ptr(a) -> int:
 
 _RECON = {"PCM": L.PCM, "PLMC": L.PLMC, "PPMC": L.PPMC}
 _SOLVER = {"HLLC": L.HLLC, "ROE": L.ROE, "HLLD": L.HLLD}
-_PREC = {"fp64": L.FP64, "mixed": L.MIXED}
+_PREC = {"fp64": L.FP64, "mixed": L.MIXED, "fp64_fast": L.FP64_FAST}
 
 
 @dataclass

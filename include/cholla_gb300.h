@@ -40,8 +40,9 @@ extern "C" {
 #define CGB_ROE  1
 #define CGB_HLLD 2
 /* arithmetic */
-#define CGB_FP64  0 /* FP64 in the reference's operation order: bit-exact with its -fmad=false build */
-#define CGB_MIXED 1 /* FP32 reconstruction and fluxes, FP64 state accumulation, energy recovery and dt */
+#define CGB_FP64      0 /* FP64 in the reference's operation order: bit-exact with its -fmad=false build */
+#define CGB_MIXED     1 /* FP32 reconstruction and fluxes, FP64 state accumulation, energy recovery and dt */
+#define CGB_FP64_FAST 2 /* FP64 with reciprocal forms, per-cell primitives and FMA (not bit-exact) */
 
 typedef struct {
   int reconstruction;    /* CGB_PCM / CGB_PLMC / CGB_PPMC */
@@ -105,6 +106,33 @@ int cgb_set_boundaries(double *d_conserved, int nx, int ny, int nz, int n_ghost,
  * (src/mhd/magnetic_divergence.cu:33-76); writes the value to *max_divb (host). */
 int cgb_max_magnetic_divergence(const double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields,
                                 double dx, double dy, double dz, double *max_divb);
+
+/* ---- box handles: device-resident stepping of many boxes (no counterpart in the reference,
+ * which can hold one box shape per process: its scratch is file-scope globals) ---- */
+typedef struct cgb_box cgb_box;
+
+/* Create a box of padded size nx*ny*nz (ny = nz = 1 for 1D) with its own scratch.
+ * flags[6]: boundary flags as in cgb_set_boundaries, applied before every step. */
+int cgb_box_create(cgb_box **box, int nx, int ny, int nz, int n_ghost, double dx, double dy, double dz,
+                   const cgb_scheme *scheme, const int flags[6]);
+int cgb_box_destroy(cgb_box *box);
+int cgb_box_n_fields(const cgb_box *box);
+/* Set the simulation time and the end time dt is clamped to (t_end <= 0: no clamp). */
+int cgb_box_set_time(cgb_box *box, double t, double t_end);
+/* Replay each step from a captured CUDA graph (needs a non-default stream). */
+int cgb_box_use_graph(cgb_box *box, int enable);
+/* Record per-kernel times with events on the launching stream (no extra synchronisation;
+ * graph replay is off while timing). */
+int cgb_box_enable_timing(cgb_box *box, int enable);
+/* Summed predictor / corrector / finalize milliseconds and the number of timed steps. */
+int cgb_box_kernel_times(cgb_box *box, double ms[3], long long *steps);
+/* Advance n_steps: ghost fill, dt = c_cfl / max inverse crossing time of the current state
+ * (clamped to t_end), VL step, temperature floor, CFL reduction for the next step.  The time
+ * step never leaves the device; nothing synchronises with the host. */
+int cgb_box_advance(cgb_box *box, double *d_conserved, int n_steps, double c_cfl, void *stream);
+/* Current time and last dt (synchronises the last stream used with the box). */
+int cgb_box_get_time(cgb_box *box, double *t, double *dt_last);
+const char *cgb_box_last_error(void);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,39 @@
+#!/usr/bin/env bash
+# Compile the reference's own hot-path CUDA kernels (unchanged, from the cholla source tree)
+# into device-only cubins under oracle/_ref/<variant>/, with the reference Makefile's device
+# flags (Makefile:70,148: -O3 -std=c++17 --expt-extended-lambda -fmad=false) for sm_103a.
+# The cubins are test infrastructure: oracle/ref_harness.cpp loads them with the CUDA driver
+# API to run the reference's VL step on the GPU as the parity and speed baseline.
+# Usage: oracle/build_ref.sh /path/to/cholla
+set -euo pipefail
+REF=${1:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+NVCC=${NVCC:-nvcc}
+FLAGS="-O3 -std=c++17 --expt-extended-lambda -fmad=false -gencode arch=compute_103a,code=sm_103a -cubin -I$REF/src"
+COMMON="-DVL -DPRECISION=2 -DDENSITY_FLOOR -DTEMPERATURE_FLOOR"
+declare -A DEFS=(
+  [hydro_ppmc_hllc_de]="$COMMON -DPPMC -DHLLC -DDE"
+  [hydro_ppmc_hllc]="$COMMON -DPPMC -DHLLC"
+  [hydro_plmc_hllc]="$COMMON -DPLMC -DHLLC"
+  [hydro_ppmc_roe_de]="$COMMON -DPPMC -DROE -DDE"
+  [mhd_plmc_hlld]="$COMMON -DPLMC -DHLLD -DMHD"
+)
+declare -A FILES=(
+  [hydro]="integrators/VL_3D_cuda.cu integrators/VL_1D_cuda.cu hydro/hydro_cuda.cu reconstruction/pcm_cuda.cu reconstruction/ppmc_cuda.cu reconstruction/plmc_cuda.cu riemann_solvers/hllc_cuda.cu riemann_solvers/roe_cuda.cu grid/cuda_boundaries.cu"
+  [mhd]="integrators/VL_3D_cuda.cu hydro/hydro_cuda.cu reconstruction/pcm_cuda.cu reconstruction/plmc_cuda.cu riemann_solvers/hlld_cuda.cu mhd/ct_electric_fields.cu mhd/magnetic_update.cu mhd/magnetic_divergence.cu grid/cuda_boundaries.cu"
+)
+pids=()
+for v in "${!DEFS[@]}"; do
+  mkdir -p "$OUT/$v"
+  kind=${v%%_*}
+  for f in ${FILES[$kind]}; do
+    o="$OUT/$v/$(basename "$f" .cu).cubin"
+    if [[ ! -f "$o" || "$REF/src/$f" -nt "$o" || "$0" -nt "$o" ]]; then
+      $NVCC $FLAGS ${DEFS[$v]} "$REF/src/$f" -o "$o" &
+      pids+=($!)
+    fi
+  done
+done
+for p in "${pids[@]}"; do wait "$p"; done
+echo "reference cubins in $OUT"

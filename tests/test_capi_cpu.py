@@ -89,3 +89,33 @@ def test_product_has_no_oracle_dependency():
         if p.suffix in (".py", ".cu", ".cuh", ".h", ".cpp"):
             text = p.read_text()
             assert "oracle" not in re.sub(r"#.*|//.*", "", text).lower() or p.name == "build.py", p
+
+
+def test_dropin_shim_exports_the_reference_symbols(tmp_path):
+    """cholla_gb300/dropin/cholla_dropin.cpp compiles against the C ABI header and defines the
+    reference's integrator entry points under their C++ (Itanium-mangled) names, so a Cholla
+    build links it in place of src/integrators/VL_3D_cuda.cu and VL_1D_cuda.cu."""
+    import shutil
+    import subprocess
+
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ not available")
+    obj = tmp_path / "dropin.o"
+    subprocess.run([cxx, "-std=c++17", "-c", "-DPPMC", "-DHLLC", "-DDE", "-DDENSITY_FLOOR", "-DTEMPERATURE_FLOOR",
+                    "-I", str(ROOT / "include"), str(ROOT / "cholla_gb300" / "dropin" / "cholla_dropin.cpp"), "-o",
+                    str(obj)], check=True)
+    out = subprocess.run(["nm", str(obj)], capture_output=True, text=True, check=True).stdout
+    defined = {ln.split()[-1] for ln in out.splitlines() if " T " in ln}
+    # VL_3D_cuda.h:9-13, VL_1D_cuda.h, hydro_cuda.h:69-70 and :90 with Real = double
+    expected = {
+        "_Z20VL_Algorithm_3D_CUDAPdS_iiiiiiidddddddiidS_",
+        "_Z17Free_Memory_VL_3Dv",
+        "_Z20VL_Algorithm_1D_CUDAPdiiidddii",
+        "_Z17Free_Memory_VL_1Dv",
+        "_Z11Calc_dt_GPUPdiiiiidddd",
+        "_Z23Apply_Temperature_FloorPdiiiiid",
+    }
+    assert expected <= defined, expected - defined
+    undefined = {ln.split()[-1] for ln in out.splitlines() if " U " in ln}
+    assert "gama" in undefined  # taken from the host code's global adiabatic index

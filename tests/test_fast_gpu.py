@@ -1,0 +1,140 @@
+"""The throughput arithmetic paths against the oracle, by tolerance (they are not bit-exact).
+
+fast FP64 (CGB_FP64_FAST): relative L1 error of every field <= 1e-12 after one step, and
+after 20 steps of the turbulence box within 10x of the oracle's own one-ULP drift.  Mixed precision (CGB_MIXED): relative L1 density
+error <= 1e-5 after 20 steps (the accuracy target of the mixed-precision form), per-field
+errors printed.  Relative L1 = sum|gpu - oracle| / sum|oracle| over real cells.
+"""
+import numpy as np
+import pytest
+
+from helpers import real_slice
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ["density", "momentum_x", "momentum_y", "momentum_z", "Energy", "GasEnergy"]
+
+
+def rel_l1(got, want, ng):
+    g, w = got[real_slice(ng)], want[real_slice(ng)]
+    return np.abs(g - w).sum(axis=(1, 2, 3)) / np.abs(w).sum(axis=(1, 2, 3))
+
+
+def _run_pair(cuda, oracle_lib, U0, ng, scheme, steps, dx):
+    from cholla_gb300 import integrator as I
+
+    o = oracle_lib
+    nf, nz, ny, nx = U0.shape
+    I.set_scheme(scheme)
+    Ug = cuda.from_numpy(U0.copy()).cuda()
+    Uo = U0.copy()
+    cfg = o.config(nx, ny, nz, ng, nf, de=scheme.dual_energy,
+                   recon={"PCM": o.PCM, "PLMC": o.PLMC, "PPMC": o.PPMC}[scheme.reconstruction],
+                   solver={"HLLC": o.HLLC, "ROE": o.ROE}[scheme.riemann_solver], gamma=scheme.gamma,
+                   dx=dx[0], dy=dx[1], dz=dx[2])
+    for _ in range(steps):
+        dt = 0.3 / o.calc_dt(cfg, Uo.reshape(-1))  # same dt sequence for both (the oracle's)
+        I.VL_Algorithm_3D_CUDA(Ug, None, nx, ny, nz, 0, 0, 0, ng, *dx, 0, 0, 0, dt, nf, 0, 0.0)
+        I.Set_Boundaries(Ug, nx, ny, nz, ng, nf, (1,) * 6)
+        o.vl_step_3d(cfg, Uo.reshape(-1), dt)
+        o.set_boundaries(cfg, Uo.reshape(-1), (1,) * 6)
+    return Ug.cpu().numpy(), Uo
+
+
+@pytest.mark.parametrize("recon", ["PCM", "PLMC", "PPMC"])
+@pytest.mark.parametrize("solver", ["HLLC", "ROE"])
+def test_fast_fp64_one_step(cuda, oracle_lib, recon, solver):
+    from cholla_gb300 import ics
+    from cholla_gb300 import integrator as I
+
+    ng = {"PCM": 2, "PLMC": 3, "PPMC": 4}[recon]
+    U0 = ics.smooth_random_box((19, 13, 11), ng, np.random.default_rng(7), dual_energy=True)
+    s = I.Scheme(reconstruction=recon, riemann_solver=solver, dual_energy=True, precision="fp64_fast")
+    got, want = _run_pair(cuda, oracle_lib, U0, ng, s, 1, (1 / 19, 1 / 13, 1 / 11))
+    err = rel_l1(got, want, ng)
+    assert np.all(err <= 1e-12), dict(zip(FIELDS, err))
+
+
+def _oracle_ulp_drift(oracle_lib, U0, ng, dx, steps):
+    """Relative L1 drift, per field, of the oracle's own trajectory after `steps` steps when
+    every initial density is moved by one ULP: the scheme's sensitivity to roundoff."""
+    o = oracle_lib
+    nf, nz, ny, nx = U0.shape
+    cfg = o.config(nx, ny, nz, ng, nf, de=True, recon=o.PPMC, solver=o.HLLC, gamma=5 / 3, dx=dx, dy=dx, dz=dx)
+    A, B = U0.copy(), U0.copy()
+    B[0] = np.nextafter(B[0], np.inf)
+    for _ in range(steps):
+        dt = 0.3 / o.calc_dt(cfg, A.reshape(-1))
+        for X in (A, B):
+            o.vl_step_3d(cfg, X.reshape(-1), dt)
+            o.set_boundaries(cfg, X.reshape(-1), (1,) * 6)
+    return rel_l1(B, A, ng)
+
+
+def test_fast_fp64_turbulence_20_steps(cuda, oracle_lib):
+    """20 steps of the rms-Mach-2 turbulence box.  The dual-energy scheme amplifies roundoff:
+    a one-ULP change of the initial densities alone moves the oracle's own result by ~1e-10
+    relative L1 after 20 steps, so no arithmetic that is not bit-identical can stay at 1e-12
+    there.  The fast FP64 form must stay within 10x of that one-ULP drift in every field (it
+    stays within 1e-12 after one step, test_fast_fp64_one_step)."""
+    from cholla_gb300 import ics
+    from cholla_gb300 import integrator as I
+
+    n, ng = 32, 4
+    U0 = ics.turbulence_box(n, ng, 5 / 3, seed=4)
+    s = I.Scheme(reconstruction="PPMC", riemann_solver="HLLC", dual_energy=True, precision="fp64_fast")
+    got, want = _run_pair(cuda, oracle_lib, U0, ng, s, 20, (1 / n,) * 3)
+    err = rel_l1(got, want, ng)
+    drift = _oracle_ulp_drift(oracle_lib, U0, ng, 1 / n, 20)
+    print("fp64_fast", {f: f"{e:.2e} (1-ulp drift {d:.2e})" for f, e, d in zip(FIELDS, err, drift)})
+    assert np.isfinite(got).all()
+    assert np.all(err <= 10 * np.maximum(drift, 1e-13)), dict(zip(FIELDS, err))
+
+
+def test_mixed_turbulence_20_steps(cuda, oracle_lib):
+    """Mixed precision on the same box: relative L1 density error <= 1e-5 after 20 steps,
+    the accuracy target of the mixed-precision form; per-field errors printed."""
+    from cholla_gb300 import ics
+    from cholla_gb300 import integrator as I
+
+    n, ng = 32, 4
+    U0 = ics.turbulence_box(n, ng, 5 / 3, seed=4)
+    s = I.Scheme(reconstruction="PPMC", riemann_solver="HLLC", dual_energy=True, precision="mixed")
+    got, want = _run_pair(cuda, oracle_lib, U0, ng, s, 20, (1 / n,) * 3)
+    err = rel_l1(got, want, ng)
+    print("mixed", {f: f"{e:.2e}" for f, e in zip(FIELDS, err)})
+    assert np.isfinite(got).all()
+    assert err[0] <= 1e-5, dict(zip(FIELDS, err))
+
+
+def test_engine_matches_dropin_sequence_bitwise(cuda):
+    """The box engine (device-side dt, fused floor + CFL reduction, CUDA-graph replay) gives
+    the same state, bit for bit, as the drop-in call sequence of the reference's main loop."""
+    from cholla_gb300 import ics
+    from cholla_gb300 import integrator as I
+    from cholla_gb300.engine import Box
+
+    n, ng, gamma = 32, 4, 5 / 3
+    U0 = ics.turbulence_box(n, ng, gamma, seed=6)
+    nf, N = U0.shape[0], U0.shape[1]
+    dx = 1 / n
+    s = I.Scheme(reconstruction="PPMC", riemann_solver="HLLC", dual_energy=True, temperature_floor=True)
+    I.set_scheme(s)
+    Ua = cuda.from_numpy(U0.copy()).cuda()
+    for _ in range(6):
+        I.Set_Boundaries(Ua, N, N, N, ng, nf, (1,) * 6)
+        dt = 0.3 / I.Calc_dt_GPU(Ua, N, N, N, ng, nf, dx, dx, dx, gamma)
+        I.VL_Algorithm_3D_CUDA(Ua, None, N, N, N, 0, 0, 0, ng, dx, dx, dx, 0, 0, 0, dt, nf, 0, 0.0)
+        I.Apply_Temperature_Floor(Ua, N, N, N, ng, nf, 0.0)
+    stream = cuda.cuda.Stream()
+    for graph in (False, True):
+        Ub = cuda.from_numpy(U0.copy()).cuda()
+        box = Box(N, N, N, ng, dx, dx, dx, s)
+        box.use_graph(graph)
+        box.advance(Ub, 6, 0.3, stream)
+        stream.synchronize()
+        t, dt_last = box.time()
+        a, b = Ua.cpu().numpy()[real_slice(ng)], Ub.cpu().numpy()[real_slice(ng)]
+        assert (a.view(np.int64) == b.view(np.int64)).all(), f"graph={graph}"
+        assert t > 0 and dt_last > 0
+        box.close()
