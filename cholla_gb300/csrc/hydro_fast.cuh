@@ -8,6 +8,8 @@
 // multiply-adds are allowed.  T is the compute type: double for the fast FP64 path (agrees
 // with the reference to ~1e-14 relative per step), float for the mixed-precision path.
 #pragma once
+#include <type_traits>
+
 #include "common.cuh"
 
 namespace cgb
@@ -115,21 +117,79 @@ __device__ __forceinline__ void ppm1(T im2, T im1, T i, T ip1, T ip2, T &L_iph, 
   R_imh = R;
 }
 
-// PPMC_VL for one cell (ppmc_cuda.cu:540-695), hydro characteristic projection.
+template <typename T>
+__device__ __forceinline__ Prim<double> widen(const Prim<T> &s)
+{
+  Prim<double> w;
+  w.d = s.d, w.vn = s.vn, w.vt1 = s.vt1, w.vt2 = s.vt2, w.p = s.p, w.ge = s.ge;
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++) w.sc[k] = s.sc[k];
+  return w;
+}
+__device__ __forceinline__ Prim<float> narrow(const Prim<double> &s)
+{
+  Prim<float> w;
+  w.d = (float)s.d, w.vn = (float)s.vn, w.vt1 = (float)s.vt1, w.vt2 = (float)s.vt2, w.p = (float)s.p;
+  w.ge = (float)s.ge;
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++) w.sc[k] = (float)s.sc[k];
+  return w;
+}
+
+template <typename T>
+__device__ __forceinline__ void ppmc_cell(const Prim<T> &cm2, const Prim<T> &cm1, const Prim<T> &c, const Prim<T> &cp1,
+                                          const Prim<T> &cp2, int ns, int de, T gamma, Prim<T> &L, Prim<T> &R);
+template <typename T>
+__device__ __forceinline__ void plmc_cell(const Prim<T> &cm, const Prim<T> &c, const Prim<T> &cp, int ns, int de,
+                                          T gamma, Prim<T> &L, Prim<T> &R);
+
+constexpr bool kWideFallback = true;
+
+// FP64 evaluation of a cell's reconstruction for the single-precision path.  The
+// characteristic variables carry +-d (vn - vref) / (2 cs) terms that cancel when the
+// primitives are formed again, so in FP32 a cell whose normal-velocity differences across the
+// stencil exceed ~32 sound speeds (cold or near-vacuum gas) would lose most of its digits.
+__device__ __noinline__ void ppmc_cell_wide(const Prim<float> &cm2, const Prim<float> &cm1, const Prim<float> &c,
+                                            const Prim<float> &cp1, const Prim<float> &cp2, int ns, int de,
+                                            float gamma, Prim<float> &L, Prim<float> &R)
+{
+  Prim<double> l, r;
+  ppmc_cell<double>(widen(cm2), widen(cm1), widen(c), widen(cp1), widen(cp2), ns, de, (double)gamma, l, r);
+  L = narrow(l), R = narrow(r);
+}
+__device__ __noinline__ void plmc_cell_wide(const Prim<float> &cm, const Prim<float> &c, const Prim<float> &cp, int ns,
+                                            int de, float gamma, Prim<float> &L, Prim<float> &R)
+{
+  Prim<double> l, r;
+  plmc_cell<double>(widen(cm), widen(c), widen(cp), ns, de, (double)gamma, l, r);
+  L = narrow(l), R = narrow(r);
+}
+
+// PPMC_VL for one cell (ppmc_cuda.cu:540-695), hydro characteristic projection.  In FP32 the
+// projection is taken in the frame of the cell's own normal velocity (PPM is equivariant under
+// a common shift of its five inputs), which removes the bulk-flow part of the cancellation.
 template <typename T>
 __device__ __forceinline__ void ppmc_cell(const Prim<T> &cm2, const Prim<T> &cm1, const Prim<T> &c, const Prim<T> &cp1,
                                           const Prim<T> &cp2, int ns, int de, T gamma, Prim<T> &L, Prim<T> &R)
 {
   T const id   = rcp(c.d);
   T const cs   = sqrtT(gamma * c.p * id);
+  if constexpr (std::is_same<T, float>::value && kWideFallback) {
+    T const dv = fmax(fmax(fabs(cm2.vn - c.vn), fabs(cm1.vn - c.vn)), fmax(fabs(cp1.vn - c.vn), fabs(cp2.vn - c.vn)));
+    if (!(dv <= T(32) * cs)) {
+      ppmc_cell_wide(cm2, cm1, c, cp1, cp2, ns, de, gamma, L, R);
+      return;
+    }
+  }
+  T const vref = std::is_same<T, float>::value ? c.vn : T(0);
   T const cs2  = cs * cs;
   T const rcs  = rcp(cs);
   T const h2c  = T(0.5) * rcs;        // 1 / (2 cs)
   T const h2c2 = T(0.5) * rcs * rcs;  // 1 / (2 cs^2)
   T const dh2c = c.d * h2c;
-  auto a0 = [&](const Prim<T> &s) { return s.p * h2c2 - dh2c * s.vn; };
+  auto a0 = [&](const Prim<T> &s) { return s.p * h2c2 - dh2c * (s.vn - vref); };
   auto a1 = [&](const Prim<T> &s) { return s.d - T(2) * s.p * h2c2; };
-  auto a4 = [&](const Prim<T> &s) { return s.p * h2c2 + dh2c * s.vn; };
+  auto a4 = [&](const Prim<T> &s) { return s.p * h2c2 + dh2c * (s.vn - vref); };
   T l0, r0, l1, r1, l2, r2, l3, r3, l4, r4;
   ppm1(a0(cm2), a0(cm1), a0(c), a0(cp1), a0(cp2), l0, r0);
   ppm1(a1(cm2), a1(cm1), a1(c), a1(cp1), a1(cp2), l1, r1);
@@ -138,12 +198,12 @@ __device__ __forceinline__ void ppmc_cell(const Prim<T> &cm2, const Prim<T> &cm1
   ppm1(a4(cm2), a4(cm1), a4(c), a4(cp1), a4(cp2), l4, r4);
   T const csid = cs * id;
   L.d   = l0 + l1 + l4;
-  L.vn  = csid * (l4 - l0);
+  L.vn  = csid * (l4 - l0) + vref;
   L.vt1 = l2;
   L.vt2 = l3;
   L.p   = cs2 * (l0 + l4);
   R.d   = r0 + r1 + r4;
-  R.vn  = csid * (r4 - r0);
+  R.vn  = csid * (r4 - r0) + vref;
   R.vt1 = r2;
   R.vt2 = r3;
   R.p   = cs2 * (r0 + r4);
@@ -168,6 +228,12 @@ __device__ __forceinline__ void plmc_cell(const Prim<T> &cm, const Prim<T> &c, c
 {
   T const id   = rcp(c.d);
   T const cs   = sqrtT(gamma * c.p * id);
+  if constexpr (std::is_same<T, float>::value && kWideFallback) {
+    if (!(fmax(fabs(c.vn - cm.vn), fabs(cp.vn - c.vn)) <= T(32) * cs)) {
+      plmc_cell_wide(cm, c, cp, ns, de, gamma, L, R);
+      return;
+    }
+  }
   T const cs2  = cs * cs;
   T const rcs  = rcp(cs);
   T const h2c  = T(0.5) * rcs;
@@ -282,8 +348,16 @@ __device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, i
   T const a   = sqrtT(asq);
   T const cfl = sqrtT(gamma * pl * idl);
   T const cfr = sqrtT(gamma * pr * idr);
-  T const Sl  = fmin(vx - a, l.vn - cfl);
-  T const Sr  = fmax(vx + a, r.vn + cfr);
+  // outer wave speeds relative to each side's own velocity, kept apart from the velocity so a
+  // cold side's sound speed is not rounded away (FP32: cf ~1e-10 against v ~1)
+  T dSl, dSr, Sl, Sr;
+  if constexpr (std::is_same<T, float>::value) {
+    dSl = fmin((vx - a) - l.vn, -cfl), dSr = fmax((vx + a) - r.vn, cfr);
+    Sl = l.vn + dSl, Sr = r.vn + dSr;
+  } else {
+    Sl = fmin(vx - a, l.vn - cfl), Sr = fmax(vx + a, r.vn + cfr);
+    dSl = Sl - l.vn, dSr = Sr - r.vn;
+  }
   T const gel = l.ge, ger = r.ge;  // specific
   if (Sl > T(0)) {
     f[0] = mxl, f[1] = mxl * l.vn + pl, f[2] = myl * l.vn, f[3] = mzl * l.vn, f[4] = (El + pl) * l.vn;
@@ -301,8 +375,35 @@ __device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, i
     if (de) f[5] = mxr * ger;
     return;
   }
-  T const ql = l.d * (Sl - l.vn), qr = r.d * (Sr - r.vn);  // mass fluxes relative to the outer waves
+  T const ql = l.d * dSl, qr = r.d * dSr;  // mass fluxes relative to the outer waves
   T const Sm  = (qr * r.vn - ql * l.vn + pl - pr) * rcp(qr - ql);
+  if (std::is_same<T, float>::value) {
+    // Single precision: the same flux in the one-sided form F*K = FK + SK (U*K - UK) (K = L
+    // when Sm >= 0, else R; Batten's symmetric sum below equals it exactly), with U*K - UK
+    // written without cancellation as k (1, SK, vt1, vt2, (EK + pK)/dK + (SK - vK) Sm, ...),
+    // k = SK (Sm - vK) / (SK - Sm).  The symmetric sum subtracts terms of the size of the
+    // wave speeds, which a near-vacuum interface state (density floored at TINY) makes ~1e9,
+    // and that cancellation costs every significant digit in FP32.
+    bool const lft = Sm >= T(0);
+    Prim<T> const &K = lft ? l : r;
+    T const SK = lft ? Sl : Sr, EK = lft ? El : Er, pK = lft ? pl : pr;
+    // SK - Sm from the separated parts; it is negative on the left and positive on the right,
+    // and only rounding of a degenerate (both sides cold) interface can bring it to zero
+    T const gap = (lft ? dSl : dSr) - (Sm - K.vn);
+    T const den = lft ? fmin(gap, T(-1e-30)) : fmax(gap, T(1e-30));
+    T const k   = SK * (Sm - K.vn) * rcp(den);
+    T const vk = K.vn + k;
+    f[0] = K.d * vk;
+    f[1] = K.d * (K.vn * K.vn + k * SK) + pK;
+    f[2] = K.d * K.vt1 * vk;
+    f[3] = K.d * K.vt2 * vk;
+    f[4] = (EK + pK) * vk + k * K.d * (SK - K.vn) * Sm;
+#pragma unroll
+    for (int q = 0; q < NS_MAX; q++)
+      if (q < ns) f[6 + q] = K.d * K.sc[q] * vk;
+    if (de) f[5] = K.d * K.ge * vk;
+    return;
+  }
   T const ps  = ql * (Sm - l.vn) + pl;
   T const isl = rcp(Sl - Sm), isr = rcp(Sr - Sm);
   T const dls = ql * isl, drs = qr * isr;
