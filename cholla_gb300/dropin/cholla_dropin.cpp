@@ -101,6 +101,10 @@ void VL_Algorithm_1D_CUDA(Real *d_conserved, int nx, int x_off, int n_ghost, Rea
 
 void Free_Memory_VL_1D() { check(cgb_free_memory_vl_3d(), "Free_Memory_VL_1D"); }
 
+// Calc_dt_GPU and Apply_Temperature_Floor are defined in src/hydro/hydro_cuda.cu next to
+// kernels other files still use; build these replacements only once those two definitions
+// are taken out of that file (-DCHOLLA_DROPIN_DT, -DCHOLLA_DROPIN_TFLOOR).
+#ifdef CHOLLA_DROPIN_DT
 Real Calc_dt_GPU(Real *dev_conserved, int nx, int ny, int nz, int n_ghost, int n_fields, Real dx, Real dy, Real dz,
                  Real gamma)
 {
@@ -109,10 +113,13 @@ Real Calc_dt_GPU(Real *dev_conserved, int nx, int ny, int nz, int n_ghost, int n
   check(cgb_calc_dt_gpu(dev_conserved, nx, ny, nz, n_ghost, n_fields, dx, dy, dz, gamma, &max_dti), "Calc_dt_GPU");
   return max_dti;
 }
+#endif
 
+#ifdef CHOLLA_DROPIN_TFLOOR
 void Apply_Temperature_Floor(Real *dev_conserved, int nx, int ny, int nz, int n_ghost, int n_fields, Real U_floor)
 {
   configure();
   check(cgb_apply_temperature_floor(dev_conserved, nx, ny, nz, n_ghost, n_fields, U_floor),
         "Apply_Temperature_Floor");
 }
+#endif

@@ -52,7 +52,7 @@ typedef struct {
   int n_scalars;         /* -DSCALAR: passive scalars after Energy (0..2) */
   int density_floor;     /* -DDENSITY_FLOOR */
   int temperature_floor; /* -DTEMPERATURE_FLOOR: applied after the step, before the CFL reduction */
-  int precision;         /* CGB_FP64 or CGB_MIXED */
+  int precision;         /* CGB_FP64, CGB_MIXED or CGB_FP64_FAST */
   double gamma;          /* adiabatic index: the reference's global `gama` (global.h:147) */
   double U_floor;        /* specific internal-energy floor used by the temperature floor */
 } cgb_scheme;

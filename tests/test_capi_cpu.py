@@ -103,6 +103,7 @@ def test_dropin_shim_exports_the_reference_symbols(tmp_path):
         pytest.skip("g++ not available")
     obj = tmp_path / "dropin.o"
     subprocess.run([cxx, "-std=c++17", "-c", "-DPPMC", "-DHLLC", "-DDE", "-DDENSITY_FLOOR", "-DTEMPERATURE_FLOOR",
+                    "-DCHOLLA_DROPIN_DT", "-DCHOLLA_DROPIN_TFLOOR",
                     "-I", str(ROOT / "include"), str(ROOT / "cholla_gb300" / "dropin" / "cholla_dropin.cpp"), "-o",
                     str(obj)], check=True)
     out = subprocess.run(["nm", str(obj)], capture_output=True, text=True, check=True).stdout
