@@ -59,6 +59,8 @@ SIGNATURES = {
     "cgb_last_error": (C.c_char_p, []),
     "cgb_version": (C.c_char_p, []),
     "cgb_vl_algorithm_3d": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _D, _D, _D, _D, _I, _I, _D, _P]),
+    "cgb_vl_algorithm_3d_static": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _D, _D, _D, _D, _I, _I, _D,
+                                        _P]),
     "cgb_vl_algorithm_1d": (_I, [_P, _I, _I, _I, _D, _D, _D, _I, _I]),
     "cgb_free_memory_vl_3d": (_I, []),
     "cgb_calc_dt_gpu": (_I, [_P, _I, _I, _I, _I, _I, _D, _D, _D, _D, C.POINTER(_D)]),

@@ -122,6 +122,62 @@ int make_box(cgb::Box &b, int nx, int ny, int nz, int ng, int nf, double dx, dou
 }
 }  // namespace
 
+// Static scratch of cgb_vl_algorithm_3d_static: a file-scope array in the module's static device
+// memory, which the driver provides when it loads the module; no call allocates it.  24 MiB
+// holds the exact FP64 step of a box of up to 393,216 padded cells with 6 fields (73^3) and the
+// fast FP64 / mixed forms up to 196,608 (58^3).
+constexpr size_t kStaticScratchBytes = size_t(24) << 20;
+static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
+
+namespace
+{
+constexpr int kMaxDevices = 64;
+void *g_static_pool[kMaxDevices] = {};  // device address of g_static_scratch, per device ordinal
+
+size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+// Bytes of static scratch one step of box b needs in the given arithmetic, and (base != null)
+// the Scratch pointers laid out from base, each array on a 256-byte boundary.
+size_t static_layout(const cgb::Box &b, int precision, unsigned char *base, cgb::Scratch *out)
+{
+  size_t const n = (size_t)b.n, nf = (size_t)b.nf;
+  size_t off = 0;
+  auto take  = [&](size_t bytes) -> void * {
+    size_t const o = off;
+    off += align256(bytes);
+    return base ? base + o : nullptr;
+  };
+  cgb::Scratch sc{};
+  sc.status = (int *)take(sizeof(int));
+  sc.dti    = (unsigned long long *)take(sizeof(unsigned long long));
+  sc.GEp    = (double *)take(n * sizeof(double));
+  sc.Epre   = (double *)take(n * sizeof(double));
+  if (precision == CGB_FP64)
+    sc.Uh = (double *)take(nf * n * sizeof(double));  // U at the half step
+  else
+    sc.W = take(2 * (nf + 1) * n * sizeof(double));  // primitives of U^n and of U^(n+1/2)
+  if (out) *out = sc;
+  return off;
+}
+
+// Device address of the static pool on the current device, looked up once per device.
+int static_pool(void **pool)
+{
+  int dev       = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(CGB_ERR_ARGS, "device ordinal beyond the static pool table");
+  if (!g_static_pool[dev]) {
+    void *p = nullptr;
+    e       = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(static scratch)");
+    g_static_pool[dev] = p;
+  }
+  *pool = g_static_pool[dev];
+  return CGB_OK;
+}
+}  // namespace
+
 extern "C" {
 
 const char *cgb_last_error(void) { return g_err.c_str(); }
@@ -175,6 +231,44 @@ int cgb_vl_algorithm_3d(double *d_conserved, double *d_grav_potential, int nx, i
   cudaError_t e = cgb::hydro_step(b, g_scheme.reconstruction, g_scheme.riemann_solver, g_scheme.precision,
                                   d_conserved, g_slot.s, dt, nullptr, 0.0, 0, 0, g_stream);
   if (e != cudaSuccess) return cuda_fail(e, "vl_algorithm_3d");
+  return CGB_OK;
+}
+
+int cgb_vl_algorithm_3d_static(double *d_conserved, double *d_grav_potential, int nx, int ny, int nz, int x_off,
+                               int y_off, int z_off, int n_ghost, double dx, double dy, double dz, double xbound,
+                               double ybound, double zbound, double dt, int n_fields, int custom_grav,
+                               double density_floor, double *host_grav_potential)
+{
+  (void)x_off, (void)y_off, (void)z_off, (void)xbound, (void)ybound, (void)zbound;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!d_conserved) return fail(CGB_ERR_ARGS, "null d_conserved");
+  if (d_grav_potential || host_grav_potential || custom_grav)
+    return fail(CGB_ERR_UNSUPPORTED, "gravity source terms are not part of this library");
+  if (ny < 2 * n_ghost + 1 || nz < 2 * n_ghost + 1 || nx < 2 * n_ghost + 1)
+    return fail(CGB_ERR_ARGS, "3D step needs at least one real cell per dimension");
+  cgb::Box b;
+  int rc = make_box(b, nx, ny, nz, n_ghost, n_fields, dx, dy, dz, density_floor, g_scheme);
+  if (rc != CGB_OK) return rc;
+  int const H = g_scheme.reconstruction == CGB_PPMC ? 4 : g_scheme.reconstruction == CGB_PLMC ? 3 : 2;
+  if (n_ghost < H) return fail(CGB_ERR_ARGS, "n_ghost too small for the reconstruction");
+  if (g_scheme.mhd) return fail(CGB_ERR_UNSUPPORTED, "MHD step not built in this version");
+  size_t const need = static_layout(b, g_scheme.precision, nullptr, nullptr);
+  if (need > kStaticScratchBytes)
+    return fail(CGB_ERR_ARGS, "box needs " + std::to_string(need) + " bytes of scratch but the static pool of "
+                              "cgb_vl_algorithm_3d_static holds " + std::to_string(kStaticScratchBytes) +
+                              "; use cgb_vl_algorithm_3d for this box");
+  void *pool = nullptr;
+  rc         = static_pool(&pool);
+  if (rc != CGB_OK) return rc;
+  cgb::Scratch sc;
+  static_layout(b, g_scheme.precision, (unsigned char *)pool, &sc);
+  // the status word collects bad-cell flags with atomicOr, so it must start at zero; every
+  // other array is written before it is read within the step
+  cudaError_t e = cudaMemsetAsync(sc.status, 0, sizeof(int), g_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "clear static status word");
+  e = cgb::hydro_step(b, g_scheme.reconstruction, g_scheme.riemann_solver, g_scheme.precision, d_conserved, sc, dt,
+                      nullptr, 0.0, 0, 0, g_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "vl_algorithm_3d_static");
   return CGB_OK;
 }
 

@@ -78,6 +78,27 @@ int cgb_vl_algorithm_3d(double *d_conserved, double *d_grav_potential, int nx, i
                         double zbound, double dt, int n_fields, int custom_grav, double density_floor,
                         double *host_grav_potential);
 
+/* The step of cgb_vl_algorithm_3d without any device allocation (no counterpart in the
+ * reference).  For callers that cannot let the library allocate device memory: a host
+ * program that has handed the device's memory to its own pool before stepping, and one that
+ * overlaps the step with work on other streams and cannot take the device-wide
+ * synchronisation that a first-call cudaMalloc, or the cudaFree of a shape change, implies.
+ * Scratch comes from a 24 MiB file-scope __device__ array of the library, which the driver
+ * maps with the module's static data (under lazy module loading: on first use, so the first
+ * call on a device is when those 24 MiB leave the free pool).  Its address is looked up once
+ * per device (cudaGetSymbolAddress, with that device current) on the first call there, so
+ * make that first call before capturing any stream that will contain this call.
+ * Limit: a box whose scratch exceeds the pool is rejected with CGB_ERR_ARGS and a message
+ * (6 fields: up to 393,216 padded cells, e.g. 73^3, with CGB_FP64; 196,608, e.g. 58^3, with
+ * CGB_FP64_FAST or CGB_MIXED).  Each call clears the pool's status word on the stream before
+ * the step; nothing else in the pool needs to start at zero.  There is one pool per device:
+ * calls that can overlap in time (from several host threads, or queued on streams that run
+ * concurrently) race on it and corrupt each other's results, so serialise them. */
+int cgb_vl_algorithm_3d_static(double *d_conserved, double *d_grav_potential, int nx, int ny, int nz, int x_off,
+                               int y_off, int z_off, int n_ghost, double dx, double dy, double dz, double xbound,
+                               double ybound, double zbound, double dt, int n_fields, int custom_grav,
+                               double density_floor, double *host_grav_potential);
+
 /* Replaces VL_Algorithm_1D_CUDA (src/integrators/VL_1D_cuda.h, VL_1D_cuda.cu:30-146). */
 int cgb_vl_algorithm_1d(double *d_conserved, int nx, int x_off, int n_ghost, double dx, double xbound, double dt,
                         int n_fields, int custom_grav);
