@@ -117,96 +117,77 @@ __device__ __forceinline__ void ppm1(T im2, T im1, T i, T ip1, T ip2, T &L_iph, 
   R_imh = R;
 }
 
-template <typename T>
-__device__ __forceinline__ Prim<double> widen(const Prim<T> &s)
-{
-  Prim<double> w;
-  w.d = s.d, w.vn = s.vn, w.vt1 = s.vt1, w.vt2 = s.vt2, w.p = s.p, w.ge = s.ge;
-#pragma unroll
-  for (int k = 0; k < NS_MAX; k++) w.sc[k] = s.sc[k];
-  return w;
-}
-__device__ __forceinline__ Prim<float> narrow(const Prim<double> &s)
-{
-  Prim<float> w;
-  w.d = (float)s.d, w.vn = (float)s.vn, w.vt1 = (float)s.vt1, w.vt2 = (float)s.vt2, w.p = (float)s.p;
-  w.ge = (float)s.ge;
-#pragma unroll
-  for (int k = 0; k < NS_MAX; k++) w.sc[k] = (float)s.sc[k];
-  return w;
-}
-
-template <typename T>
-__device__ __forceinline__ void ppmc_cell(const Prim<T> &cm2, const Prim<T> &cm1, const Prim<T> &c, const Prim<T> &cp1,
-                                          const Prim<T> &cp2, int ns, int de, T gamma, Prim<T> &L, Prim<T> &R);
-template <typename T>
-__device__ __forceinline__ void plmc_cell(const Prim<T> &cm, const Prim<T> &c, const Prim<T> &cp, int ns, int de,
-                                          T gamma, Prim<T> &L, Prim<T> &R);
-
+// FP32 path: evaluate the characteristic part of a reconstruction in FP64 where it is
+// ill-conditioned in FP32 (see ppmc_cell).
 constexpr bool kWideFallback = true;
 
-// FP64 evaluation of a cell's reconstruction for the single-precision path.  The
-// characteristic variables carry +-d (vn - vref) / (2 cs) terms that cancel when the
-// primitives are formed again, so in FP32 a cell whose normal-velocity differences across the
-// stencil exceed ~32 sound speeds (cold or near-vacuum gas) would lose most of its digits.
-__device__ __noinline__ void ppmc_cell_wide(const Prim<float> &cm2, const Prim<float> &cm1, const Prim<float> &c,
-                                            const Prim<float> &cp1, const Prim<float> &cp2, int ns, int de,
-                                            float gamma, Prim<float> &L, Prim<float> &R)
+// Characteristic part of PPMC_VL (ppmc_cuda.cu:540-695): density, normal velocity and pressure
+// at the cell's right (L*) and left (R*) faces from PPM on the projected variables
+// a0 = p/(2cs^2) - d (vn - vref)/(2cs), a1 = d - p/cs^2, a4 = p/(2cs^2) + d (vn - vref)/(2cs),
+// taken with the centre cell's (index 2) density and sound speed.  vref shifts the frame; PPM
+// is equivariant under a common shift of its five inputs, so the result does not depend on it
+// beyond rounding, but vref = centre velocity removes the bulk-flow part of the cancellation.
+template <typename T>
+__device__ __forceinline__ void ppmc_char(const T (&d)[5], const T (&vn)[5], const T (&p)[5], T gamma, T vref, T &Ld,
+                                          T &Lvn, T &Lp, T &Rd, T &Rvn, T &Rp)
 {
-  Prim<double> l, r;
-  ppmc_cell<double>(widen(cm2), widen(cm1), widen(c), widen(cp1), widen(cp2), ns, de, (double)gamma, l, r);
-  L = narrow(l), R = narrow(r);
-}
-__device__ __noinline__ void plmc_cell_wide(const Prim<float> &cm, const Prim<float> &c, const Prim<float> &cp, int ns,
-                                            int de, float gamma, Prim<float> &L, Prim<float> &R)
-{
-  Prim<double> l, r;
-  plmc_cell<double>(widen(cm), widen(c), widen(cp), ns, de, (double)gamma, l, r);
-  L = narrow(l), R = narrow(r);
+  T const id   = rcp(d[2]);
+  T const cs   = sqrtT(gamma * p[2] * id);
+  T const cs2  = cs * cs;
+  T const rcs  = rcp(cs);
+  T const h2c2 = T(0.5) * rcs * rcs;  // 1 / (2 cs^2)
+  T const dh2c = d[2] * T(0.5) * rcs;  // d / (2 cs)
+  T a0[5], a1[5], a4[5];
+#pragma unroll
+  for (int k = 0; k < 5; k++) {
+    a0[k] = p[k] * h2c2 - dh2c * (vn[k] - vref);
+    a1[k] = d[k] - T(2) * p[k] * h2c2;
+    a4[k] = p[k] * h2c2 + dh2c * (vn[k] - vref);
+  }
+  T l0, r0, l1, r1, l4, r4;
+  ppm1(a0[0], a0[1], a0[2], a0[3], a0[4], l0, r0);
+  ppm1(a1[0], a1[1], a1[2], a1[3], a1[4], l1, r1);
+  ppm1(a4[0], a4[1], a4[2], a4[3], a4[4], l4, r4);
+  T const csid = cs * id;
+  Ld  = l0 + l1 + l4;
+  Lvn = csid * (l4 - l0) + vref;
+  Lp  = cs2 * (l0 + l4);
+  Rd  = r0 + r1 + r4;
+  Rvn = csid * (r4 - r0) + vref;
+  Rp  = cs2 * (r0 + r4);
 }
 
-// PPMC_VL for one cell (ppmc_cuda.cu:540-695), hydro characteristic projection.  In FP32 the
-// projection is taken in the frame of the cell's own normal velocity (PPM is equivariant under
-// a common shift of its five inputs), which removes the bulk-flow part of the cancellation.
+// PPMC_VL for one cell: characteristic PPM of (d, vn, p), plain PPM of the transverse
+// velocities, GasEnergy and scalars, then the density and pressure floors.  In FP32 the
+// projection is taken in the frame of the centre cell's normal velocity; where the normal-velocity
+// differences across the stencil still exceed 32 sound speeds (cold or near-vacuum gas) the
+// projected variables' +-d dv/(2cs) terms would cancel away most FP32 digits, so that cell's
+// characteristic part is evaluated in FP64 from the same FP32 inputs.
 template <typename T>
 __device__ __forceinline__ void ppmc_cell(const Prim<T> &cm2, const Prim<T> &cm1, const Prim<T> &c, const Prim<T> &cp1,
                                           const Prim<T> &cp2, int ns, int de, T gamma, Prim<T> &L, Prim<T> &R)
 {
-  T const id   = rcp(c.d);
-  T const cs   = sqrtT(gamma * c.p * id);
-  if constexpr (std::is_same<T, float>::value && kWideFallback) {
-    T const dv = fmax(fmax(fabs(cm2.vn - c.vn), fabs(cm1.vn - c.vn)), fmax(fabs(cp1.vn - c.vn), fabs(cp2.vn - c.vn)));
-    if (!(dv <= T(32) * cs)) {
-      ppmc_cell_wide(cm2, cm1, c, cp1, cp2, ns, de, gamma, L, R);
-      return;
+  T const d[5] = {cm2.d, cm1.d, c.d, cp1.d, cp2.d};
+  T const v[5] = {cm2.vn, cm1.vn, c.vn, cp1.vn, cp2.vn};
+  T const p[5] = {cm2.p, cm1.p, c.p, cp1.p, cp2.p};
+  if constexpr (std::is_same<T, float>::value) {
+    float const cs = sqrtT(gamma * c.p * rcp(c.d));
+    float const dv = fmax(fmax(fabs(cm2.vn - c.vn), fabs(cm1.vn - c.vn)), fmax(fabs(cp1.vn - c.vn), fabs(cp2.vn - c.vn)));
+    if (kWideFallback && !(dv <= 32.0f * cs)) {
+      double const dw[5] = {d[0], d[1], d[2], d[3], d[4]};
+      double const vw[5] = {v[0], v[1], v[2], v[3], v[4]};
+      double const pw[5] = {p[0], p[1], p[2], p[3], p[4]};
+      double Ld, Lvn, Lp, Rd, Rvn, Rp;
+      ppmc_char<double>(dw, vw, pw, (double)gamma, 0.0, Ld, Lvn, Lp, Rd, Rvn, Rp);
+      L.d = (float)Ld, L.vn = (float)Lvn, L.p = (float)Lp, R.d = (float)Rd, R.vn = (float)Rvn, R.p = (float)Rp;
+    } else {
+      ppmc_char<float>(d, v, p, gamma, c.vn, L.d, L.vn, L.p, R.d, R.vn, R.p);
     }
+  } else {
+    ppmc_char<T>(d, v, p, gamma, T(0), L.d, L.vn, L.p, R.d, R.vn, R.p);
   }
-  T const vref = std::is_same<T, float>::value ? c.vn : T(0);
-  T const cs2  = cs * cs;
-  T const rcs  = rcp(cs);
-  T const h2c  = T(0.5) * rcs;        // 1 / (2 cs)
-  T const h2c2 = T(0.5) * rcs * rcs;  // 1 / (2 cs^2)
-  T const dh2c = c.d * h2c;
-  auto a0 = [&](const Prim<T> &s) { return s.p * h2c2 - dh2c * (s.vn - vref); };
-  auto a1 = [&](const Prim<T> &s) { return s.d - T(2) * s.p * h2c2; };
-  auto a4 = [&](const Prim<T> &s) { return s.p * h2c2 + dh2c * (s.vn - vref); };
-  T l0, r0, l1, r1, l2, r2, l3, r3, l4, r4;
-  ppm1(a0(cm2), a0(cm1), a0(c), a0(cp1), a0(cp2), l0, r0);
-  ppm1(a1(cm2), a1(cm1), a1(c), a1(cp1), a1(cp2), l1, r1);
-  ppm1(cm2.vt1, cm1.vt1, c.vt1, cp1.vt1, cp2.vt1, l2, r2);
-  ppm1(cm2.vt2, cm1.vt2, c.vt2, cp1.vt2, cp2.vt2, l3, r3);
-  ppm1(a4(cm2), a4(cm1), a4(c), a4(cp1), a4(cp2), l4, r4);
-  T const csid = cs * id;
-  L.d   = l0 + l1 + l4;
-  L.vn  = csid * (l4 - l0) + vref;
-  L.vt1 = l2;
-  L.vt2 = l3;
-  L.p   = cs2 * (l0 + l4);
-  R.d   = r0 + r1 + r4;
-  R.vn  = csid * (r4 - r0) + vref;
-  R.vt1 = r2;
-  R.vt2 = r3;
-  R.p   = cs2 * (r0 + r4);
+  ppm1(cm2.vt1, cm1.vt1, c.vt1, cp1.vt1, cp2.vt1, L.vt1, R.vt1);
+  ppm1(cm2.vt2, cm1.vt2, c.vt2, cp1.vt2, cp2.vt2, L.vt2, R.vt2);
   L.ge = R.ge = T(0);
   if (de) ppm1(cm2.ge, cm1.ge, c.ge, cp1.ge, cp2.ge, L.ge, R.ge);
 #pragma unroll
@@ -221,47 +202,74 @@ __device__ __forceinline__ void ppmc_cell(const Prim<T> &cm2, const Prim<T> &cm1
   L.p = fmax(L.p, tiny);
 }
 
-// PLMC_cuda for one cell (plmc_cuda.cu:24-300; VL, no characteristic tracing).
 template <typename T>
-__device__ __forceinline__ void plmc_cell(const Prim<T> &cm, const Prim<T> &c, const Prim<T> &cp, int ns, int de,
-                                          T gamma, Prim<T> &L, Prim<T> &R)
+__device__ __forceinline__ T plm_vl(T l, T r)  // van Leer average of two slopes
 {
-  T const id   = rcp(c.d);
-  T const cs   = sqrtT(gamma * c.p * id);
-  if constexpr (std::is_same<T, float>::value && kWideFallback) {
-    if (!(fmax(fabs(c.vn - cm.vn), fabs(cp.vn - c.vn)) <= T(32) * cs)) {
-      plmc_cell_wide(cm, c, cp, ns, de, gamma, L, R);
-      return;
-    }
-  }
+  return (l * r > T(0)) ? T(2) * l * r / (l + r) : T(0);
+}
+template <typename T>
+__device__ __forceinline__ T plm_mono(T l, T r, T cc, T vg)  // monotonised slope
+{
+  if (l * r > T(0)) return copysign(fmin(T(2) * fmin(fabs(l), fabs(r)), fmin(fabs(cc), fabs(vg))), cc);
+  return T(0);
+}
+
+// Characteristic part of PLMC_cuda (plmc_cuda.cu:24-300): the half-slopes hd, hn, hp of density,
+// normal velocity and pressure from the monotonised slopes of the projected variables
+// a0 = p/(2cs^2) - d vn/(2cs), a1 = d - p/cs^2, a4 = p/(2cs^2) + d vn/(2cs) (centre cell index 1).
+template <typename T>
+__device__ __forceinline__ void plmc_char(const T (&d)[3], const T (&vn)[3], const T (&p)[3], T gamma, T &hd, T &hn,
+                                          T &hp)
+{
+  T const id   = rcp(d[1]);
+  T const cs   = sqrtT(gamma * p[1] * id);
   T const cs2  = cs * cs;
   T const rcs  = rcp(cs);
-  T const h2c  = T(0.5) * rcs;
   T const h2c2 = T(0.5) * rcs * rcs;
-  T const dh2c = c.d * h2c;
-  auto vl      = [](T l, T r) -> T { return (l * r > T(0)) ? T(2) * l * r / (l + r) : T(0); };
-  auto mono    = [](T l, T r, T cc, T vg) -> T {
-    if (l * r > T(0)) return copysign(fmin(T(2) * fmin(fabs(l), fabs(r)), fmin(fabs(cc), fabs(vg))), cc);
-    return T(0);
-  };
+  T const dh2c = d[1] * T(0.5) * rcs;
   auto chr = [&](T sd, T sn, T sp, T &b0, T &b1, T &b4) {
     b0 = sp * h2c2 - dh2c * sn;
     b1 = sd - T(2) * sp * h2c2;
     b4 = sp * h2c2 + dh2c * sn;
   };
-  T const dLd = c.d - cm.d, dRd = cp.d - c.d, dCd = T(0.5) * (cp.d - cm.d);
-  T const dLn = c.vn - cm.vn, dRn = cp.vn - c.vn, dCn = T(0.5) * (cp.vn - cm.vn);
-  T const dL1 = c.vt1 - cm.vt1, dR1 = cp.vt1 - c.vt1, dC1 = T(0.5) * (cp.vt1 - cm.vt1);
-  T const dL2 = c.vt2 - cm.vt2, dR2 = cp.vt2 - c.vt2, dC2 = T(0.5) * (cp.vt2 - cm.vt2);
-  T const dLp = c.p - cm.p, dRp = cp.p - c.p, dCp = T(0.5) * (cp.p - cm.p);
+  T const dLd = d[1] - d[0], dRd = d[2] - d[1], dCd = T(0.5) * (d[2] - d[0]);
+  T const dLn = vn[1] - vn[0], dRn = vn[2] - vn[1], dCn = T(0.5) * (vn[2] - vn[0]);
+  T const dLp = p[1] - p[0], dRp = p[2] - p[1], dCp = T(0.5) * (p[2] - p[0]);
   T L0, L1, L4, R0, R1, R4, C0, C1, C4, G0, G1, G4;
   chr(dLd, dLn, dLp, L0, L1, L4);
   chr(dRd, dRn, dRp, R0, R1, R4);
   chr(dCd, dCn, dCp, C0, C1, C4);
-  chr(vl(dLd, dRd), vl(dLn, dRn), vl(dLp, dRp), G0, G1, G4);
-  T const m0 = mono(L0, R0, C0, G0), m1 = mono(L1, R1, C1, G1), m4 = mono(L4, R4, C4, G4);
-  T const m2 = mono(dL1, dR1, dC1, vl(dL1, dR1)), m3 = mono(dL2, dR2, dC2, vl(dL2, dR2));
-  T const hd = T(0.5) * (m0 + m1 + m4), hn = T(0.5) * cs * id * (m4 - m0), hp = T(0.5) * cs2 * (m0 + m4);
+  chr(plm_vl(dLd, dRd), plm_vl(dLn, dRn), plm_vl(dLp, dRp), G0, G1, G4);
+  T const m0 = plm_mono(L0, R0, C0, G0), m1 = plm_mono(L1, R1, C1, G1), m4 = plm_mono(L4, R4, C4, G4);
+  hd = T(0.5) * (m0 + m1 + m4);
+  hn = T(0.5) * cs * id * (m4 - m0);
+  hp = T(0.5) * cs2 * (m0 + m4);
+}
+
+// PLMC_cuda for one cell (VL, no characteristic tracing).  In FP32 a cell whose normal-velocity
+// differences exceed 32 sound speeds takes its characteristic part in FP64 (see ppmc_cell).
+template <typename T>
+__device__ __forceinline__ void plmc_cell(const Prim<T> &cm, const Prim<T> &c, const Prim<T> &cp, int ns, int de,
+                                          T gamma, Prim<T> &L, Prim<T> &R)
+{
+  T const d[3] = {cm.d, c.d, cp.d}, v[3] = {cm.vn, c.vn, cp.vn}, p[3] = {cm.p, c.p, cp.p};
+  T hd, hn, hp;
+  if constexpr (std::is_same<T, float>::value) {
+    float const cs = sqrtT(gamma * c.p * rcp(c.d));
+    if (kWideFallback && !(fmax(fabs(c.vn - cm.vn), fabs(cp.vn - c.vn)) <= 32.0f * cs)) {
+      double const dw[3] = {d[0], d[1], d[2]}, vw[3] = {v[0], v[1], v[2]}, pw[3] = {p[0], p[1], p[2]};
+      double a, b, e;
+      plmc_char<double>(dw, vw, pw, (double)gamma, a, b, e);
+      hd = (float)a, hn = (float)b, hp = (float)e;
+    } else {
+      plmc_char<float>(d, v, p, gamma, hd, hn, hp);
+    }
+  } else {
+    plmc_char<T>(d, v, p, gamma, hd, hn, hp);
+  }
+  T const dL1 = c.vt1 - cm.vt1, dR1 = cp.vt1 - c.vt1, dC1 = T(0.5) * (cp.vt1 - cm.vt1);
+  T const dL2 = c.vt2 - cm.vt2, dR2 = cp.vt2 - c.vt2, dC2 = T(0.5) * (cp.vt2 - cm.vt2);
+  T const m2 = plm_mono(dL1, dR1, dC1, plm_vl(dL1, dR1)), m3 = plm_mono(dL2, dR2, dC2, plm_vl(dL2, dR2));
   L.d = c.d + hd, R.d = c.d - hd;
   L.vn = c.vn + hn, R.vn = c.vn - hn;
   L.vt1 = c.vt1 + T(0.5) * m2, R.vt1 = c.vt1 - T(0.5) * m2;
@@ -279,7 +287,7 @@ __device__ __forceinline__ void plmc_cell(const Prim<T> &cm, const Prim<T> &c, c
   L.ge = R.ge = T(0);
   if (de) {
     T const dL = c.ge - cm.ge, dR = cp.ge - c.ge;
-    T const h  = T(0.5) * mono(dL, dR, T(0.5) * (cp.ge - cm.ge), vl(dL, dR));
+    T const h  = T(0.5) * plm_mono(dL, dR, T(0.5) * (cp.ge - cm.ge), plm_vl(dL, dR));
     L.ge = c.ge + h, R.ge = c.ge - h;
     lim(L.ge, R.ge, cm.ge, c.ge, cp.ge);
   }
@@ -288,7 +296,7 @@ __device__ __forceinline__ void plmc_cell(const Prim<T> &cm, const Prim<T> &c, c
     L.sc[k] = R.sc[k] = T(0);
     if (k < ns) {
       T const dL = c.sc[k] - cm.sc[k], dR = cp.sc[k] - c.sc[k];
-      T const h  = T(0.5) * mono(dL, dR, T(0.5) * (cp.sc[k] - cm.sc[k]), vl(dL, dR));
+      T const h  = T(0.5) * plm_mono(dL, dR, T(0.5) * (cp.sc[k] - cm.sc[k]), plm_vl(dL, dR));
       L.sc[k] = c.sc[k] + h, R.sc[k] = c.sc[k] - h;
       lim(L.sc[k], R.sc[k], cm.sc[k], c.sc[k], cp.sc[k]);
     }
@@ -385,23 +393,24 @@ __device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, i
     // wave speeds, which a near-vacuum interface state (density floored at TINY) makes ~1e9,
     // and that cancellation costs every significant digit in FP32.
     bool const lft = Sm >= T(0);
-    Prim<T> const &K = lft ? l : r;
+    // field-by-field selects (a reference to l or r would put both states in local memory)
+    T const Kd = lft ? l.d : r.d, Kv = lft ? l.vn : r.vn, Kt1 = lft ? l.vt1 : r.vt1, Kt2 = lft ? l.vt2 : r.vt2;
     T const SK = lft ? Sl : Sr, EK = lft ? El : Er, pK = lft ? pl : pr;
     // SK - Sm from the separated parts; it is negative on the left and positive on the right,
     // and only rounding of a degenerate (both sides cold) interface can bring it to zero
-    T const gap = (lft ? dSl : dSr) - (Sm - K.vn);
+    T const gap = (lft ? dSl : dSr) - (Sm - Kv);
     T const den = lft ? fmin(gap, T(-1e-30)) : fmax(gap, T(1e-30));
-    T const k   = SK * (Sm - K.vn) * rcp(den);
-    T const vk = K.vn + k;
-    f[0] = K.d * vk;
-    f[1] = K.d * (K.vn * K.vn + k * SK) + pK;
-    f[2] = K.d * K.vt1 * vk;
-    f[3] = K.d * K.vt2 * vk;
-    f[4] = (EK + pK) * vk + k * K.d * (SK - K.vn) * Sm;
+    T const k   = SK * (Sm - Kv) * rcp(den);
+    T const vk  = Kv + k;
+    f[0] = Kd * vk;
+    f[1] = Kd * (Kv * Kv + k * SK) + pK;
+    f[2] = Kd * Kt1 * vk;
+    f[3] = Kd * Kt2 * vk;
+    f[4] = (EK + pK) * vk + k * Kd * (SK - Kv) * Sm;
 #pragma unroll
     for (int q = 0; q < NS_MAX; q++)
-      if (q < ns) f[6 + q] = K.d * K.sc[q] * vk;
-    if (de) f[5] = K.d * K.ge * vk;
+      if (q < ns) f[6 + q] = Kd * (lft ? l.sc[q] : r.sc[q]) * vk;
+    if (de) f[5] = Kd * (lft ? l.ge : r.ge) * vk;
     return;
   }
   T const ps  = ql * (Sm - l.vn) + pl;
