@@ -195,10 +195,12 @@ __global__ void __launch_bounds__(TX *TY *TZ, 2)
     int const cr = cl + (dir == 0 ? 1 : dir == 1 ? BX : BX * BY);
     int const o1 = dir + 1, o2 = (dir + 1) % 3 + 1, o3 = (dir + 2) % 3 + 1;
     hf::Prim<T> L = prim_at(Ps, NB, cl, b), R = prim_at(Ps, NB, cr, b);
-    // rotate the velocities into (normal, t1, t2)
-    T const lv[3] = {L.vn, L.vt1, L.vt2}, rv[3] = {R.vn, R.vt1, R.vt2};
-    L.vn = lv[o1 - 1], L.vt1 = lv[o2 - 1], L.vt2 = lv[o3 - 1];
-    R.vn = rv[o1 - 1], R.vt1 = rv[o2 - 1], R.vt2 = rv[o3 - 1];
+    // rotate the velocities into (normal, t1, t2) with selects (a runtime-indexed array would
+    // live in local memory)
+    auto pick = [](T x, T y, T z, int k) { return k == 1 ? x : (k == 2 ? y : z); };
+    T const ua = L.vn, ub = L.vt1, uc = L.vt2, va = R.vn, vb = R.vt1, vc = R.vt2;
+    L.vn = pick(ua, ub, uc, o1), L.vt1 = pick(ua, ub, uc, o2), L.vt2 = pick(ua, ub, uc, o3);
+    R.vn = pick(va, vb, vc, o1), R.vt1 = pick(va, vb, vc, o2), R.vt2 = pick(va, vb, vc, o3);
     T f[NSLOT];
     riemann<T, SOLVER>(L, R, f, b);
 #pragma unroll
@@ -268,154 +270,47 @@ __global__ void __launch_bounds__(TX *TY *TZ, 2)
 }
 
 // ------------------------------------------------------------------------------------------
+// corrector: one sweep kernel per direction over long pencils
+// ------------------------------------------------------------------------------------------
 template <int RECON>
 struct FHalo {
   static constexpr int H = RECON == RECON_PPMC ? 3 : (RECON == RECON_PLMC ? 2 : 1);
 };
 
-template <int TX, int TY, int TZ, int RECON>
-struct FSizes {
+// A sweep block: CS = WA * WB pencils of L cells along the sweep direction DIR.  Arrays in
+// shared memory are [slot][pencil position, pencil]; along x the position is fastest (the x
+// pencils are contiguous in HBM), along y and z the pencil index is (WA consecutive x cells).
+template <int DIR, int L, int WA, int WB, int RECON>
+struct Sweep {
   static constexpr int H  = FHalo<RECON>::H;
-  static constexpr int HY = TY > 1, HZ = TZ > 1;
-  static constexpr int PX = (TX + 2 * H) * TY * TZ;
-  static constexpr int PY = HY ? TX * (TY + 2 * H) * TZ : 0;
-  static constexpr int PZ = HZ ? TX * TY * (TZ + 2 * H) : 0;
-  static constexpr int PM = PX > PY ? (PX > PZ ? PX : PZ) : (PY > PZ ? PY : PZ);
-  static constexpr int RX = (TX + 2) * TY * TZ;
-  static constexpr int RY = HY ? TX * (TY + 2) * TZ : 0;
-  static constexpr int RZ = HZ ? TX * TY * (TZ + 2) : 0;
-  static constexpr int RM = RX > RY ? (RX > RZ ? RX : RZ) : (RY > RZ ? RY : RZ);
-  static constexpr int FX = (TX + 1) * TY * TZ;
-  static constexpr int FY = HY ? TX * (TY + 1) * TZ : 0;
-  static constexpr int FZ = HZ ? TX * TY * (TZ + 1) : 0;
-  static constexpr int FM = FX > FY ? (FX > FZ ? FX : FZ) : (FY > FZ ? FY : FZ);
-  static constexpr int PER_Q = PM + (RECON == RECON_PCM ? 0 : 2 * RM) + FM;
+  static constexpr int CS = WA * WB;
+  static constexpr int NT = L * CS;  // one thread per updated cell
+  static constexpr int LA = L + 2 * H, LR = L + 2, LF = L + 1;
+  static constexpr int NP = LA * CS, NR = LR * CS, NF = LF * CS;
+  // P (loaded primitives), QL and QR (face states); the fluxes reuse P once it is consumed
+  // (PCM has no face states: its fluxes follow P)
+  static constexpr int PER_Q = RECON == RECON_PCM ? NP + NF : NP + 2 * NR;
+  static constexpr int STRIDE = DIR == 0 ? 1 : CS;
+  __device__ static int at(int a, int c, int len) { return DIR == 0 ? a + len * c : c + CS * a; }
+  __device__ static void split(int i, int len, int &a, int &c)
+  {
+    if (DIR == 0) {
+      a = i % len, c = i / len;
+    } else {
+      c = i % CS, a = i / CS;
+    }
+  }
 };
 
-template <typename T, int TX, int TY, int TZ, int RECON, int SOLVER>
-__global__ void __launch_bounds__(TX *TY *TZ, 2)
-    k_fcorr(Box b, const T *__restrict__ W, double *__restrict__ U, const double *__restrict__ GEp,
-            double *__restrict__ Epre, int *__restrict__ status, double dt, const double *__restrict__ dtp)
+// Uⁿ⁺¹ = Uⁿ + acc in FP64 (GasEnergy from its pdV partial update), the density floor, and the
+// pre-sync total energy for the dual-energy selection
+template <typename T>
+__device__ __forceinline__ void final_update(const Box &b, long long gid, const T *acc, double *__restrict__ U,
+                                             const double *__restrict__ GEp, double *__restrict__ Epre,
+                                             int *__restrict__ status)
 {
-  if (dtp) dt = *dtp;
-  using S          = FSizes<TX, TY, TZ, RECON>;
-  constexpr int H  = S::H;
-  constexpr int NT = TX * TY * TZ;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  int const ns_ = nslot(b);
-  T *Ps  = reinterpret_cast<T *>(smem_raw);
-  T *QLs = Ps + ns_ * S::PM;
-  T *QRs = (RECON == RECON_PCM) ? QLs : QLs + ns_ * S::RM;
-  T *Fs  = (RECON == RECON_PCM) ? QLs : QRs + ns_ * S::RM;
-
-  int const ng = b.ng;
-  int const x0 = ng + blockIdx.x * TX;
-  int const y0 = S::HY ? ng + blockIdx.y * TY : 0;
-  int const z0 = S::HZ ? ng + blockIdx.z * TZ : 0;
-  bool const one_d = (b.ny == 1 && b.nz == 1);
   long long const n = b.n;
-
-  int const t  = threadIdx.x;
-  int const ti = t % TX, tj = (t / TX) % TY, tk = t / (TX * TY);
-  T acc[NSLOT];
-#pragma unroll
-  for (int q = 0; q < NSLOT; q++) acc[q] = T(0);
-
-  int const ndir = one_d ? 1 : 3;
-  for (int dir = 0; dir < ndir; dir++) {
-    int const o1 = dir + 1, o2 = (dir + 1) % 3 + 1, o3 = (dir + 2) % 3 + 1;
-    int const TA = dir == 0 ? TX : dir == 1 ? TY : TZ;
-    int const TU = dir == 0 ? TY : dir == 1 ? TZ : TX;
-    int const TW = dir == 0 ? TZ : dir == 1 ? TX : TY;
-    int const LA = TA + 2 * H;
-    int const np = LA * TU * TW;
-    for (int p = t; p < np; p += NT) {
-      int const a = p % LA - H, u = (p / LA) % TU, w = p / (LA * TU);
-      int gx, gy, gz;
-      if (dir == 0) {
-        gx = x0 + a, gy = y0 + u, gz = z0 + w;
-      } else if (dir == 1) {
-        gy = y0 + a, gz = z0 + u, gx = x0 + w;
-      } else {
-        gz = z0 + a, gx = x0 + u, gy = y0 + w;
-      }
-      long long const gid = b.id(clampi(gx, 0, b.nx - 1), clampi(gy, 0, b.ny - 1), clampi(gz, 0, b.nz - 1));
-      for (int q = 0; q < ns_; q++) Ps[q * S::PM + p] = W[(long long)rot(q, o1, o2, o3) * n + gid];
-    }
-    __syncthreads();
-    int const LR = TA + 2;
-    if (RECON != RECON_PCM) {
-      int const nr = LR * TU * TW;
-      for (int r = t; r < nr; r += NT) {
-        int const a = r % LR - 1, uw = r / LR;
-        int const base = (a + H) + LA * uw;
-        hf::Prim<T> L, R;
-        if (RECON == RECON_PPMC) {
-          hf::ppmc_cell(prim_at(Ps, S::PM, base - 2, b), prim_at(Ps, S::PM, base - 1, b), prim_at(Ps, S::PM, base, b),
-                        prim_at(Ps, S::PM, base + 1, b), prim_at(Ps, S::PM, base + 2, b), b.ns, b.de, (T)b.gamma, L,
-                        R);
-        } else {
-          hf::plmc_cell(prim_at(Ps, S::PM, base - 1, b), prim_at(Ps, S::PM, base, b), prim_at(Ps, S::PM, base + 1, b),
-                        b.ns, b.de, (T)b.gamma, L, R);
-        }
-        prim_put(QLs, S::RM, r, L, b);
-        prim_put(QRs, S::RM, r, R, b);
-      }
-      __syncthreads();
-    }
-    int const LF  = TA + 1;
-    int const nfc = LF * TU * TW;
-    T *Fd         = (RECON == RECON_PCM) ? QLs : Fs;
-    for (int fi = t; fi < nfc; fi += NT) {
-      int const a = fi % LF - 1, uw = fi / LF;
-      hf::Prim<T> L, R;
-      if (RECON == RECON_PCM) {
-        int const pl = (a + H) + LA * uw;
-        L = prim_at(Ps, S::PM, pl, b);
-        R = prim_at(Ps, S::PM, pl + 1, b);
-      } else {
-        int const rl = (a + 1) + LR * uw;
-        L = prim_at(QLs, S::RM, rl, b);
-        R = prim_at(QRs, S::RM, rl + 1, b);
-      }
-      T f[NSLOT];
-      riemann<T, SOLVER>(L, R, f, b);
-#pragma unroll
-      for (int q = 0; q < NSLOT; q++)
-        if (live(q, b)) Fd[q * S::FM + fi] = f[q];
-    }
-    __syncthreads();
-    {
-      int a, u, w;
-      if (dir == 0) {
-        a = ti, u = tj, w = tk;
-      } else if (dir == 1) {
-        a = tj, u = tk, w = ti;
-      } else {
-        a = tk, u = ti, w = tj;
-      }
-      int const fm = a + LF * (u + TU * w);
-      T const dtod = (T)(dt / (dir == 0 ? b.dx : dir == 1 ? b.dy : b.dz));
-      T d[NSLOT];
-#pragma unroll
-      for (int q = 0; q < NSLOT; q++) d[q] = live(q, b) ? dtod * (Fd[q * S::FM + fm] - Fd[q * S::FM + fm + 1]) : T(0);
-      // rotated momentum components back to x, y, z
-      T const dm[3] = {d[1], d[2], d[3]};
-      acc[0] += d[0];
-      acc[o1] += dm[0];
-      acc[o2] += dm[1];
-      acc[o3] += dm[2];
-#pragma unroll
-      for (int q = 4; q < NSLOT; q++) acc[q] += d[q];
-    }
-    __syncthreads();
-  }
-
-  int const gx = x0 + ti, gy = y0 + tj, gz = z0 + tk;
-  bool real = gx < b.nx - ng;
-  if (!one_d) real = real && gy < b.ny - ng && gz < b.nz - ng;
-  if (!real) return;
-  long long const gid = b.id(gx, gy, gz);
+  bool const one_d  = (b.ny == 1 && b.nz == 1);
   double v[NSLOT];
 #pragma unroll
   for (int q = 0; q < NSLOT; q++) {
@@ -424,10 +319,10 @@ __global__ void __launch_bounds__(TX *TY *TZ, 2)
   }
   if (b.floor_on && !one_d && v[0] < b.density_floor) {
     if (v[0] > 0) {
-      double const s = b.density_floor / v[0];
-      v[0]           = b.density_floor;
-      v[1] *= s, v[2] *= s, v[3] *= s, v[4] *= s;
-      if (b.de) v[5] *= s;
+      double const sc = b.density_floor / v[0];
+      v[0]            = b.density_floor;
+      v[1] *= sc, v[2] *= sc, v[3] *= sc, v[4] *= sc;
+      if (b.de) v[5] *= sc;
     } else {
       atomicOr(status, 1);
     }
@@ -436,6 +331,160 @@ __global__ void __launch_bounds__(TX *TY *TZ, 2)
   for (int q = 0; q < NSLOT; q++)
     if (live(q, b)) U[field(q, b) * n + gid] = v[q];
   if (b.de) Epre[gid] = v[4];
+}
+
+// Sweep DIR of the corrector: reconstruction + Riemann solve on the pencils of W½, flux
+// difference dt/dx (F(i-1/2) - F(i+1/2)) per cell.  Not FINAL: the difference is added to the
+// accumulator dU (the x sweep starts it).  FINAL (the last sweep): Uⁿ⁺¹ = Uⁿ + (dU + the
+// difference) in FP64 in place, density floor, Epre = pre-sync total energy.
+template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
+__global__ void __launch_bounds__(L *WA *WB, 2)
+    k_fsweep(Box b, const T *__restrict__ W, T *__restrict__ dU, double *__restrict__ U,
+             const double *__restrict__ GEp, double *__restrict__ Epre, int *__restrict__ status, double dt,
+             const double *__restrict__ dtp)
+{
+  using S = Sweep<DIR, L, WA, WB, RECON>;
+  constexpr int H  = S::H;
+  constexpr int NT = S::NT;
+  constexpr int o1 = DIR + 1, o2 = (DIR + 1) % 3 + 1, o3 = (DIR + 2) % 3 + 1;
+  if (dtp) dt = *dtp;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int const ns_ = nslot(b);
+  T *Ps  = reinterpret_cast<T *>(smem_raw);
+  T *QLs = Ps + ns_ * S::NP;
+  T *QRs = QLs + ns_ * S::NR;
+  T *Fs  = RECON == RECON_PCM ? QLs : Ps;
+
+  int const ng     = b.ng;
+  bool const one_d = (b.ny == 1 && b.nz == 1);
+  long long const n = b.n;
+  int const a0 = blockIdx.x * L, ca0 = blockIdx.y * WA, cb0 = blockIdx.z * WB;
+  // global cell of sweep position a (real-cell coordinates, may lie in the ghosts) on pencil c
+  auto cell = [&](int a, int c, int &gx, int &gy, int &gz) {
+    int const ca = ca0 + c % WA + ng, cb = cb0 + c / WA + ng, g = a0 + a + ng;
+    if (DIR == 0) {
+      gx = g, gy = one_d ? 0 : ca, gz = one_d ? 0 : cb;
+    } else if (DIR == 1) {
+      gy = g, gx = ca, gz = cb;
+    } else {
+      gz = g, gx = ca, gy = cb;
+    }
+  };
+
+  int const t = threadIdx.x;
+  for (int p = t; p < S::NP; p += NT) {
+    int a, c, gx, gy, gz;
+    S::split(p, S::LA, a, c);
+    cell(a - H, c, gx, gy, gz);
+    long long const gid = b.id(clampi(gx, 0, b.nx - 1), clampi(gy, 0, b.ny - 1), clampi(gz, 0, b.nz - 1));
+    for (int q = 0; q < ns_; q++) Ps[q * S::NP + p] = W[(long long)rot(q, o1, o2, o3) * n + gid];
+  }
+  __syncthreads();
+  if (RECON != RECON_PCM) {
+    for (int r = t; r < S::NR; r += NT) {
+      int a, c;
+      S::split(r, S::LR, a, c);
+      int const base = S::at(a - 1 + H, c, S::LA);
+      constexpr int st = S::STRIDE;
+      hf::Prim<T> Lf, Rf;
+      if (RECON == RECON_PPMC) {
+        hf::ppmc_cell(prim_at(Ps, S::NP, base - 2 * st, b), prim_at(Ps, S::NP, base - st, b), prim_at(Ps, S::NP, base, b),
+                      prim_at(Ps, S::NP, base + st, b), prim_at(Ps, S::NP, base + 2 * st, b), b.ns, b.de, (T)b.gamma, Lf,
+                      Rf);
+      } else {
+        hf::plmc_cell(prim_at(Ps, S::NP, base - st, b), prim_at(Ps, S::NP, base, b), prim_at(Ps, S::NP, base + st, b),
+                      b.ns, b.de, (T)b.gamma, Lf, Rf);
+      }
+      prim_put(QLs, S::NR, r, Lf, b);
+      prim_put(QRs, S::NR, r, Rf, b);
+    }
+    __syncthreads();
+  }
+  for (int f = t; f < S::NF; f += NT) {
+    int a, c;
+    S::split(f, S::LF, a, c);  // face a lies between sweep positions a - 1 and a
+    hf::Prim<T> Lf, Rf;
+    if (RECON == RECON_PCM) {
+      int const pl = S::at(a - 1 + H, c, S::LA);
+      Lf = prim_at(Ps, S::NP, pl, b);
+      Rf = prim_at(Ps, S::NP, pl + S::STRIDE, b);
+    } else {
+      Lf = prim_at(QLs, S::NR, S::at(a, c, S::LR), b);
+      Rf = prim_at(QRs, S::NR, S::at(a + 1, c, S::LR), b);
+    }
+    T fl[NSLOT];
+    riemann<T, SOLVER>(Lf, Rf, fl, b);
+#pragma unroll
+    for (int q = 0; q < NSLOT; q++)
+      if (live(q, b)) Fs[q * S::NF + f] = fl[q];
+  }
+  __syncthreads();
+
+  int a, c, gx, gy, gz;
+  S::split(t, L, a, c);
+  cell(a, c, gx, gy, gz);
+  bool real = gx < b.nx - ng;
+  if (!one_d) real = real && gy < b.ny - ng && gz < b.nz - ng;
+  if (!real) return;
+  long long const gid = b.id(gx, gy, gz);
+  int const fm        = S::at(a, c, S::LF);
+  T const dtod        = (T)(dt / (DIR == 0 ? b.dx : DIR == 1 ? b.dy : b.dz));
+  T d[NSLOT];
+#pragma unroll
+  for (int q = 0; q < NSLOT; q++)
+    d[q] = live(q, b) ? dtod * (Fs[q * S::NF + fm] - Fs[q * S::NF + fm + S::STRIDE]) : T(0);
+  // rotated momenta back to x, y, z
+  T acc[NSLOT];
+  acc[0]  = d[0];
+  acc[o1] = d[1];
+  acc[o2] = d[2];
+  acc[o3] = d[3];
+#pragma unroll
+  for (int q = 4; q < NSLOT; q++) acc[q] = d[q];
+  if (!FIRST) {
+#pragma unroll
+    for (int q = 0; q < NSLOT; q++)
+      if (live(q, b)) acc[q] = dU[(long long)q * n + gid] + acc[q];
+  }
+  if constexpr (!FINAL) {
+#pragma unroll
+    for (int q = 0; q < NSLOT; q++)
+      if (live(q, b)) dU[(long long)q * n + gid] = acc[q];
+  } else {
+    final_update(b, gid, acc, U, GEp, Epre, status);
+  }
+}
+
+template <typename T, int DIR, int L, int WA, int WB, bool FIRST, bool FINAL>
+cudaError_t launch_sweep(const Box &b, int recon, int solver, const T *Wh, T *dU, double *U, const Scratch &sc,
+                         double dt, const double *dtp, cudaStream_t s)
+{
+  // real cells along the sweep (ra) and across it (rb: the WA axis, rc: the WB axis)
+  bool const one_d = (b.ny == 1 && b.nz == 1);
+  int const rx = b.nx - 2 * b.ng, ry = one_d ? 1 : b.ny - 2 * b.ng, rz = one_d ? 1 : b.nz - 2 * b.ng;
+  int const ra = DIR == 0 ? rx : DIR == 1 ? ry : rz;
+  int const rb = DIR == 0 ? ry : rx;
+  int const rc = DIR == 2 ? ry : rz;
+  dim3 grid((ra + L - 1) / L, (rb + WA - 1) / WA, (rc + WB - 1) / WB);
+  void (*k)(Box, const T *, T *, double *, const double *, double *, int *, double, const double *);
+  size_t per_q;
+#define CGB_PICK(R)                                                                                        \
+  per_q = Sweep<DIR, L, WA, WB, R>::PER_Q;                                                                \
+  k     = (solver == SOLVER_ROE) ? k_fsweep<T, DIR, L, WA, WB, R, SOLVER_ROE, FIRST, FINAL>                \
+                                 : k_fsweep<T, DIR, L, WA, WB, R, SOLVER_HLLC, FIRST, FINAL>;
+  if (recon == RECON_PPMC) {
+    CGB_PICK(RECON_PPMC)
+  } else if (recon == RECON_PLMC) {
+    CGB_PICK(RECON_PLMC)
+  } else {
+    CGB_PICK(RECON_PCM)
+  }
+#undef CGB_PICK
+  size_t const sm = sizeof(T) * (size_t)nslot(b) * per_q;
+  cudaError_t e   = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k<<<grid, L * WA * WB, sm, s>>>(b, Wh, dU, U, sc.GEp, sc.Epre, sc.status, dt, dtp);
+  return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------------------------------
@@ -560,27 +609,15 @@ cudaError_t launch_fast(const Box &b, int recon, int solver, double *U, const Sc
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   if (marks) cudaEventRecord(marks[1], s);
-  {
-    int const rx = b.nx - 2 * b.ng, ry = b.ny - 2 * b.ng, rz = b.nz - 2 * b.ng;
-    dim3 grid((rx + TX - 1) / TX, TY > 1 ? (ry + TY - 1) / TY : 1, TZ > 1 ? (rz + TZ - 1) / TZ : 1);
-    void (*k)(Box, const T *, double *, const double *, double *, int *, double, const double *);
-    size_t per_q;
-#define CGB_PICK(R)                                                                                      \
-  per_q = FSizes<TX, TY, TZ, R>::PER_Q;                                                                 \
-  k     = (solver == SOLVER_ROE) ? k_fcorr<T, TX, TY, TZ, R, SOLVER_ROE> : k_fcorr<T, TX, TY, TZ, R, SOLVER_HLLC>;
-    if (recon == RECON_PPMC) {
-      CGB_PICK(RECON_PPMC)
-    } else if (recon == RECON_PLMC) {
-      CGB_PICK(RECON_PLMC)
-    } else {
-      CGB_PICK(RECON_PCM)
-    }
-#undef CGB_PICK
-    size_t const sm = sizeof(T) * (size_t)nslot(b) * per_q;
-    if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess) return e;
-    k<<<grid, TX * TY * TZ, sm, s>>>(b, Wh, U, sc.GEp, sc.Epre, sc.status, dt, dtp);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  // corrector: x, y, z sweeps; W^n is dead after the predictor and holds the accumulator
+  if (b.ny == 1 && b.nz == 1) {
+    e = launch_sweep<T, 0, 128, 1, 1, true, true>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
+  } else {
+    e = launch_sweep<T, 0, 64, 2, 2, true, false>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
+    if (e == cudaSuccess) e = launch_sweep<T, 1, 32, 8, 1, false, false>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
+    if (e == cudaSuccess) e = launch_sweep<T, 2, 32, 8, 1, false, true>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
   }
+  if (e != cudaSuccess) return e;
   if (marks) cudaEventRecord(marks[2], s);
   return cudaSuccess;
 }

@@ -23,11 +23,54 @@ struct Prim {
   T sc[NS_MAX];
 };
 
-template <typename T>
-__device__ __forceinline__ T sgnT(T a)
+// Comparisons of the limiters.  For double they run on the integer pipes, on the IEEE bit
+// patterns: the step is bound by the FP64 pipe, where every compare and min/max is a full-rate
+// FP64 instruction (DSETP), while the integer pipes sit idle.  Results equal the FP64
+// comparisons for finite inputs (-0 and +0 compare equal).  Sign tests of a product (a*b > 0)
+// read the operands' signs, which differs from the rounded product only if it underflows to
+// zero (|a*b| < 5e-324).  The float overloads are the plain FP32 operations.
+__device__ __forceinline__ bool is_pos(double x) { return __double_as_longlong(x) > 0; }  // x > 0
+__device__ __forceinline__ bool is_neg(double x)                                          // x < 0
 {
-  return (a < T(0)) ? T(-1) : T(1);
+  return (__double_as_longlong(x) ^ (long long)0x8000000000000000ULL) > 0;
 }
+__device__ __forceinline__ unsigned long long mag_bits(double x)
+{
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+}
+__device__ __forceinline__ bool mag_lt(double a, double b) { return mag_bits(a) < mag_bits(b); }  // |a| < |b|
+__device__ __forceinline__ double mag_min(double a, double b)                                      // min(|a|, |b|)
+{
+  unsigned long long const x = mag_bits(a), y = mag_bits(b);
+  return __longlong_as_double((long long)(x < y ? x : y));
+}
+__device__ __forceinline__ double mag_max(double a, double b)  // max(|a|, |b|)
+{
+  unsigned long long const x = mag_bits(a), y = mag_bits(b);
+  return __longlong_as_double((long long)(x > y ? x : y));
+}
+// fmax(x, c) for a constant c > 0: as signed 64-bit integers, every negative double (and -0)
+// orders below every non-negative one, and non-negative doubles order by magnitude
+__device__ __forceinline__ double max_pos(double x, double c)
+{
+  return __double_as_longlong(x) < __double_as_longlong(c) ? c : x;
+}
+__device__ __forceinline__ bool is_pos(float x) { return x > 0.f; }
+__device__ __forceinline__ bool is_neg(float x) { return x < 0.f; }
+__device__ __forceinline__ bool mag_lt(float a, float b) { return fabsf(a) < fabsf(b); }
+__device__ __forceinline__ float mag_min(float a, float b) { return fminf(fabsf(a), fabsf(b)); }
+__device__ __forceinline__ float mag_max(float a, float b) { return fmaxf(fabsf(a), fabsf(b)); }
+__device__ __forceinline__ float max_pos(float x, float c) { return fmaxf(x, c); }
+__device__ __forceinline__ bool prod_pos(double a, double b)  // a * b > 0
+{
+  return is_pos(a) ? is_pos(b) : (is_neg(a) && is_neg(b));
+}
+__device__ __forceinline__ bool prod_neg(double a, double b)  // a * b < 0
+{
+  return is_pos(a) ? is_neg(b) : (is_neg(a) && is_pos(b));
+}
+__device__ __forceinline__ bool prod_pos(float a, float b) { return a * b > 0.f; }
+__device__ __forceinline__ bool prod_neg(float a, float b) { return a * b < 0.f; }
 
 template <typename T>
 struct Eps;
@@ -76,10 +119,11 @@ __device__ __forceinline__ void ppm1(T im2, T im1, T i, T ip1, T ip2, T &L_iph, 
   auto limit    = [&](T ci, T cim1, T iface, T s2i, T s2im1) -> T {
     T const s2c = T(3) * (cim1 + ci - T(2) * iface);
     T lim       = T(0);
-    if (sgnT(s2c) == sgnT(s2im1) && sgnT(s2c) == sgnT(s2i))
-      lim = sgnT(s2c) * fmin(C2 * fabs(s2im1), fmin(C2 * fabs(s2i), fabs(s2c)));
+    bool const n = is_neg(s2c);
+    // sgn(s2c) min(C2 |s2im1|, C2 |s2i|, |s2c|); C2 * min(|a|, |b|) == min(C2 |a|, C2 |b|)
+    if (n == is_neg(s2im1) && n == is_neg(s2i)) lim = copysign(mag_min(C2 * mag_min(s2im1, s2i), s2c), s2c);
     T const dl = iface - cim1, dr = ci - iface;
-    return (dl * dr < T(0)) ? T(0.5) * (cim1 + ci) - lim * sixth : iface;
+    return prod_neg(dl, dr) ? T(0.5) * (cim1 + ci) - lim * sixth : iface;
   };
   T const sl    = i - im1;
   T const sr    = ip1 - i;
@@ -95,23 +139,25 @@ __device__ __forceinline__ void ppm1(T im2, T im1, T i, T ip1, T ip2, T &L_iph, 
   L             = limit(ip1, i, L, d2ip1, d2i);
   T const sfl   = i - R;
   T const sfr   = L - i;
-  if ((sfl * sfr) <= T(0) || ((ip1 - i) * (i - im1)) <= T(0)) {
+  if (!prod_pos(sfl, sfr) || !prod_pos(ip1 - i, i - im1)) {
     T const d2f = T(6) * (R + L - T(2) * i);
-    T cmax      = fmax(fmax(fmax(fabs(im2), fabs(im1)), fmax(fabs(i), fabs(ip1))), fabs(ip2));
-    T rho       = T(0);
-    if (fabs(d2f) > Eps<T>::roundoff * cmax) {
-      T d2lim = T(0);
-      if (sgnT(d2im1) == sgnT(d2i) && sgnT(d2im1) == sgnT(d2ip1) && sgnT(d2im1) == sgnT(d2f))
-        d2lim = sgnT(d2f) * fmin(fmin(C2 * fabs(d2im1), C2 * fabs(d2i)), fmin(C2 * fabs(d2ip1), fabs(d2f)));
+    T const cmax = mag_max(mag_max(mag_max(im2, im1), mag_max(i, ip1)), ip2);
+    T rho        = T(0);
+    if (mag_lt(Eps<T>::roundoff * cmax, d2f)) {
+      T d2lim      = T(0);
+      bool const n = is_neg(d2im1);
+      if (n == is_neg(d2i) && n == is_neg(d2ip1) && n == is_neg(d2f))
+        d2lim = copysign(mag_min(C2 * mag_min(mag_min(d2im1, d2i), d2ip1), d2f), d2f);
       rho = d2lim * rcp(d2f);
     }
-    if (rho <= T(1) - Eps<T>::roundoff) {
+    // rho >= 0 (d2lim carries the sign of d2f), so rho <= 1 - eps compares magnitudes
+    if (!mag_lt(T(1) - Eps<T>::roundoff, rho)) {
       R = i - rho * sfl;
       L = i + rho * sfr;
     }
   } else {
-    if (fabs(sfl) >= T(2) * fabs(sfr)) R = i - T(2) * sfr;
-    if (fabs(sfr) >= T(2) * fabs(sfl)) L = i + T(2) * sfl;
+    if (!mag_lt(sfl, T(2) * sfr)) R = i - T(2) * sfr;
+    if (!mag_lt(sfr, T(2) * sfl)) L = i + T(2) * sfl;
   }
   L_iph = L;
   R_imh = R;
@@ -196,21 +242,21 @@ __device__ __forceinline__ void ppmc_cell(const Prim<T> &cm2, const Prim<T> &cm1
     if (k < ns) ppm1(cm2.sc[k], cm1.sc[k], c.sc[k], cp1.sc[k], cp2.sc[k], L.sc[k], R.sc[k]);
   }
   T const tiny = T(TINY);
-  R.d = fmax(R.d, tiny);
-  L.d = fmax(L.d, tiny);
-  R.p = fmax(R.p, tiny);
-  L.p = fmax(L.p, tiny);
+  R.d = max_pos(R.d, tiny);
+  L.d = max_pos(L.d, tiny);
+  R.p = max_pos(R.p, tiny);
+  L.p = max_pos(L.p, tiny);
 }
 
 template <typename T>
 __device__ __forceinline__ T plm_vl(T l, T r)  // van Leer average of two slopes
 {
-  return (l * r > T(0)) ? T(2) * l * r / (l + r) : T(0);
+  return prod_pos(l, r) ? T(2) * l * r / (l + r) : T(0);
 }
 template <typename T>
 __device__ __forceinline__ T plm_mono(T l, T r, T cc, T vg)  // monotonised slope
 {
-  if (l * r > T(0)) return copysign(fmin(T(2) * fmin(fabs(l), fabs(r)), fmin(fabs(cc), fabs(vg))), cc);
+  if (prod_pos(l, r)) return copysign(mag_min(T(2) * mag_min(l, r), mag_min(cc, vg)), cc);
   return T(0);
 }
 
@@ -302,10 +348,10 @@ __device__ __forceinline__ void plmc_cell(const Prim<T> &cm, const Prim<T> &c, c
     }
   }
   T const tiny = T(TINY);
-  R.d = fmax(R.d, tiny);
-  L.d = fmax(L.d, tiny);
-  R.p = fmax(R.p, tiny);
-  L.p = fmax(L.p, tiny);
+  R.d = max_pos(R.d, tiny);
+  L.d = max_pos(L.d, tiny);
+  R.p = max_pos(R.p, tiny);
+  L.p = max_pos(L.p, tiny);
 }
 
 // u / e > eta without the division, keeping the quotient's sign behaviour: the total energy
@@ -324,10 +370,10 @@ __device__ __forceinline__ bool ratio_gt(T u, T e, T eta)
 template <typename T>
 __device__ __forceinline__ T pressure_used(const Prim<T> &s, T E, T ig1, T g1, int de)
 {
-  if (!de) return fmax(s.p, T(TINY));
+  if (!de) return max_pos(s.p, T(TINY));
   T const eth = s.p * ig1;
   T const p   = ratio_gt(eth, E, T(ETA_1)) ? s.p : s.d * s.ge * g1;
-  return fmax(p, T(TINY));
+  return max_pos(p, T(TINY));
 }
 
 // HLLC flux (hllc_cuda.cu:19-307) from primitive interface states; f in rotated order
@@ -367,7 +413,7 @@ __device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, i
     dSl = Sl - l.vn, dSr = Sr - r.vn;
   }
   T const gel = l.ge, ger = r.ge;  // specific
-  if (Sl > T(0)) {
+  if (is_pos(Sl)) {
     f[0] = mxl, f[1] = mxl * l.vn + pl, f[2] = myl * l.vn, f[3] = mzl * l.vn, f[4] = (El + pl) * l.vn;
 #pragma unroll
     for (int k = 0; k < NS_MAX; k++)
@@ -375,7 +421,7 @@ __device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, i
     if (de) f[5] = mxl * gel;
     return;
   }
-  if (Sr < T(0)) {
+  if (is_neg(Sr)) {
     f[0] = mxr, f[1] = mxr * r.vn + pr, f[2] = myr * r.vn, f[3] = mzr * r.vn, f[4] = (Er + pr) * r.vn;
 #pragma unroll
     for (int k = 0; k < NS_MAX; k++)
@@ -385,14 +431,15 @@ __device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, i
   }
   T const ql = l.d * dSl, qr = r.d * dSr;  // mass fluxes relative to the outer waves
   T const Sm  = (qr * r.vn - ql * l.vn + pl - pr) * rcp(qr - ql);
-  if (std::is_same<T, float>::value) {
-    // Single precision: the same flux in the one-sided form F*K = FK + SK (U*K - UK) (K = L
-    // when Sm >= 0, else R; Batten's symmetric sum below equals it exactly), with U*K - UK
-    // written without cancellation as k (1, SK, vt1, vt2, (EK + pK)/dK + (SK - vK) Sm, ...),
-    // k = SK (Sm - vK) / (SK - Sm).  The symmetric sum subtracts terms of the size of the
-    // wave speeds, which a near-vacuum interface state (density floored at TINY) makes ~1e9,
-    // and that cancellation costs every significant digit in FP32.
-    bool const lft = Sm >= T(0);
+  {
+    // The flux in the one-sided form F*K = FK + SK (U*K - UK) (K = L when Sm >= 0, else R;
+    // the reference's symmetric sum (Batten eq. 27) equals it exactly), with U*K - UK written
+    // without cancellation as k (1, SK, vt1, vt2, (EK + pK)/dK + (SK - vK) Sm, ...),
+    // k = SK (Sm - vK) / (SK - Sm).  Only the upwind star state is formed, and the symmetric
+    // sum's subtraction of terms of the size of the wave speeds (~1e9 next to a near-vacuum
+    // interface state, density floored at TINY) is avoided: in FP32 that cancellation costs
+    // every significant digit, in FP64 about nine.
+    bool const lft = !is_neg(Sm);  // Sm >= 0
     // field-by-field selects (a reference to l or r would put both states in local memory)
     T const Kd = lft ? l.d : r.d, Kv = lft ? l.vn : r.vn, Kt1 = lft ? l.vt1 : r.vt1, Kt2 = lft ? l.vt2 : r.vt2;
     T const SK = lft ? Sl : Sr, EK = lft ? El : Er, pK = lft ? pl : pr;
@@ -411,33 +458,6 @@ __device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, i
     for (int q = 0; q < NS_MAX; q++)
       if (q < ns) f[6 + q] = Kd * (lft ? l.sc[q] : r.sc[q]) * vk;
     if (de) f[5] = Kd * (lft ? l.ge : r.ge) * vk;
-    return;
-  }
-  T const ps  = ql * (Sm - l.vn) + pl;
-  T const isl = rcp(Sl - Sm), isr = rcp(Sr - Sm);
-  T const dls = ql * isl, drs = qr * isr;
-  T const mxls = (mxl * (Sl - l.vn) + ps - pl) * isl;
-  T const mxrs = (mxr * (Sr - r.vn) + ps - pr) * isr;
-  T const Els  = (El * (Sl - l.vn) - pl * l.vn + ps * Sm) * isl;
-  T const Ers  = (Er * (Sr - r.vn) - pr * r.vn + ps * Sm) * isr;
-  T const aSm = fabs(Sm);
-  T const cr = Sr - aSm, cl = Sl + aSm;
-  // f = 0.5 * (F_L + F_R + (Sr-|Sm|) U*_R + (Sl+|Sm|) U*_L - Sl U_L - Sr U_R)  (Batten eq. 27)
-  f[0] = T(0.5) * (mxl + mxr + cr * drs + cl * dls - Sl * l.d - Sr * r.d);
-  f[1] = T(0.5) * (mxl * l.vn + pl + mxr * r.vn + pr + cr * mxrs + cl * mxls - Sl * mxl - Sr * mxr);
-  f[2] = T(0.5) * (myl * l.vn + myr * r.vn + cr * drs * r.vt1 + cl * dls * l.vt1 - Sl * myl - Sr * myr);
-  f[3] = T(0.5) * (mzl * l.vn + mzr * r.vn + cr * drs * r.vt2 + cl * dls * l.vt2 - Sl * mzl - Sr * mzr);
-  f[4] = T(0.5) * ((El + pl) * l.vn + (Er + pr) * r.vn + cr * Ers + cl * Els - Sl * El - Sr * Er);
-#pragma unroll
-  for (int k = 0; k < NS_MAX; k++) {
-    if (k < ns) {
-      T const ul = l.d * l.sc[k], ur = r.d * r.sc[k];
-      f[6 + k]   = T(0.5) * (ul * l.vn + ur * r.vn + cr * drs * r.sc[k] + cl * dls * l.sc[k] - Sl * ul - Sr * ur);
-    }
-  }
-  if (de) {
-    T const ul = l.d * gel, ur = r.d * ger;
-    f[5]  = T(0.5) * (ul * l.vn + ur * r.vn + cr * drs * ger + cl * dls * gel - Sl * ul - Sr * ur);
   }
 }
 
