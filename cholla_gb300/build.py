@@ -24,6 +24,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relax
 # they reproduce the reference's -fmad=false build bit for bit.
 PER_FILE = {
     "hydro_exact.cu": ["-fmad=false"],
+    "mhd_exact.cu": ["-fmad=false"],
 }
 
 

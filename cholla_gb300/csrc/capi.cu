@@ -52,6 +52,7 @@ void free_slot(ScratchSlot &sl)
   cudaFree(sl.s.dti);
   cudaFree(sl.s.status);
   cudaFree(sl.s.W);
+  cudaFree(sl.s.mhd);
   sl   = ScratchSlot{};
 }
 
@@ -70,12 +71,13 @@ int ensure_slot(int nx, int ny, int nz, int nf, int mhd)
     if (cudaMalloc(p, bytes) != cudaSuccess) return false;
     return cudaMemset(*p, 0, bytes) == cudaSuccess;
   };
-  bool ok = alloc((void **)&s.Uh, n * nf * sizeof(double)) && alloc((void **)&s.GEp, n * sizeof(double)) &&
-            alloc((void **)&s.Epre, n * sizeof(double)) && alloc((void **)&s.dti, sizeof(unsigned long long)) &&
-            alloc((void **)&s.status, sizeof(int)) && alloc((void **)&s.W, 2 * (nf + 1) * n * sizeof(double));
+  bool ok = alloc((void **)&s.dti, sizeof(unsigned long long)) && alloc((void **)&s.status, sizeof(int));
   if (ok && mhd) {
-    ok = alloc((void **)&s.emf, 3 * n * sizeof(double)) && alloc((void **)&s.Fx, n * (nf - 1) * sizeof(double)) &&
-         alloc((void **)&s.Fy, n * (nf - 1) * sizeof(double)) && alloc((void **)&s.Fz, n * (nf - 1) * sizeof(double));
+    // U½ + 6 interface-state arrays + 3 flux arrays of nf - 1 fields + 3 EMF fields
+    ok = alloc((void **)&s.mhd, ((size_t)nf + 9 * (size_t)(nf - 1) + 3) * n * sizeof(double));
+  } else if (ok) {
+    ok = alloc((void **)&s.Uh, n * nf * sizeof(double)) && alloc((void **)&s.GEp, n * sizeof(double)) &&
+         alloc((void **)&s.Epre, n * sizeof(double)) && alloc((void **)&s.W, 2 * (nf + 1) * n * sizeof(double));
   }
   g_slot.s    = s;
   g_slot.live = true;
@@ -223,11 +225,18 @@ int cgb_vl_algorithm_3d(double *d_conserved, double *d_grav_potential, int nx, i
   cgb::Box b;
   int rc = make_box(b, nx, ny, nz, n_ghost, n_fields, dx, dy, dz, density_floor, g_scheme);
   if (rc != CGB_OK) return rc;
-  int const H = g_scheme.reconstruction == CGB_PPMC ? 4 : g_scheme.reconstruction == CGB_PLMC ? 3 : 2;
+  int const H = (g_scheme.reconstruction == CGB_PPMC ? 4 : g_scheme.reconstruction == CGB_PLMC ? 3 : 2) +
+                (g_scheme.mhd ? 1 : 0);
   if (n_ghost < H) return fail(CGB_ERR_ARGS, "n_ghost too small for the reconstruction");
-  if (g_scheme.mhd) return fail(CGB_ERR_UNSUPPORTED, "MHD step not built in this version");
+  if (g_scheme.mhd && g_scheme.precision != CGB_FP64)
+    return fail(CGB_ERR_UNSUPPORTED, "the MHD step is built in exact FP64 only");
   rc = ensure_slot(nx, ny, nz, n_fields, g_scheme.mhd);
   if (rc != CGB_OK) return rc;
+  if (g_scheme.mhd) {
+    cudaError_t e = cgb::mhd_exact_step(b, g_scheme.reconstruction, d_conserved, g_slot.s.mhd, dt, nullptr, g_stream);
+    if (e != cudaSuccess) return cuda_fail(e, "vl_algorithm_3d (MHD)");
+    return CGB_OK;
+  }
   cudaError_t e = cgb::hydro_step(b, g_scheme.reconstruction, g_scheme.riemann_solver, g_scheme.precision,
                                   d_conserved, g_slot.s, dt, nullptr, 0.0, 0, 0, g_stream);
   if (e != cudaSuccess) return cuda_fail(e, "vl_algorithm_3d");
@@ -312,14 +321,15 @@ int cgb_calc_dt_gpu(const double *d_conserved, int nx, int ny, int nz, int n_gho
   b.nx = nx, b.ny = ny, b.nz = nz, b.ng = n_ghost, b.nf = expected_fields(s), b.ns = s.n_scalars;
   b.de = s.dual_energy, b.mhd = s.mhd, b.floor_on = 0, b.n = (long long)nx * ny * nz, b.gamma = gamma;
   b.dx = dx, b.dy = dy, b.dz = dz, b.density_floor = 0;
-  if (b.mhd) return fail(CGB_ERR_UNSUPPORTED, "MHD CFL not built in this version");
+  if (b.mhd && !(ny > 1 && nz > 1)) return fail(CGB_ERR_ARGS, "MHD boxes are 3D");
   if (!(nx > 1 && ((ny == 1 && nz == 1) || (ny > 1 && nz > 1)))) return fail(CGB_ERR_ARGS, "1D or 3D boxes only");
   static unsigned long long *d_dti = nullptr;
   if (!d_dti && cudaMalloc(&d_dti, sizeof(unsigned long long)) != cudaSuccess)
     return fail(CGB_ERR_NOMEM, "dt buffer");
   if (!g_dti_host && cudaMallocHost(&g_dti_host, sizeof(unsigned long long)) != cudaSuccess)
     return fail(CGB_ERR_NOMEM, "pinned dt buffer");
-  cudaError_t e = cgb::hydro_calc_dt(b, d_conserved, d_dti, g_stream);
+  cudaError_t e = b.mhd ? cgb::mhd_calc_dt(b, d_conserved, d_dti, g_stream)
+                        : cgb::hydro_calc_dt(b, d_conserved, d_dti, g_stream);
   if (e != cudaSuccess) return cuda_fail(e, "calc_dt");
   e = cudaMemcpyAsync(g_dti_host, d_dti, sizeof(unsigned long long), cudaMemcpyDeviceToHost, g_stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(g_stream);
@@ -363,9 +373,26 @@ int cgb_set_boundaries(double *d_conserved, int nx, int ny, int nz, int n_ghost,
 int cgb_max_magnetic_divergence(const double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields,
                                 double dx, double dy, double dz, double *max_divb)
 {
-  (void)d_conserved, (void)nx, (void)ny, (void)nz, (void)n_ghost, (void)n_fields, (void)dx, (void)dy, (void)dz;
-  (void)max_divb;
-  return fail(CGB_ERR_UNSUPPORTED, "MHD not built in this version");
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!d_conserved || !max_divb) return fail(CGB_ERR_ARGS, "null pointer");
+  if (!g_scheme.mhd) return fail(CGB_ERR_ARGS, "the scheme has no magnetic field");
+  cgb::Box b;
+  int const rc = make_box(b, nx, ny, nz, n_ghost, n_fields, dx, dy, dz, 0.0, g_scheme);
+  if (rc != CGB_OK) return rc;
+  if (ny < 2 || nz < 2) return fail(CGB_ERR_ARGS, "MHD boxes are 3D");
+  static unsigned long long *d_div = nullptr;
+  if (!d_div && cudaMalloc(&d_div, sizeof(unsigned long long)) != cudaSuccess)
+    return fail(CGB_ERR_NOMEM, "divergence buffer");
+  if (!g_dti_host && cudaMallocHost(&g_dti_host, sizeof(unsigned long long)) != cudaSuccess)
+    return fail(CGB_ERR_NOMEM, "pinned result buffer");
+  cudaError_t e = cgb::mhd_max_divb(b, d_conserved, d_div, g_stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(g_dti_host, d_div, sizeof(unsigned long long), cudaMemcpyDeviceToHost, g_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "max_magnetic_divergence");
+  unsigned long long const bits = *g_dti_host;
+  std::memcpy(max_divb, &bits, sizeof(double));
+  return CGB_OK;
 }
 
 }  // extern "C"

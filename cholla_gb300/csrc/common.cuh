@@ -52,6 +52,7 @@ struct Scratch {
   void *W;               // half-step primitives of the fast / mixed paths (nq fields, 8 bytes each)
   unsigned long long *dti;  // encoded max inverse time step (one per box)
   int *status;              // device status word (bad cells seen, ...)
+  double *mhd;              // MHD step: U½, 6 interface-state and 3 flux arrays, EMFs (mhd_scratch_doubles)
 };
 
 }  // namespace cgb

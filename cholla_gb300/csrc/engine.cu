@@ -57,7 +57,7 @@ int box_fail(cgb_box *bx, int code, const std::string &m)
 void free_box_mem(cgb_box *bx)
 {
   void *ps[] = {bx->s.Uh, bx->s.GEp, bx->s.Epre, bx->s.emf, bx->s.Fx, bx->s.Fy, bx->s.Fz, bx->s.dti, bx->s.status,
-                bx->dt_t, bx->s.W};
+                bx->dt_t, bx->s.W, bx->s.mhd};
   for (void *p : ps)
     if (p) cudaFree(p);
   if (bx->graph) cudaGraphExecDestroy(bx->graph);
@@ -101,6 +101,21 @@ cudaError_t one_step(cgb_box *bx, double *U, double c_cfl, cudaStream_t st, bool
     m = &bx->marks[bx->used];
     bx->used += 4;
   }
+  if (bx->b.mhd) {
+    // MHD: the step, the temperature floor, then the CFL reduction for the next step (the
+    // fast magnetosonic speed needs the cell-centred field, so it is its own pass)
+    if (m) cudaEventRecord(m[0], st);
+    if ((e = cgb::mhd_exact_step(bx->b, bx->scheme.reconstruction, U, bx->s.mhd, 0.0, bx->dt_t, st)) !=
+        cudaSuccess)
+      return e;
+    if (m) cudaEventRecord(m[1], st), cudaEventRecord(m[2], st);
+    if (bx->scheme.temperature_floor &&
+        (e = cgb::hydro_temperature_floor(bx->b, U, bx->scheme.U_floor, st)) != cudaSuccess)
+      return e;
+    if ((e = cgb::mhd_calc_dt(bx->b, U, bx->s.dti, st)) != cudaSuccess) return e;
+    if (m) cudaEventRecord(m[3], st);
+    return cudaSuccess;
+  }
   return cgb::hydro_step(bx->b, bx->scheme.reconstruction, bx->scheme.riemann_solver, bx->scheme.precision, U, bx->s,
                          0.0, bx->dt_t, bx->scheme.U_floor, bx->scheme.temperature_floor, 1, st, m);
 }
@@ -116,12 +131,13 @@ int cgb_box_create(cgb_box **out, int nx, int ny, int nz, int n_ghost, double dx
   if (!out || !scheme || !flags) return box_fail(nullptr, CGB_ERR_ARGS, "null argument");
   *out = nullptr;
   cgb_scheme const &s = *scheme;
-  if (s.mhd) return box_fail(nullptr, CGB_ERR_UNSUPPORTED, "MHD boxes not built in this version");
   if (s.precision < CGB_FP64 || s.precision > CGB_FP64_FAST) return box_fail(nullptr, CGB_ERR_ARGS, "bad precision");
-  if (s.n_scalars < 0 || s.n_scalars > cgb::NS_MAX || !(s.gamma > 1.0) || s.riemann_solver == CGB_HLLD)
-    return box_fail(nullptr, CGB_ERR_ARGS, "bad scheme");
+  if (s.n_scalars < 0 || s.n_scalars > cgb::NS_MAX || !(s.gamma > 1.0) || (s.riemann_solver == CGB_HLLD) != (s.mhd != 0))
+    return box_fail(nullptr, CGB_ERR_ARGS, "bad scheme (MHD goes with HLLD and only with it)");
+  if (s.mhd && (s.precision != CGB_FP64 || s.dual_energy || ny < 2 || nz < 2))
+    return box_fail(nullptr, CGB_ERR_UNSUPPORTED, "MHD boxes are 3D, exact FP64, without dual energy");
   bool const one_d = ny == 1 && nz == 1;
-  int const H      = s.reconstruction == CGB_PPMC ? 4 : s.reconstruction == CGB_PLMC ? 3 : 2;
+  int const H = (s.reconstruction == CGB_PPMC ? 4 : s.reconstruction == CGB_PLMC ? 3 : 2) + (s.mhd ? 1 : 0);
   if (n_ghost < H || nx < 2 * n_ghost + 1 || (!one_d && (ny < 2 * n_ghost + 1 || nz < 2 * n_ghost + 1)))
     return box_fail(nullptr, CGB_ERR_ARGS, "box too small for the reconstruction stencil");
   if (!(dx > 0 && dy > 0 && dz > 0)) return box_fail(nullptr, CGB_ERR_ARGS, "cell sizes must be positive");
@@ -132,8 +148,8 @@ int cgb_box_create(cgb_box **out, int nx, int ny, int nz, int n_ghost, double dx
   std::memcpy(bx->flags, flags, sizeof(bx->flags));
   cgb::Box &b = bx->b;
   b.nx = nx, b.ny = ny, b.nz = nz, b.ng = n_ghost, b.ns = s.n_scalars;
-  b.de = s.dual_energy ? 1 : 0, b.mhd = 0;
-  b.nf = 5 + s.n_scalars + b.de;
+  b.de = s.dual_energy ? 1 : 0, b.mhd = s.mhd ? 1 : 0;
+  b.nf = 5 + s.n_scalars + b.de + 3 * b.mhd;
   b.floor_on = one_d ? 0 : (s.density_floor ? 1 : 0);
   b.n = (long long)nx * ny * nz;
   b.gamma = s.gamma, b.dx = dx, b.dy = dy, b.dz = dz, b.density_floor = 0.0;
@@ -142,9 +158,13 @@ int cgb_box_create(cgb_box **out, int nx, int ny, int nz, int n_ghost, double dx
     if (cudaMalloc(p, bytes) != cudaSuccess) return false;
     return cudaMemset(*p, 0, bytes) == cudaSuccess;
   };
-  bool ok = al((void **)&bx->s.Uh, n * b.nf * 8) && al((void **)&bx->s.GEp, n * 8) && al((void **)&bx->s.Epre, n * 8) &&
-            al((void **)&bx->s.dti, 8) && al((void **)&bx->s.status, 4) && al((void **)&bx->dt_t, 16) &&
-            al((void **)&bx->s.W, 2 * (size_t)(b.nf + 1) * n * 8);
+  bool ok = al((void **)&bx->s.dti, 8) && al((void **)&bx->s.status, 4) && al((void **)&bx->dt_t, 16);
+  if (ok && b.mhd) {
+    ok = al((void **)&bx->s.mhd, cgb::mhd_scratch_doubles(b) * 8);
+  } else if (ok) {
+    ok = al((void **)&bx->s.Uh, n * b.nf * 8) && al((void **)&bx->s.GEp, n * 8) && al((void **)&bx->s.Epre, n * 8) &&
+         al((void **)&bx->s.W, 2 * (size_t)(b.nf + 1) * n * 8);
+  }
   if (!ok) {
     cudaGetLastError();
     free_box_mem(bx);
@@ -219,7 +239,8 @@ int cgb_box_advance(cgb_box *bx, double *d_conserved, int n_steps, double c_cfl,
   bx->last_stream = st;
   cudaError_t e;
   if (!bx->dti_valid) {
-    if ((e = cgb::hydro_calc_dt(bx->b, d_conserved, bx->s.dti, st)) != cudaSuccess)
+    if ((e = bx->b.mhd ? cgb::mhd_calc_dt(bx->b, d_conserved, bx->s.dti, st)
+                       : cgb::hydro_calc_dt(bx->b, d_conserved, bx->s.dti, st)) != cudaSuccess)
       return box_fail(bx, CGB_ERR_CUDA, cudaGetErrorString(e));
     bx->dti_valid = true;
   }

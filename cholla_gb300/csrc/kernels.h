@@ -27,6 +27,17 @@ cudaError_t negative_density_average(const Box &b, double *U, cudaStream_t s);
 cudaError_t hydro_calc_dt(const Box &b, const double *U, unsigned long long *dti, cudaStream_t s);
 cudaError_t hydro_temperature_floor(const Box &b, double *U, double U_floor, cudaStream_t s);
 
+// MHD (mhd_exact.cu): the VL step with HLLD and constrained transport, FP64 in the reference's
+// operation order.  scratch holds mhd_scratch_doubles(b) doubles and must start zeroed.
+size_t mhd_scratch_doubles(const Box &b);
+// dt_dev != null: dt is read on the device (the box engine keeps it there)
+cudaError_t mhd_exact_step(const Box &b, int recon, double *U, double *scratch, double dt, const double *dt_dev,
+                           cudaStream_t s);
+// max inverse crossing time with the fast magnetosonic speed into *dti (cleared first)
+cudaError_t mhd_calc_dt(const Box &b, const double *U, unsigned long long *dti, cudaStream_t s);
+// max |div B| over the real cells into *out (as the bits of a non-negative double; cleared first)
+cudaError_t mhd_max_divb(const Box &b, const double *U, unsigned long long *out, cudaStream_t s);
+
 // dispatch on the arithmetic: 0 = FP64 in the reference's order, 1 = mixed, 2 = fast FP64
 inline cudaError_t hydro_step(const Box &b, int recon, int solver, int precision, double *U, const Scratch &sc,
                               double dt, const double *dt_dev, double U_floor, int temp_floor, int do_dt,

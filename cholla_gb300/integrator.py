@@ -117,3 +117,11 @@ def Set_Boundaries(dev_conserved, nx, ny, nz, n_ghost, n_fields, flags) -> None:
     3 transmissive, 4 custom (untouched)."""
     arr = (C.c_int * 6)(*[int(f) for f in flags])
     L.check(L.lib().cgb_set_boundaries(_ptr(dev_conserved), nx, ny, nz, n_ghost, n_fields, arr))
+
+
+def Max_Magnetic_Divergence(dev_conserved, nx, ny, nz, n_ghost, n_fields, dx, dy, dz) -> float:
+    """Max |div B| over the real cells of an MHD state (src/mhd/magnetic_divergence.cu:33-76)."""
+    out = C.c_double(0.0)
+    L.check(L.lib().cgb_max_magnetic_divergence(_ptr(dev_conserved), nx, ny, nz, n_ghost, n_fields, dx, dy, dz,
+                                                C.byref(out)))
+    return out.value
