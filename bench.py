@@ -274,6 +274,16 @@ def run_ours(args, world, rank, local):
             bv.close()
             del Uv
 
+    # ---- ideal MHD (PLMC + HLLD + CT, exact FP64) on the same GPU: ours and the reference build ----
+    mhd = None
+    if rank == 0 and not args.no_variants:
+        mhd = run_mhd(args, dev, stream, torch)
+
+    # ---- continuous-batching serving against per-request launches (rank 0) ----
+    serving = None
+    if rank == 0 and not args.no_serving:
+        serving = run_serving(args, torch)
+
     # ---- end to end through the drop-in C ABI with host buffers ----
     e2e = None
     if rank == 0 and not args.no_e2e:
@@ -369,6 +379,8 @@ def run_ours(args, world, rank, local):
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json)",
                          "binding_ceiling": "FP64 pipe: GB300 FP64 FMA measured 1.19 TFLOP/s, divide 60 G/s"},
             "variants": others,
+            "mhd": mhd,
+            "serving": serving,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "reference_gpu": ref_gpu,
@@ -378,6 +390,83 @@ def run_ours(args, world, rank, local):
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
+
+
+def run_mhd(args, dev, stream, torch):
+    """The 3D ideal-MHD workload at n^3 (PLMC + HLLD + constrained transport, beta = 1, random
+    velocities and a divergence-free field from a random vector potential, CFL 0.3): our engine
+    step and the reference's own kernels on the same GPU, 2 timed steps each."""
+    from cholla_gb300 import ics
+    from cholla_gb300 import integrator as I
+    from cholla_gb300.engine import Box
+
+    n, gamma = args.n, 5.0 / 3.0
+    s = I.Scheme(reconstruction="PLMC", riemann_solver="HLLD", mhd=True, dual_energy=False, gamma=gamma)
+    ng = s.n_ghost()
+    U0 = ics.mhd_box(n, ng, gamma, seed=1)
+    nf, N = U0.shape[0], U0.shape[1]
+    dx = 1.0 / n
+    out = {"workload": f"3D ideal MHD {n}^3 periodic, PLMC + HLLD + CT, beta 1, CFL 0.3, exact FP64"}
+    U = torch.from_numpy(U0).to(dev)
+    box = Box(N, N, N, ng, dx, dx, dx, s)
+    box.use_graph(True)
+    box.advance(U, 1, 0.3, stream)
+    stream.synchronize()
+    k = 2
+    ms = time_box(box, U, k, stream, torch) / k
+    box.close()
+    del U
+    out["ours"] = {"ms_per_step": ms, "value": n ** 3 / (ms / 1e3), "unit": "cell-updates/s"}
+    try:
+        from oracle import reference_gpu as R
+
+        if R.available("mhd_plmc_hlld"):
+            R.init("mhd_plmc_hlld")
+            R.set_stream(stream)
+            Ur = torch.from_numpy(U0).to(dev)
+
+            def ref_step():
+                R.set_boundaries(Ur, N, N, N, ng, nf, (1,) * 6)
+                dti = R.calc_dt(Ur, N, N, N, ng, nf, dx, dx, dx, gamma)
+                R.vl_step_3d(Ur, N, N, N, ng, dx, dx, dx, 0.3 / dti, nf, gamma, 0.0)
+
+            ref_step()
+            stream.synchronize()
+            f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            for _ in range(k):
+                ref_step()
+            f1.record(stream)
+            f1.synchronize()
+            rms = f0.elapsed_time(f1) / k
+            out["reference_gpu"] = {"ms_per_step": rms, "value": n ** 3 / (rms / 1e3)}
+            out["speedup_vs_reference_build"] = rms / ms
+            del Ur
+    except Exception as ex:  # the reference build is a comparison, not part of the product
+        out["reference_gpu"] = {"unavailable": str(ex)[:200]}
+    return out
+
+
+def run_serving(args, torch):
+    """Batched serving workload: a seeded Poisson stream of independent 3D hydro jobs (sizes
+    uniform over 32^3 .. 128^3, Sedov-like blast or randomly oriented Sod tube, PPMC + HLLC mixed
+    precision, 100 steps each, admitted by free device memory), served once by the continuous
+    batching server and once by per-request launches (one engine box and CUDA graph per job on
+    its own stream), at each arrival rate.  Latency = arrival to completion of the last step."""
+    from cholla_gb300 import serve
+
+    out = {"workload": "Poisson stream of 3D hydro jobs, n in {32,48,64,96,128}, blast or Sod tube, "
+                       f"PPMC + HLLC mixed, 100 steps, {args.serve_count} requests per rate", "rates": {}}
+    for rate in [float(r) for r in args.serve_rates.split(",") if r]:
+        row = {}
+        for mode in ("batched", "per_request"):
+            reqs = serve.make_requests(rate=rate, count=args.serve_count, seed=17, steps=100)
+            row[mode] = serve.serve(torch, reqs, mode=mode)
+        b, p = row["batched"], row["per_request"]
+        row["throughput_ratio"] = b["cell_updates_per_s"] / p["cell_updates_per_s"]
+        row["p99_ratio"] = p["p99_ms"] / b["p99_ms"]
+        out["rates"][f"{rate:g}"] = row
+    return out
 
 
 def load_traffic(n, precision):
@@ -402,6 +491,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-reference-gpu", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-rates", default="10,100,2000")
+    ap.add_argument("--serve-count", type=int, default=40)
     ap.add_argument("--precision", choices=["fp64_fast", "fp64", "mixed"], default="fp64_fast")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -77,6 +77,19 @@ SIGNATURES = {
     "cgb_box_advance": (_I, [_P, _P, _I, _D, _P]),
     "cgb_box_get_time": (_I, [_P, C.POINTER(_D), C.POINTER(_D)]),
     "cgb_box_last_error": (C.c_char_p, []),
+    "cgb_batch_create": (_I, [C.POINTER(_P), C.POINTER(cgb_scheme), _D, _P]),
+    "cgb_batch_destroy": (_I, [_P]),
+    "cgb_batch_job_bytes": (C.c_longlong, [_P, _I, _I, _I]),
+    "cgb_batch_add": (_I, [_P, _P, _I, _I, _I, _I, _D, _D, _D, C.POINTER(_I), _D, C.POINTER(_I)]),
+    "cgb_batch_remove": (_I, [_P, _I]),
+    "cgb_batch_n_jobs": (_I, [_P]),
+    "cgb_batch_set_chains": (_I, [_P, _I]),
+    "cgb_batch_step": (_I, [_P, _I]),
+    "cgb_batch_job_time": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_D)]),
+    "cgb_batch_last_error": (C.c_char_p, []),
+    "cgb_ic_blast": (_I, [_P, _I, _I, _I, _I, _I, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _I, _P]),
+    "cgb_ic_shock_tube": (_I, [_P, _I, _I, _I, _I, _I, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D,
+                               _I, _P]),
 }
 
 

@@ -32,6 +32,9 @@ struct Box {
   double gamma;
   double dx, dy, dz;
   double density_floor;
+  // used by the fast / mixed forms only, set on the host by with_inverses(): 1/dx, 1/dy, 1/dz
+  // and 1/(gamma - 1), so that no kernel thread divides by them
+  double idx, idy, idz, ig1;
   __host__ __device__ long long id(int x, int y, int z) const
   {
     return (long long)x + (long long)y * nx + (long long)z * nx * ny;
@@ -41,6 +44,12 @@ struct Box {
   // number of fields carried by reconstruction / Riemann: d, m(3), E, scalars, [ge]
   __host__ __device__ int nq() const { return 5 + ns + (de ? 1 : 0); }
 };
+
+inline Box with_inverses(Box b)
+{
+  b.idx = 1.0 / b.dx, b.idy = 1.0 / b.dy, b.idz = 1.0 / b.dz, b.ig1 = 1.0 / (b.gamma - 1.0);
+  return b;
+}
 
 // Device scratch of one box, owned by the library (allocated once per box shape).
 struct Scratch {

@@ -14,6 +14,7 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "ghost.cuh"
 #include "hydro_fast.cuh"
 #include "kernels.h"
 
@@ -23,6 +24,10 @@ namespace
 {
 
 constexpr int NSLOT = 6 + NS_MAX;
+// tiles of the 3D step (single boxes and batches alike): predictor 8 x 8 x 4 cells; corrector
+// sweeps along x over 64 x 2 x 2 cells, along y and z over 32 x 8 x 1
+constexpr int PTX = 8, PTY = 8, PTZ = 4;
+constexpr int SXL = 64, SXA = 2, SXB = 2, SYL = 32, SYA = 8, SYB = 1;
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
@@ -118,35 +123,41 @@ template <typename T, int SOLVER>
 __device__ __forceinline__ void riemann(const hf::Prim<T> &L, const hf::Prim<T> &R, T *f, const Box &b)
 {
   if (SOLVER == SOLVER_ROE) {
-    hf::roe(L, R, f, b.ns, b.de, (T)b.gamma);
+    hf::roe(L, R, f, b.ns, b.de, (T)b.gamma, (T)b.ig1);
   } else {
-    hf::hllc(L, R, f, b.ns, b.de, (T)b.gamma);
+    hf::hllc(L, R, f, b.ns, b.de, (T)b.gamma, (T)b.ig1);
   }
 }
 
 // ------------------------------------------------------------------------------------------
 // primitives of every cell of the padded box
 template <typename T>
-__global__ void __launch_bounds__(256) k_fprims(Box b, const double *__restrict__ U, T *__restrict__ Wn)
+__device__ __forceinline__ void fprims_cell(const Box &b, const double *__restrict__ U, T *__restrict__ Wn, long long i)
 {
   long long const n = b.n;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double q[NSLOT];
+  double q[NSLOT];
 #pragma unroll
-    for (int s = 0; s < NSLOT; s++) q[s] = live(s, b) ? U[field(s, b) * n + i] : 0.0;
-    T w[NSLOT];
-    prim_from_cons<T>(q, b, w);
+  for (int s = 0; s < NSLOT; s++) q[s] = live(s, b) ? U[field(s, b) * n + i] : 0.0;
+  T w[NSLOT];
+  prim_from_cons<T>(q, b, w);
 #pragma unroll
-    for (int s = 0; s < NSLOT; s++)
-      if (live(s, b)) Wn[(long long)s * n + i] = w[s];
-  }
+  for (int s = 0; s < NSLOT; s++)
+    if (live(s, b)) Wn[(long long)s * n + i] = w[s];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_fprims(Box b, const double *__restrict__ U, T *__restrict__ Wn)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < b.n; i += (long long)gridDim.x * blockDim.x)
+    fprims_cell(b, U, Wn, i);
 }
 
 // ------------------------------------------------------------------------------------------
+// one TX x TY x TZ tile (block coordinates bx, by, bz) of the predictor
 template <typename T, int TX, int TY, int TZ, int SOLVER>
-__global__ void __launch_bounds__(TX *TY *TZ, 2)
-    k_fpred(Box b, const double *__restrict__ U, const T *__restrict__ Wn, T *__restrict__ W, double *__restrict__ GEp,
-            double dt, const double *__restrict__ dtp)
+__device__ __forceinline__ void fpred_tile(const Box &b, const double *__restrict__ U, const T *__restrict__ Wn,
+                                           T *__restrict__ W, double *__restrict__ GEp, double dt,
+                                           const double *__restrict__ dtp, int bx_, int by_, int bz_)
 {
   if (dtp) dt = *dtp;
   constexpr int HY = TY > 1 ? 1 : 0, HZ = TZ > 1 ? 1 : 0;
@@ -163,9 +174,9 @@ __global__ void __launch_bounds__(TX *TY *TZ, 2)
   T *Fys = Fxs + ns_ * NFX;
   T *Fzs = Fys + ns_ * NFY;
 
-  int const x0 = 1 + blockIdx.x * TX;
-  int const y0 = HY ? 1 + blockIdx.y * TY : 0;
-  int const z0 = HZ ? 1 + blockIdx.z * TZ : 0;
+  int const x0 = 1 + bx_ * TX;
+  int const y0 = HY ? 1 + by_ * TY : 0;
+  int const z0 = HZ ? 1 + bz_ * TZ : 0;
   long long const n = b.n;
 
   for (int t = threadIdx.x; t < NB; t += NT) {
@@ -221,7 +232,7 @@ __global__ void __launch_bounds__(TX *TY *TZ, 2)
   int const fx = i + (TX + 1) * (j + TY * k);
   int const fy = i + TX * (j + (TY + 1) * k);
   int const fz = i + TX * (j + TY * k);
-  T const dtodx = (T)(0.5 * dt / b.dx), dtody = (T)(0.5 * dt / b.dy), dtodz = (T)(0.5 * dt / b.dz);
+  T const dtodx = (T)(0.5 * dt * b.idx), dtody = (T)(0.5 * dt * b.idy), dtodz = (T)(0.5 * dt * b.idz);
   double q[NSLOT];
 #pragma unroll
   for (int s = 0; s < NSLOT; s++) {
@@ -267,6 +278,14 @@ __global__ void __launch_bounds__(TX *TY *TZ, 2)
 #pragma unroll
   for (int s = 0; s < NSLOT; s++)
     if (live(s, b)) W[(long long)s * n + gid] = w[s];
+}
+
+template <typename T, int TX, int TY, int TZ, int SOLVER>
+__global__ void __launch_bounds__(TX *TY *TZ, 2)
+    k_fpred(Box b, const double *__restrict__ U, const T *__restrict__ Wn, T *__restrict__ W, double *__restrict__ GEp,
+            double dt, const double *__restrict__ dtp)
+{
+  fpred_tile<T, TX, TY, TZ, SOLVER>(b, U, Wn, W, GEp, dt, dtp, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -338,10 +357,10 @@ __device__ __forceinline__ void final_update(const Box &b, long long gid, const 
 // accumulator dU (the x sweep starts it).  FINAL (the last sweep): Uⁿ⁺¹ = Uⁿ + (dU + the
 // difference) in FP64 in place, density floor, Epre = pre-sync total energy.
 template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
-__global__ void __launch_bounds__(L *WA *WB, 2)
-    k_fsweep(Box b, const T *__restrict__ W, T *__restrict__ dU, double *__restrict__ U,
-             const double *__restrict__ GEp, double *__restrict__ Epre, int *__restrict__ status, double dt,
-             const double *__restrict__ dtp)
+__device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ W, T *__restrict__ dU,
+                                            double *__restrict__ U, const double *__restrict__ GEp,
+                                            double *__restrict__ Epre, int *__restrict__ status, double dt,
+                                            const double *__restrict__ dtp, int bx_, int by_, int bz_)
 {
   using S = Sweep<DIR, L, WA, WB, RECON>;
   constexpr int H  = S::H;
@@ -358,7 +377,7 @@ __global__ void __launch_bounds__(L *WA *WB, 2)
   int const ng     = b.ng;
   bool const one_d = (b.ny == 1 && b.nz == 1);
   long long const n = b.n;
-  int const a0 = blockIdx.x * L, ca0 = blockIdx.y * WA, cb0 = blockIdx.z * WB;
+  int const a0 = bx_ * L, ca0 = by_ * WA, cb0 = bz_ * WB;
   // global cell of sweep position a (real-cell coordinates, may lie in the ghosts) on pencil c
   auto cell = [&](int a, int c, int &gx, int &gy, int &gz) {
     int const ca = ca0 + c % WA + ng, cb = cb0 + c / WA + ng, g = a0 + a + ng;
@@ -428,7 +447,7 @@ __global__ void __launch_bounds__(L *WA *WB, 2)
   if (!real) return;
   long long const gid = b.id(gx, gy, gz);
   int const fm        = S::at(a, c, S::LF);
-  T const dtod        = (T)(dt / (DIR == 0 ? b.dx : DIR == 1 ? b.dy : b.dz));
+  T const dtod        = (T)(dt * (DIR == 0 ? b.idx : DIR == 1 ? b.idy : b.idz));
   T d[NSLOT];
 #pragma unroll
   for (int q = 0; q < NSLOT; q++)
@@ -453,6 +472,16 @@ __global__ void __launch_bounds__(L *WA *WB, 2)
   } else {
     final_update(b, gid, acc, U, GEp, Epre, status);
   }
+}
+
+template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
+__global__ void __launch_bounds__(L *WA *WB, 2)
+    k_fsweep(Box b, const T *__restrict__ W, T *__restrict__ dU, double *__restrict__ U,
+             const double *__restrict__ GEp, double *__restrict__ Epre, int *__restrict__ status, double dt,
+             const double *__restrict__ dtp)
+{
+  fsweep_tile<T, DIR, L, WA, WB, RECON, SOLVER, FIRST, FINAL>(b, W, dU, U, GEp, Epre, status, dt, dtp, blockIdx.x,
+                                                              blockIdx.y, blockIdx.z);
 }
 
 template <typename T, int DIR, int L, int WA, int WB, bool FIRST, bool FINAL>
@@ -511,15 +540,15 @@ __device__ __forceinline__ void block_max_to(double v, unsigned long long *dst)
 // reciprocal of the density with one Newton step; the selection, sync, floor and the
 // maximum stay FP64.
 template <bool MIX>
-__global__ void __launch_bounds__(256) k_ffinalize(Box b, double *__restrict__ U, const double *__restrict__ Epre,
-                                                   unsigned long long *__restrict__ dti, double U_floor,
-                                                   int temp_floor, int do_dt, double idx, double idy, double idz)
+__device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict__ U, const double *__restrict__ Epre,
+                                                unsigned long long *__restrict__ dti, double U_floor, int temp_floor,
+                                                int do_dt, double idx, double idy, double idz, long long blk)
 {
   int const ng = b.ng;
   bool const one_d = (b.ny == 1 && b.nz == 1);
   int const rx = b.nx - 2 * ng, ry = one_d ? 1 : b.ny - 2 * ng, rz = one_d ? 1 : b.nz - 2 * ng;
   long long const nreal = (long long)rx * ry * rz;
-  long long const r     = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long const r     = blk * blockDim.x + threadIdx.x;
   double m = -1.0;
   if (r < nreal) {
     int const x = (int)(r % rx) + ng;
@@ -576,6 +605,14 @@ __global__ void __launch_bounds__(256) k_ffinalize(Box b, double *__restrict__ U
   if (do_dt) block_max_to(m, dti);
 }
 
+template <bool MIX>
+__global__ void __launch_bounds__(256) k_ffinalize(Box b, double *__restrict__ U, const double *__restrict__ Epre,
+                                                   unsigned long long *__restrict__ dti, double U_floor,
+                                                   int temp_floor, int do_dt, double idx, double idy, double idz)
+{
+  ffinalize_block<MIX>(b, U, Epre, dti, U_floor, temp_floor, do_dt, idx, idy, idz, blockIdx.x);
+}
+
 // ------------------------------------------------------------------------------------------
 template <typename T, int TX, int TY, int TZ>
 size_t fpred_smem(const Box &b)
@@ -613,9 +650,9 @@ cudaError_t launch_fast(const Box &b, int recon, int solver, double *U, const Sc
   if (b.ny == 1 && b.nz == 1) {
     e = launch_sweep<T, 0, 128, 1, 1, true, true>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
   } else {
-    e = launch_sweep<T, 0, 64, 2, 2, true, false>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
-    if (e == cudaSuccess) e = launch_sweep<T, 1, 32, 8, 1, false, false>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
-    if (e == cudaSuccess) e = launch_sweep<T, 2, 32, 8, 1, false, true>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
+    e = launch_sweep<T, 0, SXL, SXA, SXB, true, false>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
+    if (e == cudaSuccess) e = launch_sweep<T, 1, SYL, SYA, SYB, false, false>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
+    if (e == cudaSuccess) e = launch_sweep<T, 2, SYL, SYA, SYB, false, true>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
   }
   if (e != cudaSuccess) return e;
   if (marks) cudaEventRecord(marks[2], s);
@@ -624,22 +661,247 @@ cudaError_t launch_fast(const Box &b, int recon, int solver, double *U, const Sc
 
 }  // namespace
 
+// ==========================================================================================
+// batches: one chunk of jobs per launch, one block per tile.  The chunk (job geometry, pointers
+// and per-kind tile offsets) is the kernel's __grid_constant__ parameter: a block finds its
+// job by binary search over the chunk's offsets and runs the single-box tile code on it, with
+// the job's fields read from the constant bank.
+// ==========================================================================================
+namespace
+{
+
+__host__ __device__ inline void pred_grid(const Box &b, int &gx, int &gy, int &gz)
+{
+  gx = (b.nx - 2 + PTX - 1) / PTX, gy = (b.ny - 2 + PTY - 1) / PTY, gz = (b.nz - 2 + PTZ - 1) / PTZ;
+}
+template <int DIR, int L, int WA, int WB>
+__host__ __device__ inline void sweep_grid(const Box &b, int &ga, int &gb, int &gc)
+{
+  int const rx = b.nx - 2 * b.ng, ry = b.ny - 2 * b.ng, rz = b.nz - 2 * b.ng;
+  int const ra = DIR == 0 ? rx : DIR == 1 ? ry : rz;
+  int const rb = DIR == 0 ? ry : rx;
+  int const rc = DIR == 2 ? ry : rz;
+  ga = (ra + L - 1) / L, gb = (rb + WA - 1) / WA, gc = (rc + WB - 1) / WB;
+}
+__host__ __device__ inline long long real_cells(const Box &b)
+{
+  return (long long)(b.nx - 2 * b.ng) * (b.ny - 2 * b.ng) * (b.nz - 2 * b.ng);
+}
+
+// job j of the chunk with off[kind][j] <= tile < off[kind][j + 1]
+__device__ __forceinline__ int find_job(const BatchChunk &C, int kind, int tile)
+{
+  int lo = 0, hi = C.njobs - 1;
+  while (lo < hi) {
+    int const mid = (lo + hi + 1) >> 1;
+    if (C.off[kind][mid] <= tile)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(256) kb_ghost(const __grid_constant__ BatchChunk C)
+{
+  int const tile     = blockIdx.x;
+  int const j        = find_job(C, BK_CELLS, tile);
+  BatchJob const &J  = C.jobs[j];
+  long long const id = (long long)(tile - C.off[BK_CELLS][j]) * 256 + threadIdx.x;
+  if (id < J.b.n) ghost_cell(J.b, J.U, *reinterpret_cast<const Flags *>(J.flags), id);
+}
+
+// dt = c_cfl / max_dti clamped to t_end (as k_cfl_dt), then the reduction word is cleared for
+// this step's finalize
+__global__ void kb_cfl(const __grid_constant__ BatchChunk C, double c_cfl)
+{
+  int const j = threadIdx.x;
+  if (j >= C.njobs) return;
+  BatchJob const &J = C.jobs[j];
+  double const m    = __longlong_as_double((long long)*J.dti);
+  double dt         = c_cfl / m;
+  double const t    = J.dt_t[1];
+  if (J.t_end > 0.0 && t + dt > J.t_end) dt = J.t_end - t;
+  J.dt_t[0] = dt;
+  J.dt_t[1] = t + dt;
+  *J.dti    = 0ULL;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) kb_prims(const __grid_constant__ BatchChunk C)
+{
+  int const tile     = blockIdx.x;
+  int const j        = find_job(C, BK_CELLS, tile);
+  BatchJob const &J  = C.jobs[j];
+  long long const id = (long long)(tile - C.off[BK_CELLS][j]) * 256 + threadIdx.x;
+  if (id < J.b.n) fprims_cell<T>(J.b, J.U, (T *)J.W, id);
+}
+
+// FP32 tiles: four resident blocks per SM (64 registers), the single-box predictor's occupancy
+template <typename T, int SOLVER>
+__global__ void __launch_bounds__(PTX *PTY *PTZ, sizeof(T) == 4 ? 4 : 2)
+    kb_pred(const __grid_constant__ BatchChunk C)
+{
+  int const tile    = blockIdx.x;
+  int const j       = find_job(C, BK_PRED, tile);
+  BatchJob const &J = C.jobs[j];
+  int gx, gy, gz;
+  pred_grid(J.b, gx, gy, gz);
+  int const l = tile - C.off[BK_PRED][j];
+  T *Wn       = (T *)J.W;
+  T *Wh       = Wn + (size_t)nslot(J.b) * (size_t)J.b.n;
+  fpred_tile<T, PTX, PTY, PTZ, SOLVER>(J.b, J.U, Wn, Wh, J.GEp, 0.0, J.dt_t, l % gx, (l / gx) % gy, l / (gx * gy));
+}
+
+template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
+__global__ void __launch_bounds__(L *WA *WB, 2) kb_sweep(const __grid_constant__ BatchChunk C)
+{
+  int const kind    = BK_SWX + DIR;
+  int const tile    = blockIdx.x;
+  int const j       = find_job(C, kind, tile);
+  BatchJob const &J = C.jobs[j];
+  int ga, gb, gc;
+  sweep_grid<DIR, L, WA, WB>(J.b, ga, gb, gc);
+  int const l = tile - C.off[kind][j];
+  T *Wn       = (T *)J.W;  // holds the accumulator dU once the predictor has run
+  T *Wh       = Wn + (size_t)nslot(J.b) * (size_t)J.b.n;
+  fsweep_tile<T, DIR, L, WA, WB, RECON, SOLVER, FIRST, FINAL>(J.b, Wh, Wn, J.U, J.GEp, J.Epre, J.status, 0.0, J.dt_t,
+                                                              l % ga, (l / ga) % gb, l / (ga * gb));
+}
+
+// Average_Cell_Single_Field of the density for real cells left with non-positive density
+__global__ void __launch_bounds__(256) kb_negavg(const __grid_constant__ BatchChunk C)
+{
+  int const tile    = blockIdx.x;
+  int const j       = find_job(C, BK_REAL, tile);
+  BatchJob const &J = C.jobs[j];
+  Box const &b      = J.b;
+  if (!b.floor_on) return;
+  long long const r = (long long)(tile - C.off[BK_REAL][j]) * 256 + threadIdx.x;
+  int const ng = b.ng, rx = b.nx - 2 * ng, ry = b.ny - 2 * ng;
+  if (r >= real_cells(b)) return;
+  int const x = (int)(r % rx) + ng, y = (int)((r / rx) % ry) + ng, z = (int)(r / ((long long)rx * ry)) + ng;
+  double *U          = J.U;
+  long long const id = b.id(x, y, z);
+  if (U[id] < b.density_floor && !(U[id] > 0)) {
+    U[id] = (U[b.id(x - 1, y, z)] + U[b.id(x + 1, y, z)] + U[b.id(x, y - 1, z)] + U[b.id(x, y + 1, z)] +
+             U[b.id(x, y, z - 1)] + U[b.id(x, y, z + 1)]) /
+            6;
+  }
+}
+
+template <bool MIX>
+__global__ void __launch_bounds__(256)
+    kb_final(const __grid_constant__ BatchChunk C, double U_floor, int temp_floor, int do_dt)
+{
+  int const tile    = blockIdx.x;
+  int const j       = find_job(C, BK_REAL, tile);
+  BatchJob const &J = C.jobs[j];
+  ffinalize_block<MIX>(J.b, J.U, J.Epre, J.dti, U_floor, temp_floor, do_dt, J.b.idx, J.b.idy, J.b.idz,
+                       tile - C.off[BK_REAL][j]);
+}
+
+template <typename T, int DIR, int L, int WA, int WB, bool FIRST, bool FINAL>
+cudaError_t launch_batch_sweep(const BatchChunk &C, int recon, int solver, int nsl, cudaStream_t s)
+{
+  void (*k)(BatchChunk);
+  size_t per_q;
+#define CGB_PICK(R)                                                                                        \
+  per_q = Sweep<DIR, L, WA, WB, R>::PER_Q;                                                                \
+  k     = (solver == SOLVER_ROE) ? kb_sweep<T, DIR, L, WA, WB, R, SOLVER_ROE, FIRST, FINAL>                \
+                                 : kb_sweep<T, DIR, L, WA, WB, R, SOLVER_HLLC, FIRST, FINAL>;
+  if (recon == RECON_PPMC) {
+    CGB_PICK(RECON_PPMC)
+  } else if (recon == RECON_PLMC) {
+    CGB_PICK(RECON_PLMC)
+  } else {
+    CGB_PICK(RECON_PCM)
+  }
+#undef CGB_PICK
+  size_t const sm = sizeof(T) * (size_t)nsl * per_q;
+  cudaError_t e   = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k<<<C.total[BK_SWX + DIR], L * WA * WB, sm, s>>>(C);
+  return cudaGetLastError();
+}
+
+// primitives, predictor, x/y/z sweeps, negative-density repair and finalize of one chunk
+template <typename T>
+cudaError_t launch_core(const BatchChunk &C, int recon, int solver, int nsl, int de, double U_floor, int temp_floor,
+                        cudaStream_t s)
+{
+  cudaError_t e;
+  kb_prims<T><<<C.total[BK_CELLS], 256, 0, s>>>(C);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  {
+    constexpr int NB = (PTX + 2) * (PTY + 2) * (PTZ + 2);
+    constexpr int NF = (PTX + 1) * PTY * PTZ + PTX * (PTY + 1) * PTZ + PTX * PTY * (PTZ + 1);
+    size_t const sm  = sizeof(T) * (size_t)nsl * (NB + NF);
+    auto k = (solver == SOLVER_ROE) ? kb_pred<T, SOLVER_ROE> : kb_pred<T, SOLVER_HLLC>;
+    if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess) return e;
+    k<<<C.total[BK_PRED], PTX * PTY * PTZ, sm, s>>>(C);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
+  if ((e = launch_batch_sweep<T, 0, SXL, SXA, SXB, true, false>(C, recon, solver, nsl, s)) != cudaSuccess) return e;
+  if ((e = launch_batch_sweep<T, 1, SYL, SYA, SYB, false, false>(C, recon, solver, nsl, s)) != cudaSuccess) return e;
+  if ((e = launch_batch_sweep<T, 2, SYL, SYA, SYB, false, true>(C, recon, solver, nsl, s)) != cudaSuccess) return e;
+  kb_negavg<<<C.total[BK_REAL], 256, 0, s>>>(C);
+  constexpr bool MIX = std::is_same<T, float>::value;
+  kb_final<MIX><<<C.total[BK_REAL], 256, 0, s>>>(C, U_floor, temp_floor, 1);
+  (void)de;
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+void batch_tiles(const Box &b, int tiles[BK_NUM])
+{
+  int a, c, d;
+  tiles[BK_CELLS] = (int)((b.n + 255) / 256);
+  pred_grid(b, a, c, d);
+  tiles[BK_PRED] = a * c * d;
+  sweep_grid<0, SXL, SXA, SXB>(b, a, c, d);
+  tiles[BK_SWX] = a * c * d;
+  sweep_grid<1, SYL, SYA, SYB>(b, a, c, d);
+  tiles[BK_SWY] = a * c * d;
+  sweep_grid<2, SYL, SYA, SYB>(b, a, c, d);
+  tiles[BK_SWZ] = a * c * d;
+  tiles[BK_REAL] = (int)((real_cells(b) + 255) / 256);
+}
+
+size_t batch_w_bytes(const Box &b) { return 2 * (size_t)nslot(b) * (size_t)b.n * sizeof(double); }
+
+cudaError_t batch_chunk_step(const BatchChunk &C, int recon, int solver, int mixed, int de, int ns, double c_cfl,
+                             double U_floor, int temp_floor, cudaStream_t s)
+{
+  if (C.njobs <= 0) return cudaSuccess;
+  int const nsl = ns > 0 ? 6 + ns : 5 + (de ? 1 : 0);
+  kb_ghost<<<C.total[BK_CELLS], 256, 0, s>>>(C);
+  kb_cfl<<<1, BATCH_CHUNK, 0, s>>>(C, c_cfl);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return mixed ? launch_core<float>(C, recon, solver, nsl, de, U_floor, temp_floor, s)
+               : launch_core<double>(C, recon, solver, nsl, de, U_floor, temp_floor, s);
+}
+
+
 // bytes of W scratch the fast paths need: primitives of Uⁿ and of U½ (8 bytes covers both types)
 size_t fast_scratch_bytes(const Box &b) { return 2 * (size_t)nslot(b) * (size_t)b.n * sizeof(double); }
 
-cudaError_t hydro_fast_step(const Box &b, int recon, int solver, int mixed, double *U, const Scratch &sc, void *W,
+cudaError_t hydro_fast_step(const Box &box, int recon, int solver, int mixed, double *U, const Scratch &sc, void *W,
                             double dt, const double *dt_dev, double U_floor, int temp_floor, int do_dt,
                             cudaStream_t s, cudaEvent_t *marks)
 {
   (void)W;
+  Box const b = with_inverses(box);
   bool const one_d = (b.ny == 1 && b.nz == 1);
   cudaError_t e;
   if (mixed) {
     e = one_d ? launch_fast<float, 128, 1, 1>(b, recon, solver, U, sc, dt, dt_dev, s, marks)
-              : launch_fast<float, 8, 8, 4>(b, recon, solver, U, sc, dt, dt_dev, s, marks);
+              : launch_fast<float, PTX, PTY, PTZ>(b, recon, solver, U, sc, dt, dt_dev, s, marks);
   } else {
     e = one_d ? launch_fast<double, 128, 1, 1>(b, recon, solver, U, sc, dt, dt_dev, s, marks)
-              : launch_fast<double, 8, 8, 4>(b, recon, solver, U, sc, dt, dt_dev, s, marks);
+              : launch_fast<double, PTX, PTY, PTZ>(b, recon, solver, U, sc, dt, dt_dev, s, marks);
   }
   if (e != cudaSuccess) return e;
   if (b.floor_on && !one_d) {
@@ -652,16 +914,17 @@ cudaError_t hydro_fast_step(const Box &b, int recon, int solver, int mixed, doub
         (long long)(b.nx - 2 * ng) * (one_d ? 1 : b.ny - 2 * ng) * (one_d ? 1 : b.nz - 2 * ng);
     unsigned const grid = (unsigned)((nreal + 255) / 256);
     if (mixed) {
-      k_ffinalize<true><<<grid, 256, 0, s>>>(b, U, sc.Epre, sc.dti, U_floor, temp_floor, do_dt, 1.0 / b.dx,
-                                              1.0 / b.dy, 1.0 / b.dz);
+      k_ffinalize<true><<<grid, 256, 0, s>>>(b, U, sc.Epre, sc.dti, U_floor, temp_floor, do_dt, b.idx, b.idy,
+                                              b.idz);
     } else {
-      k_ffinalize<false><<<grid, 256, 0, s>>>(b, U, sc.Epre, sc.dti, U_floor, temp_floor, do_dt, 1.0 / b.dx,
-                                               1.0 / b.dy, 1.0 / b.dz);
+      k_ffinalize<false><<<grid, 256, 0, s>>>(b, U, sc.Epre, sc.dti, U_floor, temp_floor, do_dt, b.idx, b.idy,
+                                               b.idz);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   if (marks) cudaEventRecord(marks[3], s);
   return cudaSuccess;
 }
+
 
 }  // namespace cgb

@@ -39,6 +39,7 @@ __device__ __forceinline__ unsigned long long mag_bits(double x)
   return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
 }
 __device__ __forceinline__ bool mag_lt(double a, double b) { return mag_bits(a) < mag_bits(b); }  // |a| < |b|
+__device__ __forceinline__ bool is_zero(double x) { return mag_bits(x) == 0; }
 __device__ __forceinline__ double mag_min(double a, double b)                                      // min(|a|, |b|)
 {
   unsigned long long const x = mag_bits(a), y = mag_bits(b);
@@ -58,6 +59,7 @@ __device__ __forceinline__ double max_pos(double x, double c)
 __device__ __forceinline__ bool is_pos(float x) { return x > 0.f; }
 __device__ __forceinline__ bool is_neg(float x) { return x < 0.f; }
 __device__ __forceinline__ bool mag_lt(float a, float b) { return fabsf(a) < fabsf(b); }
+__device__ __forceinline__ bool is_zero(float x) { return x == 0.f; }
 __device__ __forceinline__ float mag_min(float a, float b) { return fminf(fabsf(a), fabsf(b)); }
 __device__ __forceinline__ float mag_max(float a, float b) { return fmaxf(fabsf(a), fabsf(b)); }
 __device__ __forceinline__ float max_pos(float x, float c) { return fmaxf(x, c); }
@@ -148,7 +150,10 @@ __device__ __forceinline__ void ppm1(T im2, T im1, T i, T ip1, T ip2, T &L_iph, 
       bool const n = is_neg(d2im1);
       if (n == is_neg(d2i) && n == is_neg(d2ip1) && n == is_neg(d2f))
         d2lim = copysign(mag_min(C2 * mag_min(mag_min(d2im1, d2i), d2ip1), d2f), d2f);
-      rho = d2lim * rcp(d2f);
+      // d2lim / d2f as a reciprocal product: |d2lim| <= |d2f|, so rho is in [0, 1]; the
+      // product is kept there when the reciprocal of a subnormal d2f overflows (0 * inf, or a
+      // subnormal d2lim times inf), where the quotient itself would be 0 or at most 1
+      if (!is_zero(d2lim)) rho = mag_min(d2lim * rcp(d2f), T(1));
     }
     // rho >= 0 (d2lim carries the sign of d2f), so rho <= 1 - eps compares magnitudes
     if (!mag_lt(T(1) - Eps<T>::roundoff, rho)) {
@@ -380,10 +385,9 @@ __device__ __forceinline__ T pressure_used(const Prim<T> &s, T E, T ig1, T g1, i
 // in fixed slots: 0 d, 1 m_n, 2 m_t1, 3 m_t2, 4 E, 5 GasEnergy, 6.. scalars.  Fixed slots keep
 // every register-array index a compile-time constant (no local memory).
 template <typename T>
-__device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, int ns, int de, T gamma)
+__device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, int ns, int de, T gamma, T ig1)
 {
   T const g1  = gamma - T(1);
-  T const ig1 = T(1) / g1;
   T const mxl = l.d * l.vn, myl = l.d * l.vt1, mzl = l.d * l.vt2;
   T const mxr = r.d * r.vn, myr = r.d * r.vt1, mzr = r.d * r.vt2;
   T const El  = l.p * ig1 + T(0.5) * l.d * (l.vn * l.vn + l.vt1 * l.vt1 + l.vt2 * l.vt2);
@@ -463,10 +467,9 @@ __device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, i
 
 // Roe flux with the HLLE fallback (roe_cuda.cu:19-400) from primitive interface states.
 template <typename T>
-__device__ __forceinline__ void roe(const Prim<T> &l, const Prim<T> &r, T *f, int ns, int de, T gamma)
+__device__ __forceinline__ void roe(const Prim<T> &l, const Prim<T> &r, T *f, int ns, int de, T gamma, T ig1)
 {
   T const g1  = gamma - T(1);
-  T const ig1 = T(1) / g1;
   T const dl = l.d, dr = r.d, vxl = l.vn, vyl = l.vt1, vzl = l.vt2, vxr = r.vn, vyr = r.vt1, vzr = r.vt2;
   T const mxl = dl * vxl, myl = dl * vyl, mzl = dl * vzl, mxr = dr * vxr, myr = dr * vyr, mzr = dr * vzr;
   T const El  = l.p * ig1 + T(0.5) * dl * (vxl * vxl + vyl * vyl + vzl * vzl);

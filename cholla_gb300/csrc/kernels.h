@@ -38,6 +38,43 @@ cudaError_t mhd_calc_dt(const Box &b, const double *U, unsigned long long *dti, 
 // max |div B| over the real cells into *out (as the bits of a non-negative double; cleared first)
 cudaError_t mhd_max_divb(const Box &b, const double *U, unsigned long long *out, cudaStream_t s);
 
+// ---- batches: many 3D boxes of one scheme, stepped together ----
+// One launch carries up to BATCH_CHUNK jobs in its parameter space (__grid_constant__), so the
+// tile code reads a job's geometry and pointers from the constant bank, as the single-box
+// kernels read their Box.  A batch of more jobs runs one chain of launches per chunk of jobs.
+constexpr int BATCH_CHUNK    = 16;
+constexpr int BATCH_MAX_JOBS = 256;
+struct BatchJob {
+  Box b;
+  double *U;                 // state (caller-owned)
+  void *W;                   // fast-path primitives: 2 * nslot * n * 8 bytes
+  double *GEp, *Epre;        // dual-energy partial update, pre-sync energy
+  unsigned long long *dti;   // max inverse crossing time (ordered double bits)
+  int *status;               // bad-cell flags
+  double *dt_t;              // [dt, t]
+  double t_end;              // clamp of t (<= 0: none)
+  int flags[6];              // boundary flags (ghost fill)
+};
+// tile kinds: cells of the padded box (256 per tile), predictor tiles (8 x 8 x 4), corrector
+// sweep tiles (x: 64 x 2 x 2, y and z: 32 x 8 x 1), real cells (256 per tile)
+enum BatchKind { BK_CELLS = 0, BK_PRED, BK_SWX, BK_SWY, BK_SWZ, BK_REAL, BK_NUM };
+struct BatchChunk {
+  int njobs;
+  int total[BK_NUM];                  // tiles of all the chunk's jobs per kind (= the grids)
+  int off[BK_NUM][BATCH_CHUNK + 1];   // first tile of each job per kind
+  BatchJob jobs[BATCH_CHUNK];
+};
+static_assert(sizeof(BatchChunk) <= 4000, "a chunk must fit the 4 KB kernel parameter space");
+// tiles of a box per kind (the tiling the batched kernels decode)
+void batch_tiles(const Box &b, int tiles[BK_NUM]);
+// W bytes a job needs
+size_t batch_w_bytes(const Box &b);
+// Launch one step of every job of chunk C on stream s (all jobs share the scheme): ghost fill,
+// dt = c_cfl / max_dti (clamped to t_end), primitives, predictor, x/y/z sweeps, negative-density
+// repair, finalize with the CFL reduction for the next step; one block per tile.
+cudaError_t batch_chunk_step(const BatchChunk &C, int recon, int solver, int mixed, int de, int ns, double c_cfl,
+                             double U_floor, int temp_floor, cudaStream_t s);
+
 // dispatch on the arithmetic: 0 = FP64 in the reference's order, 1 = mixed, 2 = fast FP64
 inline cudaError_t hydro_step(const Box &b, int recon, int solver, int precision, double *U, const Scratch &sc,
                               double dt, const double *dt_dev, double U_floor, int temp_floor, int do_dt,

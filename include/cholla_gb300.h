@@ -155,6 +155,48 @@ int cgb_box_advance(cgb_box *box, double *d_conserved, int n_steps, double c_cfl
 int cgb_box_get_time(cgb_box *box, double *t, double *dt_last);
 const char *cgb_box_last_error(void);
 
+/* ---- batches: many independent 3D boxes of one scheme advanced together (no counterpart in
+ * the reference).  Every job keeps its own state (caller-owned, device resident), scratch, dt
+ * and time; one step of the batch is one chain of launches per 16 jobs over the tiles of all
+ * of them (the chains run side by side), replayed from a captured CUDA graph.  Jobs join and
+ * leave between steps (the graph is captured again at the next step).  Fast FP64 or mixed
+ * precision, hydro. ---- */
+typedef struct cgb_batch cgb_batch;
+
+
+/* stream: the batch's own cudaStream_t (required); c_cfl: CFL number of every job. */
+int cgb_batch_create(cgb_batch **batch, const cgb_scheme *scheme, double c_cfl, void *stream);
+int cgb_batch_destroy(cgb_batch *batch);
+/* Library scratch (bytes) a job of padded size nx*ny*nz takes, for admission by free memory. */
+long long cgb_batch_job_bytes(const cgb_batch *batch, int nx, int ny, int nz);
+/* Add a box (ghosts refilled every step with flags[6], t_end <= 0: no end time); its first dt
+ * comes from a CFL reduction of d_conserved queued now. */
+int cgb_batch_add(cgb_batch *batch, double *d_conserved, int nx, int ny, int nz, int n_ghost, double dx, double dy,
+                  double dz, const int flags[6], double t_end, int *job_id);
+int cgb_batch_remove(cgb_batch *batch, int job_id);
+int cgb_batch_n_jobs(const cgb_batch *batch);
+/* Spread the jobs over at least `chains` parallel chains of launches (default 1; a chain holds
+ * at most 16 jobs), balanced by cells.  Same results bit for bit; takes effect at the next step. */
+int cgb_batch_set_chains(cgb_batch *batch, int chains);
+/* Advance every job by n_steps on the batch stream (no host synchronisation). */
+int cgb_batch_step(cgb_batch *batch, int n_steps);
+/* Time and last dt of one job (synchronises the batch stream). */
+int cgb_batch_job_time(cgb_batch *batch, int job_id, double *t, double *dt_last);
+const char *cgb_batch_last_error(void);
+
+/* ---- initial conditions on the device (the serving workload's problems) ---- */
+/* Blast: uniform density rho and pressure p, plus thermal energy `energy` spread uniformly
+ * over the cells whose centre lies within `radius` of (cx, cy, cz) (box coordinates of the real
+ * region, origin at its lower corner).  Zero velocity.  GasEnergy (dual_energy) consistent. */
+int cgb_ic_blast(double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields, double dx, double dy,
+                 double dz, double cx, double cy, double cz, double radius, double energy, double rho, double p,
+                 double gamma, int dual_energy, void *stream);
+/* Shock tube along the unit normal (nxv, nyv, nzv) through (cx, cy, cz): (rho_l, p_l) where
+ * (r - c).n < 0, (rho_r, p_r) elsewhere, zero velocity. */
+int cgb_ic_shock_tube(double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields, double dx, double dy,
+                      double dz, double cx, double cy, double cz, double nxv, double nyv, double nzv, double rho_l,
+                      double p_l, double rho_r, double p_r, double gamma, int dual_energy, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,76 @@
+"""Host logic of the serving loop without a GPU: the arrival stream and the admission /
+retirement bookkeeping, driven by a fake backend whose steps complete at once."""
+import numpy as np
+
+from cholla_gb300 import serve
+
+
+def test_poisson_stream_is_seeded_and_well_formed():
+    a = serve.make_requests(rate=100.0, count=500, seed=3)
+    b = serve.make_requests(rate=100.0, count=500, seed=3)
+    assert [(r.arrival, r.n, r.kind, r.seed) for r in a] == [(r.arrival, r.n, r.kind, r.seed) for r in b]
+    t = np.array([r.arrival for r in a])
+    assert t[0] == 0.0 and np.all(np.diff(t) >= 0)
+    assert abs(np.mean(np.diff(t)) - 0.01) < 0.002  # mean gap 1/rate
+    assert {r.n for r in a} <= set(serve.SIZES) and len({r.n for r in a}) == len(serve.SIZES)
+    assert {r.kind for r in a} == {"blast", "tube"}
+
+
+class _Done:
+    def query(self):
+        return True
+
+    def synchronize(self):
+        pass
+
+
+class FakeServer(serve._Base):
+    mode = "fake"
+
+    def __init__(self, budget, cost, max_active=256):
+        self.scheme = serve.default_scheme()
+        self.budget, self.max_active, self.depth = budget, max_active, 2
+        self.cost, self.live, self.peak_used, self.used_now, self.peak_active = cost, {}, 0, 0, 0
+
+    def _cost(self, req):
+        return self.cost
+
+    def _event(self):
+        return _Done()
+
+    def _admit(self, req):
+        self.used_now += self.cost
+        self.peak_used = max(self.peak_used, self.used_now)
+        self.live[req.rid] = req
+        self.peak_active = max(self.peak_active, len(self.live))
+        return req.rid, None
+
+    def _step(self, active):
+        out = []
+        for key, slot in active.items():
+            slot[1] -= 1
+            if slot[1] == 0:
+                out.append(key)
+        return out
+
+    def _retire(self, key):
+        self.live.pop(key)
+        self.used_now -= self.cost
+
+
+def test_admission_respects_memory_budget_and_every_request_completes():
+    reqs = serve.make_requests(rate=1e6, count=40, seed=1, steps=5)  # all arrive at once
+    srv = FakeServer(budget=10 * 100, cost=100)
+    rep = srv.run(reqs)
+    assert len(rep.requests) == 40
+    assert srv.peak_active <= 10 and srv.peak_used <= 1000
+    assert all(r.done >= r.admitted >= r.arrival for r in rep.requests)
+    s = rep.summary()
+    assert s["requests"] == 40 and s["p99_ms"] >= s["p50_ms"] >= 0
+
+
+def test_a_job_larger_than_the_budget_still_runs_alone():
+    reqs = serve.make_requests(rate=1e6, count=3, seed=2, steps=2)
+    srv = FakeServer(budget=50, cost=100)
+    rep = srv.run(reqs)
+    assert len(rep.requests) == 3 and srv.peak_active == 1
