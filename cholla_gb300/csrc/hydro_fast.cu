@@ -390,12 +390,25 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
     }
   };
 
+  // A partial tile (the box's real extent is not a multiple of the tile) skips the interface
+  // states and fluxes that no real cell needs: lim = real cells of the tile along the sweep,
+  // pencil_in(c) = pencil c lies inside the box.
+  int const ry = b.ny - 2 * ng, rz = b.nz - 2 * ng, rx = b.nx - 2 * ng;
+  int const lim = (DIR == 0 ? rx : DIR == 1 ? ry : rz) - a0;
+  auto pencil_in = [&](int c) {
+    return one_d || (ca0 + c % WA < (DIR == 0 ? ry : rx) && cb0 + c / WA < (DIR == 2 ? ry : rz));
+  };
+
   int const t = threadIdx.x;
+  // Positions past the box (a partial tile) read the nearest cell the predictor wrote (1 .. n-2;
+  // the outermost layer of W½ stays zero), so their discarded states stay physical and off the
+  // slow paths.  No real cell's stencil reaches the outermost layer.
   for (int p = t; p < S::NP; p += NT) {
     int a, c, gx, gy, gz;
     S::split(p, S::LA, a, c);
     cell(a - H, c, gx, gy, gz);
-    long long const gid = b.id(clampi(gx, 0, b.nx - 1), clampi(gy, 0, b.ny - 1), clampi(gz, 0, b.nz - 1));
+    long long const gid = b.id(clampi(gx, 1, b.nx - 2), one_d ? 0 : clampi(gy, 1, b.ny - 2),
+                               one_d ? 0 : clampi(gz, 1, b.nz - 2));
     for (int q = 0; q < ns_; q++) Ps[q * S::NP + p] = W[(long long)rot(q, o1, o2, o3) * n + gid];
   }
   __syncthreads();
@@ -403,6 +416,7 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
     for (int r = t; r < S::NR; r += NT) {
       int a, c;
       S::split(r, S::LR, a, c);
+      if (a > lim + 1 || !pencil_in(c)) continue;  // cell a0 + a - 1 feeds no real face
       int const base = S::at(a - 1 + H, c, S::LA);
       constexpr int st = S::STRIDE;
       hf::Prim<T> Lf, Rf;
@@ -422,6 +436,7 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
   for (int f = t; f < S::NF; f += NT) {
     int a, c;
     S::split(f, S::LF, a, c);  // face a lies between sweep positions a - 1 and a
+    if (a > lim || !pencil_in(c)) continue;
     hf::Prim<T> Lf, Rf;
     if (RECON == RECON_PCM) {
       int const pl = S::at(a - 1 + H, c, S::LA);

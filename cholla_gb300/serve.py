@@ -192,10 +192,11 @@ class _Base:
 class BatchedServer(_Base):
     mode = "batched"
 
-    def __init__(self, torch, **kw):
+    def __init__(self, torch, chains: int = 2, **kw):
         super().__init__(torch, **kw)
         self.stream = torch.cuda.Stream()
         self.batch = Batch(self.scheme, self.stream, c_cfl=0.3)
+        self.batch.set_chains(chains)
 
     def _cost(self, req):
         N = req.n + 2 * N_GHOST
