@@ -3,8 +3,9 @@ device initial conditions of the serving workload (blast, shock tube).
 
 One Batch owns a job table and a CUDA stream; every job keeps its torch CUDA state tensor
 resident, its own scratch, dt and time.  Batch.step(k) advances all jobs by k steps with one
-chain of launches per 16 jobs (one block per tile of all of them; the chains run side by
-side), replayed from a captured CUDA graph; jobs can be added and removed between steps (the
+chain of launches per 16 jobs (one block per tile of all of them) and one chain of the
+single-box step per large job (the chains run side by side), replayed from a captured CUDA
+graph; jobs can be added and removed between steps (the
 graph is captured again at the next step).
 """
 from __future__ import annotations
@@ -60,6 +61,14 @@ class Batch:
 
     def remove(self, job_id: int) -> None:
         _check(L.lib().cgb_batch_remove(self._h, job_id))
+
+    def hold(self, job_id: int, held: bool = True) -> None:
+        """Leave a job out of the steps (held) or put it back; it resumes where it stopped."""
+        _check(L.lib().cgb_batch_hold(self._h, job_id, int(bool(held))))
+
+    def set_solo_cells(self, cells: int) -> None:
+        """Jobs of at least `cells` padded cells run the single-box step in a chain of their own."""
+        _check(L.lib().cgb_batch_set_solo_cells(self._h, int(cells)))
 
     def set_chains(self, chains: int) -> None:
         """Spread the jobs over at least `chains` parallel chains of launches (same results)."""

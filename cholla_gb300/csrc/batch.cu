@@ -27,12 +27,15 @@ struct cgb_batch {
   std::vector<cgb::BatchJob> jobs;  // index = position in the batch
   struct Slot {
     int id;
-    void *mem;  // one stream-ordered allocation: W, GEp, Epre, dti, status, dt_t
+    void *mem;          // one stream-ordered allocation: W, GEp, Epre, dti, status, dt_t
+    bool held = false;  // left out of the steps until released
+    int flags[6];       // boundary flags as given
   };
   std::vector<Slot> slots;  // parallel to jobs
   int next_id = 1;
   bool dirty  = true;                   // the job set changed since the graph was captured
   int chains  = 1;                      // at least this many chains of launches
+  long long solo_cells = 2LL << 20;     // jobs of at least this many padded cells run solo
   cudaGraphExec_t graph = nullptr;
   std::vector<cudaStream_t> aux;        // capture streams of chunks 1, 2, ...
   std::vector<cudaEvent_t> ev;          // fork (0) and joins of the capture
@@ -209,7 +212,9 @@ int cgb_batch_add(cgb_batch *bt, double *d_conserved, int nx, int ny, int nz, in
     return bcuda(e, "batch_add");
   }
   bt->jobs.push_back(J);
-  bt->slots.push_back({bt->next_id, mem});
+  cgb_batch::Slot sl{bt->next_id, mem, false, {}};
+  for (int i = 0; i < 6; i++) sl.flags[i] = flags[i];
+  bt->slots.push_back(sl);
   *job_id   = bt->next_id++;
   bt->dirty = true;
   return CGB_OK;
@@ -238,6 +243,32 @@ int cgb_batch_remove(cgb_batch *bt, int job_id)
 
 int cgb_batch_n_jobs(const cgb_batch *bt) { return bt ? (int)bt->jobs.size() : -1; }
 
+// Hold a job out of the steps (hold = 1) or release it (hold = 0).  A held job keeps its state,
+// scratch, time and pending dt; it resumes where it stopped.  Takes effect at the next step.
+int cgb_batch_hold(cgb_batch *bt, int job_id, int hold)
+{
+  if (!bt) return bfail(CGB_ERR_ARGS, "null batch");
+  std::lock_guard<std::mutex> lk(bt->mu);
+  for (auto &sl : bt->slots) {
+    if (sl.id != job_id) continue;
+    if (sl.held != (hold != 0)) bt->dirty = true;
+    sl.held = hold != 0;
+    return CGB_OK;
+  }
+  return bfail(CGB_ERR_ARGS, "no such job");
+}
+
+// Jobs of at least `cells` padded cells run solo: their own chain of the single-box kernels
+// (the box engine's step), the others share the batched kernels.  Takes effect at the next step.
+int cgb_batch_set_solo_cells(cgb_batch *bt, long long cells)
+{
+  if (!bt || cells < 0) return bfail(CGB_ERR_ARGS, "bad argument");
+  std::lock_guard<std::mutex> lk(bt->mu);
+  if (cells != bt->solo_cells) bt->dirty = true;
+  bt->solo_cells = cells;
+  return CGB_OK;
+}
+
 // Minimum number of parallel chains of launches the jobs are spread over (1 .. BATCH_MAX_JOBS;
 // more are used when the jobs exceed BATCH_CHUNK per chain).  Takes effect at the next step.
 int cgb_batch_set_chains(cgb_batch *bt, int chains)
@@ -260,9 +291,23 @@ int cgb_batch_step(cgb_batch *bt, int n_steps)
     cudaGraphExecDestroy(bt->graph);
     bt->graph = nullptr;
   }
-  if (!bt->graph) {
-    std::vector<cgb::BatchChunk> const chunks = build_chunks(bt->jobs, bt->chains);
-    size_t const nc = chunks.size();
+  if (!bt->graph && bt->dirty) {
+    // running jobs: large ones solo (a chain of the single-box kernels each), the rest in chunks
+    std::vector<cgb::BatchJob> shared;
+    std::vector<size_t> solo;
+    for (size_t i = 0; i < bt->jobs.size(); i++) {
+      if (bt->slots[i].held) continue;
+      if (bt->jobs[i].b.n >= bt->solo_cells)
+        solo.push_back(i);
+      else
+        shared.push_back(bt->jobs[i]);
+    }
+    std::vector<cgb::BatchChunk> const chunks = build_chunks(shared, bt->chains);
+    size_t const nc = chunks.size() + solo.size();  // chains of the graph
+    if (nc == 0) {  // every job held: nothing to step
+      bt->dirty = false;
+      return CGB_OK;
+    }
     while (bt->aux.size() + 1 < nc) {
       cudaStream_t a;
       if ((e = cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking)) != cudaSuccess) return bcuda(e, "batch stream");
@@ -278,12 +323,28 @@ int cgb_batch_step(cgb_batch *bt, int n_steps)
     cudaGraph_t g;
     if ((e = cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
       return bcuda(e, "batch capture");
-    // chunk 0 on the batch stream, chunk c > 0 on aux[c - 1]: forked from and joined to it
+    // chain 0 on the batch stream, chain c > 0 on aux[c - 1]: forked from and joined to it.
+    // Chains 0 .. chunks-1 are the chunks; the solo jobs follow, each the single-box step
+    // (ghost fill, dt, step with the CFL reduction for the next), as the box engine runs it.
     cudaError_t ce = nc > 1 ? cudaEventRecord(bt->ev[0], bt->stream) : cudaSuccess;
     for (size_t c = 1; c < nc && ce == cudaSuccess; c++) ce = cudaStreamWaitEvent(bt->aux[c - 1], bt->ev[0], 0);
-    for (size_t c = 0; c < nc && ce == cudaSuccess; c++)
-      ce = cgb::batch_chunk_step(chunks[c], s.reconstruction, s.riemann_solver, mixed, s.dual_energy, s.n_scalars,
-                                 bt->c_cfl, s.U_floor, s.temperature_floor, c ? bt->aux[c - 1] : bt->stream);
+    for (size_t c = 0; c < nc && ce == cudaSuccess; c++) {
+      cudaStream_t const st = c ? bt->aux[c - 1] : bt->stream;
+      if (c < chunks.size()) {
+        ce = cgb::batch_chunk_step(chunks[c], s.reconstruction, s.riemann_solver, mixed, s.dual_energy, s.n_scalars,
+                                   bt->c_cfl, s.U_floor, s.temperature_floor, st);
+        continue;
+      }
+      size_t const i        = solo[c - chunks.size()];
+      cgb::BatchJob const &J = bt->jobs[i];
+      cgb::Scratch sc{};
+      sc.W = J.W, sc.GEp = J.GEp, sc.Epre = J.Epre, sc.dti = J.dti, sc.status = J.status;
+      ce = cgb::set_boundaries(J.b, J.U, bt->slots[i].flags, st);
+      if (ce == cudaSuccess) ce = cgb::cfl_dt(J.dti, J.dt_t, bt->c_cfl, J.t_end, st);
+      if (ce == cudaSuccess)
+        ce = cgb::hydro_step(J.b, s.reconstruction, s.riemann_solver, s.precision, J.U, sc, 0.0, J.dt_t, s.U_floor,
+                             s.temperature_floor, 1, st);
+    }
     for (size_t c = 1; c < nc && ce == cudaSuccess; c++) {
       ce = cudaEventRecord(bt->ev[c], bt->aux[c - 1]);
       if (ce == cudaSuccess) ce = cudaStreamWaitEvent(bt->stream, bt->ev[c], 0);
@@ -295,6 +356,7 @@ int cgb_batch_step(cgb_batch *bt, int n_steps)
     if (e != cudaSuccess) return bcuda(e, "batch graph");
     bt->dirty = false;
   }
+  if (!bt->graph) return CGB_OK;  // every job held
   for (int i = 0; i < n_steps; i++) {
     if ((e = cudaGraphLaunch(bt->graph, bt->stream)) != cudaSuccess) return bcuda(e, "batch step");
   }

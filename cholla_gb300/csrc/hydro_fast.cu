@@ -31,6 +31,38 @@ constexpr int SXL = 64, SXA = 2, SXB = 2, SYL = 32, SYA = 8, SYB = 1;
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// q = n / d and r = n % d for 0 <= n < 2^22 and d >= 1 from an FP32 reciprocal (relative error
+// below 2^-22, so the estimate is off by at most one and one correction makes it exact); larger
+// n take the integer division
+__device__ __forceinline__ int divmod(int n, int d, int &r)
+{
+  int q;
+  if (n < (1 << 22)) {
+    q = __float2int_rz(__int2float_rn(n) * __frcp_rn(__int2float_rn(d)));
+    r = n - q * d;
+    if (r < 0) {
+      q -= 1, r += d;
+    } else if (r >= d) {
+      q += 1, r -= d;
+    }
+  } else {
+    q = n / d, r = n - q * d;
+  }
+  return q;
+}
+
+// real-cell coordinates of the linear real index i (x fastest) in 32-bit arithmetic when i fits
+__device__ __forceinline__ void real_xyz(long long i, int rx, int ry, int &x, int &y, int &z)
+{
+  if (i < 0x7fffffffLL) {
+    unsigned const u = (unsigned)i, q = u / (unsigned)rx;
+    x = (int)(u - q * (unsigned)rx), y = (int)(q % (unsigned)ry), z = (int)(q / (unsigned)ry);
+  } else {
+    long long const q = i / rx;
+    x = (int)(i - q * rx), y = (int)(q % ry), z = (int)(q / ry);
+  }
+}
+
 // number of slots a box carries and which of them are live
 __host__ __device__ __forceinline__ int nslot(const Box &b) { return b.ns > 0 ? 6 + b.ns : 5 + b.de; }
 __device__ __forceinline__ bool live(int s, const Box &b)
@@ -68,10 +100,10 @@ __device__ __forceinline__ void prim_from_cons(const double *q, const Box &b, T 
   double p;
   if (b.de) {
     p    = hf::ratio_gt(eth, q[4], ETA_1) ? eth : q[5];
-    p    = fmax(p * (b.gamma - 1.0), TINY);
+    p    = hf::max_pos(p * (b.gamma - 1.0), TINY);
     w[5] = (T)(q[5] * id);
   } else {
-    p    = fmax((b.gamma - 1.0) * eth, TINY);
+    p    = hf::max_pos((b.gamma - 1.0) * eth, TINY);
     w[5] = T(0);
   }
   w[0] = (T)d;
@@ -538,7 +570,7 @@ __device__ __forceinline__ void block_max_to(double v, unsigned long long *dst)
 {
   __shared__ double red[32];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) v = hf::max_ord(v, __shfl_down_sync(0xffffffffu, v, o));
   int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) red[warp] = v;
   __syncthreads();
@@ -546,14 +578,14 @@ __device__ __forceinline__ void block_max_to(double v, unsigned long long *dst)
     int const nw = (blockDim.x + 31) >> 5;
     v            = (lane < nw) ? red[lane] : -1.0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    for (int o = 16; o > 0; o >>= 1) v = hf::max_ord(v, __shfl_down_sync(0xffffffffu, v, o));
     if (lane == 0 && v >= 0.0) atomicMax(dst, (unsigned long long)__double_as_longlong(v));
   }
 }
 
 // MIX: the mixed-precision form takes the sound speed's square root in FP32 and the
 // reciprocal of the density with one Newton step; the selection, sync, floor and the
-// maximum stay FP64.
+// maximum stay FP64 (maxima compare bit patterns on the integer pipe).
 template <bool MIX>
 __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict__ U, const double *__restrict__ Epre,
                                                 unsigned long long *__restrict__ dti, double U_floor, int temp_floor,
@@ -566,9 +598,11 @@ __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict
   long long const r     = blk * blockDim.x + threadIdx.x;
   double m = -1.0;
   if (r < nreal) {
-    int const x = (int)(r % rx) + ng;
-    int const y = one_d ? 0 : (int)((r / rx) % ry) + ng;
-    int const z = one_d ? 0 : (int)(r / ((long long)rx * ry)) + ng;
+    int x, y, z;
+    real_xyz(r, rx, ry, x, y, z);
+    x += ng;
+    y = one_d ? 0 : y + ng;
+    z = one_d ? 0 : z + ng;
     long long const n = b.n, id = b.id(x, y, z);
     double const d = U[id], d_inv = MIX ? rcp_nr<1>(d) : hf::rcp(d);
     double const mx = U[n + id], my = U[2 * n + id], mz = U[3 * n + id];
@@ -576,21 +610,22 @@ __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict
     double E        = U[4 * n + id];
     if (b.de) {
       long long const fge = (long long)(b.nf - 1) * n;
+      // the maxima run on the integer pipe (max_ord), which the FP64-bound finalize leaves idle
       double Emax;
       if (one_d) {
-        Emax = fmax(fmax(Epre[max(x - 1, ng)], E), Epre[min(x + 1, b.nx - ng - 1)]);
+        Emax = hf::max_ord(hf::max_ord(Epre[max(x - 1, ng)], E), Epre[min(x + 1, b.nx - ng - 1)]);
       } else {
-        Emax = fmax(Epre[b.id(max(x - 1, ng), y, z)], E);
-        Emax = fmax(Emax, Epre[b.id(min(x + 1, b.nx - ng - 1), y, z)]);
-        Emax = fmax(Emax, Epre[b.id(x, max(y - 1, ng), z)]);
-        Emax = fmax(Emax, Epre[b.id(x, min(y + 1, b.ny - ng - 1), z)]);
-        Emax = fmax(Emax, Epre[b.id(x, y, max(z - 1, ng))]);
-        Emax = fmax(Emax, Epre[b.id(x, y, min(z + 1, b.nz - ng - 1))]);
+        Emax = hf::max_ord(Epre[b.id(max(x - 1, ng), y, z)], E);
+        Emax = hf::max_ord(Emax, Epre[b.id(min(x + 1, b.nx - ng - 1), y, z)]);
+        Emax = hf::max_ord(Emax, Epre[b.id(x, max(y - 1, ng), z)]);
+        Emax = hf::max_ord(Emax, Epre[b.id(x, min(y + 1, b.ny - ng - 1), z)]);
+        Emax = hf::max_ord(Emax, Epre[b.id(x, y, max(z - 1, ng))]);
+        Emax = hf::max_ord(Emax, Epre[b.id(x, y, min(z + 1, b.nz - ng - 1))]);
       }
       double const ut = E - ke;
       // Select_Internal_Energy_3D (hydro_cuda.cu:949-1016): U/E > eta1 or U/Emax > eta2
       double Ui   = (hf::ratio_gt(ut, E, ETA_1) || hf::ratio_gt(ut, Emax, ETA_2)) ? ut : U[fge + id];
-      Ui          = fmax(Ui, TINY);
+      Ui          = hf::max_pos(Ui, TINY);
       U[fge + id] = Ui;
       E           = ke + Ui;  // Sync_Energies_3D (hydro_cuda.cu:1070-1099)
       U[4 * n + id] = E;
@@ -607,13 +642,13 @@ __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict
     }
     if (do_dt) {  // hydroInverseCrossingTime (hydro_cuda.cu:404-419)
       double const c2 = b.gamma * (E - ke) * (b.gamma - 1.0) * d_inv;
-      double const cs = MIX ? (double)sqrtf((float)fmax(c2, 0.0)) : hf::sqrtT(fmax(c2, 0.0));
+      double const cs = MIX ? (double)sqrtf((float)hf::max_pos(c2, 0.0)) : hf::sqrtT(hf::max_pos(c2, 0.0));
       double const ax = fabs(mx * d_inv) + cs;
       if (one_d) {
         m = ax * idx;
-      } else {
+      } else {  // non-negative terms: max_pos orders them by their bits
         double const ay = fabs(my * d_inv) + cs, az = fabs(mz * d_inv) + cs;
-        m = fmax(fmax(ax * idx, ay * idy), fmax(az * idz, 0.0));
+        m = hf::max_pos(hf::max_pos(ax * idx, ay * idy), hf::max_pos(az * idz, 0.0));
       }
     }
   }
@@ -762,10 +797,12 @@ __global__ void __launch_bounds__(PTX *PTY *PTZ, sizeof(T) == 4 ? 4 : 2)
   BatchJob const &J = C.jobs[j];
   int gx, gy, gz;
   pred_grid(J.b, gx, gy, gz);
-  int const l = tile - C.off[BK_PRED][j];
-  T *Wn       = (T *)J.W;
-  T *Wh       = Wn + (size_t)nslot(J.b) * (size_t)J.b.n;
-  fpred_tile<T, PTX, PTY, PTZ, SOLVER>(J.b, J.U, Wn, Wh, J.GEp, 0.0, J.dt_t, l % gx, (l / gx) % gy, l / (gx * gy));
+  int tx, ty;
+  int const tz = divmod(divmod(tile - C.off[BK_PRED][j], gx, tx), gy, ty);
+  T *Wn        = (T *)J.W;
+  T *Wh        = Wn + (size_t)nslot(J.b) * (size_t)J.b.n;
+  (void)gz;
+  fpred_tile<T, PTX, PTY, PTZ, SOLVER>(J.b, J.U, Wn, Wh, J.GEp, 0.0, J.dt_t, tx, ty, tz);
 }
 
 template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
@@ -777,11 +814,13 @@ __global__ void __launch_bounds__(L *WA *WB, 2) kb_sweep(const __grid_constant__
   BatchJob const &J = C.jobs[j];
   int ga, gb, gc;
   sweep_grid<DIR, L, WA, WB>(J.b, ga, gb, gc);
-  int const l = tile - C.off[kind][j];
-  T *Wn       = (T *)J.W;  // holds the accumulator dU once the predictor has run
-  T *Wh       = Wn + (size_t)nslot(J.b) * (size_t)J.b.n;
+  int ta, tb;
+  int const tc = divmod(divmod(tile - C.off[kind][j], ga, ta), gb, tb);
+  T *Wn        = (T *)J.W;  // holds the accumulator dU once the predictor has run
+  T *Wh        = Wn + (size_t)nslot(J.b) * (size_t)J.b.n;
+  (void)gc;
   fsweep_tile<T, DIR, L, WA, WB, RECON, SOLVER, FIRST, FINAL>(J.b, Wh, Wn, J.U, J.GEp, J.Epre, J.status, 0.0, J.dt_t,
-                                                              l % ga, (l / ga) % gb, l / (ga * gb));
+                                                              ta, tb, tc);
 }
 
 // Average_Cell_Single_Field of the density for real cells left with non-positive density

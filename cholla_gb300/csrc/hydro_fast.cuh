@@ -56,6 +56,14 @@ __device__ __forceinline__ double max_pos(double x, double c)
 {
   return __double_as_longlong(x) < __double_as_longlong(c) ? c : x;
 }
+// max(a, b) of finite doubles of either sign on the integer pipe: the bit pattern with the
+// magnitude bits flipped for negatives orders as a signed integer in the order of the values
+__device__ __forceinline__ long long ordered_key(double a)
+{
+  long long const k = __double_as_longlong(a);
+  return k ^ ((k >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double max_ord(double a, double b) { return ordered_key(a) < ordered_key(b) ? b : a; }
 __device__ __forceinline__ bool is_pos(float x) { return x > 0.f; }
 __device__ __forceinline__ bool is_neg(float x) { return x < 0.f; }
 __device__ __forceinline__ bool mag_lt(float a, float b) { return fabsf(a) < fabsf(b); }

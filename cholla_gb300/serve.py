@@ -7,9 +7,12 @@ fixed number of steps at CFL 0.3.  Requests arrive over time (a seeded Poisson s
 
 `BatchedServer` keeps one cgb_batch: requests that have arrived are admitted whenever the
 device memory budget and the job table have room, their state stays resident, and every
-iteration advances all admitted jobs by one step in one replay of the batch graph; a job
-that has done its steps leaves the batch and the next arrival takes its place (continuous
-batching).  `PerRequestServer` is the baseline: the same admission, but every job is advanced
+iteration advances the running jobs by one step in one replay of the batch graph; a job that
+has done its steps leaves the batch and the next arrival takes its place (continuous
+batching).  Which admitted jobs run is the scheduler's choice: "fcfs" (default) runs them in
+arrival order until the step holds `saturation_cells` cells, enough to fill the GPU, and holds
+the rest (first come, first served keeps the longest wait, and so the tail latency, lowest;
+the cap keeps the GPU full); "all" steps every admitted job (processor sharing).  `PerRequestServer` is the baseline: the same admission, but every job is advanced
 by its own launches of the single-box step (one box engine per job, each on its own stream),
 either launched kernel by kernel every step ("per_request") or replayed from a CUDA graph of
 its own ("per_request_graph").
@@ -192,11 +195,16 @@ class _Base:
 class BatchedServer(_Base):
     mode = "batched"
 
-    def __init__(self, torch, chains: int = 2, **kw):
+    def __init__(self, torch, chains: int = 2, policy: str = "fcfs", saturation_cells: int = 3 << 20, **kw):
         super().__init__(torch, **kw)
+        if policy not in ("fcfs", "all"):
+            raise ValueError("policy must be 'fcfs' or 'all'")
         self.stream = torch.cuda.Stream()
         self.batch = Batch(self.scheme, self.stream, c_cfl=0.3)
         self.batch.set_chains(chains)
+        self.policy = policy
+        self.saturation_cells = saturation_cells
+        self.held = set()
 
     def _cost(self, req):
         N = req.n + 2 * N_GHOST
@@ -207,16 +215,37 @@ class BatchedServer(_Base):
         jid = self.batch.add(U, N_GHOST, dx, dx, dx)
         return jid, U
 
+    def running(self, active) -> list:
+        """Keys of the jobs to step now: all of them, or (fcfs) the earliest admitted ones up to
+        the saturation cap (at least one)."""
+        if self.policy == "all":
+            return list(active)
+        run, cells = [], 0
+        for key, slot in active.items():  # admission order
+            if run and cells >= self.saturation_cells:
+                break
+            run.append(key)
+            cells += slot[0].cells
+        return run
+
     def _step(self, active):
+        run = set(self.running(active))
+        for key in active:
+            want = key not in run
+            if want != (key in self.held):
+                self.batch.hold(key, want)
+                (self.held.add if want else self.held.discard)(key)
         self.batch.step(1)
         finished = []
-        for key, slot in active.items():
+        for key in run:
+            slot = active[key]
             slot[1] -= 1
             if slot[1] == 0:
                 finished.append(key)
         return finished
 
     def _retire(self, key):
+        self.held.discard(key)
         self.batch.remove(key)
 
     def _event_stream(self):

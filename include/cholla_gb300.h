@@ -158,7 +158,8 @@ const char *cgb_box_last_error(void);
 /* ---- batches: many independent 3D boxes of one scheme advanced together (no counterpart in
  * the reference).  Every job keeps its own state (caller-owned, device resident), scratch, dt
  * and time; one step of the batch is one chain of launches per 16 jobs over the tiles of all
- * of them (the chains run side by side), replayed from a captured CUDA graph.  Jobs join and
+ * of them, and one chain of the single-box step per large job (the chains run side by side),
+ * replayed from a captured CUDA graph.  Jobs join and
  * leave between steps (the graph is captured again at the next step).  Fast FP64 or mixed
  * precision, hydro. ---- */
 typedef struct cgb_batch cgb_batch;
@@ -175,6 +176,13 @@ int cgb_batch_add(cgb_batch *batch, double *d_conserved, int nx, int ny, int nz,
                   double dz, const int flags[6], double t_end, int *job_id);
 int cgb_batch_remove(cgb_batch *batch, int job_id);
 int cgb_batch_n_jobs(const cgb_batch *batch);
+/* Hold a job out of the steps (hold = 1) or release it (0); a held job keeps its state, time and
+ * pending dt and resumes where it stopped.  Takes effect at the next step. */
+int cgb_batch_hold(cgb_batch *batch, int job_id, int hold);
+/* Jobs of at least `cells` padded cells (default 2^21) run solo: a chain of the single-box step
+ * of their own (the box engine's kernels), the others share the batched kernels.  Same results
+ * for a job whatever shares the batch; takes effect at the next step. */
+int cgb_batch_set_solo_cells(cgb_batch *batch, long long cells);
 /* Spread the jobs over at least `chains` parallel chains of launches (default 1; a chain holds
  * at most 16 jobs), balanced by cells.  Same results bit for bit; takes effect at the next step. */
 int cgb_batch_set_chains(cgb_batch *batch, int chains);

@@ -50,12 +50,14 @@ def _alone(cuda, U0, dx, scheme, steps):
     return U.cpu().numpy(), t
 
 
-def _in_batch(cuda, U0, dx, scheme, steps):
+def _in_batch(cuda, U0, dx, scheme, steps, solo_cells=None):
     from cholla_gb300.batch import Batch
 
     U = U0.clone()
     st = cuda.cuda.Stream()
     bt = Batch(scheme, st, c_cfl=0.3)
+    if solo_cells is not None:
+        bt.set_solo_cells(solo_cells)
     jid = bt.add(U, NG, dx, dx, dx)
     bt.step(steps)
     st.synchronize()
@@ -80,10 +82,17 @@ MIX5 = [(16, "blast", 1), (24, "tube", 2), (20, "blast", 3), (12, "tube", 4), (3
 MIX21 = [(8 + 2 * (i % 5), "blast" if i % 3 else "tube", 30 + i) for i in range(21)]
 
 
-@pytest.mark.parametrize("precision,jobs,chains", [("mixed", MIX5, 1), ("fp64_fast", MIX5, 1), ("mixed", MIX5, 3),
-                                                   ("mixed", MIX21, 1), ("mixed", MIX21, 4)],
-                         ids=["mixed-5", "fp64_fast-5", "mixed-5-3chains", "mixed-21", "mixed-21-4chains"])
-def test_each_job_same_alone_and_in_the_mix(cuda, precision, jobs, chains):
+# 24^3 and 32^3 jobs (32^3 and 40^3 padded) run solo when the threshold is 30000 padded cells
+SOLO = 30000
+
+
+@pytest.mark.parametrize("precision,jobs,chains,solo", [("mixed", MIX5, 1, None), ("fp64_fast", MIX5, 1, None),
+                                                        ("mixed", MIX5, 3, None), ("mixed", MIX21, 1, None),
+                                                        ("mixed", MIX21, 4, None), ("mixed", MIX5, 1, SOLO),
+                                                        ("fp64_fast", MIX5, 2, SOLO)],
+                         ids=["mixed-5", "fp64_fast-5", "mixed-5-3chains", "mixed-21", "mixed-21-4chains",
+                              "mixed-5-solo", "fp64_fast-5-solo"])
+def test_each_job_same_alone_and_in_the_mix(cuda, precision, jobs, chains, solo):
     """A job's result does not depend on the other jobs, on how they are spread over chains of
     launches (up to 16 jobs per chain, chains side by side) or on its place in them."""
     from cholla_gb300.batch import Batch
@@ -91,10 +100,12 @@ def test_each_job_same_alone_and_in_the_mix(cuda, precision, jobs, chains):
     s = _scheme(precision)
     states = [_job_state(cuda, n, k, sd, s) for n, k, sd in jobs]
     steps = 12
-    alone = [_in_batch(cuda, U, dx, s, steps) for U, dx in states]
+    alone = [_in_batch(cuda, U, dx, s, steps, solo) for U, dx in states]
     st = cuda.cuda.Stream()
     bt = Batch(s, st, c_cfl=0.3)
     bt.set_chains(chains)
+    if solo is not None:
+        bt.set_solo_cells(solo)
     mix = []
     for U0, dx in states:
         U = U0.clone()
@@ -149,6 +160,47 @@ def test_jobs_joining_and_leaving_midway(cuda):
     for U, U0, dx, steps in ((UA, UA0, dxa, 10), (UB, UB0, dxb, 6), (UC, UC0, dxc, 3)):
         ref, _ = _in_batch(cuda, U0, dx, s, steps)
         assert _same(ref[rs], U.cpu().numpy()[rs]).all()
+    bt.close()
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64_fast"])
+def test_solo_job_equals_the_box_engine_bitwise(cuda, precision):
+    """A job at or above the solo threshold runs the box engine's own step inside the batch."""
+    s = _scheme(precision)
+    for n, kind, sd in ((24, "tube", 2), (32, "blast", 5)):
+        U, dx = _job_state(cuda, n, kind, sd, s)
+        b, tb = _in_batch(cuda, U, dx, s, 6, solo_cells=SOLO)
+        e, te = _alone(cuda, U, dx, s, 6)
+        rs = real_slice(NG)
+        assert _same(b[rs], e[rs]).all(), f"{n}^3 {kind}"
+        assert tb == te
+
+
+def test_held_job_resumes_where_it_stopped(cuda):
+    """B is held for 3 of A's 7 steps: B ends 4 steps on, equal to 4 steps of B alone."""
+    from cholla_gb300.batch import Batch
+
+    s = _scheme("mixed")
+    (UA0, dxa), (UB0, dxb) = _job_state(cuda, 20, "blast", 21, s), _job_state(cuda, 16, "tube", 22, s)
+    st = cuda.cuda.Stream()
+    bt = Batch(s, st, c_cfl=0.3)
+    UA, UB = UA0.clone(), UB0.clone()
+    a = bt.add(UA, NG, dxa, dxa, dxa)
+    b = bt.add(UB, NG, dxb, dxb, dxb)
+    bt.step(2)
+    bt.hold(b)
+    bt.step(3)
+    bt.hold(b, False)
+    bt.step(2)
+    bt.hold(a)
+    bt.hold(b)
+    bt.step(1)  # everything held: no work
+    st.synchronize()
+    rs = real_slice(NG)
+    for U, U0, dx, steps, jid in ((UA, UA0, dxa, 7, a), (UB, UB0, dxb, 4, b)):
+        ref, t_ref = _in_batch(cuda, U0, dx, s, steps)
+        assert _same(ref[rs], U.cpu().numpy()[rs]).all()
+        assert bt.job_time(jid)[0] == t_ref
     bt.close()
 
 

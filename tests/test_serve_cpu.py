@@ -74,3 +74,19 @@ def test_a_job_larger_than_the_budget_still_runs_alone():
     srv = FakeServer(budget=50, cost=100)
     rep = srv.run(reqs)
     assert len(rep.requests) == 3 and srv.peak_active == 1
+
+
+def _sched(policy, cap):
+    srv = object.__new__(serve.BatchedServer)  # the scheduler alone, no batch behind it
+    srv.policy, srv.saturation_cells = policy, cap
+    return srv
+
+
+def test_fcfs_runs_the_earliest_jobs_up_to_the_saturation_cap():
+    reqs = [serve.Request(i, 0.0, n, "tube", i) for i, n in enumerate((128, 32, 96, 64, 128))]
+    active = {r.rid: [r, r.steps, None, 0] for r in reqs}  # admission order
+    cap = 128 ** 3 + 32 ** 3 + 1
+    assert _sched("fcfs", cap).running(active) == [0, 1, 2]  # stops once the cap is reached
+    assert _sched("fcfs", 1).running(active) == [0]  # at least one job
+    assert _sched("fcfs", 10 ** 12).running(active) == [0, 1, 2, 3, 4]
+    assert _sched("all", 1).running(active) == [0, 1, 2, 3, 4]
