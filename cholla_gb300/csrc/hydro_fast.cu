@@ -353,10 +353,65 @@ struct Sweep {
   }
 };
 
+// W scratch of the fast forms: 2 * nslot * n * 8 bytes.  The first half holds Wⁿ (T) and then
+// the corrector's FP64 accumulator; W½ (T) starts at the second half.
+template <typename T>
+__host__ __device__ __forceinline__ T *half_prims(T *Wn, const Box &b)
+{
+  return reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(Wn) + (size_t)nslot(b) * (size_t)b.n * sizeof(double));
+}
+
+// Corrector accumulator of one field: FP64 in the fast FP64 form; in the mixed form an FP32
+// pair (hi, lo) whose exact sum carries the value (Knuth's error-free TwoSum), so the sums stay
+// on the FP32 pipe.  Every operation is an explicitly
+// rounded intrinsic: no contraction or reassociation may change them.
+template <typename T>
+struct Acc;
+template <>
+struct Acc<double> {
+  double v;
+};
+template <>
+struct __align__(8) Acc<float> {
+  float hi, lo;
+};
+
+// s + e == a + b exactly (TwoSum)
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+  s              = __fadd_rn(a, b);
+  float const bb = __fsub_rn(s, a);
+  e              = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// the increment k * fl - k * fr of a cell from its two faces; each product is rounded once, as
+// the face's other cell rounds it
+__device__ __forceinline__ Acc<double> flux_diff(double k, double fl, double fr)
+{
+  return {__dsub_rn(__dmul_rn(k, fl), __dmul_rn(k, fr))};
+}
+__device__ __forceinline__ Acc<float> flux_diff(float k, float fl, float fr)
+{
+  Acc<float> r;
+  two_sum(__fmul_rn(k, fl), -__fmul_rn(k, fr), r.hi, r.lo);
+  return r;
+}
+__device__ __forceinline__ Acc<double> acc_add(Acc<double> a, Acc<double> b) { return {__dadd_rn(a.v, b.v)}; }
+__device__ __forceinline__ Acc<float> acc_add(Acc<float> a, Acc<float> b)
+{
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  float const t = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+  Acc<float> r;  // renormalise; TwoSum, since cancellation in hi can leave |t| > |s|
+  two_sum(s, t, r.hi, r.lo);
+  return r;
+}
+__device__ __forceinline__ double acc_value(Acc<double> a) { return a.v; }
+__device__ __forceinline__ double acc_value(Acc<float> a) { return __dadd_rn((double)a.hi, (double)a.lo); }
+
 // Uⁿ⁺¹ = Uⁿ + acc in FP64 (GasEnergy from its pdV partial update), the density floor, and the
 // pre-sync total energy for the dual-energy selection
-template <typename T>
-__device__ __forceinline__ void final_update(const Box &b, long long gid, const T *acc, double *__restrict__ U,
+__device__ __forceinline__ void final_update(const Box &b, long long gid, const double *acc, double *__restrict__ U,
                                              const double *__restrict__ GEp, double *__restrict__ Epre,
                                              int *__restrict__ status)
 {
@@ -366,7 +421,7 @@ __device__ __forceinline__ void final_update(const Box &b, long long gid, const 
 #pragma unroll
   for (int q = 0; q < NSLOT; q++) {
     v[q] = 0.0;
-    if (live(q, b)) v[q] = (q == 5 ? GEp[gid] : U[field(q, b) * n + gid]) + (double)acc[q];
+    if (live(q, b)) v[q] = (q == 5 ? GEp[gid] : U[field(q, b) * n + gid]) + acc[q];
   }
   if (b.floor_on && !one_d && v[0] < b.density_floor) {
     if (v[0] > 0) {
@@ -495,34 +550,41 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
   long long const gid = b.id(gx, gy, gz);
   int const fm        = S::at(a, c, S::LF);
   T const dtod        = (T)(dt * (DIR == 0 ? b.idx : DIR == 1 ? b.idy : b.idz));
-  T d[NSLOT];
+  // Conservation: each face's scaled flux dtod * F is rounded the same way for both of its
+  // cells (an uncontracted product) and the cell's increment is their exact difference, summed
+  // over the three sweeps in an accumulator of at least 48 significant bits (W^n's space, 8
+  // bytes per field): FP64 in the fast FP64 form, an FP32 (hi, lo) pair built with error-free
+  // sums in the mixed form.  So the updates telescope to accumulation roundoff in both.
+  Acc<T> acc[NSLOT];
 #pragma unroll
-  for (int q = 0; q < NSLOT; q++)
-    d[q] = live(q, b) ? dtod * (Fs[q * S::NF + fm] - Fs[q * S::NF + fm + S::STRIDE]) : T(0);
-  // rotated momenta back to x, y, z
-  T acc[NSLOT];
-  acc[0]  = d[0];
-  acc[o1] = d[1];
-  acc[o2] = d[2];
-  acc[o3] = d[3];
-#pragma unroll
-  for (int q = 4; q < NSLOT; q++) acc[q] = d[q];
+  for (int q = 0; q < NSLOT; q++) {
+    int const qq = q == 1 ? o1 : q == 2 ? o2 : q == 3 ? o3 : q;  // rotated momenta back to x, y, z
+    if (live(q, b)) acc[qq] = flux_diff(dtod, Fs[q * S::NF + fm], Fs[q * S::NF + fm + S::STRIDE]);
+  }
+  Acc<T> *__restrict__ dA = reinterpret_cast<Acc<T> *>(dU);
   if (!FIRST) {
 #pragma unroll
     for (int q = 0; q < NSLOT; q++)
-      if (live(q, b)) acc[q] = dU[(long long)q * n + gid] + acc[q];
+      if (live(q, b)) acc[q] = acc_add(dA[(long long)q * n + gid], acc[q]);
   }
   if constexpr (!FINAL) {
 #pragma unroll
     for (int q = 0; q < NSLOT; q++)
-      if (live(q, b)) dU[(long long)q * n + gid] = acc[q];
+      if (live(q, b)) dA[(long long)q * n + gid] = acc[q];
   } else {
-    final_update(b, gid, acc, U, GEp, Epre, status);
+    double inc[NSLOT];
+#pragma unroll
+    for (int q = 0; q < NSLOT; q++) inc[q] = live(q, b) ? acc_value(acc[q]) : 0.0;
+    final_update(b, gid, inc, U, GEp, Epre, status);
   }
 }
 
+// Mixed-precision sweeps are latency-bound (FP32 reconstruction chains, FMA pipe under 20% at
+// two blocks per SM): five resident blocks per SM (51 registers, spills to L1) take the 256^3
+// corrector from 6.8 to 4.1 ms (two: 6.8, three: 5.2, four: 4.3, six: 4.07).  The FP64 sweeps
+// are FP64-pipe bound at two.
 template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
-__global__ void __launch_bounds__(L *WA *WB, 2)
+__global__ void __launch_bounds__(L *WA *WB, sizeof(T) == 4 ? 5 : 2)
     k_fsweep(Box b, const T *__restrict__ W, T *__restrict__ dU, double *__restrict__ U,
              const double *__restrict__ GEp, double *__restrict__ Epre, int *__restrict__ status, double dt,
              const double *__restrict__ dtp)
@@ -678,7 +740,7 @@ cudaError_t launch_fast(const Box &b, int recon, int solver, double *U, const Sc
                         const double *dtp, cudaStream_t s, cudaEvent_t *marks)
 {
   T *Wn = (T *)sc.W;
-  T *Wh = Wn + (size_t)nslot(b) * (size_t)b.n;
+  T *Wh = half_prims(Wn, b);
   cudaError_t e;
   if (marks) cudaEventRecord(marks[0], s);
   {
@@ -800,13 +862,13 @@ __global__ void __launch_bounds__(PTX *PTY *PTZ, sizeof(T) == 4 ? 4 : 2)
   int tx, ty;
   int const tz = divmod(divmod(tile - C.off[BK_PRED][j], gx, tx), gy, ty);
   T *Wn        = (T *)J.W;
-  T *Wh        = Wn + (size_t)nslot(J.b) * (size_t)J.b.n;
+  T *Wh        = half_prims(Wn, J.b);
   (void)gz;
   fpred_tile<T, PTX, PTY, PTZ, SOLVER>(J.b, J.U, Wn, Wh, J.GEp, 0.0, J.dt_t, tx, ty, tz);
 }
 
 template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
-__global__ void __launch_bounds__(L *WA *WB, 2) kb_sweep(const __grid_constant__ BatchChunk C)
+__global__ void __launch_bounds__(L *WA *WB, sizeof(T) == 4 ? 5 : 2) kb_sweep(const __grid_constant__ BatchChunk C)
 {
   int const kind    = BK_SWX + DIR;
   int const tile    = blockIdx.x;
@@ -817,7 +879,7 @@ __global__ void __launch_bounds__(L *WA *WB, 2) kb_sweep(const __grid_constant__
   int ta, tb;
   int const tc = divmod(divmod(tile - C.off[kind][j], ga, ta), gb, tb);
   T *Wn        = (T *)J.W;  // holds the accumulator dU once the predictor has run
-  T *Wh        = Wn + (size_t)nslot(J.b) * (size_t)J.b.n;
+  T *Wh        = half_prims(Wn, J.b);
   (void)gc;
   fsweep_tile<T, DIR, L, WA, WB, RECON, SOLVER, FIRST, FINAL>(J.b, Wh, Wn, J.U, J.GEp, J.Epre, J.status, 0.0, J.dt_t,
                                                               ta, tb, tc);

@@ -2,7 +2,7 @@
 
 The reference has no random-field initial condition, so these generators are new: a
 lognormal density and k^-2 velocity fields for the turbulence-like hydro box, a curl of a
-k^-3 vector potential for MHD, the Sod tube, and the Sedov-like blasts and rotated Sod
+k^-3 vector potential for MHD (spectra summed over shells of |k|), the Sod tube, and the Sedov-like blasts and rotated Sod
 tubes of the serving workload.  Every array is field-major [f, z, y, x] with ghost cells,
 matching U[f*n_cells + x + y*nx + z*nx*ny].
 """
@@ -18,13 +18,17 @@ def n_fields(dual_energy: bool, mhd: bool = False, n_scalars: int = 0) -> int:
 
 
 def gaussian_random_field(n: int, slope: float, rng: np.random.Generator) -> np.ndarray:
-    """Periodic unit-variance Gaussian random field on n^3 cells with power spectrum k^slope."""
+    """Periodic unit-variance Gaussian random field on n^3 cells whose spectrum, summed over
+    shells of |k| (the turbulence convention, E(k) dk), goes as k^slope: Fourier amplitudes
+    |f_k| ~ k^((slope - 2) / 2).  (A k^-2 slope is Burgers-like: smooth at the grid scale.  With
+    the slope put on |f_k|^2 instead, a k^-2 field is white at the grid scale, with Mach-2 jumps
+    between neighbouring cells from which even the exact FP64 scheme fails within a few steps.)"""
     k = np.fft.fftfreq(n) * n
     kr = np.fft.rfftfreq(n) * n
     kk = np.sqrt(k[:, None, None] ** 2 + k[None, :, None] ** 2 + kr[None, None, :] ** 2)
     amp = np.zeros_like(kk)
     nz = kk > 0
-    amp[nz] = kk[nz] ** (slope / 2.0)
+    amp[nz] = kk[nz] ** ((slope - 2.0) / 2.0)
     noise = rng.standard_normal((n, n, n))
     f = np.fft.irfftn(np.fft.rfftn(noise) * amp, s=(n, n, n), axes=(0, 1, 2))
     f -= f.mean()
@@ -39,8 +43,9 @@ def pad_periodic(real: np.ndarray, ng: int) -> np.ndarray:
 
 def turbulence_box(n: int, ng: int = 4, gamma: float = 5.0 / 3.0, seed: int = 0, sigma: float = 0.5,
                    mach: float = 2.0, pressure: float = 1.0, dual_energy: bool = True) -> np.ndarray:
-    """Periodic cube of side 1: lognormal density (mean 1, sigma) from a k^-2 field, three
-    independent k^-2 velocity fields scaled to rms Mach `mach`, uniform pressure."""
+    """Periodic cube of side 1: lognormal density (mean 1, sigma) from a Gaussian field with a
+    k^-2 shell spectrum, three independent k^-2 velocity fields scaled to rms Mach `mach`,
+    uniform pressure."""
     rng = np.random.default_rng(seed)
     g = gaussian_random_field(n, -2.0, rng)
     rho = np.exp(sigma * g - 0.5 * sigma * sigma)
@@ -58,10 +63,32 @@ def turbulence_box(n: int, ng: int = 4, gamma: float = 5.0 / 3.0, seed: int = 0,
     return pad_periodic(U, ng)
 
 
+def blast_box(n: int, ng: int = 4, gamma: float = 5.0 / 3.0, centre=(0.5, 0.5, 0.5), radius: float = 3.0,
+              energy: float = 1.0, rho: float = 1.0, p: float = 1e-5, dual_energy: bool = True) -> np.ndarray:
+    """Host copy of the serving workload's Sedov-like blast (the device version is cgb_ic_blast):
+    uniform rho and p, plus thermal energy `energy` spread evenly over the cells whose centres
+    lie within `radius` cells of `centre` (box coordinates, side 1).  Zero velocity."""
+    dx = 1.0 / n
+    c = (np.arange(n) + 0.5) * dx
+    z, y, x = np.meshgrid(c, c, c, indexing="ij")
+    r2 = (x - centre[0]) ** 2 + (y - centre[1]) ** 2 + (z - centre[2]) ** 2
+    inside = r2 < (radius * dx) ** 2
+    eint = np.full((n, n, n), p / (gamma - 1.0))
+    eint[inside] += energy / (inside.sum() * dx ** 3)
+    nf = n_fields(dual_energy)
+    U = np.zeros((nf, n, n, n))
+    U[0] = rho
+    U[4] = eint
+    if dual_energy:
+        U[nf - 1] = eint
+    return pad_periodic(U, ng)
+
+
 def mhd_box(n: int, ng: int = 4, gamma: float = 5.0 / 3.0, seed: int = 0, beta: float = 1.0,
             vrms: float = 1.0) -> np.ndarray:
     """Periodic MHD cube of side 1: density 1, pressure 1, k^-2 velocity (rms vrms), face-centred
-    B = discrete curl of a k^-3 vector potential scaled to plasma beta, so div B = 0 to roundoff.
+    B = discrete curl of a k^-3 vector potential (shell spectra) scaled to plasma beta, so
+    div B = 0 to roundoff.
     The curl uses the stencil of Init_Magnetic_Field_With_Vector_Potential
     (src/utils/mhd_utilities.cu:22-44)."""
     rng = np.random.default_rng(seed)

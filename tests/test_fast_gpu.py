@@ -1,9 +1,9 @@
 """The throughput arithmetic paths against the oracle, by tolerance (they are not bit-exact).
 
-fast FP64 (CGB_FP64_FAST): relative L1 error of every field <= 1e-12 after one step, and
-after 20 steps of the turbulence box within 10x of the oracle's own one-ULP drift.  Mixed precision (CGB_MIXED): relative L1 density
-error <= 1e-5 after 20 steps (the accuracy target of the mixed-precision form), per-field
-errors printed.  Relative L1 = sum|gpu - oracle| / sum|oracle| over real cells.
+fast FP64 (CGB_FP64_FAST): relative L1 error of every field <= 1e-12 after one step and after
+20 steps of the turbulence box.  Mixed precision (CGB_MIXED): relative L1 density error <= 1e-5
+after 20 steps (the accuracy target of the mixed-precision form), per-field errors printed.
+Relative L1 = sum|gpu - oracle| / sum|oracle| over real cells.
 """
 import numpy as np
 import pytest
@@ -55,28 +55,8 @@ def test_fast_fp64_one_step(cuda, oracle_lib, recon, solver):
     assert np.all(err <= 1e-12), dict(zip(FIELDS, err))
 
 
-def _oracle_ulp_drift(oracle_lib, U0, ng, dx, steps):
-    """Relative L1 drift, per field, of the oracle's own trajectory after `steps` steps when
-    every initial density is moved by one ULP: the scheme's sensitivity to roundoff."""
-    o = oracle_lib
-    nf, nz, ny, nx = U0.shape
-    cfg = o.config(nx, ny, nz, ng, nf, de=True, recon=o.PPMC, solver=o.HLLC, gamma=5 / 3, dx=dx, dy=dx, dz=dx)
-    A, B = U0.copy(), U0.copy()
-    B[0] = np.nextafter(B[0], np.inf)
-    for _ in range(steps):
-        dt = 0.3 / o.calc_dt(cfg, A.reshape(-1))
-        for X in (A, B):
-            o.vl_step_3d(cfg, X.reshape(-1), dt)
-            o.set_boundaries(cfg, X.reshape(-1), (1,) * 6)
-    return rel_l1(B, A, ng)
-
-
 def test_fast_fp64_turbulence_20_steps(cuda, oracle_lib):
-    """20 steps of the rms-Mach-2 turbulence box.  The dual-energy scheme amplifies roundoff:
-    a one-ULP change of the initial densities alone moves the oracle's own result by ~1e-10
-    relative L1 after 20 steps, so no arithmetic that is not bit-identical can stay at 1e-12
-    there.  The fast FP64 form must stay within 10x of that one-ULP drift in every field (it
-    stays within 1e-12 after one step, test_fast_fp64_one_step)."""
+    """20 steps of the rms-Mach-2 turbulence box: every field within 1e-12 relative L1."""
     from cholla_gb300 import ics
     from cholla_gb300 import integrator as I
 
@@ -85,19 +65,15 @@ def test_fast_fp64_turbulence_20_steps(cuda, oracle_lib):
     s = I.Scheme(reconstruction="PPMC", riemann_solver="HLLC", dual_energy=True, precision="fp64_fast")
     got, want = _run_pair(cuda, oracle_lib, U0, ng, s, 20, (1 / n,) * 3)
     err = rel_l1(got, want, ng)
-    drift = _oracle_ulp_drift(oracle_lib, U0, ng, 1 / n, 20)
-    print("fp64_fast", {f: f"{e:.2e} (1-ulp drift {d:.2e})" for f, e, d in zip(FIELDS, err, drift)})
+    print("fp64_fast", {f: f"{e:.2e}" for f, e in zip(FIELDS, err)})
     assert np.isfinite(got).all()
-    assert np.all(err <= 10 * np.maximum(drift, 1e-13)), dict(zip(FIELDS, err))
+    assert np.all(err <= 1e-12), dict(zip(FIELDS, err))
 
 
 @pytest.mark.parametrize("seed,mach", [(4, 2.0), (6, 3.0)])
 def test_mixed_turbulence_20_steps(cuda, oracle_lib, seed, mach):
-    """Mixed precision, 20 steps of rms-Mach-2 and -3 turbulence boxes: finite everywhere, and
-    relative L1 density error <= 1e-5 (the accuracy target of the mixed-precision form) or,
-    where the FP64 scheme itself is less reproducible than that, within 10x of the oracle's own
-    one-ULP drift.  The Mach-3 box has cold, near-vacuum cells where FP32 characteristic
-    projection and HLLC star states are ill-conditioned; per-field errors are printed."""
+    """Mixed precision, 20 steps of rms-Mach-2 and -3 turbulence boxes: finite everywhere and
+    relative L1 density error <= 1e-5 (the accuracy target of the mixed-precision form)."""
     from cholla_gb300 import ics
     from cholla_gb300 import integrator as I
 
@@ -106,10 +82,9 @@ def test_mixed_turbulence_20_steps(cuda, oracle_lib, seed, mach):
     s = I.Scheme(reconstruction="PPMC", riemann_solver="HLLC", dual_energy=True, precision="mixed")
     got, want = _run_pair(cuda, oracle_lib, U0, ng, s, 20, (1 / n,) * 3)
     err = rel_l1(got, want, ng)
-    drift = _oracle_ulp_drift(oracle_lib, U0, ng, 1 / n, 20)
-    print(f"mixed seed {seed} mach {mach}", {f: f"{e:.2e} (1-ulp drift {d:.2e})" for f, e, d in zip(FIELDS, err, drift)})
+    print(f"mixed seed {seed} mach {mach}", {f: f"{e:.2e}" for f, e in zip(FIELDS, err)})
     assert np.isfinite(got).all()
-    assert err[0] <= max(1e-5, 10 * drift[0]), dict(zip(FIELDS, err))
+    assert err[0] <= 1e-5, dict(zip(FIELDS, err))
 
 
 def test_engine_matches_dropin_sequence_bitwise(cuda):

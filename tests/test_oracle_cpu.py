@@ -42,27 +42,33 @@ def test_oracle_conserves_on_periodic_box(oracle_lib):
     assert np.all(np.abs(tot - tot0) <= 1e-12 * np.abs(U[real_slice(4)]).sum(axis=(1, 2, 3)))
 
 
-def test_ulp_sensitivity_of_the_scheme(oracle_lib):
-    """Why the FP64 path is held to bit-exactness: the reference scheme amplifies rounding.
-    A one-ULP change of every density grows by orders of magnitude within a few steps of the
-    Mach-2 turbulence box (the dual-energy select and the limiter switches are discontinuous),
-    so 'within 1e-12 relative L1 after N steps' is only guaranteed by reproducing the
-    reference's arithmetic exactly."""
-    from cholla_gb300 import ics
-
-    o = oracle_lib
-    n, ng = 24, 4
-    A = ics.turbulence_box(n, ng, 5 / 3, seed=4)
+def _ulp_growth(o, A, steps=8):
+    n, ng = A.shape[1] - 8, 4
     B = A.copy()
     B[0] = np.nextafter(B[0], np.inf)
     nf, N = A.shape[0], A.shape[1]
     cfg = o.config(N, N, N, ng, nf, de=True, recon=o.PPMC, solver=o.HLLC, gamma=5 / 3, dx=1 / n, dy=1 / n, dz=1 / n)
     errs = []
-    for _ in range(8):
+    for _ in range(steps):
         dt = 0.3 / o.calc_dt(cfg, A.reshape(-1))
         for X in (A, B):
             o.vl_step_3d(cfg, X.reshape(-1), dt)
             o.set_boundaries(cfg, X.reshape(-1), (1,) * 6)
         rs = real_slice(ng)
         errs.append(np.abs(A - B)[rs].sum() / np.abs(A[rs]).sum())
-    assert errs[-1] > 100 * errs[0], errs
+    return errs
+
+
+def test_ulp_sensitivity_of_the_scheme(oracle_lib):
+    """How the reference scheme treats rounding.  On the smooth turbulence box a one-ULP change
+    of every density stays at rounding level; at the strong Sedov-like blast (p = 1e-5 outside
+    the sphere, a symmetric configuration) it grows by orders of magnitude within a few steps,
+    because the limiter and dual-energy switches flip.  So 'within 1e-12 relative L1 after N
+    steps' is guaranteed in general only by reproducing the reference's arithmetic exactly,
+    and the throughput forms are compared with the exact form on smooth problems."""
+    from cholla_gb300 import ics
+
+    smooth = _ulp_growth(oracle_lib, ics.turbulence_box(24, 4, 5 / 3, seed=4))
+    assert max(smooth) < 1e-14, smooth
+    blast = _ulp_growth(oracle_lib, ics.blast_box(24, 4, 5 / 3))
+    assert blast[-1] > 100 * blast[0], blast
