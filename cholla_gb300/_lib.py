@@ -85,6 +85,7 @@ SIGNATURES = {
     "cgb_batch_n_jobs": (_I, [_P]),
     "cgb_batch_set_chains": (_I, [_P, _I]),
     "cgb_batch_hold": (_I, [_P, _I, _I]),
+    "cgb_selftest_conversions": (_I, [_P, C.c_longlong, _P, _P]),
     "cgb_batch_set_solo_cells": (_I, [_P, C.c_longlong]),
     "cgb_batch_step": (_I, [_P, _I]),
     "cgb_batch_job_time": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_D)]),

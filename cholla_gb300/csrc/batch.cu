@@ -1,9 +1,10 @@
 // batch.cu -- the batch handle API: many independent 3D boxes of one scheme, each with its own
 // state, scratch, time step and time, advanced together (kernels in hydro_fast.cu).  The jobs
 // are cut into chunks of BATCH_CHUNK; each chunk is one chain of launches whose kernels carry
-// the chunk in their parameters, one block per tile of all its jobs.  The chains are parallel
-// branches of one CUDA graph, replayed every step and captured again after the job set changes
-// (jobs join and leave between steps).
+// the chunk in their parameters, one block per tile of all its jobs; large jobs run the
+// single-box step in a chain of their own.  The chains run side by side (forked streams); a
+// job set that holds for two steps is captured into a CUDA graph and replayed (jobs join and
+// leave between steps).
 //
 // No counterpart in the reference: it holds one box shape per process (its scratch and launch
 // parameters are file-scope globals, src/global/global_cuda.cu:1-16, VL_3D_cuda.cu:141).
@@ -40,6 +41,11 @@ struct cgb_batch {
   std::vector<cudaStream_t> aux;        // capture streams of chunks 1, 2, ...
   std::vector<cudaEvent_t> ev;          // fork (0) and joins of the capture
   cudaMemPool_t pool = nullptr;         // job scratch; keeps freed memory for the next job
+  struct Plan {
+    std::vector<cgb::BatchChunk> chunks;  // shared-kernel chains
+    std::vector<size_t> solo;             // jobs run by the single-box step, one chain each
+  } plan;
+  int stable      = 0;                  // steps since the job set last changed
   long long steps = 0;
   std::mutex mu;
 };
@@ -95,6 +101,70 @@ std::vector<cgb::BatchChunk> build_chunks(const std::vector<cgb::BatchJob> &jobs
     for (int k = 0; k < cgb::BK_NUM; k++) C.off[k][C.njobs] = C.total[k];
   }
   return out;
+}
+// the running jobs as chains: large ones solo, the rest in chunks; streams and events for them
+cudaError_t make_plan(cgb_batch &bt)
+{
+  std::vector<cgb::BatchJob> shared;
+  bt.plan.solo.clear();
+  for (size_t i = 0; i < bt.jobs.size(); i++) {
+    if (bt.slots[i].held) continue;
+    if (bt.jobs[i].b.n >= bt.solo_cells)
+      bt.plan.solo.push_back(i);
+    else
+      shared.push_back(bt.jobs[i]);
+  }
+  bt.plan.chunks  = build_chunks(shared, bt.chains);
+  size_t const nc = bt.plan.chunks.size() + bt.plan.solo.size();
+  cudaError_t e;
+  while (bt.aux.size() + 1 < nc) {
+    cudaStream_t a;
+    if ((e = cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking)) != cudaSuccess) return e;
+    bt.aux.push_back(a);
+  }
+  while (bt.ev.size() < nc) {
+    cudaEvent_t v;
+    if ((e = cudaEventCreateWithFlags(&v, cudaEventDisableTiming)) != cudaSuccess) return e;
+    bt.ev.push_back(v);
+  }
+  return cudaSuccess;
+}
+
+// One step of every chain of the plan, queued on the batch stream: chain 0 on it, chain c > 0
+// on aux[c - 1], forked from and joined back to it by events (the same calls build the graph
+// under capture).  Chains 0 .. chunks-1 are the chunks; the solo jobs follow, each the
+// single-box step (ghost fill, dt, step with the CFL reduction for the next) as the box
+// engine runs it.
+cudaError_t launch_plan(cgb_batch &bt)
+{
+  cgb_scheme const &s = bt.scheme;
+  int const mixed     = s.precision == CGB_MIXED ? 1 : 0;
+  auto const &chunks  = bt.plan.chunks;
+  size_t const nc     = chunks.size() + bt.plan.solo.size();
+  cudaError_t e       = nc > 1 ? cudaEventRecord(bt.ev[0], bt.stream) : cudaSuccess;
+  for (size_t c = 1; c < nc && e == cudaSuccess; c++) e = cudaStreamWaitEvent(bt.aux[c - 1], bt.ev[0], 0);
+  for (size_t c = 0; c < nc && e == cudaSuccess; c++) {
+    cudaStream_t const st = c ? bt.aux[c - 1] : bt.stream;
+    if (c < chunks.size()) {
+      e = cgb::batch_chunk_step(chunks[c], s.reconstruction, s.riemann_solver, mixed, s.dual_energy, s.n_scalars,
+                                bt.c_cfl, s.U_floor, s.temperature_floor, st);
+      continue;
+    }
+    size_t const i         = bt.plan.solo[c - chunks.size()];
+    cgb::BatchJob const &J = bt.jobs[i];
+    cgb::Scratch sc{};
+    sc.W = J.W, sc.GEp = J.GEp, sc.Epre = J.Epre, sc.dti = J.dti, sc.status = J.status;
+    e = cgb::set_boundaries(J.b, J.U, bt.slots[i].flags, st);
+    if (e == cudaSuccess) e = cgb::cfl_dt(J.dti, J.dt_t, bt.c_cfl, J.t_end, st);
+    if (e == cudaSuccess)
+      e = cgb::hydro_step(J.b, s.reconstruction, s.riemann_solver, s.precision, J.U, sc, 0.0, J.dt_t, s.U_floor,
+                          s.temperature_floor, 1, st);
+  }
+  for (size_t c = 1; c < nc && e == cudaSuccess; c++) {
+    e = cudaEventRecord(bt.ev[c], bt.aux[c - 1]);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(bt.stream, bt.ev[c], 0);
+  }
+  return e;
 }
 }  // namespace
 
@@ -287,78 +357,32 @@ int cgb_batch_step(cgb_batch *bt, int n_steps)
   std::lock_guard<std::mutex> lk(bt->mu);
   if (bt->jobs.empty() || n_steps == 0) return CGB_OK;
   cudaError_t e;
-  if (bt->dirty && bt->graph) {
-    cudaGraphExecDestroy(bt->graph);
+  if (bt->dirty) {
+    if (bt->graph) cudaGraphExecDestroy(bt->graph);
     bt->graph = nullptr;
+    if ((e = make_plan(*bt)) != cudaSuccess) return bcuda(e, "batch plan");
+    bt->dirty  = false;
+    bt->stable = 0;
   }
-  if (!bt->graph && bt->dirty) {
-    // running jobs: large ones solo (a chain of the single-box kernels each), the rest in chunks
-    std::vector<cgb::BatchJob> shared;
-    std::vector<size_t> solo;
-    for (size_t i = 0; i < bt->jobs.size(); i++) {
-      if (bt->slots[i].held) continue;
-      if (bt->jobs[i].b.n >= bt->solo_cells)
-        solo.push_back(i);
-      else
-        shared.push_back(bt->jobs[i]);
-    }
-    std::vector<cgb::BatchChunk> const chunks = build_chunks(shared, bt->chains);
-    size_t const nc = chunks.size() + solo.size();  // chains of the graph
-    if (nc == 0) {  // every job held: nothing to step
-      bt->dirty = false;
-      return CGB_OK;
-    }
-    while (bt->aux.size() + 1 < nc) {
-      cudaStream_t a;
-      if ((e = cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking)) != cudaSuccess) return bcuda(e, "batch stream");
-      bt->aux.push_back(a);
-    }
-    while (bt->ev.size() < nc) {
-      cudaEvent_t v;
-      if ((e = cudaEventCreateWithFlags(&v, cudaEventDisableTiming)) != cudaSuccess) return bcuda(e, "batch event");
-      bt->ev.push_back(v);
-    }
-    cgb_scheme const &s = bt->scheme;
-    int const mixed     = s.precision == CGB_MIXED ? 1 : 0;
-    cudaGraph_t g;
-    if ((e = cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
-      return bcuda(e, "batch capture");
-    // chain 0 on the batch stream, chain c > 0 on aux[c - 1]: forked from and joined to it.
-    // Chains 0 .. chunks-1 are the chunks; the solo jobs follow, each the single-box step
-    // (ghost fill, dt, step with the CFL reduction for the next), as the box engine runs it.
-    cudaError_t ce = nc > 1 ? cudaEventRecord(bt->ev[0], bt->stream) : cudaSuccess;
-    for (size_t c = 1; c < nc && ce == cudaSuccess; c++) ce = cudaStreamWaitEvent(bt->aux[c - 1], bt->ev[0], 0);
-    for (size_t c = 0; c < nc && ce == cudaSuccess; c++) {
-      cudaStream_t const st = c ? bt->aux[c - 1] : bt->stream;
-      if (c < chunks.size()) {
-        ce = cgb::batch_chunk_step(chunks[c], s.reconstruction, s.riemann_solver, mixed, s.dual_energy, s.n_scalars,
-                                   bt->c_cfl, s.U_floor, s.temperature_floor, st);
-        continue;
-      }
-      size_t const i        = solo[c - chunks.size()];
-      cgb::BatchJob const &J = bt->jobs[i];
-      cgb::Scratch sc{};
-      sc.W = J.W, sc.GEp = J.GEp, sc.Epre = J.Epre, sc.dti = J.dti, sc.status = J.status;
-      ce = cgb::set_boundaries(J.b, J.U, bt->slots[i].flags, st);
-      if (ce == cudaSuccess) ce = cgb::cfl_dt(J.dti, J.dt_t, bt->c_cfl, J.t_end, st);
-      if (ce == cudaSuccess)
-        ce = cgb::hydro_step(J.b, s.reconstruction, s.riemann_solver, s.precision, J.U, sc, 0.0, J.dt_t, s.U_floor,
-                             s.temperature_floor, 1, st);
-    }
-    for (size_t c = 1; c < nc && ce == cudaSuccess; c++) {
-      ce = cudaEventRecord(bt->ev[c], bt->aux[c - 1]);
-      if (ce == cudaSuccess) ce = cudaStreamWaitEvent(bt->stream, bt->ev[c], 0);
-    }
-    e = cudaStreamEndCapture(bt->stream, &g);
-    if (ce != cudaSuccess || e != cudaSuccess) return bcuda(ce != cudaSuccess ? ce : e, "batch capture");
-    e = cudaGraphInstantiate(&bt->graph, g, 0);
-    cudaGraphDestroy(g);
-    if (e != cudaSuccess) return bcuda(e, "batch graph");
-    bt->dirty = false;
-  }
-  if (!bt->graph) return CGB_OK;  // every job held
+  if (bt->plan.chunks.empty() && bt->plan.solo.empty()) return CGB_OK;  // every job held
   for (int i = 0; i < n_steps; i++) {
-    if ((e = cudaGraphLaunch(bt->graph, bt->stream)) != cudaSuccess) return bcuda(e, "batch step");
+    // A job set that changes every step or two (arrivals, departures, holds) is launched
+    // directly: a capture and instantiation per change would cost more host time than the
+    // launches.  Once it has held for two steps it is captured and replayed.
+    if (!bt->graph && bt->stable >= 2) {
+      cudaGraph_t g;
+      if ((e = cudaStreamBeginCapture(bt->stream, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
+        return bcuda(e, "batch capture");
+      cudaError_t const ce = launch_plan(*bt);
+      e                    = cudaStreamEndCapture(bt->stream, &g);
+      if (ce != cudaSuccess || e != cudaSuccess) return bcuda(ce != cudaSuccess ? ce : e, "batch capture");
+      e = cudaGraphInstantiate(&bt->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return bcuda(e, "batch graph");
+    }
+    e = bt->graph ? cudaGraphLaunch(bt->graph, bt->stream) : launch_plan(*bt);
+    if (e != cudaSuccess) return bcuda(e, "batch step");
+    bt->stable++;
   }
   bt->steps += n_steps;
   return CGB_OK;

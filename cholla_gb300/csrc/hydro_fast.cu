@@ -81,10 +81,28 @@ __device__ __forceinline__ int rot(int q, int o1, int o2, int o3)
 template <int steps>
 __device__ __forceinline__ double rcp_nr(double d)
 {
-  double r = (double)__frcp_rn((float)d);
+  double r = hf::to_f64(__frcp_rn(hf::to_f32(d)));
 #pragma unroll
   for (int i = 0; i < steps; i++) r = fma(r, fma(-d, r, 1.0), r);
   return r;
+}
+
+// FP64 value to the compute type and back (integer-pipe conversions in the mixed form)
+template <typename T>
+__device__ __forceinline__ T narrow(double x)
+{
+  if constexpr (std::is_same<T, float>::value)
+    return hf::to_f32(x);
+  else
+    return x;
+}
+template <typename T>
+__device__ __forceinline__ double widen(T a)
+{
+  if constexpr (std::is_same<T, float>::value)
+    return hf::to_f64(a);
+  else
+    return a;
 }
 
 // Primitives (T) of one cell from its FP64 conserved state q (slots), pressure recovered in
@@ -101,25 +119,30 @@ __device__ __forceinline__ void prim_from_cons(const double *q, const Box &b, T 
   if (b.de) {
     p    = hf::ratio_gt(eth, q[4], ETA_1) ? eth : q[5];
     p    = hf::max_pos(p * (b.gamma - 1.0), TINY);
-    w[5] = (T)(q[5] * id);
+    w[5] = narrow<T>(q[5] * id);
   } else {
     p    = hf::max_pos((b.gamma - 1.0) * eth, TINY);
     w[5] = T(0);
   }
-  w[0] = (T)d;
+  w[0] = narrow<T>(d);
   if (mix) {
-    float const idf = (float)id;
-    w[1] = (T)((float)q[1] * idf);
-    w[2] = (T)((float)q[2] * idf);
-    w[3] = (T)((float)q[3] * idf);
+    float const idf = hf::to_f32(id);
+    w[1] = (T)(hf::to_f32(q[1]) * idf);
+    w[2] = (T)(hf::to_f32(q[2]) * idf);
+    w[3] = (T)(hf::to_f32(q[3]) * idf);
   } else {
     w[1] = (T)(q[1] * id);
     w[2] = (T)(q[2] * id);
     w[3] = (T)(q[3] * id);
   }
-  w[4] = (T)p;
+  w[4] = narrow<T>(p);
 #pragma unroll
-  for (int k = 0; k < NS_MAX; k++) w[6 + k] = (k < b.ns) ? (T)(mix ? (float)q[6 + k] * (float)id : q[6 + k] * id) : T(0);
+  for (int k = 0; k < NS_MAX; k++) {
+    if constexpr (std::is_same<T, float>::value)
+      w[6 + k] = (k < b.ns) ? hf::to_f32(q[6 + k]) * hf::to_f32(id) : 0.f;
+    else
+      w[6 + k] = (k < b.ns) ? q[6 + k] * id : 0.0;
+  }
 }
 
 template <typename T>
@@ -264,7 +287,7 @@ __device__ __forceinline__ void fpred_tile(const Box &b, const double *__restric
   int const fx = i + (TX + 1) * (j + TY * k);
   int const fy = i + TX * (j + (TY + 1) * k);
   int const fz = i + TX * (j + TY * k);
-  T const dtodx = (T)(0.5 * dt * b.idx), dtody = (T)(0.5 * dt * b.idy), dtodz = (T)(0.5 * dt * b.idz);
+  T const dtodx = narrow<T>(0.5 * dt * b.idx), dtody = narrow<T>(0.5 * dt * b.idy), dtodz = narrow<T>(0.5 * dt * b.idz);
   double q[NSLOT];
 #pragma unroll
   for (int s = 0; s < NSLOT; s++) {
@@ -275,7 +298,7 @@ __device__ __forceinline__ void fpred_tile(const Box &b, const double *__restric
         a += dtody * (Fys[s * NFY + fy] - Fys[s * NFY + fy + TX]);
         a += dtodz * (Fzs[s * NFZ + fz] - Fzs[s * NFZ + fz + TX * TY]);
       }
-      q[s] = U[field(s, b) * n + gid] + (double)a;
+      q[s] = U[field(s, b) * n + gid] + widen(a);
     }
   }
   if (b.de) {
@@ -286,18 +309,18 @@ __device__ __forceinline__ void fpred_tile(const Box &b, const double *__restric
     if (one_d) {
       double const d = U[gid], id = 1.0 / d;
       double const mx = U[n + gid], my = U[2 * n + gid], mz = U[3 * n + gid];
-      Ph = (T)((U[4 * n + gid] - 0.5 * (mx * mx + my * my + mz * mz) * id) * (b.gamma - 1.0));
+      Ph = narrow<T>((U[4 * n + gid] - 0.5 * (mx * mx + my * my + mz * mz) * id) * (b.gamma - 1.0));
     }
     T div = dtodx * (Ps[NB + c - 1] - Ps[NB + c + 1]);
     if (!one_d)
       div += dtody * (Ps[2 * NB + c - BX] - Ps[2 * NB + c + BX]) +
              dtodz * (Ps[3 * NB + c - BX * BY] - Ps[3 * NB + c + BX * BY]);
-    q[5] += (double)(T(0.5) * Ph * div);
+    q[5] += widen(T(0.5) * Ph * div);
     int const ng = b.ng;
     bool real    = gx >= ng && gx < b.nx - ng;
     if (!one_d) real = real && gy >= ng && gy < b.ny - ng && gz >= ng && gz < b.nz - ng;
     // full-dt partial update (hydro_cuda.cu:754-833): twice the half-step pdV term
-    if (real) GEp[gid] = U[(long long)(b.nf - 1) * n + gid] + (double)(P * div);
+    if (real) GEp[gid] = U[(long long)(b.nf - 1) * n + gid] + widen(P * div);
   }
   if (b.floor_on && !one_d && q[0] < b.density_floor) {
     double const s = b.density_floor / q[0];
@@ -407,7 +430,7 @@ __device__ __forceinline__ Acc<float> acc_add(Acc<float> a, Acc<float> b)
   return r;
 }
 __device__ __forceinline__ double acc_value(Acc<double> a) { return a.v; }
-__device__ __forceinline__ double acc_value(Acc<float> a) { return __dadd_rn((double)a.hi, (double)a.lo); }
+__device__ __forceinline__ double acc_value(Acc<float> a) { return __dadd_rn(hf::to_f64(a.hi), hf::to_f64(a.lo)); }
 
 // Uⁿ⁺¹ = Uⁿ + acc in FP64 (GasEnergy from its pdV partial update), the density floor, and the
 // pre-sync total energy for the dual-energy selection
@@ -549,7 +572,7 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
   if (!real) return;
   long long const gid = b.id(gx, gy, gz);
   int const fm        = S::at(a, c, S::LF);
-  T const dtod        = (T)(dt * (DIR == 0 ? b.idx : DIR == 1 ? b.idy : b.idz));
+  T const dtod        = narrow<T>(dt * (DIR == 0 ? b.idx : DIR == 1 ? b.idy : b.idz));
   // Conservation: each face's scaled flux dtod * F is rounded the same way for both of its
   // cells (an uncontracted product) and the cell's increment is their exact difference, summed
   // over the three sweeps in an accumulator of at least 48 significant bits (W^n's space, 8
@@ -704,7 +727,7 @@ __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict
     }
     if (do_dt) {  // hydroInverseCrossingTime (hydro_cuda.cu:404-419)
       double const c2 = b.gamma * (E - ke) * (b.gamma - 1.0) * d_inv;
-      double const cs = MIX ? (double)sqrtf((float)hf::max_pos(c2, 0.0)) : hf::sqrtT(hf::max_pos(c2, 0.0));
+      double const cs = MIX ? hf::to_f64(sqrtf(hf::to_f32(hf::max_pos(c2, 0.0)))) : hf::sqrtT(hf::max_pos(c2, 0.0));
       double const ax = fabs(mx * d_inv) + cs;
       if (one_d) {
         m = ax * idx;

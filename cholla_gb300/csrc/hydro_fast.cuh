@@ -23,6 +23,36 @@ struct Prim {
   T sc[NS_MAX];
 };
 
+// binary64 <-> binary32 conversions on the integer pipe.  The hardware conversions issue on the
+// FP64 pipe, which bounds the mixed form's FP64 stages (half of their FP64 instructions were
+// conversions); these reproduce them bit for bit from the IEEE 754 formats: a binary32 in
+// the normal range widens exactly (exponent rebased by 1023 - 127, fraction shifted by 29
+// bits); a binary64 narrows by truncating the fraction to 23 bits and rounding to nearest,
+// ties to even (up when the 29 dropped bits exceed half an ulp, or equal it with an odd kept
+// fraction; a carry into the exponent is the correct result, up to infinity).  Zeros,
+// subnormals, infinities, NaNs and results outside the binary32 normal range take the
+// hardware conversion.
+__device__ __forceinline__ double to_f64(float f)
+{
+  unsigned const u = __float_as_uint(f);
+  unsigned const e = (u >> 23) & 0xffu;
+  if (e - 1u < 254u)
+    return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3)), (int)(u << 29));
+  return (double)f;
+}
+__device__ __forceinline__ float to_f32(double x)
+{
+  unsigned const hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  unsigned const e = (hi >> 20) & 0x7ffu;
+  if (e - 897u < 254u) {
+    unsigned const m    = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    unsigned const rest = lo & 0x1fffffffu, half = 0x10000000u;
+    unsigned const r    = ((hi & 0x80000000u) | ((e - 896u) << 23)) + m;
+    return __uint_as_float(r + ((rest > half) | ((rest == half) & (m & 1u))));
+  }
+  return (float)x;
+}
+
 // Comparisons of the limiters.  For double they run on the integer pipes, on the IEEE bit
 // patterns: the step is bound by the FP64 pipe, where every compare and min/max is a full-rate
 // FP64 instruction (DSETP), while the integer pipes sit idle.  Results equal the FP64
@@ -99,9 +129,9 @@ struct Eps<float> {
 // divide / square root is used.  FP32: the hardware approximations (about 1 ulp).
 __device__ __forceinline__ double rcp(double d)
 {
-  float const f = (float)d;
+  float const f = to_f32(d);
   if (!(fabsf(f) > 1e-30f && fabsf(f) < 1e30f)) return 1.0 / d;
-  double r = (double)__frcp_rn(f);
+  double r = to_f64(__frcp_rn(f));
   r        = fma(r, fma(-d, r, 1.0), r);
   return fma(r, fma(-d, r, 1.0), r);
 }
@@ -109,9 +139,9 @@ __device__ __forceinline__ float rcp(float d) { return __frcp_rn(d); }
 
 __device__ __forceinline__ double sqrtT(double x)
 {
-  float const f = (float)x;
+  float const f = to_f32(x);
   if (!(f > 1e-30f && f < 1e30f)) return sqrt(x);
-  double y       = (double)rsqrtf(f);
+  double y       = to_f64(rsqrtf(f));
   double const h = 0.5 * x;
   y              = y * fma(-h * y, y, 1.5);
   y              = y * fma(-h * y, y, 1.5);

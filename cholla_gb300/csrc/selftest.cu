@@ -1,0 +1,42 @@
+// selftest.cu -- device self-checks of arithmetic helpers that replace hardware instructions:
+// the integer-pipe binary64 <-> binary32 conversions of hydro_fast.cuh against the hardware
+// conversions, bit for bit.
+#include <cuda_runtime.h>
+
+#include "../../include/cholla_gb300.h"
+#include "hydro_fast.cuh"
+
+namespace
+{
+// mismatches: [0] narrowing (to_f32 vs (float)), [1] widening (to_f64 vs (double)); each input
+// bit pattern is also read as the binary32 of its low word for the widening check
+__global__ void k_check_conversions(const double *__restrict__ x, long long n, unsigned long long *__restrict__ bad)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double const v = x[i];
+    float const a = cgb::hf::to_f32(v), b = (float)v;
+    if (__float_as_uint(a) != __float_as_uint(b)) atomicAdd(&bad[0], 1ULL);
+    float const f = __uint_as_float((unsigned)__double2loint(v));
+    double const c = cgb::hf::to_f64(f), d = (double)f;
+    if (__double_as_longlong(c) != __double_as_longlong(d)) atomicAdd(&bad[1], 1ULL);
+  }
+}
+}  // namespace
+
+extern "C" int cgb_selftest_conversions(const double *d_values, long long n, unsigned long long *mismatches,
+                                        void *stream)
+{
+  if (!d_values || n < 0 || !mismatches) return CGB_ERR_ARGS;
+  cudaStream_t const s  = (cudaStream_t)stream;
+  unsigned long long *d = nullptr;
+  cudaError_t e         = cudaMallocAsync((void **)&d, 2 * sizeof(unsigned long long), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), s);
+  if (e == cudaSuccess && n > 0) {
+    k_check_conversions<<<1024, 256, 0, s>>>(d_values, n, d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(mismatches, d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (d) cudaFreeAsync(d, s);
+  return e == cudaSuccess ? CGB_OK : CGB_ERR_CUDA;
+}

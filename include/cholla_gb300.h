@@ -192,6 +192,11 @@ int cgb_batch_step(cgb_batch *batch, int n_steps);
 int cgb_batch_job_time(cgb_batch *batch, int job_id, double *t, double *dt_last);
 const char *cgb_batch_last_error(void);
 
+/* ---- self-check: the integer-pipe binary64 <-> binary32 conversions of the mixed form against
+ * the hardware conversions, on the n doubles at d_values (and the binary32 in each low word);
+ * mismatches[0] (narrowing) and [1] (widening) receive the counts.  Synchronises `stream`. ---- */
+int cgb_selftest_conversions(const double *d_values, long long n, unsigned long long *mismatches, void *stream);
+
 /* ---- initial conditions on the device (the serving workload's problems) ---- */
 /* Blast: uniform density rho and pressure p, plus thermal energy `energy` spread uniformly
  * over the cells whose centre lies within `radius` of (cx, cy, cz) (box coordinates of the real

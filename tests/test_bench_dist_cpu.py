@@ -1,0 +1,59 @@
+"""The bench's multi-process host logic on CPU with gloo, world size 2: the barrier and the
+max-over-ranks reduction that bracket the timed region, and the reference arm launched the
+way the driver launches it for N > 1 (torchrun, rank 0 alone runs and prints one line)."""
+import json
+import os
+import socket
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _free_port() -> int:
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out_dir):
+    import argparse
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    sys.path.insert(0, str(ROOT))
+    import torch.distributed as dist
+
+    import bench
+
+    w, r, _ = bench.dist_setup(argparse.Namespace(impl="reference"))
+    bench.barrier(w)
+    m = bench.max_over_ranks(w, 1.5 + r)  # the slowest rank's time wins
+    Path(out_dir, f"rank{r}.json").write_text(json.dumps({"world": w, "rank": r, "max": m}))
+    dist.destroy_process_group()
+
+
+def test_barrier_and_max_over_ranks_gloo(tmp_path):
+    import torch.multiprocessing as mp
+
+    mp.spawn(_rank_main, args=(2, _free_port(), str(tmp_path)), nprocs=2, join=True)
+    got = [json.loads((tmp_path / f"rank{r}.json").read_text()) for r in range(2)]
+    assert [g["rank"] for g in got] == [0, 1]
+    assert all(g["world"] == 2 and g["max"] == 2.5 for g in got)
+
+
+@pytest.mark.timeout(600)
+def test_reference_arm_under_torchrun_prints_one_line(oracle_lib):
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
+           "127.0.0.1", "--master-port", str(_free_port()), "bench.py", "--impl", "reference", "--gpus", "2",
+           "--steps", "1", "--warmup", "3"]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout[-2000:]
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
