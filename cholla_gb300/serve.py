@@ -12,7 +12,9 @@ has done its steps leaves the batch and the next arrival takes its place (contin
 batching).  Which admitted jobs run is the scheduler's choice: "fcfs" (default) runs them in
 arrival order until the step holds `saturation_cells` cells, enough to fill the GPU, and holds
 the rest (first come, first served keeps the longest wait, and so the tail latency, lowest;
-the cap keeps the GPU full); "all" steps every admitted job (processor sharing).  `PerRequestServer` is the baseline: the same admission, but every job is advanced
+the cap keeps the GPU full); "all" steps every admitted job (processor sharing).  The batch's
+schedule (chains, solo threshold) is picked by the autotuner (`tune.py`) on the workload's
+size mix when the server starts.  `PerRequestServer` is the baseline: the same admission, but every job is advanced
 by its own launches of the single-box step (one box engine per job, each on its own stream),
 either launched kernel by kernel every step ("per_request") or replayed from a CUDA graph of
 its own ("per_request_graph").
@@ -189,19 +191,29 @@ class _Base:
                 if wait > 0:
                     time.sleep(min(wait, 0.01))
         wall = time.perf_counter() - t0
-        return Report(self.mode, done, wall, launched)
+        return Report(self.mode, done, wall, launched, dict(getattr(self, "extra", {})))
 
 
 class BatchedServer(_Base):
     mode = "batched"
 
-    def __init__(self, torch, chains: int = 2, policy: str = "fcfs", saturation_cells: int = 3 << 20, **kw):
+    def __init__(self, torch, chains: int | None = None, policy: str = "fcfs", saturation_cells: int = 3 << 20,
+                 autotune: bool = True, **kw):
         super().__init__(torch, **kw)
         if policy not in ("fcfs", "all"):
             raise ValueError("policy must be 'fcfs' or 'all'")
         self.stream = torch.cuda.Stream()
         self.batch = Batch(self.scheme, self.stream, c_cfl=0.3)
-        self.batch.set_chains(chains)
+        self.extra = {}
+        if autotune and chains is None:  # schedule picked by measurement on the workload's size mix
+            from .tune import tune_batch
+
+            t = tune_batch(torch, self.scheme, [n for n in SIZES for _ in range(2)])
+            self.batch.set_chains(t["chains"])
+            self.batch.set_solo_cells(t["solo_cells"])
+            self.extra["tuned"] = {"chains": t["chains"], "solo_cells": t["solo_cells"]}
+        else:
+            self.batch.set_chains(chains or 2)
         self.policy = policy
         self.saturation_cells = saturation_cells
         self.held = set()

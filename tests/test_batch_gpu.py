@@ -213,3 +213,15 @@ def test_serving_loop_completes_a_request_stream(cuda, mode):
     assert summ["requests"] == 12
     assert 0 < summ["p50_ms"] <= summ["p99_ms"]
     assert summ["cell_updates_per_s"] > 0
+
+
+def test_autotuner_picks_a_measured_candidate(cuda):
+    from cholla_gb300 import tune
+
+    s = _scheme("mixed")
+    r = tune.tune_batch(cuda, s, [16, 24, 32, 40], steps=2, warmup=2)
+    assert len(r["table"]) == len(tune.CHAINS) * len(tune.SOLO_CELLS)
+    assert all(row["ms_per_step"] > 0 for row in r["table"])
+    best = min(r["table"], key=lambda row: row["ms_per_step"])
+    assert (r["chains"], r["solo_cells"]) == (best["chains"], best["solo_cells"])
+    assert tune.tune_batch(cuda, s, [40, 32, 24, 16]) is r  # cached per size mix
