@@ -20,8 +20,9 @@ LIB = OUT / "libchollagb.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           "-I", str(HERE.parent / "include")]
-# Per-file flags.  The FP64 kernels keep every multiply and add separately rounded so that
-# they reproduce the reference's -fmad=false build bit for bit.
+# Per-file flags.  The exact FP64 kernels keep every multiply and add separately rounded so
+# that they reproduce the reference's -fmad=false build bit for bit (mhd_fast.cu compiles the
+# same MHD source with contraction: the fast FP64 form).
 PER_FILE = {
     "hydro_exact.cu": ["-fmad=false"],
     "mhd_exact.cu": ["-fmad=false"],

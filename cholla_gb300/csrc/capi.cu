@@ -228,12 +228,13 @@ int cgb_vl_algorithm_3d(double *d_conserved, double *d_grav_potential, int nx, i
   int const H = (g_scheme.reconstruction == CGB_PPMC ? 4 : g_scheme.reconstruction == CGB_PLMC ? 3 : 2) +
                 (g_scheme.mhd ? 1 : 0);
   if (n_ghost < H) return fail(CGB_ERR_ARGS, "n_ghost too small for the reconstruction");
-  if (g_scheme.mhd && g_scheme.precision != CGB_FP64)
-    return fail(CGB_ERR_UNSUPPORTED, "the MHD step is built in exact FP64 only");
+  if (g_scheme.mhd && g_scheme.precision == CGB_MIXED)
+    return fail(CGB_ERR_UNSUPPORTED, "the MHD step is built in exact and fast FP64 only");
   rc = ensure_slot(nx, ny, nz, n_fields, g_scheme.mhd);
   if (rc != CGB_OK) return rc;
   if (g_scheme.mhd) {
-    cudaError_t e = cgb::mhd_exact_step(b, g_scheme.reconstruction, d_conserved, g_slot.s.mhd, dt, nullptr, g_stream);
+    cudaError_t e = cgb::mhd_step(b, g_scheme.reconstruction, g_scheme.precision, d_conserved, g_slot.s.mhd, dt, nullptr,
+                                  g_stream);
     if (e != cudaSuccess) return cuda_fail(e, "vl_algorithm_3d (MHD)");
     return CGB_OK;
   }
@@ -260,7 +261,7 @@ int cgb_vl_algorithm_3d_static(double *d_conserved, double *d_grav_potential, in
   if (rc != CGB_OK) return rc;
   int const H = g_scheme.reconstruction == CGB_PPMC ? 4 : g_scheme.reconstruction == CGB_PLMC ? 3 : 2;
   if (n_ghost < H) return fail(CGB_ERR_ARGS, "n_ghost too small for the reconstruction");
-  if (g_scheme.mhd) return fail(CGB_ERR_UNSUPPORTED, "MHD step not built in this version");
+  if (g_scheme.mhd) return fail(CGB_ERR_UNSUPPORTED, "the static-pool step is hydro only");
   size_t const need = static_layout(b, g_scheme.precision, nullptr, nullptr);
   if (need > kStaticScratchBytes)
     return fail(CGB_ERR_ARGS, "box needs " + std::to_string(need) + " bytes of scratch but the static pool of "

@@ -105,7 +105,7 @@ cudaError_t one_step(cgb_box *bx, double *U, double c_cfl, cudaStream_t st, bool
     // MHD: the step, the temperature floor, then the CFL reduction for the next step (the
     // fast magnetosonic speed needs the cell-centred field, so it is its own pass)
     if (m) cudaEventRecord(m[0], st);
-    if ((e = cgb::mhd_exact_step(bx->b, bx->scheme.reconstruction, U, bx->s.mhd, 0.0, bx->dt_t, st)) !=
+    if ((e = cgb::mhd_step(bx->b, bx->scheme.reconstruction, bx->scheme.precision, U, bx->s.mhd, 0.0, bx->dt_t, st)) !=
         cudaSuccess)
       return e;
     if (m) cudaEventRecord(m[1], st), cudaEventRecord(m[2], st);
@@ -134,8 +134,8 @@ int cgb_box_create(cgb_box **out, int nx, int ny, int nz, int n_ghost, double dx
   if (s.precision < CGB_FP64 || s.precision > CGB_FP64_FAST) return box_fail(nullptr, CGB_ERR_ARGS, "bad precision");
   if (s.n_scalars < 0 || s.n_scalars > cgb::NS_MAX || !(s.gamma > 1.0) || (s.riemann_solver == CGB_HLLD) != (s.mhd != 0))
     return box_fail(nullptr, CGB_ERR_ARGS, "bad scheme (MHD goes with HLLD and only with it)");
-  if (s.mhd && (s.precision != CGB_FP64 || s.dual_energy || ny < 2 || nz < 2))
-    return box_fail(nullptr, CGB_ERR_UNSUPPORTED, "MHD boxes are 3D, exact FP64, without dual energy");
+  if (s.mhd && (s.precision == CGB_MIXED || s.dual_energy || ny < 2 || nz < 2))
+    return box_fail(nullptr, CGB_ERR_UNSUPPORTED, "MHD boxes are 3D, exact or fast FP64, without dual energy");
   bool const one_d = ny == 1 && nz == 1;
   int const H = (s.reconstruction == CGB_PPMC ? 4 : s.reconstruction == CGB_PLMC ? 3 : 2) + (s.mhd ? 1 : 0);
   if (n_ghost < H || nx < 2 * n_ghost + 1 || (!one_d && (ny < 2 * n_ghost + 1 || nz < 2 * n_ghost + 1)))

@@ -33,6 +33,15 @@ size_t mhd_scratch_doubles(const Box &b);
 // dt_dev != null: dt is read on the device (the box engine keeps it there)
 cudaError_t mhd_exact_step(const Box &b, int recon, double *U, double *scratch, double dt, const double *dt_dev,
                            cudaStream_t s);
+// the same step with multiply-adds contracted (fast FP64 form of MHD)
+cudaError_t mhd_fast_step(const Box &b, int recon, double *U, double *scratch, double dt, const double *dt_dev,
+                          cudaStream_t s);
+inline cudaError_t mhd_step(const Box &b, int recon, int precision, double *U, double *scratch, double dt,
+                            const double *dt_dev, cudaStream_t s)
+{
+  return precision == 2 ? mhd_fast_step(b, recon, U, scratch, dt, dt_dev, s)
+                        : mhd_exact_step(b, recon, U, scratch, dt, dt_dev, s);
+}
 // max inverse crossing time with the fast magnetosonic speed into *dti (cleared first)
 cudaError_t mhd_calc_dt(const Box &b, const double *U, unsigned long long *dti, cudaStream_t s);
 // max |div B| over the real cells into *out (as the bits of a non-negative double; cleared first)
