@@ -94,6 +94,7 @@ __device__ __forceinline__ long long ordered_key(double a)
   return k ^ ((k >> 63) & 0x7fffffffffffffffLL);
 }
 __device__ __forceinline__ double max_ord(double a, double b) { return ordered_key(a) < ordered_key(b) ? b : a; }
+__device__ __forceinline__ double min_ord(double a, double b) { return ordered_key(b) < ordered_key(a) ? b : a; }
 __device__ __forceinline__ bool is_pos(float x) { return x > 0.f; }
 __device__ __forceinline__ bool is_neg(float x) { return x < 0.f; }
 __device__ __forceinline__ bool mag_lt(float a, float b) { return fabsf(a) < fabsf(b); }

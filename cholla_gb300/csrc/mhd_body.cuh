@@ -1,8 +1,10 @@
 // mhd_body.cuh -- the VL step of ideal MHD with constrained transport in FP64, written in the
-// reference's operation order.  Compiled twice: mhd_exact.cu (-fmad=false: bit-identical to
-// the reference build) and mhd_fast.cu (multiply-adds contracted into FMAs: the fast FP64
-// form).  The includer defines CGB_MHD_NS (kernel namespace), CGB_MHD_STEP (the step's name)
-// and CGB_MHD_REDUCTIONS (1: also define the scratch size, CFL and div B entry points).
+// reference's operation order.  Compiled twice: mhd_exact.cu (-fmad=false, the reference's own
+// operations: bit-identical to the reference build) and mhd_fast.cu (the fast FP64 form: the
+// helpers mdiv, msqrt, mmin, ... below switch to reciprocal, Newton and integer-pipe forms,
+// and multiply-adds are contracted into FMAs).  The includer defines CGB_MHD_NS (kernel
+// namespace), CGB_MHD_STEP (the step's name), CGB_MHD_FAST and CGB_MHD_REDUCTIONS (1: also
+// define the scratch size, CFL and div B entry points).
 //
 // Stages of VL_Algorithm_3D_CUDA with MHD (src/integrators/VL_3D_cuda.cu:38-360), one kernel
 // each, interface states and fluxes in HBM as the reference keeps them (the step is bound by the
@@ -16,6 +18,9 @@
 #include "common.cuh"
 #include "hydro_math.cuh"
 #include "kernels.h"
+#if CGB_MHD_FAST
+#include "hydro_fast.cuh"
+#endif
 
 namespace cgb
 {
@@ -23,6 +28,32 @@ namespace CGB_MHD_NS
 {
 
 constexpr double HLLD_SMALL = 1.0e-8;  // src/riemann_solvers/hlld_cuda.h:56
+
+// The arithmetic that the two builds do differently.  Exact (CGB_MHD_FAST 0): the reference's
+// operations themselves.  Fast: quotients as products with a reciprocal (FP32 seed + two
+// Newton steps, shared where a denominator repeats: mdivr with minv), square roots and
+// reciprocal square roots from FP32 seeds with Newton steps, and minima, maxima and sign tests
+// on the integer pipe (the step is bound by the FP64 pipe).  Each fast form is within an ulp
+// or two of the exact one.
+#if CGB_MHD_FAST
+__device__ __forceinline__ double mdiv(double a, double b) { return a * hf::rcp(b); }
+__device__ __forceinline__ double minv(double b) { return hf::rcp(b); }
+__device__ __forceinline__ double mdivr(double a, double, double rb) { return a * rb; }
+__device__ __forceinline__ double msqrt(double x) { return hf::sqrtT(x); }
+__device__ __forceinline__ double mrsqrt(double x) { return hf::rcp(hf::sqrtT(x)); }
+__device__ __forceinline__ double mmin(double a, double b) { return hf::min_ord(a, b); }
+__device__ __forceinline__ double mmax(double a, double b) { return hf::max_ord(a, b); }
+__device__ __forceinline__ bool mpos(double l, double r) { return hf::prod_pos(l, r); }  // l * r > 0
+#else
+__device__ __forceinline__ double mdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ double minv(double) { return 0.0; }  // unused by mdivr
+__device__ __forceinline__ double mdivr(double a, double b, double) { return a / b; }
+__device__ __forceinline__ double msqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ double mrsqrt(double x) { return rsqrt(x); }
+__device__ __forceinline__ double mmin(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ double mmax(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ bool mpos(double l, double r) { return l * r > 0.0; }
+#endif
 
 __device__ __forceinline__ double dot3(double a1, double a2, double a3, double b1, double b2, double b3)
 {
@@ -50,8 +81,8 @@ __device__ __forceinline__ double magnetosonic(double d, double p, double bx, do
   double const bSquared  = bXSquared + ((by * by) + (bz * bz));
   double const term1     = gamma * p + bSquared;
   double term2           = (term1 * term1) - 4. * gamma * p * bXSquared;
-  term2                  = sqrt(term2);
-  return sqrt((term1 + choice * term2) / (2.0 * fmax(d, TINY)));
+  term2                  = msqrt(term2);
+  return msqrt(mdiv(term1 + choice * term2, 2.0 * mmax(d, TINY)));
 }
 __device__ __forceinline__ double cfast(double d, double p, double bx, double by, double bz, double g)
 {
@@ -79,9 +110,10 @@ __device__ __forceinline__ MPrim load_data(const Box &b, const double *U, int x,
   long long const id = b.id(x, y, z), n = b.n;
   MPrim P;
   P.d  = U[id];
-  P.vx = U[o1 * n + id] / P.d;
-  P.vy = U[o2 * n + id] / P.d;
-  P.vz = U[o3 * n + id] / P.d;
+  double const rd = minv(P.d);
+  P.vx = mdivr(U[o1 * n + id], P.d, rd);
+  P.vy = mdivr(U[o2 * n + id], P.d, rd);
+  P.vz = mdivr(U[o3 * n + id], P.d, rd);
   double cbx, cby, cbz;
   cc_b(b, U, x, y, z, cbx, cby, cbz);
   if (o1 == 1) {
@@ -94,9 +126,9 @@ __device__ __forceinline__ MPrim load_data(const Box &b, const double *U, int x,
   // hydro_utilities.h:34-45 Calc_Pressure_Primitive
   double pressure = U[4 * n + id] - 0.5 * P.d * sqm(P.vx, P.vy, P.vz);
   pressure -= magE(P.bx, P.by, P.bz);
-  P.p = fmax((b.gamma - 1.) * pressure, TINY);
+  P.p = mmax((b.gamma - 1.) * pressure, TINY);
 #pragma unroll
-  for (int s = 0; s < NS_MAX; s++) P.sc[s] = s < b.ns ? U[(long long)(5 + s) * n + id] / P.d : 0.0;
+  for (int s = 0; s < NS_MAX; s++) P.sc[s] = s < b.ns ? mdivr(U[(long long)(5 + s) * n + id], P.d, rd) : 0.0;
   return P;
 }
 
@@ -117,41 +149,45 @@ __device__ __forceinline__ Eig eigenvectors(const MPrim &p, double cs, double cs
       e.af = 0.0;
       e.as = 1.0;
     } else {
-      e.af = sqrt(num1 / denom);
-      e.as = sqrt(num2 / denom);
+      double const rden = minv(denom);
+      e.af = msqrt(mdivr(num1, denom, rden));
+      e.as = msqrt(mdivr(num2, denom, rden));
     }
   }
   double const bd = rhypot(p.by, p.bz);
   e.by            = isfinite(bd) ? p.by * bd : 1.0;
   e.bz            = isfinite(bd) ? p.bz * bd : 0.0;
   e.sign          = copysign(1.0, p.bx);
-  e.nfs           = 0.5 / cs2;
+  e.nfs           = mdiv(0.5, cs2);
   e.qpf           = e.sign * e.nfs * e.af * e.cf;
   e.qps           = e.sign * e.nfs * e.as * e.cs;
   e.qf            = e.sign * e.af * e.cf;
   e.qs            = e.sign * e.as * e.cs;
-  e.Af            = e.af * cs * sqrt(p.d);
-  e.As            = e.as * cs * sqrt(p.d);
-  e.Apf           = 0.5 * e.af / (cs * sqrt(p.d));
-  e.Aps           = 0.5 * e.as / (cs * sqrt(p.d));
+  double const sd = msqrt(p.d), rcsd = minv(cs * sd);
+  e.Af            = e.af * cs * sd;
+  e.As            = e.as * cs * sd;
+  e.Apf           = mdivr(0.5 * e.af, cs * sd, rcsd);
+  e.Aps           = mdivr(0.5 * e.as, cs * sd, rcsd);
   return e;
 }
 
 // reconstruction.h:378-437 Primitive_To_Characteristic (MHD)
-__device__ __forceinline__ Chr prim_to_char(const MPrim &p, const MPrim &s, const Eig &e, double cs2)
+__device__ __forceinline__ Chr prim_to_char(const MPrim &p, const MPrim &s, const Eig &e, double cs2, double rd,
+                                            double rcs2)
 {
   Chr o;
-  double const isd = rsqrt(p.d);
-  o.a[0] = e.nfs * e.af * (s.p / p.d - e.cf * s.vx) + e.qps * (e.by * s.vy + e.bz * s.vz) +
+  double const isd = mrsqrt(p.d);
+  double const pd  = mdivr(s.p, p.d, rd);
+  o.a[0] = e.nfs * e.af * (pd - e.cf * s.vx) + e.qps * (e.by * s.vy + e.bz * s.vz) +
            e.Aps * (e.by * s.by + e.bz * s.bz);
   o.a[1] = 0.5 * (e.by * (s.bz * e.sign * isd + s.vz) - e.bz * (s.by * e.sign * isd + s.vy));
-  o.a[2] = e.nfs * e.as * (s.p / p.d - e.cs * s.vx) - e.qpf * (e.by * s.vy + e.bz * s.vz) -
+  o.a[2] = e.nfs * e.as * (pd - e.cs * s.vx) - e.qpf * (e.by * s.vy + e.bz * s.vz) -
            e.Apf * (e.by * s.by + e.bz * s.bz);
-  o.a[3] = s.d - s.p / cs2;
-  o.a[4] = e.nfs * e.as * (s.p / p.d + e.cs * s.vx) + e.qpf * (e.by * s.vy + e.bz * s.vz) -
+  o.a[3] = s.d - mdivr(s.p, cs2, rcs2);
+  o.a[4] = e.nfs * e.as * (pd + e.cs * s.vx) + e.qpf * (e.by * s.vy + e.bz * s.vz) -
            e.Apf * (e.by * s.by + e.bz * s.bz);
   o.a[5] = 0.5 * (e.by * (s.bz * e.sign * isd - s.vz) - e.bz * (s.by * e.sign * isd - s.vy));
-  o.a[6] = e.nfs * e.af * (s.p / p.d + e.cf * s.vx) - e.qps * (e.by * s.vy + e.bz * s.vz) +
+  o.a[6] = e.nfs * e.af * (pd + e.cf * s.vx) - e.qps * (e.by * s.vy + e.bz * s.vz) +
            e.Aps * (e.by * s.by + e.bz * s.bz);
   return o;
 }
@@ -167,8 +203,9 @@ __device__ __forceinline__ MPrim char_to_prim(const MPrim &p, const Chr &c, cons
   o.vz = e.bz * (e.qs * (a[0] - a[6]) + e.qf * (a[4] - a[2])) + e.by * (a[1] - a[5]);
   o.p  = p.d * cs2 * (e.af * (a[0] + a[6]) + e.as * (a[2] + a[4]));
   o.bx = 0.0;
-  o.by = e.by * (e.As * (a[0] + a[6]) - e.Af * (a[2] + a[4])) - e.bz * e.sign * sqrt(p.d) * (a[5] + a[1]);
-  o.bz = e.bz * (e.As * (a[0] + a[6]) - e.Af * (a[2] + a[4])) + e.by * e.sign * sqrt(p.d) * (a[5] + a[1]);
+  double const sd = msqrt(p.d);
+  o.by = e.by * (e.As * (a[0] + a[6]) - e.Af * (a[2] + a[4])) - e.bz * e.sign * sd * (a[5] + a[1]);
+  o.bz = e.bz * (e.As * (a[0] + a[6]) - e.Af * (a[2] + a[4])) + e.by * e.sign * sd * (a[5] + a[1]);
 #pragma unroll
   for (int s = 0; s < NS_MAX; s++) o.sc[s] = 0.0;
   return o;
@@ -187,7 +224,7 @@ __device__ __forceinline__ void write_data(const Box &b, const MPrim &s, double 
   Q[(long long)(b.fB() + 1) * n + id] = s.bz;
   double const bx = U[(long long)(b.fB() + (o1 - 1)) * n + id];
   // hydro_utilities.h:106-118 Calc_Energy_Primitive
-  double energy = (fmax(s.p, TINY) / (b.gamma - 1.)) + 0.5 * s.d * sqm(s.vx, s.vy, s.vz);
+  double energy = mdiv(mmax(s.p, TINY), b.gamma - 1.) + 0.5 * s.d * sqm(s.vx, s.vy, s.vz);
   energy += magE(bx, s.by, s.bz);
   Q[4 * n + id] = energy;
   for (int k = 0; k < b.ns; k++) Q[(long long)(5 + k) * n + id] = s.d * s.sc[k];
@@ -275,22 +312,23 @@ __global__ void k_ppmc(Box b, const double *__restrict__ U, double *QL, double *
     MPrim const cip1 = load_data(b, U, x + sx, y + sy, z + sz, o1, o2, o3);
     MPrim const cim2 = load_data(b, U, x - 2 * sx, y - 2 * sy, z - 2 * sz, o1, o2, o3);
     MPrim const cip2 = load_data(b, U, x + 2 * sx, y + 2 * sy, z + 2 * sz, o1, o2, o3);
-    double const cs  = sqrt(b.gamma * ci.p / ci.d);  // hydro_utilities.h:209 Calc_Sound_Speed
-    double const cs2 = cs * cs;
+    double const rd  = minv(ci.d);
+    double const cs  = msqrt(mdivr(b.gamma * ci.p, ci.d, rd));  // hydro_utilities.h:209 Calc_Sound_Speed
+    double const cs2 = cs * cs, rcs2 = minv(cs2);
     Eig const e      = eigenvectors(ci, cs, cs2, b.gamma);
-    Chr const ai = prim_to_char(ci, ci, e, cs2), aim1 = prim_to_char(ci, cim1, e, cs2),
-              aim2 = prim_to_char(ci, cim2, e, cs2), aip1 = prim_to_char(ci, cip1, e, cs2),
-              aip2 = prim_to_char(ci, cip2, e, cs2);
+    Chr const ai = prim_to_char(ci, ci, e, cs2, rd, rcs2), aim1 = prim_to_char(ci, cim1, e, cs2, rd, rcs2),
+              aim2 = prim_to_char(ci, cim2, e, cs2, rd, rcs2), aip1 = prim_to_char(ci, cip1, e, cs2, rd, rcs2),
+              aip2 = prim_to_char(ci, cip2, e, cs2, rd, rcs2);
     Chr aR, aL;
 #pragma unroll
     for (int k = 0; k < 7; k++) hx::ppm1(aim2.a[k], aim1.a[k], ai.a[k], aip1.a[k], aip2.a[k], aL.a[k], aR.a[k]);
     MPrim L = char_to_prim(ci, aL, e, cs2);
     MPrim R = char_to_prim(ci, aR, e, cs2);
     for (int s = 0; s < b.ns; s++) hx::ppm1(cim2.sc[s], cim1.sc[s], ci.sc[s], cip1.sc[s], cip2.sc[s], L.sc[s], R.sc[s]);
-    R.d = fmax(R.d, TINY);
-    L.d = fmax(L.d, TINY);
-    R.p = fmax(R.p, TINY);
-    L.p = fmax(L.p, TINY);
+    R.d = mmax(R.d, TINY);
+    L.d = mmax(L.d, TINY);
+    R.p = mmax(R.p, TINY);
+    L.p = mmax(L.p, TINY);
     write_data(b, L, QL, U, id, o1, o2, o3);
     write_data(b, R, QR, U, b.id(x - sx, y - sy, z - sz), o1, o2, o3);
   }
@@ -310,8 +348,9 @@ __global__ void k_plmc(Box b, const double *__restrict__ U, double *QL, double *
     MPrim const ci   = load_data(b, U, x, y, z, o1, o2, o3);
     MPrim const cimo = load_data(b, U, x - sx, y - sy, z - sz, o1, o2, o3);
     MPrim const cipo = load_data(b, U, x + sx, y + sy, z + sz, o1, o2, o3);
-    double const cs  = sqrt(b.gamma * ci.p / ci.d);
-    double const cs2 = cs * cs;
+    double const rd  = minv(ci.d);
+    double const cs  = msqrt(mdivr(b.gamma * ci.p, ci.d, rd));
+    double const cs2 = cs * cs, rcs2 = minv(cs2);
     Eig const e      = eigenvectors(ci, cs, cs2, b.gamma);
     // reconstruction.h:224-296 Compute_Slope / Van_Leer_Slope
     auto slope = [&](const MPrim &l, const MPrim &r, double coef) {
@@ -328,7 +367,7 @@ __global__ void k_plmc(Box b, const double *__restrict__ U, double *QL, double *
       for (int k = 0; k < NS_MAX; k++) s.sc[k] = k < b.ns ? coef * (r.sc[k] - l.sc[k]) : 0.0;
       return s;
     };
-    auto vl = [](double l, double r) -> double { return (l * r > 0.0) ? 2.0 * l * r / (l + r) : 0.0; };
+    auto vl = [](double l, double r) -> double { return mpos(l, r) ? mdiv(2.0 * l * r, l + r) : 0.0; };
     MPrim const dL = slope(cimo, ci, 1.0);
     MPrim const dR = slope(ci, cipo, 1.0);
     MPrim const dC = slope(cimo, cipo, 0.5);
@@ -343,14 +382,14 @@ __global__ void k_plmc(Box b, const double *__restrict__ U, double *QL, double *
     dG.bz = vl(dL.bz, dR.bz);
 #pragma unroll
     for (int k = 0; k < NS_MAX; k++) dG.sc[k] = k < b.ns ? vl(dL.sc[k], dR.sc[k]) : 0.0;
-    Chr const aL = prim_to_char(ci, dL, e, cs2), aR = prim_to_char(ci, dR, e, cs2), aC = prim_to_char(ci, dC, e, cs2),
-              aG = prim_to_char(ci, dG, e, cs2);
+    Chr const aL = prim_to_char(ci, dL, e, cs2, rd, rcs2), aR = prim_to_char(ci, dR, e, cs2, rd, rcs2),
+              aC = prim_to_char(ci, dC, e, cs2, rd, rcs2), aG = prim_to_char(ci, dG, e, cs2, rd, rcs2);
     // reconstruction.h:512-559 Monotonize_Characteristic_Return_Primitive
     auto mono = [](double l, double r, double cc, double vg) -> double {
-      if (l * r > 0.0) {
-        double const la = 2.0 * fmin(fabs(l), fabs(r));
-        double const lb = fmin(fabs(cc), fabs(vg));
-        return copysign(fmin(la, lb), cc);
+      if (mpos(l, r)) {
+        double const la = 2.0 * mmin(fabs(l), fabs(r));
+        double const lb = mmin(fabs(cc), fabs(vg));
+        return copysign(mmin(la, lb), cc);
       }
       return 0.0;
     };
@@ -380,10 +419,10 @@ __global__ void k_plmc(Box b, const double *__restrict__ U, double *QL, double *
     MPrim R = lin(-1.0);
     // reconstruction.h:686-723 Plm_Limit_Interfaces
     auto lim = [](double &l, double &r, double vm, double vi, double vp) {
-      r = fmax(fmin(vi, vm), r);
-      r = fmin(fmax(vi, vm), r);
-      l = fmax(fmin(vi, vp), l);
-      l = fmin(fmax(vi, vp), l);
+      r = mmax(mmin(vi, vm), r);
+      r = mmin(mmax(vi, vm), r);
+      l = mmax(mmin(vi, vp), l);
+      l = mmin(mmax(vi, vp), l);
     };
     lim(L.d, R.d, cimo.d, ci.d, cipo.d);
     lim(L.vx, R.vx, cimo.vx, ci.vx, cipo.vx);
@@ -395,10 +434,10 @@ __global__ void k_plmc(Box b, const double *__restrict__ U, double *QL, double *
 #pragma unroll
     for (int k = 0; k < NS_MAX; k++)
       if (k < b.ns) lim(L.sc[k], R.sc[k], cimo.sc[k], ci.sc[k], cipo.sc[k]);
-    R.d = fmax(R.d, TINY);
-    L.d = fmax(L.d, TINY);
-    R.p = fmax(R.p, TINY);
-    L.p = fmax(L.p, TINY);
+    R.d = mmax(R.d, TINY);
+    L.d = mmax(L.d, TINY);
+    R.p = mmax(R.p, TINY);
+    L.p = mmax(L.p, TINY);
     write_data(b, L, QL, U, id, o1, o2, o3);
     write_data(b, R, QR, U, b.id(x - sx, y - sy, z - sz), o1, o2, o3);
   }
@@ -427,21 +466,22 @@ __device__ __forceinline__ HState hlld_load(const Box &b, const double *Q, doubl
   long long const n = b.n;
   HState s;
   s.d  = Q[t];
-  s.d  = fmax(s.d, TINY);
-  s.vx = Q[t + n * o1] / s.d;
-  s.vy = Q[t + n * o2] / s.d;
-  s.vz = Q[t + n * o3] / s.d;
+  s.d  = mmax(s.d, TINY);
+  double const rd = minv(s.d);
+  s.vx = mdivr(Q[t + n * o1], s.d, rd);
+  s.vy = mdivr(Q[t + n * o2], s.d, rd);
+  s.vz = mdivr(Q[t + n * o3], s.d, rd);
   s.E  = Q[t + n * 4];
-  s.E  = fmax(s.E, TINY);
+  s.E  = mmax(s.E, TINY);
   s.by = Q[t + n * b.fB()];
   s.bz = Q[t + n * (b.fB() + 1)];
 #pragma unroll
-  for (int k = 0; k < NS_MAX; k++) s.sc[k] = k < b.ns ? Q[t + n * (5 + k)] / s.d : 0.0;
+  for (int k = 0; k < NS_MAX; k++) s.sc[k] = k < b.ns ? mdivr(Q[t + n * (5 + k)], s.d, rd) : 0.0;
   double pressure = s.E - 0.5 * s.d * sqm(s.vx, s.vy, s.vz);
   pressure -= magE(bx, s.by, s.bz);
-  s.p = fmax((b.gamma - 1.) * pressure, TINY);
+  s.p = mmax((b.gamma - 1.) * pressure, TINY);
   double const pt = s.p + magE(bx, s.by, s.bz);  // mhd_utilities.h computeTotalPressure
-  s.pt            = fmax(pt, TINY);
+  s.pt            = mmax(pt, TINY);
   return s;
 }
 __device__ __forceinline__ HFlux hlld_nonstar(const HState &s, double bx)
@@ -459,7 +499,8 @@ __device__ __forceinline__ HFlux hlld_nonstar(const HState &s, double bx)
 __device__ __forceinline__ HStar hlld_star(const HState &s, double SM, double S, double bx, double ptStar)
 {
   HStar st;
-  st.d = s.d * (S - s.vx) / (S - SM);
+  double const rsm = minv(S - SM);
+  st.d = mdivr(s.d * (S - s.vx), S - SM, rsm);
   if (fabs(s.d * (S - s.vx) * (S - SM) - (bx * bx)) < ptStar * HLLD_SMALL) {
     st.vy = s.vy;
     st.vz = s.vz;
@@ -467,18 +508,19 @@ __device__ __forceinline__ HStar hlld_star(const HState &s, double SM, double S,
     st.bz = s.bz;
   } else {
     double const denom = s.d * (S - s.vx) * (S - SM) - (bx * bx);
-    double coef        = bx * (SM - s.vx) / denom;
+    double const rden  = minv(denom);
+    double coef        = mdivr(bx * (SM - s.vx), denom, rden);
     st.vy              = s.vy - s.by * coef;
     st.vz              = s.vz - s.bz * coef;
     double tp          = (S - s.vx);
     tp                 = tp * tp;
-    coef               = (s.d * tp - (bx * bx)) / denom;
+    coef               = mdivr(s.d * tp - (bx * bx), denom, rden);
     st.by              = s.by * coef;
     st.bz              = s.bz * coef;
   }
-  st.E = (s.E * (S - s.vx) - s.pt * s.vx + ptStar * SM +
-          bx * (dot3(s.vx, s.vy, s.vz, bx, s.by, s.bz) - dot3(SM, st.vy, st.vz, bx, st.by, st.bz))) /
-         (S - SM);
+  st.E = mdivr(s.E * (S - s.vx) - s.pt * s.vx + ptStar * SM +
+                   bx * (dot3(s.vx, s.vy, s.vz, bx, s.by, s.bz) - dot3(SM, st.vy, st.vz, bx, st.by, st.bz)),
+               S - SM, rsm);
   return st;
 }
 __device__ __forceinline__ HFlux hlld_starflux(const HStar &st, const HState &s, const HFlux &f, double SM, double S)
@@ -504,8 +546,8 @@ __device__ __forceinline__ HDStar hlld_dstar(const HStar &L, const HStar &R, dou
       o.vy = R.vy, o.vz = R.vz, o.by = R.by, o.bz = R.bz, o.ER = R.E;
     }
   } else {
-    double const sqrtDL = sqrt(L.d), sqrtDR = sqrt(R.d);
-    double const inv    = 1.0 / (sqrtDL + sqrtDR);
+    double const sqrtDL = msqrt(L.d), sqrtDR = msqrt(R.d);
+    double const inv    = mdiv(1.0, sqrtDL + sqrtDR);
     double const sgnb   = copysign(1.0, bx);
     o.vy = inv * (sqrtDL * L.vy + sqrtDR * R.vy + sgnb * (R.by - L.by));
     o.vz = inv * (sqrtDL * L.vz + sqrtDR * R.vz + sgnb * (R.bz - L.bz));
@@ -555,9 +597,9 @@ __global__ void k_hlld(Box b, const double *__restrict__ QL, const double *__res
     };
     double const cL = cfast(sL.d, sL.p, bx, sL.by, sL.bz, b.gamma);
     double const cR = cfast(sR.d, sR.p, bx, sR.by, sR.bz, b.gamma);
-    double const cmax = fmax(cL, cR);
-    double const SL = fmin(sL.vx, sR.vx) - cmax;
-    double const SR = fmax(sL.vx, sR.vx) + cmax;
+    double const cmax = mmax(cL, cR);
+    double const SL = mmin(sL.vx, sR.vx) - cmax;
+    double const SR = mmax(sL.vx, sR.vx) + cmax;
     HFlux const fL = hlld_nonstar(sL, bx);
     if (SL > 0.0) {
       ret(fL, sL);
@@ -571,19 +613,19 @@ __global__ void k_hlld(Box b, const double *__restrict__ QL, const double *__res
     double SM;
     {
       double const rd = SR - sR.vx, ld = SL - sL.vx;
-      SM = (rd * sR.d * sR.vx - ld * sL.d * sL.vx - sR.pt + sL.pt) / (rd * sR.d - ld * sL.d);
+      SM = mdiv(rd * sR.d * sR.vx - ld * sL.d * sL.vx - sR.pt + sL.pt, rd * sR.d - ld * sL.d);
     }
-    double const ptStar = (sR.d * sL.pt * (SR - sR.vx) - sL.d * sR.pt * (SL - sL.vx) +
-                           sL.d * sR.d * (SR - sR.vx) * (SL - sL.vx) * (sR.vx - sL.vx)) /
-                          (sR.d * (SR - sR.vx) - sL.d * (SL - sL.vx));
+    double const ptStar = mdiv(sR.d * sL.pt * (SR - sR.vx) - sL.d * sR.pt * (SL - sL.vx) +
+                                   sL.d * sR.d * (SR - sR.vx) * (SL - sL.vx) * (sR.vx - sL.vx),
+                               sR.d * (SR - sR.vx) - sL.d * (SL - sL.vx));
     HStar const stL = hlld_star(sL, SM, SL, bx, ptStar);
-    double const SLStar = SM + -1 * (fabs(bx) / sqrt(fmax(stL.d, TINY)));
+    double const SLStar = SM + -1 * mdiv(fabs(bx), msqrt(mmax(stL.d, TINY)));
     if (SLStar > 0.0 and SL <= 0.0) {
       ret(hlld_starflux(stL, sL, fL, SM, SL), sL);
       continue;
     }
     HStar const stR = hlld_star(sR, SM, SR, bx, ptStar);
-    double const SRStar = SM + 1 * (fabs(bx) / sqrt(fmax(stR.d, TINY)));
+    double const SRStar = SM + 1 * mdiv(fabs(bx), msqrt(mmax(stR.d, TINY)));
     if (SRStar <= 0.0 and SR >= 0.0) {
       ret(hlld_starflux(stR, sR, fR, SM, SR), sR);
       continue;

@@ -3,4 +3,5 @@
 #define CGB_MHD_NS mx
 #define CGB_MHD_STEP mhd_exact_step
 #define CGB_MHD_REDUCTIONS 1
+#define CGB_MHD_FAST 0
 #include "mhd_body.cuh"
