@@ -44,6 +44,8 @@ __device__ __forceinline__ double mrsqrt(double x) { return hf::rcp(hf::sqrtT(x)
 __device__ __forceinline__ double mmin(double a, double b) { return hf::min_ord(a, b); }
 __device__ __forceinline__ double mmax(double a, double b) { return hf::max_ord(a, b); }
 __device__ __forceinline__ bool mpos(double l, double r) { return hf::prod_pos(l, r); }  // l * r > 0
+__device__ __forceinline__ bool mgt0(double x) { return hf::is_pos(x); }                  // x > 0
+__device__ __forceinline__ bool mlt0(double x) { return hf::is_neg(x); }                  // x < 0
 #else
 __device__ __forceinline__ double mdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ double minv(double) { return 0.0; }  // unused by mdivr
@@ -53,6 +55,8 @@ __device__ __forceinline__ double mrsqrt(double x) { return rsqrt(x); }
 __device__ __forceinline__ double mmin(double a, double b) { return fmin(a, b); }
 __device__ __forceinline__ double mmax(double a, double b) { return fmax(a, b); }
 __device__ __forceinline__ bool mpos(double l, double r) { return l * r > 0.0; }
+__device__ __forceinline__ bool mgt0(double x) { return x > 0.0; }
+__device__ __forceinline__ bool mlt0(double x) { return x < 0.0; }
 #endif
 
 __device__ __forceinline__ double dot3(double a1, double a2, double a3, double b1, double b2, double b3)
@@ -601,12 +605,12 @@ __global__ void k_hlld(Box b, const double *__restrict__ QL, const double *__res
     double const SL = mmin(sL.vx, sR.vx) - cmax;
     double const SR = mmax(sL.vx, sR.vx) + cmax;
     HFlux const fL = hlld_nonstar(sL, bx);
-    if (SL > 0.0) {
+    if (mgt0(SL)) {
       ret(fL, sL);
       continue;
     }
     HFlux const fR = hlld_nonstar(sR, bx);
-    if (SR < 0.0) {
+    if (mlt0(SR)) {
       ret(fR, sR);
       continue;
     }
@@ -666,7 +670,7 @@ __device__ __forceinline__ double ct_slope(const Box &b, const double *flux, con
   double const M3      = U[ic + (long long)(m2 + 1) * n];
   double const B2c     = 0.5 * (U[ic + (long long)(m1 + fB) * n] + U[iB2 + (long long)(m1 + fB) * n]);
   double const B3c     = 0.5 * (U[ic + (long long)(m2 + fB) * n] + U[iB3 + (long long)(m2 + fB) * n]);
-  double const ec      = (M3 * B2c - M2 * B3c) / density;
+  double const ec      = mdiv(M3 * B2c - M2 * B3c, density);
   double const ef      = fluxSign * flux[iflux + (long long)(int(fluxSign == 1) + fB) * n];
   return ef - ec;
 }
@@ -688,8 +692,8 @@ __global__ void k_ct(Box b, const double *__restrict__ Fx, const double *__restr
       return ct_slope(b, fl, U, sg, cd, a, c, cc, d, x, y, z);
     };
     auto pick = [](double sgnUp, double pos, double neg) {
-      if (sgnUp > 0.0) return pos;
-      if (sgnUp < 0.0) return neg;
+      if (mgt0(sgnUp)) return pos;
+      if (mlt0(sgnUp)) return neg;
       return 0.5 * (pos + neg);
     };
     double syp, syn, szp, szn, sxp, sxn, fyp, fyn, fzp, fzn, fxp, fxn;
