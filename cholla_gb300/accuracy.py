@@ -68,8 +68,9 @@ def run(torch, n: int = 64, steps: int = 10, seed: int = 0, forms=("mixed", "fp6
            "baseline": "exact FP64 form (bit-identical to the reference build)", "t_end": float(sum(dts)),
            "seconds": {"fp64": t_exact}, "rel_l1": {}, "conservation": {}}
     mom_scale = ref[1:4].abs().sum()  # momenta drift relative to the total absolute momentum
+    drift_m = (U[real][1:4].sum(dim=(1, 2, 3)) - sums0[1:4]).abs().max() / mom_scale
     res["conservation"]["fp64"] = {"mass": float(((U[real][0].sum() - sums0[0]) / sums0[0]).abs()),
-                                   "momentum": float((U[real][1:4].sum(dim=(1, 2, 3)) - sums0[1:4]).abs().max() / mom_scale)}
+                                   "momentum": float(drift_m)}
     del U
     for form in forms:
         Uf = host.to("cuda")
@@ -79,8 +80,9 @@ def run(torch, n: int = 64, steps: int = 10, seed: int = 0, forms=("mixed", "fp6
         cur = Uf[real]
         err = (cur - ref).abs().sum(dim=(1, 2, 3)) / denom
         res["rel_l1"][form] = {FIELDS[i]: float(err[i]) for i in range(cur.shape[0])}
+        drift_m = (cur[1:4].sum(dim=(1, 2, 3)) - sums0[1:4]).abs().max() / mom_scale
         res["conservation"][form] = {"mass": float(((cur[0].sum() - sums0[0]) / sums0[0]).abs()),
-                                     "momentum": float((cur[1:4].sum(dim=(1, 2, 3)) - sums0[1:4]).abs().max() / mom_scale)}
+                                     "momentum": float(drift_m)}
         del Uf, cur
     return res
 

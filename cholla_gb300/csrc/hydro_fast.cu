@@ -966,7 +966,7 @@ cudaError_t launch_batch_sweep(const BatchChunk &C, int recon, int solver, int n
 
 // primitives, predictor, x/y/z sweeps, negative-density repair and finalize of one chunk
 template <typename T>
-cudaError_t launch_core(const BatchChunk &C, int recon, int solver, int nsl, int de, double U_floor, int temp_floor,
+cudaError_t launch_core(const BatchChunk &C, int recon, int solver, int nsl, double U_floor, int temp_floor,
                         cudaStream_t s)
 {
   cudaError_t e;
@@ -987,7 +987,6 @@ cudaError_t launch_core(const BatchChunk &C, int recon, int solver, int nsl, int
   kb_negavg<<<C.total[BK_REAL], 256, 0, s>>>(C);
   constexpr bool MIX = std::is_same<T, float>::value;
   kb_final<MIX><<<C.total[BK_REAL], 256, 0, s>>>(C, U_floor, temp_floor, 1);
-  (void)de;
   return cudaGetLastError();
 }
 
@@ -1019,19 +1018,18 @@ cudaError_t batch_chunk_step(const BatchChunk &C, int recon, int solver, int mix
   kb_cfl<<<1, BATCH_CHUNK, 0, s>>>(C, c_cfl);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return mixed ? launch_core<float>(C, recon, solver, nsl, de, U_floor, temp_floor, s)
-               : launch_core<double>(C, recon, solver, nsl, de, U_floor, temp_floor, s);
+  return mixed ? launch_core<float>(C, recon, solver, nsl, U_floor, temp_floor, s)
+               : launch_core<double>(C, recon, solver, nsl, U_floor, temp_floor, s);
 }
 
 
 // bytes of W scratch the fast paths need: primitives of Uⁿ and of U½ (8 bytes covers both types)
 size_t fast_scratch_bytes(const Box &b) { return 2 * (size_t)nslot(b) * (size_t)b.n * sizeof(double); }
 
-cudaError_t hydro_fast_step(const Box &box, int recon, int solver, int mixed, double *U, const Scratch &sc, void *W,
-                            double dt, const double *dt_dev, double U_floor, int temp_floor, int do_dt,
-                            cudaStream_t s, cudaEvent_t *marks)
+cudaError_t hydro_fast_step(const Box &box, int recon, int solver, int mixed, double *U, const Scratch &sc, double dt,
+                            const double *dt_dev, double U_floor, int temp_floor, int do_dt, cudaStream_t s,
+                            cudaEvent_t *marks)
 {
-  (void)W;
   Box const b = with_inverses(box);
   bool const one_d = (b.ny == 1 && b.nz == 1);
   cudaError_t e;

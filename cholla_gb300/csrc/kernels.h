@@ -19,9 +19,9 @@ cudaError_t hydro_exact_step(const Box &b, int recon, int solver, double *U, con
 cudaError_t cfl_dt(const unsigned long long *dti, double *dt_t, double c_cfl, double t_end, cudaStream_t s);
 // Fast FP64 (mixed = 0) or mixed-precision (mixed = 1) step (hydro_fast.cu).  sc.W holds the
 // primitives of Uⁿ and of U½: 2 * (nf + 1) fields of 8 bytes cover both element types.
-cudaError_t hydro_fast_step(const Box &b, int recon, int solver, int mixed, double *U, const Scratch &sc, void *W,
-                            double dt, const double *dt_dev, double U_floor, int temp_floor, int do_dt,
-                            cudaStream_t s, cudaEvent_t *marks = nullptr);
+cudaError_t hydro_fast_step(const Box &b, int recon, int solver, int mixed, double *U, const Scratch &sc, double dt,
+                            const double *dt_dev, double U_floor, int temp_floor, int do_dt, cudaStream_t s,
+                            cudaEvent_t *marks = nullptr);
 // Average_Cell_Single_Field of the density for real cells left with negative density
 cudaError_t negative_density_average(const Box &b, double *U, cudaStream_t s);
 cudaError_t hydro_calc_dt(const Box &b, const double *U, unsigned long long *dti, cudaStream_t s);
@@ -91,7 +91,7 @@ inline cudaError_t hydro_step(const Box &b, int recon, int solver, int precision
 {
   if (precision == 0)
     return hydro_exact_step(b, recon, solver, U, sc, dt, dt_dev, U_floor, temp_floor, do_dt, s, marks);
-  return hydro_fast_step(b, recon, solver, precision == 1 ? 1 : 0, U, sc, sc.W, dt, dt_dev, U_floor, temp_floor,
+  return hydro_fast_step(b, recon, solver, precision == 1 ? 1 : 0, U, sc, dt, dt_dev, U_floor, temp_floor,
                          do_dt, s, marks);
 }
 

@@ -7,17 +7,18 @@ fixed number of steps at CFL 0.3.  Requests arrive over time (a seeded Poisson s
 
 `BatchedServer` keeps one cgb_batch: requests that have arrived are admitted whenever the
 device memory budget and the job table have room, their state stays resident, and every
-iteration advances the running jobs by one step in one replay of the batch graph; a job that
-has done its steps leaves the batch and the next arrival takes its place (continuous
-batching).  Which admitted jobs run is the scheduler's choice: "fcfs" (default) runs them in
-arrival order until the step holds `saturation_cells` cells, enough to fill the GPU, and holds
-the rest (first come, first served keeps the longest wait, and so the tail latency, lowest;
-the cap keeps the GPU full); "all" steps every admitted job (processor sharing).  The batch's
-schedule (chains, solo threshold) is picked by the autotuner (`tune.py`) on the workload's
-size mix when the server starts.  `PerRequestServer` is the baseline: the same admission, but every job is advanced
-by its own launches of the single-box step (one box engine per job, each on its own stream),
-either launched kernel by kernel every step ("per_request") or replayed from a CUDA graph of
-its own ("per_request_graph").
+iteration advances the running jobs by one batch step; a job that has done its steps leaves
+the batch and the next arrival takes its place (continuous batching).  Which admitted jobs run
+is the scheduler's choice: "fcfs" (default) runs them in arrival order until the step holds
+`saturation_cells` cells, enough to fill the GPU, and holds the rest (first come, first served
+keeps the longest wait, and so the tail latency, lowest; the cap keeps the GPU full); "all"
+steps every admitted job (processor sharing).  The batch's schedule (chains, solo threshold)
+is picked by the autotuner (`tune.py`) on the workload's size mix when the server starts.
+
+`PerRequestServer` is the baseline: the same admission, but every job is advanced by its own
+launches of the single-box step (one box engine per job, each on its own stream), either
+kernel by kernel every step ("per_request") or replayed from a CUDA graph of its own
+("per_request_graph").
 
 Latency of a request = time from its arrival to the completion on the GPU of its last step
 (observed from the host by polling that step's event).  Throughput = cell updates of all
