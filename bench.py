@@ -464,8 +464,8 @@ def run_serving(args, torch):
     modes = serve.MODES
     out = {"workload": "Poisson stream of 3D hydro jobs, n in {32,48,64,96,128}, blast or Sod tube, "
                        f"PPMC + HLLC mixed, 100 steps, {args.serve_count} requests per rate",
-           "batched_server": "first come first served up to 3 Mi cells per step (rest held), 2 chains, "
-                             "jobs of >= 2 Mi padded cells solo",
+           "batched_server": "first come first served up to 3 Mi cells per step (rest held); batch schedule "
+                             "(chains, solo threshold) autotuned on the size mix at start-up (see each row's 'tuned')",
            "rates": {}}
     for mode in modes:  # module loading, first captures and allocator growth outside the timed runs
         serve.serve(torch, serve.make_requests(rate=2000.0, count=6, seed=99, steps=5), mode=mode)
