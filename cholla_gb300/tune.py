@@ -8,6 +8,8 @@ GPU.  `tune_batch` builds a representative batch of the given sizes (seeded blas
 tube states), times a few steps of every candidate with CUDA events on the batch stream, and
 returns the fastest.  Results are cached per (sizes, scheme) in memory and, when a path is
 given, in a JSON file, so a server tunes once per size mix.
+
+    python -m cholla_gb300.tune --sizes 32,48,64,96,128 --repeat 2 [--precision mixed] [--cache f.json]
 """
 from __future__ import annotations
 
@@ -71,3 +73,26 @@ def tune_batch(torch, scheme, sizes, steps: int = 6, warmup: int = 2, cache_path
         stored[key] = out
         path.write_text(json.dumps(stored, indent=1))
     return out
+
+
+def main():
+    import argparse
+
+    import torch
+
+    from .serve import default_scheme
+
+    ap = argparse.ArgumentParser(description="time the batch schedules on a size mix and print the table")
+    ap.add_argument("--sizes", default="32,48,64,96,128", help="real cells per side of the jobs")
+    ap.add_argument("--repeat", type=int, default=2, help="jobs per size")
+    ap.add_argument("--precision", choices=["mixed", "fp64_fast"], default="mixed")
+    ap.add_argument("--cache", default=None, help="JSON file to read and extend")
+    a = ap.parse_args()
+    scheme = default_scheme()
+    scheme.precision = a.precision
+    sizes = [int(x) for x in a.sizes.split(",") if x] * a.repeat
+    print(json.dumps(tune_batch(torch, scheme, sizes, cache_path=a.cache), indent=1))
+
+
+if __name__ == "__main__":
+    main()
