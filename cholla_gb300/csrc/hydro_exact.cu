@@ -250,8 +250,10 @@ struct CorrSizes {
   static constexpr int PER_Q = PM + (RECON == RECON_PCM ? 0 : 2 * RM) + FM;
 };
 
+// Two resident blocks per SM (128 registers, some spilled to L1) instead of the one that 164
+// registers allow: 256^3 corrector 274 -> 241 ms; three blocks spill more and lose (249 ms).
 template <int TX, int TY, int TZ, int RECON, int SOLVER>
-__global__ void __launch_bounds__(TX *TY *TZ) k_corrector(Box b, const double *__restrict__ Uh, double *__restrict__ U,
+__global__ void __launch_bounds__(TX *TY *TZ, 2) k_corrector(Box b, const double *__restrict__ Uh, double *__restrict__ U,
                                                           const double *__restrict__ GEp, double *__restrict__ Epre,
                                                           int *__restrict__ status, double dt,
                                                           const double *__restrict__ dtp)
