@@ -650,6 +650,269 @@ __global__ void k_temperature_floor(Box b, double *__restrict__ U, double U_floo
   }
 }
 
+// ------------------------------------------------------------------------------------------
+// The exact corrector as one sweep per direction over long pencils (x: 64 x 2 x 2 cells per
+// block, y and z: 32 x 8 x 1), for boxes whose scratch has room for an FP64 accumulator: the
+// fused 8 x 8 x 4 tile recomputes a third of its interface states in halos, these about 6%.
+// Every operation and its order are the fused corrector's: primitives from U½ (Load_Data),
+// PPMC / PLMC, the Riemann solver, d = dtod * (F(a-1/2) - F(a+1/2)); the x sweep stores d, the
+// y sweep adds its own (acc + d), the z sweep adds its own and writes U + acc with the floor
+// and the pre-sync energy, exactly as the fused kernel's register accumulator does.
+// ------------------------------------------------------------------------------------------
+template <int DIR, int L, int WA, int WB, int RECON>
+struct XSweep {
+  static constexpr int H  = Halo<RECON>::H;
+  static constexpr int CS = WA * WB;
+  static constexpr int NT = L * CS;
+  static constexpr int LA = L + 2 * H, LR = L + 2, LF = L + 1;
+  static constexpr int NP = LA * CS, NR = LR * CS, NF = LF * CS;
+  // the pencil (primitives, or conserved for PCM), QL, QR; the fluxes reuse the pencil once it
+  // is consumed (PCM: they follow it)
+  static constexpr int PER_Q  = RECON == RECON_PCM ? NP + NF : NP + 2 * NR;
+  static constexpr int STRIDE = DIR == 0 ? 1 : CS;
+  // position a of pencil c in an array of row length len: x sweeps keep a fastest, y and z
+  // sweeps the pencil index (x), so that neighbouring threads touch neighbouring x
+  __device__ static int at(int a, int c, int len) { return DIR == 0 ? a + len * c : c + CS * a; }
+  __device__ static void split(int i, int len, int &a, int &c)
+  {
+    if (DIR == 0) {
+      a = i % len, c = i / len;
+    } else {
+      c = i % CS, a = i / CS;
+    }
+  }
+};
+
+template <int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
+__global__ void __launch_bounds__(L *WA *WB, 2)
+    k_xsweep(Box b, const double *__restrict__ Uh, double *__restrict__ A, double *__restrict__ U,
+             const double *__restrict__ GEp, double *__restrict__ Epre, int *__restrict__ status, double dt,
+             const double *__restrict__ dtp)
+{
+  if (dtp) dt = *dtp;
+  using S            = XSweep<DIR, L, WA, WB, RECON>;
+  constexpr int H    = S::H;
+  constexpr int NT   = S::NT;
+  constexpr int ST   = S::STRIDE;
+  extern __shared__ double smem[];
+  int const nq = b.nq();
+  double *Ps   = smem;
+  double *QLs  = Ps + nq * S::NP;
+  double *QRs  = QLs + nq * S::NR;
+  double *Fs   = (RECON == RECON_PCM) ? QLs : Ps;
+  int o1, o2, o3;
+  rot(DIR, o1, o2, o3);
+  int const ng      = b.ng;
+  long long const n = b.n;
+  int const a0 = blockIdx.x * L, ca0 = blockIdx.y * WA, cb0 = blockIdx.z * WB;
+  int const rx = b.nx - 2 * ng, ry = b.ny - 2 * ng, rz = b.nz - 2 * ng;
+  // partial tiles skip the interface states and fluxes no real cell needs
+  int const lim  = (DIR == 0 ? rx : DIR == 1 ? ry : rz) - a0;
+  auto pencil_in = [&](int c) { return ca0 + c % WA < (DIR == 0 ? ry : rx) && cb0 + c / WA < (DIR == 2 ? ry : rz); };
+  auto cell      = [&](int a, int c, int &gx, int &gy, int &gz) {
+    int const ca = ca0 + c % WA + ng, cb = cb0 + c / WA + ng, g = a0 + a + ng;
+    if (DIR == 0) {
+      gx = g, gy = ca, gz = cb;
+    } else if (DIR == 1) {
+      gy = g, gx = ca, gz = cb;
+    } else {
+      gz = g, gx = ca, gy = cb;
+    }
+  };
+  int const t = threadIdx.x;
+  // 1. pencils of U½ -> primitives (Load_Data); positions past the box read the nearest cell
+  //    the predictor wrote (1 .. n-2) and feed only skipped interfaces
+  for (int p = t; p < S::NP; p += NT) {
+    int a, c, gx, gy, gz;
+    S::split(p, S::LA, a, c);
+    cell(a - H, c, gx, gy, gz);
+    long long const gid = b.id(clampi(gx, 1, b.nx - 2), clampi(gy, 1, b.ny - 2), clampi(gz, 1, b.nz - 2));
+    double q[NQ_MAX];
+#pragma unroll
+    for (int qq = 0; qq < NQ_MAX; qq++) {
+      if (qq < nq) {
+        int const src = (qq == 1) ? o1 : (qq == 2) ? o2 : (qq == 3) ? o3 : field_of_q(qq, b);
+        q[qq]         = Uh[(long long)src * n + gid];
+      }
+    }
+    if (RECON == RECON_PCM) {
+#pragma unroll
+      for (int qq = 0; qq < NQ_MAX; qq++)
+        if (qq < nq) Ps[qq * S::NP + p] = q[qq];
+    } else {
+      hx::Prim const P = hx::load_prim(q, b.ns, b.de, b.gamma);
+      Ps[0 * S::NP + p] = P.d;
+      Ps[1 * S::NP + p] = P.vn;
+      Ps[2 * S::NP + p] = P.vt1;
+      Ps[3 * S::NP + p] = P.vt2;
+      Ps[4 * S::NP + p] = P.p;
+#pragma unroll
+      for (int k = 0; k < NS_MAX; k++)
+        if (k < b.ns) Ps[(5 + k) * S::NP + p] = P.sc[k];
+      if (b.de) Ps[(5 + b.ns) * S::NP + p] = P.ge;
+    }
+  }
+  __syncthreads();
+  // 2. reconstruction: recon position a holds cell a - 1 (QL at its right face, QR at its left)
+  if (RECON != RECON_PCM) {
+    for (int r = t; r < S::NR; r += NT) {
+      int a, c;
+      S::split(r, S::LR, a, c);
+      if (a > lim + 1 || !pencil_in(c)) continue;
+      int const base = S::at(a - 1 + H, c, S::LA);
+      auto prim_at   = [&](int off) {
+        hx::Prim P;
+        int const pi = base + off * ST;
+        P.d          = Ps[0 * S::NP + pi];
+        P.vn         = Ps[1 * S::NP + pi];
+        P.vt1        = Ps[2 * S::NP + pi];
+        P.vt2        = Ps[3 * S::NP + pi];
+        P.p          = Ps[4 * S::NP + pi];
+#pragma unroll
+        for (int k = 0; k < NS_MAX; k++) P.sc[k] = (k < b.ns) ? Ps[(5 + k) * S::NP + pi] : 0.0;
+        P.ge = b.de ? Ps[(5 + b.ns) * S::NP + pi] : 0.0;
+        return P;
+      };
+      hx::Prim Lp, Rp;
+      if (RECON == RECON_PPMC) {
+        hx::ppmc_cell(prim_at(-2), prim_at(-1), prim_at(0), prim_at(1), prim_at(2), b.ns, b.de, b.gamma, Lp, Rp);
+      } else {
+        hx::plmc_cell(prim_at(-1), prim_at(0), prim_at(1), b.ns, b.de, b.gamma, Lp, Rp);
+      }
+      double qLv[NQ_MAX], qRv[NQ_MAX];
+      hx::prim_to_q(Lp, qLv, b.ns, b.de, b.gamma);
+      hx::prim_to_q(Rp, qRv, b.ns, b.de, b.gamma);
+#pragma unroll
+      for (int qq = 0; qq < NQ_MAX; qq++) {
+        if (qq < nq) {
+          QLs[qq * S::NR + r] = qLv[qq];
+          QRs[qq * S::NR + r] = qRv[qq];
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // 3. Riemann problems: face a lies between cells a - 1 and a
+  for (int f = t; f < S::NF; f += NT) {
+    int a, c;
+    S::split(f, S::LF, a, c);
+    if (a > lim || !pencil_in(c)) continue;
+    double qL[NQ_MAX], qR[NQ_MAX], fl[NQ_MAX];
+    if (RECON == RECON_PCM) {
+      int const pl = S::at(a - 1 + H, c, S::LA), pr = pl + ST;
+#pragma unroll
+      for (int qq = 0; qq < NQ_MAX; qq++) {
+        if (qq < nq) {
+          qL[qq] = Ps[qq * S::NP + pl];
+          qR[qq] = Ps[qq * S::NP + pr];
+        }
+      }
+    } else {
+      int const rl = S::at(a, c, S::LR), rr = rl + ST;
+#pragma unroll
+      for (int qq = 0; qq < NQ_MAX; qq++) {
+        if (qq < nq) {
+          qL[qq] = QLs[qq * S::NR + rl];
+          qR[qq] = QRs[qq * S::NR + rr];
+        }
+      }
+    }
+    if (SOLVER == SOLVER_ROE) {
+      hx::roe(qL, qR, fl, b.ns, b.de, b.gamma);
+    } else {
+      hx::hllc(qL, qR, fl, b.ns, b.de, b.gamma);
+    }
+#pragma unroll
+    for (int qq = 0; qq < NQ_MAX; qq++)
+      if (qq < nq) Fs[qq * S::NF + f] = fl[qq];
+  }
+  __syncthreads();
+  // 4. this thread's cell: the flux difference of the sweep added to the accumulator
+  int a, c, gx, gy, gz;
+  S::split(t, L, a, c);
+  cell(a, c, gx, gy, gz);
+  if (!(gx < b.nx - ng && gy < b.ny - ng && gz < b.nz - ng)) return;
+  long long const gid = b.id(gx, gy, gz);
+  int const fm        = S::at(a, c, S::LF);
+  double const dtod   = dt / (DIR == 0 ? b.dx : DIR == 1 ? b.dy : b.dz);
+  double acc[NQ_MAX];
+#pragma unroll
+  for (int qq = 0; qq < NQ_MAX; qq++) acc[qq] = 0.0;
+#pragma unroll
+  for (int qq = 0; qq < NQ_MAX; qq++) {
+    if (qq < nq) {
+      int const dst  = (qq == 1) ? o1 : (qq == 2) ? o2 : (qq == 3) ? o3 : qq;
+      double const d = dtod * (Fs[qq * S::NF + fm] - Fs[qq * S::NF + fm + ST]);
+#pragma unroll
+      for (int cc = 0; cc < NQ_MAX; cc++)
+        if (cc == dst) acc[cc] = FIRST ? d : A[(long long)cc * n + gid] + d;
+    }
+  }
+  if constexpr (!FINAL) {
+#pragma unroll
+    for (int qq = 0; qq < NQ_MAX; qq++)
+      if (qq < nq) A[(long long)qq * n + gid] = acc[qq];
+    return;
+  }
+  // conserved update of real cells (hydro_cuda.cu:172-402), in place, as in k_corrector
+  double v[NQ_MAX];
+#pragma unroll
+  for (int qq = 0; qq < NQ_MAX; qq++) {
+    if (qq < nq) {
+      int const f     = field_of_q(qq, b);
+      double const u0 = (b.de && qq == nq - 1) ? GEp[gid] : U[(long long)f * n + gid];
+      v[qq]           = u0 + acc[qq];
+    }
+  }
+  if (b.floor_on) {
+    double const floor = b.density_floor;
+    if (v[0] < floor) {
+      if (v[0] > 0) {
+        double const dens_0 = v[0];
+        v[0]                = floor;
+        v[1] *= (floor / dens_0);
+        v[2] *= (floor / dens_0);
+        v[3] *= (floor / dens_0);
+        v[4] *= (floor / dens_0);
+        if (b.de) v[nq - 1] *= (floor / dens_0);
+      } else {
+        atomicOr(status, 1);  // negative density: averaged by the finalize kernel
+      }
+    }
+  }
+#pragma unroll
+  for (int qq = 0; qq < NQ_MAX; qq++)
+    if (qq < nq) U[(long long)field_of_q(qq, b) * n + gid] = v[qq];
+  if (b.de) Epre[gid] = v[4];
+}
+
+template <int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
+cudaError_t launch_xsweep(const Box &b, const double *Uh, double *A, double *U, const Scratch &sc, double dt,
+                          const double *dtp, cudaStream_t s)
+{
+  using S         = XSweep<DIR, L, WA, WB, RECON>;
+  size_t const sm = sizeof(double) * (size_t)b.nq() * S::PER_Q;
+  auto k          = k_xsweep<DIR, L, WA, WB, RECON, SOLVER, FIRST, FINAL>;
+  cudaError_t e   = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  int const rx = b.nx - 2 * b.ng, ry = b.ny - 2 * b.ng, rz = b.nz - 2 * b.ng;
+  int const ra = DIR == 0 ? rx : DIR == 1 ? ry : rz, rb = DIR == 0 ? ry : rx, rc = DIR == 2 ? ry : rz;
+  dim3 grid((ra + L - 1) / L, (rb + WA - 1) / WA, (rc + WB - 1) / WB);
+  k<<<grid, L * WA * WB, sm, s>>>(b, Uh, A, U, sc.GEp, sc.Epre, sc.status, dt, dtp);
+  return cudaGetLastError();
+}
+
+// the three exact sweeps of one recon / solver pair
+template <int RECON, int SOLVER>
+cudaError_t launch_xsweeps(const Box &b, double *U, const Scratch &sc, double dt, const double *dtp, cudaStream_t s)
+{
+  double *A     = static_cast<double *>(sc.W);
+  cudaError_t e = launch_xsweep<0, 64, 2, 2, RECON, SOLVER, true, false>(b, sc.Uh, A, U, sc, dt, dtp, s);
+  if (e == cudaSuccess) e = launch_xsweep<1, 32, 8, 1, RECON, SOLVER, false, false>(b, sc.Uh, A, U, sc, dt, dtp, s);
+  if (e == cudaSuccess) e = launch_xsweep<2, 32, 8, 1, RECON, SOLVER, false, true>(b, sc.Uh, A, U, sc, dt, dtp, s);
+  return e;
+}
+
 template <int TX, int TY, int TZ, int SOLVER>
 size_t predictor_smem(const Box &b)
 {
@@ -707,7 +970,11 @@ cudaError_t dispatch_step(const Box &b, int recon, int solver, double *U, const 
   }
   if (e != cudaSuccess) return e;
   if (marks) cudaEventRecord(marks[1], s);
-#define CGB_CORR(R, SV) launch_corrector<TX, TY, TZ, R, SV>(b, sc.Uh, U, sc.GEp, sc.Epre, sc.status, dt, dtp, s)
+  // 3D with an accumulator in the scratch: the three sweeps; else the fused tile corrector
+  bool const sweeps = TY > 1 && sc.W != nullptr;
+#define CGB_CORR(R, SV)                                                                                   \
+  (sweeps ? launch_xsweeps<R, SV>(b, U, sc, dt, dtp, s)                                                   \
+          : launch_corrector<TX, TY, TZ, R, SV>(b, sc.Uh, U, sc.GEp, sc.Epre, sc.status, dt, dtp, s))
   if (recon == RECON_PPMC) {
     e = (solver == SOLVER_ROE) ? CGB_CORR(RECON_PPMC, SOLVER_ROE) : CGB_CORR(RECON_PPMC, SOLVER_HLLC);
   } else if (recon == RECON_PLMC) {
