@@ -11,6 +11,7 @@ by the oracle's std::mt19937_64 helper with the seed and ranges recorded here.
 from __future__ import annotations
 
 import json
+import math
 import re
 import sys
 from pathlib import Path
@@ -115,6 +116,81 @@ def dt_tests(src_dir: Path) -> dict:
     return {"calc_dt_3d": calc, "hydro_inverse_crossing_time": ict}
 
 
+def _matching(s: str, i: int) -> int:
+    """Index of the brace that closes the one at s[i]."""
+    depth = 0
+    for j in range(i, len(s)):
+        depth += (s[j] == "{") - (s[j] == "}")
+        if depth == 0:
+            return j
+    raise ValueError("unbalanced braces")
+
+
+def _cpp_value(expr: str, consts: dict) -> float:
+    """A C++ arithmetic literal expression of the test sources (numbers, named constants,
+    std::sqrt, M_PI) as a float."""
+    e = expr.strip().replace("std::sqrt", "math.sqrt").replace("std::pow", "math.pow").replace("M_PI", "math.pi")
+    e = re.sub(r"(?<![\w.])(\d+)\.(?![\d\w])", r"\1.0", e)  # "2." -> "2.0"
+    return float(eval(e, {"math": math, "__builtins__": {}}, dict(consts)))
+
+
+def hlld_cases(src_dir: Path) -> dict:
+    """The known-answer flux tests of mhd::Calculate_HLLD_Fluxes_CUDA: per case the left and
+    right primitive states (density, vx, vy, vz, pressure, Bx, By, Bz), gamma, the interface
+    directions the test loops over, and the fiducial flux (density, momenta, energy, Bx, By,
+    Bz).  Cases whose states the test edits in place are kept only for the edits recognised
+    here (Bx sign flips); the rest are counted as skipped."""
+    s = re.sub(r"//[^\n]*", "", (src_dir / "riemann_solvers/hlld_cuda_tests.cu").read_text())
+    cases, skipped = [], 0
+    for m in re.finditer(r"TEST_F\(tMHDCalculateHLLDFluxesCUDA,\s*(\w+)\)", s):
+        i = s.index("{", m.end())
+        body = s[i:_matching(s, i) + 1]
+        consts = {}
+        for c in re.finditer(r"Real\s+const\s+(\w+)\s*=\s*([^;{]+);", body):
+            try:
+                consts[c.group(1)] = _cpp_value(c.group(2), consts)
+            except Exception:
+                pass
+        states = {}
+        for st in re.finditer(r"(\w+)\s*=\s*Primitive_2_Conserved\(\s*\{([^}]*)\}", body):
+            states[st.group(1)] = [_cpp_value(x, consts) for x in st.group(2).split(",")]
+        dirs = [0, 1, 2] if re.search(r"for\s*\(size_t direction", body) else [0]
+        for f in re.finditer(r"fiducialFlux\s*\{", body):
+            k = body.index("{", f.start())
+            k2 = _matching(body, k)
+            fid = [_cpp_value(x, consts) for x in body[k + 1:k2].split(",")]
+            call = re.search(r"Compute_Fluxes\(\s*(\w+)\s*,\s*(\w+)\s*,\s*gamma", body[k2:])
+            if not call:
+                skipped += 1
+                continue
+            between = body[k2:k2 + call.start()]
+            left, right = call.group(1), call.group(2)
+            flips = {}
+            for nm in (left, right):
+                base = re.search(rf"\b{nm}\s*=\s*(\w+)\s*[,;]", between)
+                if base and re.search(rf"{nm}\[5\]\s*=\s*-{nm}\[5\]", between):
+                    flips[nm] = base.group(1)
+            def state(nm):
+                if nm in flips:
+                    v = list(states[flips[nm]])
+                    v[5] = -v[5]
+                    return v
+                return states.get(nm)
+            L, R = state(left), state(right)
+            edits = re.sub(r"(std::vector<Real>\s+const\s+scalarFlux\s*\{[^}]*\};|Real\s+thermalEnergyFlux\s*=[^;]*;)",
+                           "", between)
+            edits = re.sub(r"std::vector<Real>\s+(\w+)\s*=\s*(\w+)\s*,\s*(\w+)\s*=\s*(\w+)\s*;", "", edits)
+            edits = re.sub(r"\w+\[5\]\s*=\s*-\w+\[5\]\s*;", "", edits)
+            edits = re.sub(r"^\s*\}\s*;|std::vector<Real>\s+const\s+testFluxes\s*=\s*$", "", edits.strip()).strip()
+            if L is None or R is None or len(fid) != 8 or edits:
+                skipped += 1
+                continue
+            cases.append({"test": m.group(1), "gamma": consts["gamma"], "left": L, "right": R, "directions": dirs,
+                          "fiducial": fid})
+    return {"cases": cases, "skipped": skipped, "rule": {"abs": 2.7e-15, "ulps": 7},
+            "source": "src/riemann_solvers/hlld_cuda_tests.cu:30-1875"}
+
+
 def main() -> None:
     root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     src = root / "src"
@@ -124,6 +200,7 @@ def main() -> None:
         "plmc": plmc(src),
         "ppm_single_variable": ppm_single_variable(src),
         "dt": dt_tests(src),
+        "hlld": hlld_cases(src),
     }
     out = HERE / "reference_fiducials.json"
     out.write_text(json.dumps(data, indent=1))

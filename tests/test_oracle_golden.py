@@ -114,3 +114,57 @@ def test_hydro_inverse_crossing_time_reference_fiducial(oracle_lib):
     got = o.calc_dt(cfg, np.ascontiguousarray(U.ravel()))
     # the oracle recomputes v = m * (1/d), the reference test passes v directly: allow a few ULP
     assert abs(got - g["fiducial"]) <= 1e-15 * abs(g["fiducial"]) * 8
+
+
+def _sqm(a, b, c):
+    return a * a + ((b * b) + (c * c))  # math_utils::SquareMagnitude (dotProduct order)
+
+
+def _hlld_conserved(p, gamma):
+    """Primitive_2_Conserved of the reference's HLLD tests (hydro_utilities::Calc_Energy_Primitive
+    with the magnetic energy), in its operation order."""
+    d, vx, vy, vz, P, bx, by, bz = p
+    energy = (max(P, 1.0e-20) / (gamma - 1.0)) + 0.5 * d * _sqm(vx, vy, vz)
+    energy += 0.5 * _sqm(bx, by, bz)
+    return [d, vx * d, vy * d, vz * d, energy, bx, by, bz]
+
+
+def _hlld_flux(o, left, right, gamma, direction):
+    """Compute_Fluxes of the reference's HLLD test fixture on the oracle: momenta rotated to the
+    interface's frame, Bx taken out as the face field, one cell, the fluxes rotated back with a
+    zero Bx flux inserted."""
+    def rot_in(s):
+        s = list(s)
+        s[1:4] = s[4 - direction:4] + s[1:4 - direction]
+        return s
+
+    L, R = rot_in(left), rot_in(right)
+    bface = np.array([L[5]])
+    QL = np.array(L[:5] + L[6:])
+    QR = np.array(R[:5] + R[6:])
+    F = np.zeros(7)
+    cfg = o.config(1, 1, 1, 0, 8, mhd=True, recon=o.PLMC, solver=o.HLLD, gamma=gamma)
+    o.lib().orc_hlld(C.byref(cfg), QL, QR, bface, F, direction)
+    f = list(F[:5]) + [0.0] + list(F[5:])
+    f[1:4] = f[1 + direction:4] + f[1:1 + direction]
+    return np.array(f)
+
+
+def test_hlld_reference_known_answers(oracle_lib):
+    """mhd::Calculate_HLLD_Fluxes_CUDA known-answer tests (Brio & Wu, Dai & Woodward, Ryu &
+    Jones, Einfeldt, constant states; every interface direction the test loops over), with the
+    reference test's own rule: |diff| <= 2.7e-15 or <= 7 ULP."""
+    g = GOLD["hlld"]
+    assert len(g["cases"]) >= 60
+    rule = g["rule"]
+    n_checked = 0
+    for case in g["cases"]:
+        gamma = case["gamma"]
+        L, R = _hlld_conserved(case["left"], gamma), _hlld_conserved(case["right"], gamma)
+        fid = np.array(case["fiducial"])
+        for direction in case["directions"]:
+            got = _hlld_flux(oracle_lib, L, R, gamma, direction)
+            ok = nearly_equal(fid, got, abs_eps=rule["abs"], ulps=rule["ulps"])
+            assert ok.all(), (case["test"], direction, fid, got)
+            n_checked += 1
+    assert n_checked >= 180
