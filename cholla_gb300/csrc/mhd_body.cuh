@@ -870,14 +870,14 @@ __global__ void k_calc_dt(Box b, const double *__restrict__ U, unsigned long lon
 __global__ void k_max_divb(Box b, const double *__restrict__ U, unsigned long long *__restrict__ out)
 {
   long long const n = b.n;
-  int const ng      = b.ng;
   __shared__ double red[32];
   double m = 0.0;
   CGB_CELLS(id)
   {
     int x, y, z;
     xyz(b, id, x, y, z);
-    if (!(x >= ng && x < b.nx - ng && y >= ng && y < b.ny - ng && z >= ng && z < b.nz - ng)) continue;
+    // the reference's thread guard: every cell from index 2 up, the upper ghost layers included
+    if (!(x > 1 && y > 1 && z > 1)) continue;
     long long const fB = b.fB();
     double const div = fabs((U[fB * n + id] - U[fB * n + b.id(x - 1, y, z)]) / b.dx +
                             (U[(fB + 1) * n + id] - U[(fB + 1) * n + b.id(x, y - 1, z)]) / b.dy +

@@ -120,7 +120,9 @@ def Set_Boundaries(dev_conserved, nx, ny, nz, n_ghost, n_fields, flags) -> None:
 
 
 def Max_Magnetic_Divergence(dev_conserved, nx, ny, nz, n_ghost, n_fields, dx, dy, dz) -> float:
-    """Max |div B| over the real cells of an MHD state (src/mhd/magnetic_divergence.cu:33-76)."""
+    """Max |div B| of an MHD state over the cells with x, y, z >= 2, upper ghost layers included,
+    as the reference's kernel measures it (src/mhd/magnetic_divergence.cu:33-105): fill the ghost
+    cells first."""
     out = C.c_double(0.0)
     L.check(L.lib().cgb_max_magnetic_divergence(_ptr(dev_conserved), nx, ny, nz, n_ghost, n_fields, dx, dy, dz,
                                                 C.byref(out)))

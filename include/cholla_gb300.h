@@ -123,8 +123,11 @@ int cgb_apply_temperature_floor(double *d_conserved, int nx, int ny, int nz, int
  * flags[6] = {x-lower, x-upper, y-lower, y-upper, z-lower, z-upper}. */
 int cgb_set_boundaries(double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields, const int flags[6]);
 
-/* Maximum |div B| over the real cells (MHD).  Replaces calculateMagneticDivergence
- * (src/mhd/magnetic_divergence.cu:33-76); writes the value to *max_divb (host). */
+/* Maximum |div B| (MHD) over the cells with x, y, z >= 2 of the whole box, upper ghost layers
+ * included, as the reference's thread guard has it: fill the ghost cells first.  Replaces
+ * calculateMagneticDivergence / checkMagneticDivergence (src/mhd/magnetic_divergence.cu:33-105);
+ * writes the value to *max_divb (host).  n_ghost is checked like every entry point's but does
+ * not change the range. */
 int cgb_max_magnetic_divergence(const double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields,
                                 double dx, double dy, double dz, double *max_divb);
 

@@ -62,6 +62,7 @@ def lib() -> C.CDLL:
             "orc_vl_step_3d": [P, _DP, C.c_double],
             "orc_vl_step_1d": [P, _DP, C.c_double],
             "orc_mt19937_uniform": [C.c_ulonglong, C.c_double, C.c_double, C.c_size_t, _DP],
+            "orc_mt19937_32_uniform": [C.c_ulong, C.c_double, C.c_double, C.c_size_t, _DP],
             "orc_ppm_single_variable": [C.c_double] * 5 + [C.POINTER(C.c_double)] * 2,
             "orc_set_threads": [C.c_int],
         }
@@ -70,6 +71,8 @@ def lib() -> C.CDLL:
             getattr(h, name).restype = C.c_int if name.startswith("orc_vl_step") else None
         h.orc_calc_dt.argtypes = [P, _DP]
         h.orc_calc_dt.restype = C.c_double
+        h.orc_ct_slope.argtypes = [P, _DP, _DP, C.c_double] + [C.c_int] * 8
+        h.orc_ct_slope.restype = C.c_double
         h.orc_max_divB.argtypes = [P, _DP]
         h.orc_max_divB.restype = C.c_double
         h.orc_get_threads.restype = C.c_int
@@ -86,6 +89,12 @@ def config(nx, ny, nz, n_ghost, n_fields, *, n_scalars=0, de=False, mhd=False, r
 def mt_uniform(seed: int, a: float, b: float, n: int) -> np.ndarray:
     out = np.empty(n, dtype=np.float64)
     lib().orc_mt19937_uniform(seed, a, b, n, out)
+    return out
+
+
+def mt32_uniform(seed: int, a: float, b: float, n: int) -> np.ndarray:
+    out = np.empty(n, dtype=np.float64)
+    lib().orc_mt19937_32_uniform(seed, a, b, n, out)
     return out
 
 

@@ -388,6 +388,12 @@ void orc_mt19937_uniform(unsigned long long seed, double a, double b, size_t n, 
   std::uniform_real_distribution<double> dist(a, b);
   for (size_t i = 0; i < n; i++) out[i] = dist(prng);
 }
+void orc_mt19937_32_uniform(unsigned long seed, double a, double b, size_t n, double *out)
+{
+  std::mt19937 prng(seed);
+  std::uniform_real_distribution<double> dist(a, b);
+  for (size_t i = 0; i < n; i++) out[i] = dist(prng);
+}
 int orc_get_threads(void) { return g_threads > 0 ? g_threads : omp_get_max_threads(); }
 
 void orc_ppm_single_variable(double im2, double im1, double i, double ip1, double ip2, double *L_iph, double *R_imh)
@@ -1131,6 +1137,13 @@ inline double ct_slope(const Grid &g, const double *flux, const double *U, doubl
 }
 }  // namespace
 
+double orc_ct_slope(const orc_config *c, const double *flux, const double *U, double flux_sign, int ct_dir, int cq1,
+                    int cq2, int fq1, int fq2, int x, int y, int z)
+{
+  Grid g(c);
+  return ct_slope(g, flux, U, flux_sign, ct_dir, cq1, cq2, fq1, fq2, x, y, z);
+}
+
 void orc_ct_electric_fields(const orc_config *c, const double *Fx, const double *Fy, const double *Fz,
                             const double *U, double *emf)
 {
@@ -1527,17 +1540,17 @@ double orc_calc_dt(const orc_config *c, const double *U)
   return result;
 }
 
-// src/mhd/magnetic_divergence.cu:33-76 calculateMagneticDivergence: max |div B| over real cells
+// src/mhd/magnetic_divergence.cu:33-76 calculateMagneticDivergence: max |div B| over the cells that
+// its thread guard (:50) admits, x, y, z > 1 up to the last cell, so the upper ghost layers count
 double orc_max_divB(const orc_config *c, const double *U)
 {
   Grid g(c);
   size_t const n = g.n;
-  int const ng   = g.ng;
   double const dx = c->dx, dy = c->dy, dz = c->dz;
   double result = 0.0;
-  for (int z = ng; z < g.nz - ng; z++)
-    for (int y = ng; y < g.ny - ng; y++)
-      for (int x = ng; x < g.nx - ng; x++) {
+  for (int z = 2; z < g.nz; z++)
+    for (int y = 2; y < g.ny; y++)
+      for (int x = 2; x < g.nx; x++) {
         size_t const id = g.id(x, y, z);
         double const div =
             fabs((U[(size_t)g.fB * n + id] - U[(size_t)g.fB * n + g.id(x - 1, y, z)]) / dx +
@@ -1628,7 +1641,7 @@ void orc_set_boundaries(const orc_config *c, double *U, const int flags_in[6])
     if ((dir < 2 && g.nx <= 1) || (dir >= 2 && dir < 4 && g.ny <= 1) || (dir >= 4 && g.nz <= 1)) continue;
     if (flags[dir] == 4 || flags[dir] == 5) continue;
     // boundary_conditions.cpp Set_Boundary_Extents
-    int imin[3], imax[3];
+    int imin[3] = {0, 0, 0}, imax[3] = {0, 0, 0};
     int jl = 0, ju = g.ny, kl = 0, ku = g.nz;
     if (g.ny > 1) jl = ng, ju = g.ny - ng;
     if (g.nz > 1) kl = ng, ku = g.nz - ng;

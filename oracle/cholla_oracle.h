@@ -47,6 +47,9 @@ void orc_plmc(const orc_config *c, const double *U, double *QL, double *QR, int 
 void orc_hllc(const orc_config *c, const double *QL, const double *QR, double *F, int dir);
 void orc_roe(const orc_config *c, const double *QL, const double *QR, double *F, int dir);
 void orc_hlld(const orc_config *c, const double *QL, const double *QR, const double *Bface, double *F, int dir);
+/* one CT slope at cell (x, y, z) (ct_electric_fields.h:66-120 _ctSlope) */
+double orc_ct_slope(const orc_config *c, const double *flux, const double *U, double flux_sign, int ct_dir, int cq1,
+                    int cq2, int fq1, int fq2, int x, int y, int z);
 void orc_ct_electric_fields(const orc_config *c, const double *Fx, const double *Fy, const double *Fz,
                             const double *U, double *emf);
 void orc_update_magnetic(const orc_config *c, const double *src, double *dst, const double *emf, double dt);
@@ -59,6 +62,7 @@ void orc_de_select(const orc_config *c, double *U);
 void orc_de_sync(const orc_config *c, double *U);
 void orc_temperature_floor(const orc_config *c, double *U, double U_floor);
 double orc_calc_dt(const orc_config *c, const double *U);
+/* max |div B| over the cells with x, y, z >= 2 of the whole box, ghost layers included */
 double orc_max_divB(const orc_config *c, const double *U);
 void orc_set_boundaries(const orc_config *c, double *U, const int flags[6]);
 
@@ -73,6 +77,9 @@ int orc_vl_step_1d(const orc_config *c, double *U, double dt);
 /* std::mt19937_64(seed) + std::uniform_real_distribution<double>(a, b), n draws: the input
  * generator of the reference's unit tests (e.g. src/reconstruction/ppmc_cuda_tests.cu:131-132) */
 void orc_mt19937_uniform(unsigned long long seed, double a, double b, size_t n, double *out);
+/* the same with the 32-bit std::mt19937 (src/mhd/magnetic_divergence_tests.cu:47-48,
+ * src/mhd/ct_electric_fields_tests.cu:197-198) */
+void orc_mt19937_32_uniform(unsigned long seed, double a, double b, size_t n, double *out);
 
 /* threads used by the OpenMP loops (0 = library default) */
 void orc_set_threads(int n);

@@ -6,7 +6,7 @@ Run in a container where the reference source tree is mounted (default /root/ref
 
 Only numbers are taken from the reference's test files (fiducial outputs and the literal
 inputs of the small known-answer tests); the inputs of the randomised tests are regenerated
-by the oracle's std::mt19937_64 helper with the seed and ranges recorded here.
+by the oracle's std::mt19937_64 / std::mt19937 helpers with the seeds and ranges recorded here.
 """
 from __future__ import annotations
 
@@ -191,6 +191,78 @@ def hlld_cases(src_dir: Path) -> dict:
             "source": "src/riemann_solvers/hlld_cuda_tests.cu:30-1875"}
 
 
+def _test_bodies(s: str, suite: str) -> dict:
+    """{test name: body} of the TEST_F / TEST blocks of one suite, comments removed."""
+    s = re.sub(r"//[^\n]*", "", s)
+    out = {}
+    for m in re.finditer(rf"TEST(?:_F)?\({suite},\s*(\w+)\)", s):
+        i = s.index("{", m.end())
+        out[m.group(1)] = s[i:_matching(s, i) + 1]
+    return out
+
+
+def _at_assignments(body: str, name: str) -> dict:
+    return {k: float(v) for k, v in re.findall(rf"{name}\.at\((\d+)\)\s*=\s*([-+0-9.eE]+)\s*;", body)}
+
+
+def _fixture_value(s: str, name: str) -> float:
+    return float(re.search(rf"\b{name}\s*=\s*([-+0-9.eE]+)\s*[,;]", s).group(1))
+
+
+def mhd_unit_cases(src_dir: Path) -> dict:
+    """Known answers of the MHD kernels: the CT electric fields and the face-field update on
+    iota-filled grids (every array holds 0, 1, 2, ... continuing from the previous one), the CT
+    slope at the centre of a 5^3 grid and the maximum divergence of a 104^3 grid, both filled
+    from std::mt19937(1) draws.  Every entry not named in `fiducial` keeps its -999 fill."""
+    ct_src = (src_dir / "mhd/ct_electric_fields_tests.cu").read_text()
+    ct = []
+    for name, body in _test_bodies(ct_src, "tMHDCalculateCTElectricFields").items():
+        if re.search(r"fluxX\.at\(i\)\s*=\s*-fluxX\.at\(i\)", body):
+            edit = "negate_first_field"
+        elif re.search(r"fluxX\.at\(i\)\s*=\s*0(\.0*)?\s*;", body):
+            edit = "zero_first_field"
+        elif "fluxX.at(i)" in body:
+            continue
+        else:
+            edit = "none"
+        ct.append({"test": name, "edit": edit, "fiducial": _at_assignments(body, "fiducialData")})
+    n_ct = int(_fixture_value(ct_src, "size_t const nx"))
+    slope_body = _test_bodies(ct_src, "tMHDCTSlope")["CorrectInputExpectCorrectOutput"]
+    fid, _ = initializer(slope_body, "fiducial_data")
+    calls = re.findall(r"_ctSlope\(flux\.data\(\),\s*conserved\.data\(\),\s*([-\d]+),\s*([-\d]+),\s*([-\d]+),"
+                       r"\s*([-\d]+),\s*([-\d]+),\s*([-\d]+),", slope_body)
+    rng = re.search(r"doubleRand\(([-\d.]+),\s*([-\d.]+)\)", slope_body)
+    up_src = (src_dir / "mhd/magnetic_update_tests.cu").read_text()
+    up_body = _test_bodies(up_src, "tMHDUpdateMagneticField3D")["CorrectInputExpectCorrectOutput"]
+    div_src = (src_dir / "mhd/magnetic_divergence_tests.cu").read_text()
+    div_body = _test_bodies(div_src, "tMHDGrid3DcheckMagneticDivergence")["CorrectInputExpectCorrectOutput"]
+    div_rng = re.search(r"doubleRand\(([-\d.]+),\s*([-\d.]+)\)", div_body)
+    scale = float(re.search(r"doubleRand\(prng\)\s*/\s*([-+0-9.eE]+)", div_body).group(1))
+    fid_div = re.search(r"fiducialDivergence\s*=\s*([-+0-9.eE]+)\s*/\s*([-+0-9.eE]+)", div_body)
+    return {
+        "rule": {"abs": 1e-14, "ulps": 4},
+        "ct_electric_fields": {"n": n_ct, "n_fields": 8, "n_flux_fields": 7, "cases": ct,
+                               "source": "src/mhd/ct_electric_fields_tests.cu:35-178"},
+        "ct_slope": {"n": int(re.search(r"size_t const nx\s*=\s*(\d+)", slope_body).group(1)), "n_fields": 8,
+                     "seed": int(re.search(r"std::mt19937 prng\((\d+)\)", slope_body).group(1)),
+                     "range": [float(rng.group(1)), float(rng.group(2))],
+                     "calls": [[int(v) for v in c] for c in calls], "fiducial": [float(v) for v in fid],
+                     "source": "src/mhd/ct_electric_fields_tests.cu:183-272"},
+        "update_magnetic": {"n": int(_fixture_value(up_src, "size_t const nx")), "n_fields": 8,
+                            "dt": _fixture_value(up_src, "Real const dt"), "dx": _fixture_value(up_src, "dx"),
+                            "fiducial": _at_assignments(up_body, "fiducialData"),
+                            "source": "src/mhd/magnetic_update_tests.cu:28-124"},
+        "max_divergence": {"n_real": int(re.search(r"gridSize\s*=\s*(\d+)", div_body).group(1)),
+                           "n_ghost": int(re.search(r"n_ghost\s*=\s*(\d+)", div_body).group(1)),
+                           "n_fields": int(re.search(r"n_fields\s*=\s*(\d+)", div_body).group(1)),
+                           "dx": float(re.search(r"G\.H\.dx\s*=\s*([-+0-9.eE]+)", div_body).group(1)),
+                           "seed": int(re.search(r"std::mt19937 prng\((\d+)\)", div_body).group(1)),
+                           "range": [float(div_rng.group(1)), float(div_rng.group(2))], "scale": scale,
+                           "fiducial": float(fid_div.group(1)) / float(fid_div.group(2)),
+                           "source": "src/mhd/magnetic_divergence_tests.cu:27-65"},
+    }
+
+
 def main() -> None:
     root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     src = root / "src"
@@ -201,6 +273,7 @@ def main() -> None:
         "ppm_single_variable": ppm_single_variable(src),
         "dt": dt_tests(src),
         "hlld": hlld_cases(src),
+        "mhd_unit": mhd_unit_cases(src),
     }
     out = HERE / "reference_fiducials.json"
     out.write_text(json.dumps(data, indent=1))

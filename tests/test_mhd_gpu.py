@@ -113,16 +113,42 @@ def test_mhd_divergence_stays_at_roundoff(cuda):
     I.set_scheme(s)
     G = cuda.from_numpy(U0.copy()).cuda()
     b_scale = np.abs(U0[5:8]).max() / dx
+    I.Set_Boundaries(G, N, N, N, ng, nf, (1,) * 6)
     d0 = I.Max_Magnetic_Divergence(G, N, N, N, ng, nf, dx, dx, dx)
     for _ in range(10):
         I.Set_Boundaries(G, N, N, N, ng, nf, (1,) * 6)
         dt = 0.3 / I.Calc_dt_GPU(G, N, N, N, ng, nf, dx, dx, dx, gamma)
         I.VL_Algorithm_3D_CUDA(G, None, N, N, N, 0, 0, 0, ng, dx, dx, dx, 0, 0, 0, dt, nf, 0, 0.0)
+    # the face-B update also runs over the ghost layers, where the reference's HLLD sees the
+    # unfilled outermost interface states; the ghost fill replaces them before the measure
+    I.Set_Boundaries(G, N, N, N, ng, nf, (1,) * 6)
     d1 = I.Max_Magnetic_Divergence(G, N, N, N, ng, nf, dx, dx, dx)
-    # real cells only: the face-B update also runs over the ghost layers, where the reference's
-    # HLLD sees the unfilled outermost interface states; the next ghost fill replaces them
     assert np.isfinite(G.cpu().numpy()[real_slice(ng)]).all()
     assert d0 < 1e-12 * b_scale and d1 < 1e-11 * b_scale, (d0, d1, b_scale)
+
+
+def test_max_divergence_reference_known_answer(cuda, oracle_lib):
+    """cgb_max_magnetic_divergence on the reference's known-answer grid: 104^3 cells of
+    std::mt19937(1) draws in [1, 5) / 1e15, dx = 3; the result within 4 ULP of the fiducial
+    and equal to the oracle's."""
+    import ctypes as C
+    import json
+    from pathlib import Path
+
+    from cholla_gb300 import integrator as I
+
+    g = json.loads((Path(__file__).parent / "golden" / "reference_fiducials.json").read_text())
+    g = g["mhd_unit"]["max_divergence"]
+    n, ng, nf, dx = g["n_real"] + 2 * g["n_ghost"], g["n_ghost"], g["n_fields"], g["dx"]
+    U = oracle_lib.mt32_uniform(g["seed"], *g["range"], nf * n ** 3) / g["scale"]
+    cfg = oracle_lib.config(n, n, n, ng, nf, mhd=True, dx=dx, dy=dx, dz=dx)
+    want = oracle_lib.lib().orc_max_divB(C.byref(cfg), U)
+    I.set_scheme(_scheme("PLMC"))
+    got = I.Max_Magnetic_Divergence(cuda.from_numpy(U).cuda(), n, n, n, ng, nf, dx, dx, dx)
+    from helpers import ulp_diff
+
+    assert got == want, (got, want)
+    assert ulp_diff(g["fiducial"], got) <= 4, (got, g["fiducial"])
 
 
 def test_mhd_engine_matches_dropin_bitwise(cuda):
@@ -185,4 +211,5 @@ def test_mhd_fast_fp64_within_1e12_of_exact(cuda, recon):
     assert np.isfinite(f[real_slice(ng)]).all()
     assert np.all(err <= 1e-12), dict(zip(FIELDS, err))
     b_scale = np.abs(U0[5:8]).max() / dx
+    I.Set_Boundaries(Uf, N, N, N, ng, nf, (1,) * 6)
     assert I.Max_Magnetic_Divergence(Uf, N, N, N, ng, nf, dx, dx, dx) < 1e-11 * b_scale

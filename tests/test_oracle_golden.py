@@ -168,3 +168,89 @@ def test_hlld_reference_known_answers(oracle_lib):
             assert ok.all(), (case["test"], direction, fid, got)
             n_checked += 1
     assert n_checked >= 180
+
+
+def _iota_chain(*sizes):
+    """Arrays holding 0, 1, 2, ... where each continues from the previous one's last value
+    (the fixtures' chained std::iota fills)."""
+    out, start = [], 0
+    for n in sizes:
+        out.append(np.arange(start, start + n, dtype=np.float64))
+        start += n
+    return out
+
+
+def _expect_filled(n, fiducial, fill=-999.0):
+    expect = np.full(n, fill)
+    for k, v in fiducial.items():
+        expect[int(k)] = v
+    return expect
+
+
+def test_ct_electric_fields_reference_known_answers(oracle_lib):
+    """Calculate_CT_Electric_Fields on the 2^3 iota grid: positive, negated and zero first flux
+    field; entries 7, 15, 23 (the one cell the guard admits) carry the fiducials, the rest -999."""
+    o = oracle_lib
+    g, rule = GOLD["mhd_unit"]["ct_electric_fields"], GOLD["mhd_unit"]["rule"]
+    n = g["n"]
+    nc = n ** 3
+    cfg = o.config(n, n, n, 0, g["n_fields"], mhd=True)
+    assert len(g["cases"]) == 3
+    for case in g["cases"]:
+        Fx, Fy, Fz, U = _iota_chain(nc * g["n_flux_fields"], nc * g["n_flux_fields"], nc * g["n_flux_fields"],
+                                    nc * g["n_fields"])
+        for F in (Fx, Fy, Fz):
+            if case["edit"] == "negate_first_field":
+                F[:nc] = -F[:nc]
+            elif case["edit"] == "zero_first_field":
+                F[:nc] = 0.0
+        emf = np.full(3 * nc, -999.0)
+        o.lib().orc_ct_electric_fields(C.byref(cfg), Fx, Fy, Fz, U, emf)
+        expect = _expect_filled(3 * nc, case["fiducial"])
+        ok = nearly_equal(expect, emf, abs_eps=rule["abs"], ulps=rule["ulps"])
+        assert ok.all(), (case["test"], np.nonzero(~ok)[0], emf[~ok], expect[~ok])
+
+
+def test_ct_slope_reference_known_answers(oracle_lib):
+    """The 24 CT-slope argument patterns the electric-field kernel uses, at the centre of a 5^3
+    grid of std::mt19937(1) draws in [-5, 5) (conserved first, then flux)."""
+    o = oracle_lib
+    g, rule = GOLD["mhd_unit"]["ct_slope"], GOLD["mhd_unit"]["rule"]
+    n, nf = g["n"], g["n_fields"]
+    nc = n ** 3
+    draws = o.mt32_uniform(g["seed"], *g["range"], 2 * nf * nc)
+    U, flux = draws[:nf * nc].copy(), draws[nf * nc:].copy()
+    cfg = o.config(n, n, n, 0, nf, mhd=True)
+    c = n // 2
+    got = np.array([o.lib().orc_ct_slope(C.byref(cfg), flux, U, float(a[0]), *a[1:], c, c, c) for a in g["calls"]])
+    assert len(got) == len(g["fiducial"]) == 24
+    assert nearly_equal(np.array(g["fiducial"]), got, abs_eps=rule["abs"], ulps=rule["ulps"]).all()
+
+
+def test_update_magnetic_reference_known_answers(oracle_lib):
+    """Update_Magnetic_Field_3D on the 3^3 iota grid (dt 3.2, dx = dy = dz = 2.5): the centre
+    cell's three face fields (entries 148, 175, 202) change, every other entry keeps -999."""
+    o = oracle_lib
+    g, rule = GOLD["mhd_unit"]["update_magnetic"], GOLD["mhd_unit"]["rule"]
+    n, nf = g["n"], g["n_fields"]
+    nc = n ** 3
+    src, emf = _iota_chain(nc * nf, 3 * nc)
+    dst = np.full(nc * nf, -999.0)
+    cfg = o.config(n, n, n, 0, nf, mhd=True, dx=g["dx"], dy=g["dx"], dz=g["dx"])
+    o.lib().orc_update_magnetic(C.byref(cfg), src, dst, emf, g["dt"])
+    expect = _expect_filled(nc * nf, g["fiducial"])
+    ok = nearly_equal(expect, dst, abs_eps=rule["abs"], ulps=rule["ulps"])
+    assert ok.all(), (np.nonzero(~ok)[0], dst[~ok], expect[~ok])
+
+
+def test_max_divergence_reference_known_answer(oracle_lib):
+    """Max |div B| of a 104^3 grid of std::mt19937(1) draws in [1, 5) / 1e15 with dx = 3, over
+    the cells x, y, z >= 2 of the whole box.  The reference's own rule (1e-14 absolute) passes
+    any value below 1.4e-14, so the oracle is held to 4 ULP here."""
+    o = oracle_lib
+    g = GOLD["mhd_unit"]["max_divergence"]
+    n = g["n_real"] + 2 * g["n_ghost"]
+    U = o.mt32_uniform(g["seed"], *g["range"], g["n_fields"] * n ** 3) / g["scale"]
+    cfg = o.config(n, n, n, g["n_ghost"], g["n_fields"], mhd=True, dx=g["dx"], dy=g["dx"], dz=g["dx"])
+    got = o.lib().orc_max_divB(C.byref(cfg), U)
+    assert nearly_equal(g["fiducial"], got, abs_eps=0.0, ulps=4)
