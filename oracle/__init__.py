@@ -65,12 +65,25 @@ def lib() -> C.CDLL:
             "orc_mt19937_32_uniform": [C.c_ulong, C.c_double, C.c_double, C.c_size_t, _DP],
             "orc_ppm_single_variable": [C.c_double] * 5 + [C.POINTER(C.c_double)] * 2,
             "orc_set_threads": [C.c_int],
+            "orc_t_load_data": [P, _DP, C.c_int, C.c_int, C.c_int, C.c_int, _DP],
+            "orc_t_write_data": [P, _DP, _DP, _DP, C.c_size_t, C.c_int],
+            "orc_t_compute_slope": [P, _DP, _DP, C.c_double, _DP],
+            "orc_t_van_leer_slope": [P, _DP, _DP, _DP],
+            "orc_t_eigenvectors": [_DP, C.c_double, C.c_double, C.c_double, _DP],
+            "orc_t_prim_to_char": [C.c_int, _DP, _DP, _DP, C.c_double, C.c_double, _DP],
+            "orc_t_char_to_prim": [C.c_int, _DP, _DP, _DP, C.c_double, C.c_double, _DP],
+            "orc_t_monotonize_characteristic": [P, _DP, C.c_void_p * 4, C.c_void_p * 4, _DP, C.c_double, C.c_double,
+                                                _DP],
+            "orc_t_calc_interface_linear": [P, _DP, _DP, C.c_double, _DP],
+            "orc_t_plm_limit_interfaces": [P, _DP, _DP, _DP, _DP, _DP],
         }
         for name, args in sig.items():
             getattr(h, name).argtypes = args
             getattr(h, name).restype = C.c_int if name.startswith("orc_vl_step") else None
         h.orc_calc_dt.argtypes = [P, _DP]
         h.orc_calc_dt.restype = C.c_double
+        h.orc_t_thread_guard.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int]
+        h.orc_t_thread_guard.restype = C.c_int
         h.orc_ct_slope.argtypes = [P, _DP, _DP, C.c_double] + [C.c_int] * 8
         h.orc_ct_slope.restype = C.c_double
         h.orc_max_divB.argtypes = [P, _DP]

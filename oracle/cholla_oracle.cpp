@@ -364,6 +364,120 @@ bool guard(const Grid &g, int x, int y, int z)
   return out;
 }
 
+// reconstruction.h:224-247 Compute_Slope: coef * (right - left) per primitive field
+Prim compute_slope(const Grid &g, const Prim &l, const Prim &r, double coef)
+{
+  Prim s;
+  std::memset(&s, 0, sizeof(s));
+  s.d  = coef * (r.d - l.d);
+  s.vx = coef * (r.vx - l.vx);
+  s.vy = coef * (r.vy - l.vy);
+  s.vz = coef * (r.vz - l.vz);
+  s.p  = coef * (r.p - l.p);
+  if (g.mhd) {
+    s.by = coef * (r.by - l.by);
+    s.bz = coef * (r.bz - l.bz);
+  }
+  if (g.de) s.ge = coef * (r.ge - l.ge);
+  for (int k = 0; k < g.ns; k++) s.sc[k] = coef * (r.sc[k] - l.sc[k]);
+  return s;
+}
+
+// reconstruction.h:258-296 Van_Leer_Slope: harmonic mean where the one-sided slopes agree in sign
+inline double van_leer(double l, double r)
+{
+  if (l * r > 0.0) {
+    return 2.0 * l * r / (l + r);
+  } else {
+    return 0.0;
+  }
+}
+Prim van_leer_slope(const Grid &g, const Prim &dL, const Prim &dR)
+{
+  Prim dG;
+  std::memset(&dG, 0, sizeof(dG));
+  dG.d  = van_leer(dL.d, dR.d);
+  dG.vx = van_leer(dL.vx, dR.vx);
+  dG.vy = van_leer(dL.vy, dR.vy);
+  dG.vz = van_leer(dL.vz, dR.vz);
+  dG.p  = van_leer(dL.p, dR.p);
+  if (g.mhd) {
+    dG.by = van_leer(dL.by, dR.by);
+    dG.bz = van_leer(dL.bz, dR.bz);
+  }
+  if (g.de) dG.ge = van_leer(dL.ge, dR.ge);
+  for (int k = 0; k < g.ns; k++) dG.sc[k] = van_leer(dL.sc[k], dR.sc[k]);
+  return dG;
+}
+
+// reconstruction.h:512-559 Monotonize_Characteristic_Return_Primitive
+inline double monotonize(double l, double r, double cc, double vg)
+{
+  if (l * r > 0.0) {
+    double const la = 2.0 * fmin(fabs(l), fabs(r));
+    double const lb = fmin(fabs(cc), fabs(vg));
+    return copysign(fmin(la, lb), cc);
+  } else {
+    return 0.0;
+  }
+}
+Prim monotonize_characteristic(const Grid &g, const Prim &p, const Prim &dL, const Prim &dR, const Prim &dC,
+                               const Prim &dG, const Chr &aL, const Chr &aR, const Chr &aC, const Chr &aG,
+                               const Eig &e, double cs, double cs2)
+{
+  Chr am;
+  int const nchar = g.mhd ? 7 : 5;
+  for (int k = 0; k < 7; k++) am.a[k] = 0.0;
+  for (int k = 0; k < nchar; k++) am.a[k] = monotonize(aL.a[k], aR.a[k], aC.a[k], aG.a[k]);
+  Prim dm = char_to_prim(g.mhd, p, am, e, cs, cs2);
+  if (g.de) dm.ge = monotonize(dL.ge, dR.ge, dC.ge, dG.ge);
+  for (int k = 0; k < g.ns; k++) dm.sc[k] = monotonize(dL.sc[k], dR.sc[k], dC.sc[k], dG.sc[k]);
+  return dm;
+}
+
+// reconstruction.h:645-673 Calc_Interface_Linear: cell + sign * slope / 2
+Prim calc_interface_linear(const Grid &g, const Prim &c, const Prim &dm, double sign)
+{
+  Prim o;
+  std::memset(&o, 0, sizeof(o));
+  auto f = [&sign](double st, double sl) -> double { return st + sign * 0.5 * sl; };
+  o.d  = f(c.d, dm.d);
+  o.vx = f(c.vx, dm.vx);
+  o.vy = f(c.vy, dm.vy);
+  o.vz = f(c.vz, dm.vz);
+  o.p  = f(c.p, dm.p);
+  if (g.mhd) {
+    o.by = f(c.by, dm.by);
+    o.bz = f(c.bz, dm.bz);
+  }
+  if (g.de) o.ge = f(c.ge, dm.ge);
+  for (int k = 0; k < g.ns; k++) o.sc[k] = f(c.sc[k], dm.sc[k]);
+  return o;
+}
+
+// reconstruction.h:686-723 Plm_Limit_Interfaces: each interface value within its two cells' range
+inline void plm_limit(double &l, double &r, double vm, double vi, double vp)
+{
+  r = fmax(fmin(vi, vm), r);
+  r = fmin(fmax(vi, vm), r);
+  l = fmax(fmin(vi, vp), l);
+  l = fmin(fmax(vi, vp), l);
+}
+void plm_limit_interfaces(const Grid &g, Prim &L, Prim &R, const Prim &cm, const Prim &ci, const Prim &cp)
+{
+  plm_limit(L.d, R.d, cm.d, ci.d, cp.d);
+  plm_limit(L.vx, R.vx, cm.vx, ci.vx, cp.vx);
+  plm_limit(L.vy, R.vy, cm.vy, ci.vy, cp.vy);
+  plm_limit(L.vz, R.vz, cm.vz, ci.vz, cp.vz);
+  plm_limit(L.p, R.p, cm.p, ci.p, cp.p);
+  if (g.mhd) {
+    plm_limit(L.by, R.by, cm.by, ci.by, cp.by);
+    plm_limit(L.bz, R.bz, cm.bz, ci.bz, cp.bz);
+  }
+  if (g.de) plm_limit(L.ge, R.ge, cm.ge, ci.ge, cp.ge);
+  for (int k = 0; k < g.ns; k++) plm_limit(L.sc[k], R.sc[k], cm.sc[k], ci.sc[k], cp.sc[k]);
+}
+
 template <typename F>
 void par_cells(const Grid &g, F f)
 {
@@ -399,6 +513,121 @@ int orc_get_threads(void) { return g_threads > 0 ? g_threads : omp_get_max_threa
 void orc_ppm_single_variable(double im2, double im1, double i, double ip1, double ip2, double *L_iph, double *R_imh)
 {
   ppm1(im2, im1, i, ip1, ip2, *L_iph, *R_imh);
+}
+
+// ---- reconstruction building blocks, one call each, for the reference's helper unit tests
+// (src/reconstruction/reconstruction_tests.cu).  A primitive state travels as 9 doubles
+// (density, vx, vy, vz, pressure, Bx, By, Bz, gas energy), a characteristic one as 7, the MHD
+// eigenvector set as the 18 members of reconstruction::EigenVecs in declaration order.
+}  // extern "C"
+namespace
+{
+Prim unpack_prim(const double *v)
+{
+  Prim p;
+  std::memset(&p, 0, sizeof(p));
+  p.d = v[0], p.vx = v[1], p.vy = v[2], p.vz = v[3], p.p = v[4], p.bx = v[5], p.by = v[6], p.bz = v[7], p.ge = v[8];
+  return p;
+}
+void pack_prim(const Prim &p, double *v)
+{
+  v[0] = p.d, v[1] = p.vx, v[2] = p.vy, v[3] = p.vz, v[4] = p.p, v[5] = p.bx, v[6] = p.by, v[7] = p.bz, v[8] = p.ge;
+}
+Chr unpack_chr(const double *v)
+{
+  Chr a;
+  for (int k = 0; k < 7; k++) a.a[k] = v[k];
+  return a;
+}
+Eig unpack_eig(const double *v)
+{
+  Eig e;
+  static_assert(sizeof(Eig) == 18 * sizeof(double), "EigenVecs has 18 members");
+  std::memcpy(&e, v, sizeof(e));
+  return e;
+}
+}  // namespace
+extern "C" {
+
+int orc_t_thread_guard(const orc_config *c, int order, int x, int y, int z)
+{
+  Grid g(c);
+  return order == 2 ? guard<2>(g, x, y, z) : guard<3>(g, x, y, z);
+}
+
+void orc_t_load_data(const orc_config *c, const double *U, int x, int y, int z, int dir, double *out)
+{
+  Grid g(c);
+  int o1, o2, o3;
+  perm(dir, o1, o2, o3);
+  pack_prim(load_data(g, U, x, y, z, o1, o2, o3), out);
+}
+
+void orc_t_write_data(const orc_config *c, const double *state, double *Q, const double *U, size_t id, int dir)
+{
+  Grid g(c);
+  int o1, o2, o3;
+  perm(dir, o1, o2, o3);
+  write_data(g, unpack_prim(state), Q, U, id, o1, o2, o3);
+}
+
+void orc_t_compute_slope(const orc_config *c, const double *left, const double *right, double coef, double *out)
+{
+  Grid g(c);
+  pack_prim(compute_slope(g, unpack_prim(left), unpack_prim(right), coef), out);
+}
+
+void orc_t_van_leer_slope(const orc_config *c, const double *left, const double *right, double *out)
+{
+  Grid g(c);
+  pack_prim(van_leer_slope(g, unpack_prim(left), unpack_prim(right)), out);
+}
+
+void orc_t_eigenvectors(const double *prim, double cs, double cs2, double gamma, double *out)
+{
+  Eig const e = eigenvectors(unpack_prim(prim), cs, cs2, gamma);
+  std::memcpy(out, &e, sizeof(e));
+}
+
+void orc_t_prim_to_char(int mhd, const double *prim, const double *slope, const double *eig, double cs, double cs2,
+                        double *out)
+{
+  Chr const a = prim_to_char(mhd != 0, unpack_prim(prim), unpack_prim(slope), unpack_eig(eig), cs, cs2);
+  for (int k = 0; k < 7; k++) out[k] = a.a[k];
+}
+
+void orc_t_char_to_prim(int mhd, const double *prim, const double *chr, const double *eig, double cs, double cs2,
+                        double *out)
+{
+  pack_prim(char_to_prim(mhd != 0, unpack_prim(prim), unpack_chr(chr), unpack_eig(eig), cs, cs2), out);
+}
+
+void orc_t_monotonize_characteristic(const orc_config *c, const double *prim, const double *const del[4],
+                                     const double *const del_a[4], const double *eig, double cs, double cs2,
+                                     double *out)
+{
+  Grid g(c);
+  Prim const d0 = unpack_prim(del[0]), d1 = unpack_prim(del[1]), d2 = unpack_prim(del[2]), d3 = unpack_prim(del[3]);
+  Chr const a0 = unpack_chr(del_a[0]), a1 = unpack_chr(del_a[1]), a2 = unpack_chr(del_a[2]), a3 = unpack_chr(del_a[3]);
+  pack_prim(monotonize_characteristic(g, unpack_prim(prim), d0, d1, d2, d3, a0, a1, a2, a3, unpack_eig(eig), cs, cs2),
+            out);
+}
+
+void orc_t_calc_interface_linear(const orc_config *c, const double *cell, const double *slope, double sign,
+                                 double *out)
+{
+  Grid g(c);
+  pack_prim(calc_interface_linear(g, unpack_prim(cell), unpack_prim(slope), sign), out);
+}
+
+void orc_t_plm_limit_interfaces(const orc_config *c, double *l_iph, double *r_imh, const double *cell_im1,
+                                const double *cell_i, const double *cell_ip1)
+{
+  Grid g(c);
+  Prim L = unpack_prim(l_iph), R = unpack_prim(r_imh);
+  plm_limit_interfaces(g, L, R, unpack_prim(cell_im1), unpack_prim(cell_i), unpack_prim(cell_ip1));
+  pack_prim(L, l_iph);
+  pack_prim(R, r_imh);
 }
 
 // src/reconstruction/pcm_cuda.cu:256-424 PCM_Reconstruction_3D (and :13-121 for 1D)
@@ -502,105 +731,18 @@ void orc_plmc(const orc_config *c, const double *U, double *QL, double *QR, int 
     Eig e;
     std::memset(&e, 0, sizeof(e));
     if (g.mhd) e = eigenvectors(ci, cs, cs2, g.gamma);
-    // reconstruction.h:224-296 Compute_Slope / Van_Leer_Slope
-    auto slope = [&](const Prim &l, const Prim &r, double coef) {
-      Prim s;
-      std::memset(&s, 0, sizeof(s));
-      s.d  = coef * (r.d - l.d);
-      s.vx = coef * (r.vx - l.vx);
-      s.vy = coef * (r.vy - l.vy);
-      s.vz = coef * (r.vz - l.vz);
-      s.p  = coef * (r.p - l.p);
-      if (g.mhd) {
-        s.by = coef * (r.by - l.by);
-        s.bz = coef * (r.bz - l.bz);
-      }
-      if (g.de) s.ge = coef * (r.ge - l.ge);
-      for (int k = 0; k < g.ns; k++) s.sc[k] = coef * (r.sc[k] - l.sc[k]);
-      return s;
-    };
-    auto vl = [](double l, double r) -> double {
-      if (l * r > 0.0) {
-        return 2.0 * l * r / (l + r);
-      } else {
-        return 0.0;
-      }
-    };
-    Prim const dL = slope(cimo, ci, 1.0);
-    Prim const dR = slope(ci, cipo, 1.0);
-    Prim const dC = slope(cimo, cipo, 0.5);
-    Prim dG;
-    std::memset(&dG, 0, sizeof(dG));
-    dG.d  = vl(dL.d, dR.d);
-    dG.vx = vl(dL.vx, dR.vx);
-    dG.vy = vl(dL.vy, dR.vy);
-    dG.vz = vl(dL.vz, dR.vz);
-    dG.p  = vl(dL.p, dR.p);
-    if (g.mhd) {
-      dG.by = vl(dL.by, dR.by);
-      dG.bz = vl(dL.bz, dR.bz);
-    }
-    if (g.de) dG.ge = vl(dL.ge, dR.ge);
-    for (int k = 0; k < g.ns; k++) dG.sc[k] = vl(dL.sc[k], dR.sc[k]);
-    Chr const aL = prim_to_char(g.mhd, ci, dL, e, cs, cs2);
-    Chr const aR = prim_to_char(g.mhd, ci, dR, e, cs, cs2);
-    Chr const aC = prim_to_char(g.mhd, ci, dC, e, cs, cs2);
-    Chr const aG = prim_to_char(g.mhd, ci, dG, e, cs, cs2);
-    // reconstruction.h:512-559 Monotonize_Characteristic_Return_Primitive
-    auto mono = [](double l, double r, double cc, double vg) -> double {
-      if (l * r > 0.0) {
-        double const la = 2.0 * fmin(fabs(l), fabs(r));
-        double const lb = fmin(fabs(cc), fabs(vg));
-        return copysign(fmin(la, lb), cc);
-      } else {
-        return 0.0;
-      }
-    };
-    Chr am;
-    int const nchar = g.mhd ? 7 : 5;
-    for (int k = 0; k < 7; k++) am.a[k] = 0.0;
-    for (int k = 0; k < nchar; k++) am.a[k] = mono(aL.a[k], aR.a[k], aC.a[k], aG.a[k]);
-    Prim dm = char_to_prim(g.mhd, ci, am, e, cs, cs2);
-    if (g.de) dm.ge = mono(dL.ge, dR.ge, dC.ge, dG.ge);
-    for (int k = 0; k < g.ns; k++) dm.sc[k] = mono(dL.sc[k], dR.sc[k], dC.sc[k], dG.sc[k]);
-    // reconstruction.h:645-673 Calc_Interface_Linear
-    auto lin = [&](double sign) {
-      Prim o;
-      std::memset(&o, 0, sizeof(o));
-      auto f = [&sign](double st, double sl) -> double { return st + sign * 0.5 * sl; };
-      o.d  = f(ci.d, dm.d);
-      o.vx = f(ci.vx, dm.vx);
-      o.vy = f(ci.vy, dm.vy);
-      o.vz = f(ci.vz, dm.vz);
-      o.p  = f(ci.p, dm.p);
-      if (g.mhd) {
-        o.by = f(ci.by, dm.by);
-        o.bz = f(ci.bz, dm.bz);
-      }
-      if (g.de) o.ge = f(ci.ge, dm.ge);
-      for (int k = 0; k < g.ns; k++) o.sc[k] = f(ci.sc[k], dm.sc[k]);
-      return o;
-    };
-    Prim L = lin(1.0);
-    Prim R = lin(-1.0);
-    // reconstruction.h:686-723 Plm_Limit_Interfaces
-    auto lim = [](double &l, double &r, double vm, double vi, double vp) {
-      r = fmax(fmin(vi, vm), r);
-      r = fmin(fmax(vi, vm), r);
-      l = fmax(fmin(vi, vp), l);
-      l = fmin(fmax(vi, vp), l);
-    };
-    lim(L.d, R.d, cimo.d, ci.d, cipo.d);
-    lim(L.vx, R.vx, cimo.vx, ci.vx, cipo.vx);
-    lim(L.vy, R.vy, cimo.vy, ci.vy, cipo.vy);
-    lim(L.vz, R.vz, cimo.vz, ci.vz, cipo.vz);
-    lim(L.p, R.p, cimo.p, ci.p, cipo.p);
-    if (g.mhd) {
-      lim(L.by, R.by, cimo.by, ci.by, cipo.by);
-      lim(L.bz, R.bz, cimo.bz, ci.bz, cipo.bz);
-    }
-    if (g.de) lim(L.ge, R.ge, cimo.ge, ci.ge, cipo.ge);
-    for (int k = 0; k < g.ns; k++) lim(L.sc[k], R.sc[k], cimo.sc[k], ci.sc[k], cipo.sc[k]);
+    Prim const dL = compute_slope(g, cimo, ci, 1.0);
+    Prim const dR = compute_slope(g, ci, cipo, 1.0);
+    Prim const dC = compute_slope(g, cimo, cipo, 0.5);
+    Prim const dG = van_leer_slope(g, dL, dR);
+    Chr const aL  = prim_to_char(g.mhd, ci, dL, e, cs, cs2);
+    Chr const aR  = prim_to_char(g.mhd, ci, dR, e, cs, cs2);
+    Chr const aC  = prim_to_char(g.mhd, ci, dC, e, cs, cs2);
+    Chr const aG  = prim_to_char(g.mhd, ci, dG, e, cs, cs2);
+    Prim const dm = monotonize_characteristic(g, ci, dL, dR, dC, dG, aL, aR, aC, aG, e, cs, cs2);
+    Prim L        = calc_interface_linear(g, ci, dm, 1.0);
+    Prim R        = calc_interface_linear(g, ci, dm, -1.0);
+    plm_limit_interfaces(g, L, R, cimo, ci, cipo);
     R.d = fmax(R.d, TINY);
     L.d = fmax(L.d, TINY);
     R.p = fmax(R.p, TINY);

@@ -70,6 +70,32 @@ void orc_set_boundaries(const orc_config *c, double *U, const int flags[6]);
 void orc_ppm_single_variable(double im2, double im1, double i, double ip1, double ip2, double *L_iph,
                              double *R_imh);
 
+/* ---- reconstruction building blocks, for the reference's helper unit tests
+ * (src/reconstruction/reconstruction_tests.cu).  Primitive states are 9 doubles (density,
+ * vx, vy, vz, pressure, Bx, By, Bz, gas energy), characteristic states 7, MHD eigenvector sets
+ * the 18 members of reconstruction::EigenVecs in order.  dir 0/1/2 picks the x/y/z
+ * permutation of the momenta. ---- */
+int orc_t_thread_guard(const orc_config *c, int order, int x, int y, int z);                          /* :95-119 */
+void orc_t_load_data(const orc_config *c, const double *U, int x, int y, int z, int dir, double *out); /* :139-212 */
+void orc_t_write_data(const orc_config *c, const double *state, double *Q, const double *U, size_t id,
+                      int dir);                                                                        /* :918-968 */
+void orc_t_compute_slope(const orc_config *c, const double *left, const double *right, double coef,
+                         double *out);                                                                 /* :224-247 */
+void orc_t_van_leer_slope(const orc_config *c, const double *left, const double *right, double *out); /* :258-296 */
+void orc_t_eigenvectors(const double *prim, double cs, double cs2, double gamma, double *out);        /* :310-361 */
+void orc_t_prim_to_char(int mhd, const double *prim, const double *slope, const double *eig, double cs, double cs2,
+                        double *out);                                                                  /* :378-437 */
+void orc_t_char_to_prim(int mhd, const double *prim, const double *chr, const double *eig, double cs, double cs2,
+                        double *out);                                                                  /* :453-491 */
+/* del = {del_L, del_R, del_C, del_G} (primitive), del_a = the same four in characteristic variables */
+void orc_t_monotonize_characteristic(const orc_config *c, const double *prim, const double *const del[4],
+                                     const double *const del_a[4], const double *eig, double cs, double cs2,
+                                     double *out);                                                     /* :512-559 */
+void orc_t_calc_interface_linear(const orc_config *c, const double *cell, const double *slope, double sign,
+                                 double *out);                                                         /* :645-673 */
+void orc_t_plm_limit_interfaces(const orc_config *c, double *l_iph, double *r_imh, const double *cell_im1,
+                                const double *cell_i, const double *cell_ip1);                         /* :686-723 */
+
 /* ---- the step: VL_Algorithm_3D_CUDA / VL_Algorithm_1D_CUDA ---- */
 int orc_vl_step_3d(const orc_config *c, double *U, double dt);
 int orc_vl_step_1d(const orc_config *c, double *U, double dt);

@@ -113,7 +113,30 @@ def dt_tests(src_dir: Path) -> dict:
     ict["fiducial"] = float(re.search(r"fiducialInverseCrossingTime\s*=\s*([-0-9.eE]+)", blk).group(1))
     ict["gamma"] = 5.0 / 3.0
     ict["source"] = "src/hydro/hydro_cuda_tests.cu:89-110"
-    return {"calc_dt_3d": calc, "hydro_inverse_crossing_time": ict}
+    t2 = s.index("TEST(tMHDMhdInverseCrossingTime")
+    blk = s[t2:s.index("TEST(", t2 + 10)]
+    names += ["magneticX", "magneticY", "magneticZ"]
+    mct = {n: float(re.search(rf"double const {n}\s*=\s*([-0-9.eE]+)", blk).group(1)) for n in names}
+    mct["fiducial"] = float(re.search(r"fiducialInverseCrossingTime\s*=\s*([-0-9.eE]+)", blk).group(1))
+    mct["gamma"] = 5.0 / 3.0
+    mct["source"] = "src/hydro/hydro_cuda_tests.cu:116-142"
+    return {"calc_dt_3d": calc, "hydro_inverse_crossing_time": ict, "mhd_inverse_crossing_time": mct}
+
+
+def hllc_cases(src_dir: Path) -> dict:
+    """The HLLC known answer: a Sod high-pressure state against itself (primitive density,
+    pressure, velocities and gamma as the test writes them) and its fiducial flux."""
+    s = re.sub(r"//[^\n]*", "", (src_dir / "riemann_solvers/hllc_cuda_tests.cu").read_text())
+    cases = []
+    for name, body in _test_bodies(s, "tHYDROCalculateHLLCFluxesCUDA").items():
+        consts = {}
+        for c in re.finditer(r"Real\s+const\s+(\w+)\s*=\s*([^;{]+);", body):
+            consts[c.group(1)] = _cpp_value(c.group(2), consts)
+        fid, _ = initializer(body, "fiducialFluxes")
+        prim = [consts[k] for k in ("density", "velocityX", "velocityY", "velocityZ", "pressure")]
+        cases.append({"test": name, "left": prim, "right": prim, "gamma": consts["gamma"],
+                      "fiducial": [float(v) for v in fid]})
+    return {"cases": cases, "source": "src/riemann_solvers/hllc_cuda_tests.cu:152-176"}
 
 
 def _matching(s: str, i: int) -> int:
@@ -129,7 +152,7 @@ def _matching(s: str, i: int) -> int:
 def _cpp_value(expr: str, consts: dict) -> float:
     """A C++ arithmetic literal expression of the test sources (numbers, named constants,
     std::sqrt, M_PI) as a float."""
-    e = expr.strip().replace("std::sqrt", "math.sqrt").replace("std::pow", "math.pow").replace("M_PI", "math.pi")
+    e = " ".join(expr.split()).replace("std::sqrt", "math.sqrt").replace("std::pow", "math.pow").replace("M_PI", "math.pi")
     e = re.sub(r"(?<![\w.])(\d+)\.(?![\d\w])", r"\1.0", e)  # "2." -> "2.0"
     return float(eval(e, {"math": math, "__builtins__": {}}, dict(consts)))
 
@@ -263,6 +286,76 @@ def mhd_unit_cases(src_dir: Path) -> dict:
     }
 
 
+def _preprocess(src: str, defined: set) -> str:
+    """The source with `#ifdef` / `#ifndef` / `#else` / `#endif` branches resolved for the given
+    macros (other directives dropped)."""
+    out, stack = [], []
+    for line in src.splitlines():
+        t = line.strip()
+        m = re.match(r"#\s*(ifdef|ifndef)\s+(\w+)", t)
+        if m:
+            cond = (m.group(2) in defined) == (m.group(1) == "ifdef")
+            stack.append([cond, all(c for c, _ in stack)])
+            continue
+        if re.match(r"#\s*else\b", t):
+            stack[-1][0] = not stack[-1][0]
+            continue
+        if re.match(r"#\s*endif\b", t):
+            stack.pop()
+            continue
+        if t.startswith("#"):
+            continue
+        if all(c for c, _ in stack):
+            out.append(line)
+    return "\n".join(out)
+
+
+def reconstruction_helpers(src_dir: Path) -> dict:
+    """The helper unit tests of src/reconstruction/reconstruction_tests.cu that sit on the VL
+    path, for the MHD and the hydro build: per test the literal structs it builds
+    (reconstruction::Primitive / Characteristic / EigenVecs, in member order), its scalar
+    constants, field assignments, fiducial maps and any per-field tolerance it passes."""
+    raw = (src_dir / "reconstruction/reconstruction_tests.cu").read_text()
+    names = ["tMHDReconstructionPrimitive2Characteristic", "tMHDReconstructionCharacteristic2Primitive",
+             "tMHDReconstructionComputeEigenvectors", "tALLReconstructionThreadGuard", "tALLReconstructionLoadData",
+             "tALLReconstructionComputeSlope", "tALLReconstructionVanLeerSlope",
+             "tALLReconstructionMonotonizeCharacteristicReturnPrimitive", "tALLReconstructionCalcInterfaceLinear",
+             "tALLReconstructionWriteData", "tHYDROReconstructionPlmLimitInterfaces"]
+    out = {}
+    for build, defined in (("mhd", {"MHD"}), ("hydro", set())):
+        src = re.sub(r"//[^\n]*", "", _preprocess(raw, defined))
+        tests = {}
+        for name in names:
+            bodies = _test_bodies(src, name)
+            if not bodies:
+                continue
+            body = bodies["CorrectInputExpectCorrectOutput"]
+            structs = {m.group(2): [_cpp_value(v, {}) for v in m.group(3).split(",") if v.strip()]
+                       for m in re.finditer(r"reconstruction::(?:Primitive|Characteristic|EigenVecs)\s+(const\s+)?(\w+)"
+                                            r"\s*\{([^}]*)\}", body)}
+            consts = {}
+            for m in re.finditer(r"(?:Real|int|size_t)\s+const\s+([^;]+);", body):
+                for part in m.group(1).split(","):
+                    k, _, v = part.partition("=")
+                    try:
+                        consts[k.strip().lstrip("&")] = _cpp_value(v, consts)
+                    except Exception:
+                        pass
+            fields = {}
+            for m in re.finditer(r"(\w+)\.(\w+)\s*=\s*([-+0-9.eE]+)\s*;", body):
+                fields.setdefault(m.group(1), {})[m.group(2)] = float(m.group(3))
+            fmap = re.search(r"unordered_map<int,\s*double>\s+\w+\s*=\s*\{(.*?)\};", body, re.S)
+            tol = {m.group(1): float(m.group(2)) for m in re.finditer(
+                r"Check_Results\(fiducial_\w+\.(\w+),\s*host_results\.\w+,\s*\"\w+\",\s*([-+0-9.eE]+)\)", body)}
+            tests[name] = {"structs": structs, "consts": consts, "fields": fields,
+                           "map": {int(a): float(b) for a, b in re.findall(r"\{\s*(\d+)\s*,\s*([-+0-9.eE]+)\s*\}",
+                                                                          fmap.group(1))} if fmap else {},
+                           "at": _at_assignments(body, "fiducial_vals"), "abs_tolerance": tol}
+        out[build] = tests
+    out["source"] = "src/reconstruction/reconstruction_tests.cu:51-699"
+    return out
+
+
 def main() -> None:
     root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     src = root / "src"
@@ -271,7 +364,9 @@ def main() -> None:
         "ppmc_vl": ppmc_vl(src),
         "plmc": plmc(src),
         "ppm_single_variable": ppm_single_variable(src),
+        "reconstruction_helpers": reconstruction_helpers(src),
         "dt": dt_tests(src),
+        "hllc": hllc_cases(src),
         "hlld": hlld_cases(src),
         "mhd_unit": mhd_unit_cases(src),
     }
