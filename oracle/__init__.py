@@ -76,6 +76,14 @@ def lib() -> C.CDLL:
                                                 _DP],
             "orc_t_calc_interface_linear": [P, _DP, _DP, C.c_double, _DP],
             "orc_t_plm_limit_interfaces": [P, _DP, _DP, _DP, _DP, _DP],
+            "orc_t_hlld_load_state": [P, _DP, C.c_double, C.c_size_t, C.c_int, _DP],
+            "orc_t_hlld_return_fluxes": [P, C.c_size_t, C.c_int, _DP, _DP, _DP],
+            "orc_t_hlld_lr_speeds": [_DP, _DP, C.c_double, C.c_double, _DP],
+            "orc_t_hlld_nonstar_fluxes": [_DP, C.c_double, _DP],
+            "orc_t_hlld_star_state": [_DP, _DP, C.c_double, C.c_double, C.c_double, _DP],
+            "orc_t_hlld_star_fluxes": [_DP, _DP, _DP, _DP, C.c_double, _DP],
+            "orc_t_hlld_double_star_state": [_DP, _DP, C.c_double, C.c_double, _DP, _DP],
+            "orc_t_hlld_double_star_fluxes": [_DP, C.c_double, _DP, _DP, _DP, _DP, C.c_double, C.c_double, _DP],
         }
         for name, args in sig.items():
             getattr(h, name).argtypes = args
@@ -84,6 +92,11 @@ def lib() -> C.CDLL:
         h.orc_calc_dt.restype = C.c_double
         h.orc_t_thread_guard.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int]
         h.orc_t_thread_guard.restype = C.c_int
+        for name, args in (("orc_t_hlld_middle_speed", [_DP, _DP, _DP]),
+                           ("orc_t_hlld_star_speed", [_DP, _DP, C.c_double, C.c_double]),
+                           ("orc_t_hlld_star_total_pressure", [_DP, _DP, _DP])):
+            getattr(h, name).argtypes = args
+            getattr(h, name).restype = C.c_double
         h.orc_ct_slope.argtypes = [P, _DP, _DP, C.c_double] + [C.c_int] * 8
         h.orc_ct_slope.restype = C.c_double
         h.orc_max_divB.argtypes = [P, _DP]

@@ -1181,35 +1181,62 @@ HFlux hlld_dstarflux(const HDStar &ds, double dsE, const HStar &st, const HState
   o.bz = f.bz - S * s.bz - sd * st.bz + SStar * ds.bz;
   return o;
 }
+// hlld_cuda.cu approximateLRWaveSpeeds: outermost signal speeds from the larger fast speed
+void hlld_lr_speeds(const HState &sL, const HState &sR, double bx, double gamma, HSpeeds &sp)
+{
+  double const cL   = cfast(sL.d, sL.p, bx, sL.by, sL.bz, gamma);
+  double const cR   = cfast(sR.d, sR.p, bx, sR.by, sR.bz, gamma);
+  double const cmax = fmax(cL, cR);
+  sp.L              = fmin(sL.vx, sR.vx) - cmax;
+  sp.R              = fmax(sL.vx, sR.vx) + cmax;
+}
+// hlld_cuda.cu approximateMiddleWaveSpeed: the contact speed
+double hlld_middle_speed(const HState &sL, const HState &sR, const HSpeeds &sp)
+{
+  double const rd = sp.R - sR.vx, ld = sp.L - sL.vx;
+  return (rd * sR.d * sR.vx - ld * sL.d * sL.vx - sR.pt + sL.pt) / (rd * sR.d - ld * sL.d);
+}
+// hlld_cuda.cu approximateStarWaveSpeed: the Alfven wave bounding one star region (side -1 / +1)
+double hlld_star_speed(const HStar &st, const HSpeeds &sp, double bx, double side)
+{
+  return sp.M + side * (fabs(bx) / sqrt(fmax(st.d, TINY)));
+}
+// hlld_cuda.cu starTotalPressure: total pressure in the star regions
+double hlld_pt_star(const HState &sL, const HState &sR, const HSpeeds &sp)
+{
+  return (sR.d * sL.pt * (sp.R - sR.vx) - sL.d * sR.pt * (sp.L - sL.vx) +
+          sL.d * sR.d * (sp.R - sR.vx) * (sp.L - sL.vx) * (sR.vx - sL.vx)) /
+         (sR.d * (sp.R - sR.vx) - sL.d * (sp.L - sL.vx));
+}
+// hlld_cuda.cu returnFluxes: the flux of one interface into the permuted flux fields; passive
+// scalars and the thermal energy are advected with the density flux of the upwind state
+void hlld_return(const Grid &g, double *F, size_t t, int o1, int o2, int o3, const HFlux &f, const HState &s)
+{
+  size_t const n = g.n;
+  F[t]                  = f.d;
+  F[t + n * o1]         = f.mx;
+  F[t + n * o2]         = f.my;
+  F[t + n * o3]         = f.mz;
+  F[t + n * 4]          = f.E;
+  F[t + n * g.fB]       = f.by;
+  F[t + n * (g.fB + 1)] = f.bz;
+  for (int k = 0; k < g.ns; k++) F[t + n * (5 + k)] = s.sc[k] * f.d;
+  if (g.de) F[t + n * g.fGE] = s.ge * f.d;
+}
 }  // namespace
 
 void orc_hlld(const orc_config *c, const double *QL, const double *QR, const double *Bface, double *F, int dir)
 {
   Grid g(c);
-  size_t const n = g.n;
   int o1, o2, o3;
   perm(dir, o1, o2, o3);
   par_cells(g, [&](size_t t) {
-    double const bx   = Bface[t];
-    HState const sL   = hlld_load(g, QL, bx, t, o1, o2, o3);
-    HState const sR   = hlld_load(g, QR, bx, t, o1, o2, o3);
-    auto ret = [&](const HFlux &f, const HState &s) {
-      F[t]                = f.d;
-      F[t + n * o1]       = f.mx;
-      F[t + n * o2]       = f.my;
-      F[t + n * o3]       = f.mz;
-      F[t + n * 4]        = f.E;
-      F[t + n * g.fB]     = f.by;
-      F[t + n * (g.fB + 1)] = f.bz;
-      for (int k = 0; k < g.ns; k++) F[t + n * (5 + k)] = s.sc[k] * f.d;
-      if (g.de) F[t + n * g.fGE] = s.ge * f.d;
-    };
-    double const cL = cfast(sL.d, sL.p, bx, sL.by, sL.bz, g.gamma);
-    double const cR = cfast(sR.d, sR.p, bx, sR.by, sR.bz, g.gamma);
-    double const cmax = fmax(cL, cR);
+    double const bx = Bface[t];
+    HState const sL = hlld_load(g, QL, bx, t, o1, o2, o3);
+    HState const sR = hlld_load(g, QR, bx, t, o1, o2, o3);
+    auto ret        = [&](const HFlux &f, const HState &s) { hlld_return(g, F, t, o1, o2, o3, f, s); };
     HSpeeds sp;
-    sp.L  = fmin(sL.vx, sR.vx) - cmax;
-    sp.R  = fmax(sL.vx, sR.vx) + cmax;
+    hlld_lr_speeds(sL, sR, bx, g.gamma, sp);
     HFlux fL = hlld_nonstar(sL, bx);
     if (sp.L > 0.0) {
       ret(fL, sL);
@@ -1220,21 +1247,16 @@ void orc_hlld(const orc_config *c, const double *QL, const double *QR, const dou
       ret(fR, sR);
       return;
     }
-    {
-      double const rd = sp.R - sR.vx, ld = sp.L - sL.vx;
-      sp.M = (rd * sR.d * sR.vx - ld * sL.d * sL.vx - sR.pt + sL.pt) / (rd * sR.d - ld * sL.d);
-    }
-    double const ptStar = (sR.d * sL.pt * (sp.R - sR.vx) - sL.d * sR.pt * (sp.L - sL.vx) +
-                           sL.d * sR.d * (sp.R - sR.vx) * (sp.L - sL.vx) * (sR.vx - sL.vx)) /
-                          (sR.d * (sp.R - sR.vx) - sL.d * (sp.L - sL.vx));
-    HStar const stL = hlld_star(sL, sp, sp.L, bx, ptStar);
-    sp.LStar        = sp.M + -1 * (fabs(bx) / sqrt(fmax(stL.d, TINY)));
+    sp.M                = hlld_middle_speed(sL, sR, sp);
+    double const ptStar = hlld_pt_star(sL, sR, sp);
+    HStar const stL     = hlld_star(sL, sp, sp.L, bx, ptStar);
+    sp.LStar            = hlld_star_speed(stL, sp, bx, -1);
     if (sp.LStar > 0.0 and sp.L <= 0.0) {
       ret(hlld_starflux(stL, sL, fL, sp, sp.L), sL);
       return;
     }
     HStar const stR = hlld_star(sR, sp, sp.R, bx, ptStar);
-    sp.RStar        = sp.M + 1 * (fabs(bx) / sqrt(fmax(stR.d, TINY)));
+    sp.RStar        = hlld_star_speed(stR, sp, bx, 1);
     if (sp.RStar <= 0.0 and sp.R >= 0.0) {
       ret(hlld_starflux(stR, sR, fR, sp, sp.R), sR);
       return;
@@ -1249,6 +1271,112 @@ void orc_hlld(const orc_config *c, const double *QL, const double *QR, const dou
       return;
     }
   });
+}
+
+// ---- HLLD building blocks, one call each, for the reference's HLLD-internal unit tests
+// (src/riemann_solvers/hlld_cuda_tests.cu:1877-2400).  States travel packed in the member order
+// of mhd::internal::State (9), StarState (6), DoubleStarState (6), Flux (7) and Speeds (5).
+}  // extern "C"
+namespace
+{
+HState unpack_hstate(const double *v)
+{
+  HState s;
+  std::memset(&s, 0, sizeof(s));
+  s.d = v[0], s.vx = v[1], s.vy = v[2], s.vz = v[3], s.E = v[4], s.by = v[5], s.bz = v[6], s.p = v[7], s.pt = v[8];
+  return s;
+}
+void pack_hstate(const HState &s, double *v)
+{
+  v[0] = s.d, v[1] = s.vx, v[2] = s.vy, v[3] = s.vz, v[4] = s.E, v[5] = s.by, v[6] = s.bz, v[7] = s.p, v[8] = s.pt;
+}
+HStar unpack_hstar(const double *v) { return HStar{v[0], v[1], v[2], v[3], v[4], v[5]}; }
+void pack_hstar(const HStar &s, double *v) { v[0] = s.d, v[1] = s.vy, v[2] = s.vz, v[3] = s.E, v[4] = s.by, v[5] = s.bz; }
+HFlux unpack_hflux(const double *v) { return HFlux{v[0], v[1], v[2], v[3], v[4], v[5], v[6]}; }
+void pack_hflux(const HFlux &f, double *v)
+{
+  v[0] = f.d, v[1] = f.mx, v[2] = f.my, v[3] = f.mz, v[4] = f.E, v[5] = f.by, v[6] = f.bz;
+}
+HSpeeds unpack_speeds(const double *v) { return HSpeeds{v[0], v[1], v[2], v[3], v[4]}; }
+HDStar unpack_hdstar(const double *v)
+{
+  HDStar d;
+  d.vy = v[0], d.vz = v[1], d.by = v[2], d.bz = v[3], d.EL = v[4], d.ER = v[5];
+  return d;
+}
+}  // namespace
+extern "C" {
+
+void orc_t_hlld_load_state(const orc_config *c, const double *Q, double bx, size_t t, int dir, double *out)
+{
+  Grid g(c);
+  int o1, o2, o3;
+  perm(dir, o1, o2, o3);
+  pack_hstate(hlld_load(g, Q, bx, t, o1, o2, o3), out);
+}
+
+void orc_t_hlld_return_fluxes(const orc_config *c, size_t t, int dir, double *F, const double *flux,
+                              const double *state)
+{
+  Grid g(c);
+  int o1, o2, o3;
+  perm(dir, o1, o2, o3);
+  hlld_return(g, F, t, o1, o2, o3, unpack_hflux(flux), unpack_hstate(state));
+}
+
+void orc_t_hlld_lr_speeds(const double *stateL, const double *stateR, double bx, double gamma, double *speeds)
+{
+  HSpeeds sp{0, 0, 0, 0, 0};
+  hlld_lr_speeds(unpack_hstate(stateL), unpack_hstate(stateR), bx, gamma, sp);
+  speeds[0] = sp.L, speeds[1] = sp.LStar, speeds[2] = sp.M, speeds[3] = sp.RStar, speeds[4] = sp.R;
+}
+
+double orc_t_hlld_middle_speed(const double *stateL, const double *stateR, const double *speeds)
+{
+  return hlld_middle_speed(unpack_hstate(stateL), unpack_hstate(stateR), unpack_speeds(speeds));
+}
+
+double orc_t_hlld_star_speed(const double *star, const double *speeds, double bx, double side)
+{
+  return hlld_star_speed(unpack_hstar(star), unpack_speeds(speeds), bx, side);
+}
+
+double orc_t_hlld_star_total_pressure(const double *stateL, const double *stateR, const double *speeds)
+{
+  return hlld_pt_star(unpack_hstate(stateL), unpack_hstate(stateR), unpack_speeds(speeds));
+}
+
+void orc_t_hlld_nonstar_fluxes(const double *state, double bx, double *flux)
+{
+  pack_hflux(hlld_nonstar(unpack_hstate(state), bx), flux);
+}
+
+void orc_t_hlld_star_state(const double *state, const double *speeds, double S, double bx, double pt_star,
+                           double *star)
+{
+  pack_hstar(hlld_star(unpack_hstate(state), unpack_speeds(speeds), S, bx, pt_star), star);
+}
+
+void orc_t_hlld_star_fluxes(const double *star, const double *state, const double *flux, const double *speeds,
+                            double S, double *out)
+{
+  pack_hflux(hlld_starflux(unpack_hstar(star), unpack_hstate(state), unpack_hflux(flux), unpack_speeds(speeds), S),
+             out);
+}
+
+void orc_t_hlld_double_star_state(const double *starL, const double *starR, double bx, double pt_star,
+                                  const double *speeds, double *out)
+{
+  HDStar const d = hlld_dstar(unpack_hstar(starL), unpack_hstar(starR), bx, pt_star, unpack_speeds(speeds));
+  out[0] = d.vy, out[1] = d.vz, out[2] = d.by, out[3] = d.bz, out[4] = d.EL, out[5] = d.ER;
+}
+
+void orc_t_hlld_double_star_fluxes(const double *dstar, double dstar_energy, const double *star, const double *state,
+                                   const double *flux, const double *speeds, double S, double S_star, double *out)
+{
+  pack_hflux(hlld_dstarflux(unpack_hdstar(dstar), dstar_energy, unpack_hstar(star), unpack_hstate(state),
+                            unpack_hflux(flux), unpack_speeds(speeds), S, S_star),
+             out);
 }
 
 // src/mhd/ct_electric_fields.h:66-118 _ctSlope and ct_electric_fields.cu:20-279

@@ -96,6 +96,26 @@ void orc_t_calc_interface_linear(const orc_config *c, const double *cell, const 
 void orc_t_plm_limit_interfaces(const orc_config *c, double *l_iph, double *r_imh, const double *cell_im1,
                                 const double *cell_i, const double *cell_ip1);                         /* :686-723 */
 
+/* ---- HLLD building blocks, for the reference's HLLD-internal unit tests
+ * (src/riemann_solvers/hlld_cuda_tests.cu:1877-2400).  Packed in the member order of
+ * mhd::internal::State (9 doubles), StarState (6), DoubleStarState (6), Flux (7), Speeds (5). ---- */
+void orc_t_hlld_load_state(const orc_config *c, const double *Q, double bx, size_t t, int dir, double *out);
+void orc_t_hlld_return_fluxes(const orc_config *c, size_t t, int dir, double *F, const double *flux,
+                              const double *state);
+void orc_t_hlld_lr_speeds(const double *stateL, const double *stateR, double bx, double gamma, double *speeds);
+double orc_t_hlld_middle_speed(const double *stateL, const double *stateR, const double *speeds);
+double orc_t_hlld_star_speed(const double *star, const double *speeds, double bx, double side);
+double orc_t_hlld_star_total_pressure(const double *stateL, const double *stateR, const double *speeds);
+void orc_t_hlld_nonstar_fluxes(const double *state, double bx, double *flux);
+void orc_t_hlld_star_state(const double *state, const double *speeds, double S, double bx, double pt_star,
+                           double *star);
+void orc_t_hlld_star_fluxes(const double *star, const double *state, const double *flux, const double *speeds,
+                            double S, double *out);
+void orc_t_hlld_double_star_state(const double *starL, const double *starR, double bx, double pt_star,
+                                  const double *speeds, double *out);
+void orc_t_hlld_double_star_fluxes(const double *dstar, double dstar_energy, const double *star, const double *state,
+                                   const double *flux, const double *speeds, double S, double S_star, double *out);
+
 /* ---- the step: VL_Algorithm_3D_CUDA / VL_Algorithm_1D_CUDA ---- */
 int orc_vl_step_3d(const orc_config *c, double *U, double dt);
 int orc_vl_step_1d(const orc_config *c, double *U, double dt);

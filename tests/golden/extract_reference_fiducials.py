@@ -356,6 +356,47 @@ def reconstruction_helpers(src_dir: Path) -> dict:
     return out
 
 
+def _braces(src: str, name: str):
+    """JSON value of the brace initializer that follows `name` (std::nan -> NaN)."""
+    m = re.search(rf"\b{re.escape(name)}\s*(=\s*)?\{{", src)
+    i = src.index("{", m.start())
+    text = src[i:_matching(src, i) + 1]
+    text = re.sub(r"std::nan\(\"0\"\)", "NaN", text)
+    return braces_to_json(text)
+
+
+def hlld_internal_cases(src_dir: Path) -> dict:
+    """The HLLD-internal unit tests (mhd::internal::*): the shared TestParams (two cases of left
+    and right states, star states, fluxes, speeds, the star total pressure and the normal field)
+    and per test its fiducial vectors and the per-field absolute tolerances it passes."""
+    s = re.sub(r"//[^\n]*", "", (src_dir / "riemann_solvers/hlld_cuda_tests.cu").read_text())
+    i = s.index("struct TestParams")
+    tp_src = s[i:_matching(s, s.index("{", i)) + 1]
+    params = {k: _braces(tp_src, k) for k in ("magneticX", "stateLVec", "stateRVec", "starStateLVec", "starStateRVec",
+                                              "totalPressureStar", "DoubleStarStateVec", "flux", "starFlux", "speed")}
+    params["gamma"] = _cpp_value(re.search(r"double const gamma\s*=\s*([^;]+);", tp_src).group(1), {})
+    tests = {}
+    for m in re.finditer(r"TEST\((tMHDHlldInternal\w+),\s*(\w+)\)", s):
+        j = s.index("{", m.end())
+        body = s[j:_matching(s, j) + 1]
+        fid = {}
+        for f in re.finditer(r"std::vector<[\w:]+>\s+(?:const\s+)?(fiducial\w+)\s*\{", body):
+            fid[f.group(1)] = _braces(body, f.group(1))
+        tol = {t.group(1): float(t.group(2)) for t in re.finditer(
+            r"Check_Results\(fiducial\w+(?:\[i\]|\.at\(i\))\.(\w+),\s*test\w+\.\w+,[^;]*?,\s*([-+0-9.eE]+)\)", body)}
+        mult = re.search(r"totalPressureStarMultiplier\s*=\s*([-+0-9.eE]+)", body)
+        entry = {"fiducial": fid, "abs_tolerance": tol,
+                 "multiplier": float(mult.group(1)) if mult else None}
+        if m.group(1) == "tMHDHlldInternalReturnFluxes":
+            entry["flux"] = _braces(body, "inputFlux")
+            entry["state"] = _braces(body, "inputState")
+            entry["dummy"] = float(re.search(r"dummyValue\s*=\s*([-+0-9.eE]+)", body).group(1))
+        if m.group(1) == "tMHDHlldInternalLoadState":
+            entry["n_cells"] = int(re.search(r"n_cells\s*=\s*(\d+)", body).group(1))
+        tests[m.group(1) + "." + m.group(2)] = entry
+    return {"params": params, "tests": tests, "source": "src/riemann_solvers/hlld_cuda_tests.cu:1811-2400"}
+
+
 def main() -> None:
     root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     src = root / "src"
@@ -368,6 +409,7 @@ def main() -> None:
         "dt": dt_tests(src),
         "hllc": hllc_cases(src),
         "hlld": hlld_cases(src),
+        "hlld_internal": hlld_internal_cases(src),
         "mhd_unit": mhd_unit_cases(src),
     }
     out = HERE / "reference_fiducials.json"
