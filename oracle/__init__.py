@@ -76,6 +76,8 @@ def lib() -> C.CDLL:
                                                 _DP],
             "orc_t_calc_interface_linear": [P, _DP, _DP, C.c_double, _DP],
             "orc_t_plm_limit_interfaces": [P, _DP, _DP, _DP, _DP, _DP],
+            "orc_t_cell_centered_b": [_DP, C.c_size_t, C.c_int, C.c_int, C.c_int, C.c_size_t, C.c_int, C.c_int,
+                                      C.c_int, _DP],
             "orc_t_hlld_load_state": [P, _DP, C.c_double, C.c_size_t, C.c_int, _DP],
             "orc_t_hlld_return_fluxes": [P, C.c_size_t, C.c_int, _DP, _DP, _DP],
             "orc_t_hlld_lr_speeds": [_DP, _DP, C.c_double, C.c_double, _DP],
@@ -92,7 +94,14 @@ def lib() -> C.CDLL:
         h.orc_calc_dt.restype = C.c_double
         h.orc_t_thread_guard.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int]
         h.orc_t_thread_guard.restype = C.c_int
-        for name, args in (("orc_t_hlld_middle_speed", [_DP, _DP, _DP]),
+        D = C.c_double
+        for name, args in (("orc_t_pressure_primitive", [D] * 6 + [C.c_int] + [D] * 3),
+                           ("orc_t_energy_primitive", [D] * 6 + [C.c_int] + [D] * 3),
+                           ("orc_t_pressure_from_de", [D] * 4), ("orc_t_kinetic_energy", [D] * 4),
+                           ("orc_t_magnetic_energy", [D] * 3), ("orc_t_total_pressure", [D] * 4),
+                           ("orc_t_fast_magnetosonic", [D] * 6), ("orc_t_slow_magnetosonic", [D] * 6),
+                           ("orc_t_alfven_speed", [D] * 2),
+                           ("orc_t_hlld_middle_speed", [_DP, _DP, _DP]),
                            ("orc_t_hlld_star_speed", [_DP, _DP, C.c_double, C.c_double]),
                            ("orc_t_hlld_star_total_pressure", [_DP, _DP, _DP])):
             getattr(h, name).argtypes = args

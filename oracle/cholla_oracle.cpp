@@ -102,13 +102,17 @@ inline void perm(int dir, int &o1, int &o2, int &o3)
 }
 
 // mhd_utilities.h:205-237 cellCenteredMagneticFields
+inline void cc_b_strided(const double *U, size_t n_cells, int nx, int ny, int fB, size_t id, int x, int y, int z,
+                         double &bx, double &by, double &bz)
+{
+  const double *Bx = U + (size_t)fB * n_cells, *By = U + (size_t)(fB + 1) * n_cells, *Bz = U + (size_t)(fB + 2) * n_cells;
+  bx = (x > 0) ? 0.5 * (Bx[id] + Bx[id - 1]) : Bx[id];
+  by = (y > 0) ? 0.5 * (By[id] + By[id - (size_t)nx]) : By[id];
+  bz = (z > 0) ? 0.5 * (Bz[id] + Bz[id - (size_t)nx * ny]) : Bz[id];
+}
 inline void cc_b(const Grid &g, const double *U, int x, int y, int z, double &bx, double &by, double &bz)
 {
-  size_t const id = g.id(x, y, z);
-  const double *Bx = U + (size_t)g.fB * g.n, *By = U + (size_t)(g.fB + 1) * g.n, *Bz = U + (size_t)(g.fB + 2) * g.n;
-  bx = (x > 0) ? 0.5 * (Bx[id] + Bx[g.id(x - 1, y, z)]) : Bx[id];
-  by = (y > 0) ? 0.5 * (By[id] + By[g.id(x, y - 1, z)]) : By[id];
-  bz = (z > 0) ? 0.5 * (Bz[id] + Bz[g.id(x, y, z - 1)]) : Bz[id];
+  cc_b_strided(U, g.n, g.nx, g.ny, g.fB, g.id(x, y, z), x, y, z, bx, by, bz);
 }
 
 // mhd_utilities.h:38-59 _magnetosonicSpeed
@@ -130,6 +134,28 @@ inline double cslow(double d, double p, double bx, double by, double bz, double 
   return magnetosonic(d, p, bx, by, bz, gamma, -1.0);
 }
 inline double magE(double bx, double by, double bz) { return 0.5 * sqmag(bx, by, bz); }  // mhd_utilities.h:84
+// hydro_utilities.h:162-166 Calc_Kinetic_Energy_From_Velocity
+inline double kinetic_energy(double d, double vx, double vy, double vz) { return 0.5 * d * sqmag(vx, vy, vz); }
+// hydro_utilities.h:34-45 Calc_Pressure_Primitive: gas pressure from total energy, floored at TINY
+inline double pressure_primitive(double E, double d, double vx, double vy, double vz, double gamma, bool mhd,
+                                 double bx, double by, double bz)
+{
+  double pressure = E - kinetic_energy(d, vx, vy, vz);
+  if (mhd) pressure -= magE(bx, by, bz);
+  return fmax((gamma - 1.) * pressure, TINY);
+}
+// hydro_utilities.h:106-118 Calc_Energy_Primitive: total energy from a (floored) pressure
+inline double energy_primitive(double P, double d, double vx, double vy, double vz, double gamma, bool mhd,
+                               double bx, double by, double bz)
+{
+  double energy = (fmax(P, TINY) / (gamma - 1.)) + kinetic_energy(d, vx, vy, vz);
+  if (mhd) energy += magE(bx, by, bz);
+  return energy;
+}
+// mhd_utilities.h:117-124 computeTotalPressure: gas plus magnetic pressure, floored at TINY
+inline double total_pressure(double p, double bx, double by, double bz) { return fmax(p + magE(bx, by, bz), TINY); }
+// mhd_utilities.h:176-180 alfvenSpeed
+inline double alfven_speed(double bx, double d) { return fabs(bx) / sqrt(fmax(d, TINY)); }
 
 // ============================================================================================
 // Reconstruction (src/reconstruction/reconstruction.h)
@@ -177,9 +203,7 @@ Prim load_data(const Grid &g, const double *U, int x, int y, int z, int o1, int 
     P.ge = GE / P.d;
   } else {
     // hydro_utilities.h:34-45 Calc_Pressure_Primitive
-    double pressure = U[4 * n + id] - 0.5 * P.d * sqmag(P.vx, P.vy, P.vz);
-    if (g.mhd) pressure -= magE(P.bx, P.by, P.bz);
-    P.p = fmax((g.gamma - 1.) * pressure, TINY);
+    P.p = pressure_primitive(U[4 * n + id], P.d, P.vx, P.vy, P.vz, g.gamma, g.mhd, P.bx, P.by, P.bz);
   }
   for (int s = 0; s < g.ns; s++) P.sc[s] = U[(size_t)(5 + s) * n + id] / P.d;
   return P;
@@ -340,11 +364,9 @@ void write_data(const Grid &g, const Prim &s, double *Q, const double *U, size_t
     Q[(size_t)(g.fB + 1) * n + id] = s.bz;
     bx                             = U[(size_t)(g.fB + (o1 - 1)) * n + id];
     // hydro_utilities.h:106-118 Calc_Energy_Primitive
-    double energy = (fmax(s.p, TINY) / (g.gamma - 1.)) + 0.5 * s.d * sqmag(s.vx, s.vy, s.vz);
-    energy += magE(bx, s.by, s.bz);
-    Q[4 * n + id] = energy;
+    Q[4 * n + id] = energy_primitive(s.p, s.d, s.vx, s.vy, s.vz, g.gamma, true, bx, s.by, s.bz);
   } else {
-    Q[4 * n + id] = (fmax(s.p, TINY) / (g.gamma - 1.)) + 0.5 * s.d * sqmag(s.vx, s.vy, s.vz);
+    Q[4 * n + id] = energy_primitive(s.p, s.d, s.vx, s.vy, s.vz, g.gamma, false, 0.0, 0.0, 0.0);
   }
   if (g.de) Q[(size_t)g.fGE * n + id] = s.d * s.ge;
   for (int k = 0; k < g.ns; k++) Q[(size_t)(5 + k) * n + id] = s.d * s.sc[k];
@@ -548,6 +570,39 @@ Eig unpack_eig(const double *v)
 }
 }  // namespace
 extern "C" {
+
+// ---- hydro / MHD utilities on the path (src/utils/hydro_utilities.h, mhd_utilities.h) ----
+double orc_t_pressure_primitive(double E, double d, double vx, double vy, double vz, double gamma, int mhd, double bx,
+                                double by, double bz)
+{
+  return pressure_primitive(E, d, vx, vy, vz, gamma, mhd != 0, bx, by, bz);
+}
+double orc_t_energy_primitive(double P, double d, double vx, double vy, double vz, double gamma, int mhd, double bx,
+                              double by, double bz)
+{
+  return energy_primitive(P, d, vx, vy, vz, gamma, mhd != 0, bx, by, bz);
+}
+double orc_t_pressure_from_de(double E, double U_total, double U_advected, double gamma)
+{
+  return pressure_from_de(E, U_total, U_advected, gamma);
+}
+double orc_t_kinetic_energy(double d, double vx, double vy, double vz) { return kinetic_energy(d, vx, vy, vz); }
+double orc_t_magnetic_energy(double bx, double by, double bz) { return magE(bx, by, bz); }
+double orc_t_total_pressure(double p, double bx, double by, double bz) { return total_pressure(p, bx, by, bz); }
+double orc_t_fast_magnetosonic(double d, double p, double bx, double by, double bz, double gamma)
+{
+  return cfast(d, p, bx, by, bz, gamma);
+}
+double orc_t_slow_magnetosonic(double d, double p, double bx, double by, double bz, double gamma)
+{
+  return cslow(d, p, bx, by, bz, gamma);
+}
+double orc_t_alfven_speed(double bx, double d) { return alfven_speed(bx, d); }
+void orc_t_cell_centered_b(const double *U, size_t id, int x, int y, int z, size_t n_cells, int nx, int ny, int fB,
+                           double *out)
+{
+  cc_b_strided(U, n_cells, nx, ny, fB, id, x, y, z, out[0], out[1], out[2]);
+}
 
 int orc_t_thread_guard(const orc_config *c, int order, int x, int y, int z)
 {
@@ -1087,12 +1142,9 @@ HState hlld_load(const Grid &g, const double *Q, double bx, size_t t, int o1, in
     double const Ent = 0.5 * s.d * sqmag(s.vx, s.vy, s.vz) + magE(bx, s.by, s.bz);
     s.p          = fmax(pressure_from_de(s.E, s.E - Ent, s.ge * s.d, g.gamma), TINY);
   } else {
-    double pressure = s.E - 0.5 * s.d * sqmag(s.vx, s.vy, s.vz);
-    pressure -= magE(bx, s.by, s.bz);
-    s.p = fmax((g.gamma - 1.) * pressure, TINY);
+    s.p = pressure_primitive(s.E, s.d, s.vx, s.vy, s.vz, g.gamma, true, bx, s.by, s.bz);
   }
-  double pt = s.p + magE(bx, s.by, s.bz);  // mhd_utilities.h computeTotalPressure
-  s.pt      = fmax(pt, TINY);
+  s.pt = total_pressure(s.p, bx, s.by, s.bz);
   return s;
 }
 HFlux hlld_nonstar(const HState &s, double bx)
@@ -1199,7 +1251,7 @@ double hlld_middle_speed(const HState &sL, const HState &sR, const HSpeeds &sp)
 // hlld_cuda.cu approximateStarWaveSpeed: the Alfven wave bounding one star region (side -1 / +1)
 double hlld_star_speed(const HStar &st, const HSpeeds &sp, double bx, double side)
 {
-  return sp.M + side * (fabs(bx) / sqrt(fmax(st.d, TINY)));
+  return sp.M + side * alfven_speed(bx, st.d);
 }
 // hlld_cuda.cu starTotalPressure: total pressure in the star regions
 double hlld_pt_star(const HState &sL, const HState &sR, const HSpeeds &sp)

@@ -96,6 +96,24 @@ void orc_t_calc_interface_linear(const orc_config *c, const double *cell, const 
 void orc_t_plm_limit_interfaces(const orc_config *c, double *l_iph, double *r_imh, const double *cell_im1,
                                 const double *cell_i, const double *cell_ip1);                         /* :686-723 */
 
+/* ---- hydro / MHD utilities on the path (hydro_utilities.h, mhd_utilities.h), for the reference's
+ * utility unit tests (src/utils/hydro_utilities_tests.cpp, mhd_utilities_tests.cu) ---- */
+double orc_t_pressure_primitive(double E, double d, double vx, double vy, double vz, double gamma, int mhd, double bx,
+                                double by, double bz);
+double orc_t_energy_primitive(double P, double d, double vx, double vy, double vz, double gamma, int mhd, double bx,
+                              double by, double bz);
+double orc_t_pressure_from_de(double E, double U_total, double U_advected, double gamma);
+double orc_t_kinetic_energy(double d, double vx, double vy, double vz);
+double orc_t_magnetic_energy(double bx, double by, double bz);
+double orc_t_total_pressure(double p, double bx, double by, double bz);
+double orc_t_fast_magnetosonic(double d, double p, double bx, double by, double bz, double gamma);
+double orc_t_slow_magnetosonic(double d, double p, double bx, double by, double bz, double gamma);
+double orc_t_alfven_speed(double bx, double d);
+/* the three cell-centred fields of cell (x, y, z) at flat index id of a grid with the given
+ * x / y strides and n_cells per field, magnetic_x at field fB */
+void orc_t_cell_centered_b(const double *U, size_t id, int x, int y, int z, size_t n_cells, int nx, int ny, int fB,
+                           double *out);
+
 /* ---- HLLD building blocks, for the reference's HLLD-internal unit tests
  * (src/riemann_solvers/hlld_cuda_tests.cu:1877-2400).  Packed in the member order of
  * mhd::internal::State (9 doubles), StarState (6), DoubleStarState (6), Flux (7), Speeds (5). ---- */

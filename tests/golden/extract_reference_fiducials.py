@@ -397,6 +397,48 @@ def hlld_internal_cases(src_dir: Path) -> dict:
     return {"params": params, "tests": tests, "source": "src/riemann_solvers/hlld_cuda_tests.cu:1811-2400"}
 
 
+def _vectors(body: str) -> dict:
+    """Every `std::vector<double> [const] name{...}` of a test body, by name."""
+    return {m.group(1): [_cpp_value(v, {}) for v in m.group(2).split(",") if v.strip()]
+            for m in re.finditer(r"std::vector<double>\s+(?:const\s+)?(\w+)\s*\{([^}]*)\}", body)}
+
+
+def utility_cases(src_dir: Path) -> dict:
+    """The unit tests of the hydro and MHD utility functions that the VL step calls (for the MHD
+    and the hydro build where the fiducials differ): the shared TestParams vectors and per test
+    its fiducial vector, its multipliers (`coef` scalars or vectors) and the first case it loops
+    from."""
+    out = {}
+    for key, rel in (("hydro_utilities", "utils/hydro_utilities_tests.cpp"),
+                     ("mhd_utilities", "utils/mhd_utilities_tests.cu")):
+        raw = (src_dir / rel).read_text()
+        for build, defined in (("mhd", {"MHD"}), ("hydro", set())):
+            src = re.sub(r"//[^\n]*", "", _preprocess(raw, defined))
+            i = src.index("struct TestParams")
+            params = _vectors(src[i:_matching(src, src.index("{", i)) + 1])
+            params["gamma"] = 5.0 / 3.0
+            tests = {}
+            for m in re.finditer(r"TEST\((\w+),\s*(\w+)\)", src):
+                j = src.index("{", m.end())
+                body = src[j:_matching(src, j) + 1]
+                coef = re.search(r"double const coef\s*=\s*([-+0-9.eE]+)", body)
+                start = re.search(r"for \(size_t i = (\d+);", body)
+                consts = {}
+                for c in re.finditer(r"(?:double|Real|size_t)\s+const\s+([^;]+);", body):
+                    for part in c.group(1).split(","):
+                        k, _, v = part.partition("=")
+                        try:
+                            consts[k.strip()] = _cpp_value(v, consts)
+                        except Exception:
+                            pass
+                tests[m.group(1) + "." + m.group(2)] = {
+                    "vectors": _vectors(body), "coef": float(coef.group(1)) if coef else None,
+                    "start": int(start.group(1)) if start else 0, "consts": consts}
+            out.setdefault(key, {})[build] = {"params": params, "tests": tests}
+        out[key]["source"] = "src/" + rel
+    return out
+
+
 def main() -> None:
     root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     src = root / "src"
@@ -410,6 +452,7 @@ def main() -> None:
         "hllc": hllc_cases(src),
         "hlld": hlld_cases(src),
         "hlld_internal": hlld_internal_cases(src),
+        "utilities": utility_cases(src),
         "mhd_unit": mhd_unit_cases(src),
     }
     out = HERE / "reference_fiducials.json"
