@@ -3,7 +3,8 @@
 The reference has no random-field initial condition, so these generators are new: a
 lognormal density and k^-2 velocity fields for the turbulence-like hydro box, a curl of a
 k^-3 vector potential for MHD (spectra summed over shells of |k|), the Sod tube, and the Sedov-like blasts and rotated Sod
-tubes of the serving workload.  Every array is field-major [f, z, y, x] with ghost cells,
+tubes of the serving workload.  `linear_wave` restates the reference's Linear_Wave initial
+condition, on which its system tests measure the scheme's error.  Every array is field-major [f, z, y, x] with ghost cells,
 matching U[f*n_cells + x + y*nx + z*nx*ny].
 """
 from __future__ import annotations
@@ -138,6 +139,50 @@ def sod_1d(nx: int = 100, ng: int = 4, gamma: float = 1.4, dual_energy: bool = F
         if dual_energy:
             U[nf - 1, mask] = p / (gamma - 1.0)
     return np.ascontiguousarray(U), dx
+
+
+def linear_wave(nx: int, ny: int, nz: int, ng: int, dx: float, dy: float, dz: float, *, gamma: float, rho: float,
+                P: float, A: float, eigen: dict, vx: float = 0.0, B=(0.0, 0.0, 0.0), pitch: float = 0.0,
+                yaw: float = 0.0, wave_length: float = 1.0, mhd: bool = False, bounds=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """Linear wave initial condition (src/grid/initial_conditions.cpp:302-425 Grid3D::Linear_Wave):
+    a background state (rho, vx, P, B) plus A * sin(k x_rot) times the right eigenvector `eigen`
+    (keys rho, MomentumX/Y/Z, E, and Bx/By/Bz for MHD), along the direction rotated by pitch and
+    yaw; k = 2 pi / wave_length.  Cell-centred positions x = bound + dx (i - ng) + dx / 2.  As in
+    the reference, the face fields are set from the same cell-centred sine on the real cells
+    only and the hydro fields on the real cells plus the first lower ghost layer; fill the ghost
+    cells (periodic) before the first step.  Returns U[f, z, y, x] with ghost cells."""
+    sy, cy, sp, cp = math.sin(yaw), math.cos(yaw), math.sin(pitch), math.cos(pitch)
+    kw = 2.0 * math.pi / wave_length
+    Nx, Ny, Nz = nx + 2 * ng, ny + 2 * ng, nz + 2 * ng
+    nf = n_fields(False, mhd)
+    U = np.zeros((nf, Nz, Ny, Nx))
+    x = bounds[0] + dx * (np.arange(Nx) - ng) + 0.5 * dx
+    y = bounds[1] + dy * (np.arange(Ny) - ng) + 0.5 * dy
+    z = bounds[2] + dz * (np.arange(Nz) - ng) + 0.5 * dz
+    Z, Y, X = np.meshgrid(z, y, x, indexing="ij")
+    sine = np.sin((cp * (X * cy + Y * sy) + Z * sp) * kw)
+    e = {k: float(eigen.get(k, 0.0)) for k in ("rho", "MomentumX", "MomentumY", "MomentumZ", "E", "Bx", "By", "Bz")}
+    if mhd:
+        r = (slice(ng, Nz - ng), slice(ng, Ny - ng), slice(ng, Nx - ng))
+        bx = B[0] + A * e["Bx"] * sine[r]
+        by = B[1] + A * e["By"] * sine[r]
+        bz = B[2] + A * e["Bz"] * sine[r]
+        U[5][r] = bx * cp * cy - by * sy - bz * sp * cy
+        U[6][r] = bx * cp * sy + by * cy - bz * sp * sy
+        U[7][r] = bx * sp + bz * cp
+    h = (slice(ng - 1, Nz - ng), slice(ng - 1, Ny - ng), slice(ng - 1, Nx - ng))
+    sh = sine[h]
+    U[0][h] = rho + A * e["rho"] * sh
+    mx = rho * vx + A * e["MomentumX"] * sh
+    my = A * e["MomentumY"] * sh
+    mz = A * e["MomentumZ"] * sh
+    U[1][h] = mx * cp * cy - my * sy - mz * sp * cy
+    U[2][h] = mx * cp * sy + my * cy - mz * sp * sy
+    U[3][h] = mx * sp + mz * cp
+    U[4][h] = P / (gamma - 1.0) + 0.5 * rho * vx * vx + A * sh * e["E"]
+    if mhd:
+        U[4][h] += 0.5 * (B[0] * B[0] + B[1] * B[1] + B[2] * B[2])
+    return np.ascontiguousarray(U)
 
 
 def sedov_box(n: int, ng: int, rng: np.random.Generator, gamma: float = 5.0 / 3.0, energy: float = 1.0,

@@ -218,7 +218,7 @@ def _test_bodies(s: str, suite: str) -> dict:
     """{test name: body} of the TEST_F / TEST blocks of one suite, comments removed."""
     s = re.sub(r"//[^\n]*", "", s)
     out = {}
-    for m in re.finditer(rf"TEST(?:_F)?\({suite},\s*(\w+)\)", s):
+    for m in re.finditer(rf"TEST(?:_F|_P)?\({suite},\s*(\w+)\)", s):
         i = s.index("{", m.end())
         out[m.group(1)] = s[i:_matching(s, i) + 1]
     return out
@@ -287,18 +287,32 @@ def mhd_unit_cases(src_dir: Path) -> dict:
 
 
 def _preprocess(src: str, defined: set) -> str:
-    """The source with `#ifdef` / `#ifndef` / `#else` / `#endif` branches resolved for the given
-    macros (other directives dropped)."""
-    out, stack = [], []
+    """The source with `#ifdef` / `#ifndef` / `#if defined(X)` / `#elif defined(X)` / `#else` /
+    `#endif` branches resolved for the given macros (other directives dropped)."""
+    def cond_of(expr: str) -> bool:
+        m = re.fullmatch(r"\s*(?:defined\s*\(\s*(\w+)\s*\)|defined\s+(\w+)|(\w+))\s*", expr)
+        return bool(m) and (m.group(1) or m.group(2) or m.group(3)) in defined
+
+    out, stack = [], []  # entries: [this branch active, some branch taken]
     for line in src.splitlines():
         t = line.strip()
         m = re.match(r"#\s*(ifdef|ifndef)\s+(\w+)", t)
         if m:
-            cond = (m.group(2) in defined) == (m.group(1) == "ifdef")
-            stack.append([cond, all(c for c, _ in stack)])
+            c = (m.group(2) in defined) == (m.group(1) == "ifdef")
+            stack.append([c, c])
+            continue
+        m = re.match(r"#\s*if\s+(.*)", t)
+        if m:
+            c = cond_of(re.sub(r"//.*", "", m.group(1)))
+            stack.append([c, c])
+            continue
+        m = re.match(r"#\s*elif\s+(.*)", t)
+        if m:
+            c = not stack[-1][1] and cond_of(re.sub(r"//.*", "", m.group(1)))
+            stack[-1] = [c, stack[-1][1] or c]
             continue
         if re.match(r"#\s*else\b", t):
-            stack[-1][0] = not stack[-1][0]
+            stack[-1] = [not stack[-1][1], True]
             continue
         if re.match(r"#\s*endif\b", t):
             stack.pop()
@@ -439,6 +453,62 @@ def utility_cases(src_dir: Path) -> dict:
     return out
 
 
+def hydro_system_cases(src_dir: Path) -> dict:
+    """The analytic hydro system tests (src/system_tests/hydro_system_tests.cpp): the linear
+    sound and contact waves on 64 x 32 x 32 cells run for one wave period (expected step count,
+    per-field L1 bound, bound on the norm of the L1 vector and on the maximum error, per
+    reconstruction), and the 3D sound wave at t = 0.05 against the analytic sine (settings from
+    its input file)."""
+    raw = (src_dir / "system_tests/hydro_system_tests.cpp").read_text()
+    out = {"linear_waves": {}, "source": "src/system_tests/hydro_system_tests.cpp:99-306"}
+    for recon in ("PCM", "PLMC", "PPMC"):
+        src = re.sub(r"//[^\n]*", "", _preprocess(raw, {recon}))
+        allowed = {k: float(v) for k, v in re.findall(r"double static constexpr (allowedL1Error|allowedError)\s*=\s*"
+                                                      r"([-+0-9.eE]+)", src)}
+        i = src.index("void Set_Launch_Params")
+        body = src[i:_matching(src, src.index("{", i)) + 1]
+        setup = {k: _cpp_value(v, {}) for k, v in re.findall(r"(?:size_t|double) const (N|domain|gamma)\s*=\s*([^;]+);",
+                                                            body)}
+        waves = {}
+        for name, tb in _test_bodies(src, "tHYDROtMHDSYSTEMLinearWavesParameterizedMpi").items():
+            consts = {}
+            for c in re.finditer(r"(?:double|int) const (\w+)\s*=\s*([^;]+);", tb):
+                consts[c.group(1)] = _cpp_value(c.group(2), consts)
+            call = re.search(r"runL1ErrorTest\(([^,]+),\s*([^)]+)\)", tb)
+            scale = lambda e: _cpp_value(e, allowed)
+            waves[name] = {"wave_speed": consts["waveSpeed"], "n_steps": int(consts["numTimeSteps"]),
+                           "eigen": {k[len("rEigenVec_"):]: v for k, v in consts.items() if k.startswith("rEigenVec_")},
+                           "vx": consts.get("velocityX", 0.0),
+                           "max_l1": scale(call.group(1)), "max_error": scale(call.group(2))}
+        out["linear_waves"][recon] = {"setup": setup, "waves": waves}
+    src = re.sub(r"//[^\n]*", "", _preprocess(raw, set()))
+    tb = _test_bodies(src, "tHYDROtMHDSYSTEMSoundWave3D")["CorrectInputExpectCorrectOutput"]
+    consts = {}
+    for c in re.finditer(r"double (?:const )?(\w+)\s*=\s*([^;]+);", tb):
+        try:
+            consts[c.group(1)] = _cpp_value(c.group(2), consts)
+        except Exception:
+            pass
+    settings = {}
+    for line in (src_dir / "system_tests/input_files/tHYDROtMHDSYSTEMSoundWave3D_CorrectInputExpectCorrectOutput.txt"
+                 ).read_text().splitlines():
+        k, eq, v = line.partition("=")
+        if eq and not line.startswith("#"):
+            try:
+                settings[k.strip()] = float(v.strip().strip("'"))
+            except ValueError:
+                pass
+    # the reference loosens the tolerance per reconstruction in its MHD build ("about the error
+    # between PCM and PPMP in hydro"); its hydro build (PLMC) keeps the plain one
+    pcm = re.sub(r"//[^\n]*", "", _preprocess(raw, {"MHD", "PCM"}))
+    pcm_body = _test_bodies(pcm, "tHYDROtMHDSYSTEMSoundWave3D")["CorrectInputExpectCorrectOutput"]
+    pcm_tol = float(re.findall(r"tolerance\s*=\s*([-+0-9.eE]+)\s*;", pcm_body)[-1])
+    out["sound_wave_3d"] = {"time": consts["time"], "amplitude": consts["amplitude"],
+                            "tolerance": {"PCM": pcm_tol, "PLMC": consts["tolerance"], "PPMC": consts["tolerance"]},
+                            "settings": settings, "source": "src/system_tests/hydro_system_tests.cpp:99-132"}
+    return out
+
+
 def main() -> None:
     root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     src = root / "src"
@@ -453,6 +523,7 @@ def main() -> None:
         "hlld": hlld_cases(src),
         "hlld_internal": hlld_internal_cases(src),
         "utilities": utility_cases(src),
+        "hydro_system": hydro_system_cases(src),
         "mhd_unit": mhd_unit_cases(src),
     }
     out = HERE / "reference_fiducials.json"

@@ -1,0 +1,76 @@
+"""The reference's analytic hydro system tests run through the oracle (CPU only), with the
+reference hydro build's scheme (PLMC + HLLC, src/builds make.type.hydro):
+
+* linear sound and contact waves on 64 x 32 x 32 cells for the time the wave needs to cross
+  the box (src/system_tests/hydro_system_tests.cpp:136-306): the exact step count the
+  reference expects, each field's L1 change, the norm of the L1 vector and the largest change
+  within the reference's bounds;
+* the 3D sound wave (hydro_system_tests.cpp:99-132) against the analytic travelling sine.
+
+Parameters and bounds come from tests/golden/reference_fiducials.json.
+"""
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from helpers import l1_errors, linear_wave_setup, real_slice, run_reference_loop
+
+SYS = json.loads((Path(__file__).parent / "golden" / "reference_fiducials.json").read_text())["hydro_system"]
+NG = {"PCM": 2, "PLMC": 3, "PPMC": 4}
+
+
+def _oracle_box(o, recon, shape, ng, dx, gamma):
+    Nx, Ny, Nz = shape
+    return o.config(Nx, Ny, Nz, ng, 5, recon={"PCM": o.PCM, "PLMC": o.PLMC, "PPMC": o.PPMC}[recon], solver=o.HLLC,
+                    gamma=gamma, dx=dx, dy=dx, dz=dx)
+
+
+@pytest.mark.parametrize("wave", ["SoundWaveRightMovingCorrectInputExpectCorrectOutput",
+                                  "HydroContactWaveCorrectInputExpectCorrectOutput"])
+def test_linear_wave_oracle(oracle_lib, wave):
+    o, recon = oracle_lib, "PLMC"
+    lw = SYS["linear_waves"][recon]
+    w = lw["waves"][wave]
+    ng = NG[recon]
+    U, shape, dx, tout = linear_wave_setup(lw["setup"], w, ng)
+    cfg = _oracle_box(o, recon, shape, ng, dx, lw["setup"]["gamma"])
+    U = np.ascontiguousarray(U.ravel())
+    o.set_boundaries(cfg, U, (1,) * 6)
+    U0 = U.copy()
+    n, t = run_reference_loop(lambda dt: o.vl_step_3d(cfg, U, dt), lambda: o.calc_dt(cfg, U),
+                              lambda: o.set_boundaries(cfg, U, (1,) * 6), tout)
+    assert n == w["n_steps"] and t == tout, (n, t)
+    Nx, Ny, Nz = shape
+    l1, norm, worst = l1_errors(U0.reshape(5, Nz, Ny, Nx), U.reshape(5, Nz, Ny, Nx), ng)
+    assert (l1 < w["max_l1"]).all() and norm < w["max_l1"] and worst < w["max_error"], (l1, norm, worst)
+
+
+def test_sound_wave_3d_oracle(oracle_lib):
+    """64^3 sound wave (A = 1e-5, P = 0.6, c = 1) at t = 0.05: density and x momentum at every
+    real cell within 1e-7 of the analytic sine (hydro build tolerance)."""
+    o, recon = oracle_lib, "PLMC"
+    sw = SYS["sound_wave_3d"]
+    st = sw["settings"]
+    n, ng = int(st["nx"]), NG[recon]
+    dx = st["xlen"] / n
+    eigen = {k[len("rEigenVec_"):]: v for k, v in st.items() if k.startswith("rEigenVec_")}
+    from cholla_gb300 import ics
+
+    U = ics.linear_wave(n, n, n, ng, dx, dx, dx, gamma=st["gamma"], rho=st["rho"], P=st["P"], A=st["A"], eigen=eigen)
+    N = n + 2 * ng
+    cfg = _oracle_box(o, recon, (N, N, N), ng, dx, st["gamma"])
+    U = np.ascontiguousarray(U.ravel())
+    o.set_boundaries(cfg, U, (1,) * 6)
+    _, t = run_reference_loop(lambda dt: o.vl_step_3d(cfg, U, dt), lambda: o.calc_dt(cfg, U),
+                              lambda: o.set_boundaries(cfg, U, (1,) * 6), sw["time"])
+    assert t == sw["time"]
+    U = U.reshape(5, N, N, N)[real_slice(ng)]
+    kx = 2 * math.pi * dx
+    phase = kx * 0.5 - 1.0 * sw["time"] * 2 * math.pi
+    expect = sw["amplitude"] * np.sin(kx * np.arange(n) + phase)  # along x, the same in y and z
+    for field, const in ((0, 1.0), (1, 0.0)):
+        err = np.abs(U[field] - (const + expect[None, None, :])).max()
+        assert err <= sw["tolerance"][recon], (field, err)

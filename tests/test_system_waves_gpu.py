@@ -1,0 +1,140 @@
+"""The reference's analytic hydro system tests through libchollagb on the GPU
+(src/system_tests/hydro_system_tests.cpp:99-306), HLLC, every reconstruction:
+
+* linear sound (both directions) and contact waves on 64 x 32 x 32 cells for one crossing of
+  the box, driven like the reference's main loop through the drop-in C ABI (exact FP64) and
+  through the box engine (exact and fast FP64, dt on the device, clamped to the output time):
+  the reference's step count, each field's L1 change, the norm of the L1 vector and the largest
+  change within the bounds the reference sets for that reconstruction;
+* the exact form's final state equal, bit for bit, to the oracle's after the full crossing;
+* the 64^3 sound wave at t = 0.05 within the analytic travelling sine's tolerance: 1e-7 (the
+  hydro build's) for PLMC and PPMC, 1e-6 for PCM (the reference's PCM tolerance; its hydro
+  build is PLMC and never runs this test with PCM).
+
+Mixed precision is not held to these bounds: its single-precision fluxes cannot resolve a
+1e-6 perturbation to 1e-8 (its accuracy contract is a 1e-5 relative L1 density error).
+"""
+import json
+import math
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from helpers import l1_errors, linear_wave_setup, real_slice, run_reference_loop
+
+pytestmark = pytest.mark.gpu
+
+SYS = json.loads((Path(__file__).parent / "golden" / "reference_fiducials.json").read_text())["hydro_system"]
+NG = {"PCM": 2, "PLMC": 3, "PPMC": 4}
+WAVES = ["SoundWaveRightMovingCorrectInputExpectCorrectOutput", "SoundWaveLeftMovingCorrectInputExpectCorrectOutput",
+         "HydroContactWaveCorrectInputExpectCorrectOutput"]
+
+
+def _scheme(recon, precision="fp64"):
+    from cholla_gb300 import integrator as I
+
+    return I.Scheme(reconstruction=recon, riemann_solver="HLLC", dual_energy=False, gamma=5.0 / 3.0,
+                    precision=precision)
+
+
+def _dropin_run(cuda, recon, U, shape, dx, tout, gamma):
+    from cholla_gb300 import integrator as I
+
+    Nx, Ny, Nz = shape
+    ng = NG[recon]
+    I.set_scheme(_scheme(recon))
+    G = cuda.from_numpy(U.copy()).cuda()
+    fill = lambda: I.Set_Boundaries(G, Nx, Ny, Nz, ng, 5, (1,) * 6)  # noqa: E731
+    fill()
+    U0 = G.cpu().numpy()
+    n, t = run_reference_loop(
+        lambda dt: I.VL_Algorithm_3D_CUDA(G, None, Nx, Ny, Nz, 0, 0, 0, ng, dx, dx, dx, 0, 0, 0, dt, 5, 0, 0.0),
+        lambda: I.Calc_dt_GPU(G, Nx, Ny, Nz, ng, 5, dx, dx, dx, gamma), fill, tout)
+    return U0, G.cpu().numpy(), n, t
+
+
+def _check_bounds(U0, U1, ng, w):
+    l1, norm, worst = l1_errors(U0, U1, ng)
+    assert (l1 < w["max_l1"]).all(), (l1, w["max_l1"])
+    assert norm < w["max_l1"] and worst < w["max_error"], (norm, worst, w)
+
+
+@pytest.mark.parametrize("recon", ["PCM", "PLMC", "PPMC"])
+@pytest.mark.parametrize("wave", WAVES)
+def test_linear_wave_dropin_exact(cuda, recon, wave):
+    lw = SYS["linear_waves"][recon]
+    w = lw["waves"][wave]
+    U, shape, dx, tout = linear_wave_setup(lw["setup"], w, NG[recon])
+    U0, U1, n, t = _dropin_run(cuda, recon, U, shape, dx, tout, lw["setup"]["gamma"])
+    assert n == w["n_steps"] and t == tout, (n, t)
+    _check_bounds(U0, U1, NG[recon], w)
+
+
+def test_linear_wave_exact_matches_oracle_bitwise(cuda, oracle_lib):
+    """PLMC sound wave: the drop-in exact path and the oracle, each driven by its own dt
+    reduction, end the 214-step crossing on the same state bit for bit."""
+    o, recon = oracle_lib, "PLMC"
+    lw = SYS["linear_waves"][recon]
+    w = lw["waves"][WAVES[0]]
+    ng = NG[recon]
+    U, shape, dx, tout = linear_wave_setup(lw["setup"], w, ng)
+    _, got, n, _ = _dropin_run(cuda, recon, U, shape, dx, tout, lw["setup"]["gamma"])
+    Nx, Ny, Nz = shape
+    cfg = o.config(Nx, Ny, Nz, ng, 5, recon=o.PLMC, solver=o.HLLC, gamma=lw["setup"]["gamma"], dx=dx, dy=dx, dz=dx)
+    Uo = np.ascontiguousarray(U.ravel())
+    o.set_boundaries(cfg, Uo, (1,) * 6)
+    no, _ = run_reference_loop(lambda dt: o.vl_step_3d(cfg, Uo, dt), lambda: o.calc_dt(cfg, Uo),
+                               lambda: o.set_boundaries(cfg, Uo, (1,) * 6), tout)
+    want = Uo.reshape(5, Nz, Ny, Nx)
+    assert n == no == w["n_steps"]
+    rs = real_slice(ng)
+    assert np.array_equal(got[rs].view(np.int64), want[rs].view(np.int64))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fast"])
+@pytest.mark.parametrize("recon", ["PLMC", "PPMC"])
+@pytest.mark.parametrize("wave", [WAVES[0], WAVES[2]])
+def test_linear_wave_box_engine(cuda, precision, recon, wave):
+    """The box engine keeps dt on the device and clamps the last step to the output time: after
+    the reference's step count less one the time is short of it, after one more it is there."""
+    from cholla_gb300.engine import Box
+
+    lw = SYS["linear_waves"][recon]
+    w = lw["waves"][wave]
+    ng = NG[recon]
+    U, (Nx, Ny, Nz), dx, tout = linear_wave_setup(lw["setup"], w, ng)
+    G = cuda.from_numpy(U.copy()).cuda()
+    box = Box(Nx, Ny, Nz, ng, dx, dx, dx, _scheme(recon, precision))  # padded sizes, as the reference's H.nx
+    try:
+        box.set_time(0.0, tout)
+        box.advance(G, w["n_steps"] - 1)  # each step fills the ghost cells before it reads them
+        t_before, _ = box.time()
+        box.advance(G, 1)
+        t_end, _ = box.time()
+    finally:
+        box.close()
+    assert t_before < tout and t_end == tout, (t_before, t_end, tout)
+    _check_bounds(U, G.cpu().numpy(), ng, w)  # real cells: the initial condition itself
+
+
+@pytest.mark.parametrize("recon", ["PCM", "PLMC", "PPMC"])
+def test_sound_wave_3d_dropin(cuda, recon):
+    sw = SYS["sound_wave_3d"]
+    st = sw["settings"]
+    n, ng = int(st["nx"]), NG[recon]
+    dx = st["xlen"] / n
+    eigen = {k[len("rEigenVec_"):]: v for k, v in st.items() if k.startswith("rEigenVec_")}
+    from cholla_gb300 import ics
+
+    U = ics.linear_wave(n, n, n, ng, dx, dx, dx, gamma=st["gamma"], rho=st["rho"], P=st["P"], A=st["A"], eigen=eigen)
+    N = n + 2 * ng
+    _, U1, _, t = _dropin_run(cuda, recon, U, (N, N, N), dx, sw["time"], st["gamma"])
+    assert t == sw["time"]
+    R = U1[real_slice(ng)]
+    kx = 2 * math.pi * dx
+    phase = kx * 0.5 - 1.0 * sw["time"] * 2 * math.pi
+    expect = sw["amplitude"] * np.sin(kx * np.arange(n) + phase)
+    for field, const in ((0, 1.0), (1, 0.0)):
+        err = np.abs(R[field] - (const + expect[None, None, :])).max()
+        assert err <= sw["tolerance"][recon], (field, err)
