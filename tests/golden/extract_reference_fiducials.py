@@ -509,6 +509,80 @@ def hydro_system_cases(src_dir: Path) -> dict:
     return out
 
 
+def mhd_system_cases(src_dir: Path) -> dict:
+    """The MHD linear-wave system tests at angles (src/system_tests/mhd_system_tests.cpp:30-541):
+    fast, slow and Alfven waves in both directions and the contact wave, each along x, y and z
+    (the instantiated pitch / yaw / domain / direction tuples), with the step count per
+    direction and the L1 / maximum-error bounds per reconstruction; and the N = 16 runs whose
+    L1 norm must be four times the N = 32 one (second-order convergence)."""
+    raw = (src_dir / "system_tests/mhd_system_tests.cpp").read_text()
+    base = re.sub(r"//[^\n]*", "", _preprocess(raw, {"MHD", "PLMC"}))
+    inst = base[base.index("INSTANTIATE_TEST_SUITE_P(, tMHDSYSTEMLinearWavesParameterizedAngle"):]
+    inst = inst[:inst.index(";")]
+    angles = [[_cpp_value(v, {}) for v in t.split(",")]
+              for t in re.findall(r"std::make_tuple\(([^)]*)\)", inst)]
+    tests = {}
+    for recon in ("PCM", "PLMC", "PPMC"):
+        src = re.sub(r"//[^\n]*", "", _preprocess(raw, {"MHD", recon}))
+        for name, tb in _test_bodies(src, "tMHDSYSTEMLinearWavesParameterizedAngle").items():
+            consts = {}
+            for c in re.finditer(r"double const (\w+)\s*=\s*([^;]+);", tb):
+                try:
+                    consts[c.group(1)] = _cpp_value(c.group(2), consts)
+                except NameError:  # values read back from the runner (the L2 norms)
+                    pass
+            call = re.search(r"Set_Launch_Params\(([^;]*)\);", tb).group(1)
+            args = [a.strip() for a in call.split(",")]
+            entry = tests.setdefault(name, {
+                "wave_speed": consts["waveSpeed"],
+                "n_steps": [int(v) for v in _braces(tb, "numTimeSteps")],
+                "eigen": {k[len("rEigenVec_"):]: v for k, v in consts.items() if k.startswith("rEigenVec_")},
+                "vx": _cpp_value(args[13], consts) if len(args) > 13 else 0.0,
+                "N": int(args[14]) if len(args) > 14 else 32, "bounds": {}})
+            b = re.search(r"runL1ErrorTest\(([^,]+),\s*([^)]+)\)", tb)
+            entry["bounds"][recon] = [_cpp_value(b.group(1), {}), _cpp_value(b.group(2), {})]
+            conv = re.search(r"high_res_l2norms\[\"(\w+)_\"", tb)
+            if conv and "Convergence" in name:
+                tol = re.search(r"Check_Results\(\s*([-+0-9.eE]+),[^;]*,\s*\"\",\s*([-+0-9.eE]+)\)", tb)
+                entry["convergence"] = {"of": conv.group(1), "ratio": float(tol.group(1)), "tolerance": float(tol.group(2))}
+            elif conv:
+                entry["key"] = conv.group(1)
+    return {"angles": angles, "tests": tests, "B": [1.0, 1.5, 0.0], "gamma": 5.0 / 3.0, "amplitude": 1e-6,
+            "source": "src/system_tests/mhd_system_tests.cpp:30-541"}
+
+
+def _settings(path: Path) -> dict:
+    out = {}
+    for line in path.read_text().splitlines():
+        k, eq, v = line.partition("=")
+        if eq and not line.lstrip().startswith("#"):
+            try:
+                out[k.strip()] = float(v.strip().strip("'"))
+            except ValueError:
+                pass
+    return out
+
+
+def constant_state_cases(src_dir: Path) -> dict:
+    """The constant-state system tests: the settings of their input files and, for the hydro
+    one, the analytic values the test checks (hydro_system_tests.cpp:84-97).  The MHD ones
+    (mhd_system_tests.cpp:710-722) compare with data files absent here; a constant state is
+    their only possible answer."""
+    inp = src_dir / "system_tests/input_files"
+    raw = re.sub(r"//[^\n]*", "", (src_dir / "system_tests/hydro_system_tests.cpp").read_text())
+    body = _test_bodies(raw, "tHYDROtMHDSYSTEMConstant")["CorrectInputExpectCorrectOutput"]
+    expect = {k: float(v) for k, v in re.findall(r"analyticConstant\(testObject,\s*\"(\w+)\",\s*([-+0-9.eE]+)\)", body)}
+    return {
+        "hydro": {"settings": _settings(inp / "tHYDROtMHDSYSTEMConstant_CorrectInputExpectCorrectOutput.txt"),
+                  "expect": expect, "abs_tolerance": 5.0e-12},
+        "mhd_field": {"settings": _settings(
+            inp / "tMHDSYSTEMParameterizedMpi_ConstantWithMagneticFieldCorrectInputExpectCorrectOutput.txt")},
+        "mhd_zero_field": {"settings": _settings(
+            inp / "tMHDSYSTEMParameterizedMpi_ConstantWithZeroMagneticFieldCorrectInputExpectCorrectOutput.txt")},
+        "source": "src/system_tests/hydro_system_tests.cpp:84-97, mhd_system_tests.cpp:710-722",
+    }
+
+
 def main() -> None:
     root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
     src = root / "src"
@@ -524,6 +598,8 @@ def main() -> None:
         "hlld_internal": hlld_internal_cases(src),
         "utilities": utility_cases(src),
         "hydro_system": hydro_system_cases(src),
+        "mhd_system": mhd_system_cases(src),
+        "constant_states": constant_state_cases(src),
         "mhd_unit": mhd_unit_cases(src),
     }
     out = HERE / "reference_fiducials.json"

@@ -70,3 +70,64 @@ def l1_errors(U0: np.ndarray, U1: np.ndarray, ng: int, n_hydro: int = 5):
     d = np.abs(U1[rs][:n_hydro] - U0[rs][:n_hydro])
     l1 = np.array([math.fsum(f.ravel()) / f.size for f in d])
     return l1, float(np.sqrt((l1 ** 2).sum())), float(d.max())
+
+
+def mhd_wave_setup(sysd: dict, case: dict, angle, N: int | None = None):
+    """(real cells per side, dx, tout, pitch, yaw) of one MHD linear-wave system test
+    (src/system_tests/mhd_system_tests.cpp:39-121): N^3 real cells of side 0.5 with the wave's
+    direction (1 x, 2 y, 3 z) doubled, run for the time the wave needs to cross the long side."""
+    pitch, yaw, domain, direction = angle
+    N = N or case["N"]
+    n = [N, N, N]
+    n[int(direction) - 1] *= 2
+    return n, domain / N, 2 * domain / case["wave_speed"], pitch, yaw
+
+
+def mhd_wave_state(sysd: dict, case: dict, angle, ng: int, N: int | None = None):
+    """(U, padded shape, dx, tout): the Linear_Wave state of the test, background B = (1, 1.5, 0)
+    rotated with the wave by (pitch, yaw)."""
+    from cholla_gb300 import ics
+
+    n, dx, tout, pitch, yaw = mhd_wave_setup(sysd, case, angle, N)
+    U = ics.linear_wave(n[0], n[1], n[2], ng, dx, dx, dx, gamma=sysd["gamma"], rho=1.0, P=1.0 / sysd["gamma"],
+                        A=sysd["amplitude"], eigen=case["eigen"], vx=case["vx"], B=tuple(sysd["B"]), pitch=pitch,
+                        yaw=yaw, mhd=True)
+    return U, (n[0] + 2 * ng, n[1] + 2 * ng, n[2] + 2 * ng), dx, tout
+
+
+def l1_errors_mhd(U0: np.ndarray, U1: np.ndarray, ng: int):
+    """The system tests' L1 errors for an MHD state: the five hydro fields over the real cells,
+    each face field over the faces the reference writes out (one more, the lower face of the
+    first real cell, along its own direction); the norm of the eight and the largest change."""
+    l1h, _, worst = l1_errors(U0, U1, ng)
+    out = list(l1h)
+    for k in range(3):
+        sl = [slice(ng, -ng)] * 3  # [z, y, x]
+        sl[2 - k] = slice(ng - 1, -ng)
+        d = np.abs(U1[(5 + k, *sl)] - U0[(5 + k, *sl)])
+        out.append(math.fsum(d.ravel()) / d.size)
+        worst = max(worst, float(d.max()))
+    l1 = np.array(out)
+    return l1, float(np.sqrt((l1 ** 2).sum())), worst
+
+
+def constant_state(st: dict, ng: int, mhd: bool = False, dual_energy: bool = False):
+    """(U, padded shape, dx) of the Constant initial condition (src/grid/initial_conditions.cpp:
+    180-238) on the settings of a system-test input file: uniform rho, momenta rho v, energy
+    P / (gamma - 1) + rho v^2 / 2 (without a magnetic term, as the reference writes it) and
+    uniform face fields; filled everywhere, which the periodic ghost fill would give anyway."""
+    n = [int(st["nx"]), int(st["ny"]), int(st["nz"])]
+    shape = tuple(k + 2 * ng for k in n)
+    nf = 5 + (3 if mhd else 0) + (1 if dual_energy else 0)
+    U = np.zeros((nf, shape[2], shape[1], shape[0]))
+    rho, g = st["rho"], st["gamma"]
+    v = (st["vx"], st["vy"], st["vz"])
+    U[0] = rho
+    for k in range(3):
+        U[1 + k] = rho * v[k]
+    U[4] = st["P"] / (g - 1.0) + 0.5 * rho * (v[0] * v[0] + v[1] * v[1] + v[2] * v[2])
+    if mhd:
+        U[5], U[6], U[7] = st["Bx"], st["By"], st["Bz"]
+    if dual_energy:
+        U[nf - 1] = st["P"] / (g - 1.0)
+    return np.ascontiguousarray(U), shape, st["xlen"] / n[0]

@@ -31,11 +31,10 @@ WAVES = ["SoundWaveRightMovingCorrectInputExpectCorrectOutput", "SoundWaveLeftMo
          "HydroContactWaveCorrectInputExpectCorrectOutput"]
 
 
-def _scheme(recon, precision="fp64"):
+def _scheme(recon, precision="fp64", gamma=5.0 / 3.0):
     from cholla_gb300 import integrator as I
 
-    return I.Scheme(reconstruction=recon, riemann_solver="HLLC", dual_energy=False, gamma=5.0 / 3.0,
-                    precision=precision)
+    return I.Scheme(reconstruction=recon, riemann_solver="HLLC", dual_energy=False, gamma=gamma, precision=precision)
 
 
 def _dropin_run(cuda, recon, U, shape, dx, tout, gamma):
@@ -43,7 +42,7 @@ def _dropin_run(cuda, recon, U, shape, dx, tout, gamma):
 
     Nx, Ny, Nz = shape
     ng = NG[recon]
-    I.set_scheme(_scheme(recon))
+    I.set_scheme(_scheme(recon, gamma=gamma))
     G = cuda.from_numpy(U.copy()).cuda()
     fill = lambda: I.Set_Boundaries(G, Nx, Ny, Nz, ng, 5, (1,) * 6)  # noqa: E731
     fill()
@@ -138,3 +137,51 @@ def test_sound_wave_3d_dropin(cuda, recon):
     for field, const in ((0, 1.0), (1, 0.0)):
         err = np.abs(R[field] - (const + expect[None, None, :])).max()
         assert err <= sw["tolerance"][recon], (field, err)
+
+
+CONST = json.loads((Path(__file__).parent / "golden" / "reference_fiducials.json").read_text())["constant_states"]
+
+
+def test_constant_state_dropin_exact(cuda):
+    """hydro_system_tests.cpp:84-97 through the drop-in C ABI (PLMC + HLLC, 32^3, to t = 100):
+    the real cells keep their values bit for bit, the test's analytic values within 5e-12."""
+    from helpers import constant_state
+
+    st, recon = CONST["hydro"]["settings"], "PLMC"
+    U, shape, dx = constant_state(st, NG[recon])
+    U0, U1, n, t = _dropin_run(cuda, recon, U, shape, dx, st["tout"], st["gamma"])
+    assert t == st["tout"] and n > 10
+    rs = real_slice(NG[recon])
+    assert np.array_equal(U1[rs].view(np.int64), U0[rs].view(np.int64))
+    for f, name in enumerate(["density", "momentum_x", "momentum_y", "momentum_z", "Energy"]):
+        assert np.abs(U1[f][rs[1:]] - CONST["hydro"]["expect"][name]).max() <= CONST["hydro"]["abs_tolerance"]
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp64_fast", "mixed"])
+def test_constant_state_box_engine(cuda, precision):
+    """The same constant state (with dual energy) through the box engine in each arithmetic
+    form: equal fluxes on both faces of every cell leave every conserved value, the thermal
+    energy included, unchanged bit for bit."""
+    from cholla_gb300 import integrator as I
+    from cholla_gb300.engine import Box
+    from helpers import constant_state
+
+    st, recon = CONST["hydro"]["settings"], "PPMC"
+    ng = NG[recon]
+    U, (Nx, Ny, Nz), dx = constant_state(st, ng, dual_energy=True)
+    G = cuda.from_numpy(U.copy()).cuda()
+    s = I.Scheme(reconstruction=recon, riemann_solver="HLLC", dual_energy=True, gamma=st["gamma"],
+                 precision=precision)
+    box = Box(Nx, Ny, Nz, ng, dx, dx, dx, s)
+    try:
+        box.set_time(0.0, st["tout"])
+        t, n = 0.0, 0
+        while t < st["tout"] and n < 1000:
+            box.advance(G, 1)
+            t, _ = box.time()
+            n += 1
+    finally:
+        box.close()
+    assert t == st["tout"] and n > 10, (t, n)
+    rs = real_slice(ng)
+    assert np.array_equal(G.cpu().numpy()[rs].view(np.int64), U[rs].view(np.int64))
