@@ -11,6 +11,7 @@ import json
 from pathlib import Path
 
 import numpy as np
+import pytest
 
 from helpers import l1_errors_mhd, mhd_wave_state, run_reference_loop
 
@@ -56,3 +57,24 @@ def test_constant_states_oracle(oracle_lib):
         R = U.reshape(8, Nz, Ny, Nx)[real_slice(ng)]
         R0 = U0.reshape(8, Nz, Ny, Nx)[real_slice(ng)]
         assert np.array_equal(R.view(np.int64), R0.view(np.int64)), key
+
+
+
+@pytest.mark.parametrize("di", [1, 2], ids=["y", "z"])
+def test_fast_wave_low_resolution_rotated_oracle(oracle_lib, di):
+    """The N = 16 fast wave of the convergence test along y (yaw = pi/2) and z (pitch = pi/2):
+    the reference's step count for that direction and its bounds for the low-resolution run
+    (mhd_system_tests.cpp:391-425), checking the rotated initial condition on the CPU."""
+    o = oracle_lib
+    case, angle, ng = SYS["tests"]["FastMagnetosonicWaveExpectSecondOrderConvergence"], SYS["angles"][di], 4
+    U, (Nx, Ny, Nz), dx, tout = mhd_wave_state(SYS, case, angle, ng)
+    cfg = o.config(Nx, Ny, Nz, ng, 8, mhd=True, recon=o.PLMC, solver=o.HLLD, gamma=SYS["gamma"], dx=dx, dy=dx, dz=dx)
+    U = np.ascontiguousarray(U.ravel())
+    o.set_boundaries(cfg, U, (1,) * 6)
+    U0 = U.copy()
+    n, t = run_reference_loop(lambda dt: o.vl_step_3d(cfg, U, dt), lambda: o.calc_dt(cfg, U),
+                              lambda: o.set_boundaries(cfg, U, (1,) * 6), tout)
+    assert n == case["n_steps"][di] and t == tout, (n, t)
+    l1, norm, worst = l1_errors_mhd(U0.reshape(8, Nz, Ny, Nx), U.reshape(8, Nz, Ny, Nx), ng)
+    max_l1, max_error = case["bounds"]["PLMC"]
+    assert (l1 < max_l1).all() and norm < max_l1 and worst < max_error, (l1, norm, worst)
