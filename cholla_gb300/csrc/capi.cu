@@ -23,6 +23,7 @@ thread_local std::string g_err;
 
 struct ScratchSlot {
   int nx = 0, ny = 0, nz = 0, nf = 0, mhd = -1;
+  int dev = -1;  // device the scratch was allocated on
   cgb::Scratch s{};
   bool live = false;
 };
@@ -42,6 +43,9 @@ int cuda_fail(cudaError_t e, const char *where)
 void free_slot(ScratchSlot &sl)
 {
   if (!sl.live) return;
+  int cur = -1;
+  bool const other = cudaGetDevice(&cur) == cudaSuccess && sl.dev >= 0 && sl.dev != cur;
+  if (other) cudaSetDevice(sl.dev);  // free on the device that owns the scratch
   cudaFree(sl.s.Uh);
   cudaFree(sl.s.GEp);
   cudaFree(sl.s.Epre);
@@ -53,12 +57,17 @@ void free_slot(ScratchSlot &sl)
   cudaFree(sl.s.status);
   cudaFree(sl.s.W);
   cudaFree(sl.s.mhd);
-  sl   = ScratchSlot{};
+  if (other) cudaSetDevice(cur);
+  sl = ScratchSlot{};
 }
 
 int ensure_slot(int nx, int ny, int nz, int nf, int mhd)
 {
-  if (g_slot.live && g_slot.nx == nx && g_slot.ny == ny && g_slot.nz == nz && g_slot.nf == nf && g_slot.mhd == mhd)
+  int dev       = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (g_slot.live && g_slot.nx == nx && g_slot.ny == ny && g_slot.nz == nz && g_slot.nf == nf &&
+      g_slot.mhd == mhd && g_slot.dev == dev)
     return CGB_OK;
   free_slot(g_slot);
   size_t const n = (size_t)nx * ny * nz;
@@ -86,7 +95,7 @@ int ensure_slot(int nx, int ny, int nz, int nf, int mhd)
     free_slot(g_slot);
     return fail(CGB_ERR_NOMEM, "scratch allocation failed");
   }
-  g_slot.nx = nx, g_slot.ny = ny, g_slot.nz = nz, g_slot.nf = nf, g_slot.mhd = mhd;
+  g_slot.nx = nx, g_slot.ny = ny, g_slot.nz = nz, g_slot.nf = nf, g_slot.mhd = mhd, g_slot.dev = dev;
   return CGB_OK;
 }
 
@@ -137,6 +146,24 @@ constexpr int kMaxDevices = 64;
 void *g_static_pool[kMaxDevices] = {};  // device address of g_static_scratch, per device ordinal
 
 size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+// One-word results of the device reductions (0: CFL max, 1: max |div B|), one per device.
+unsigned long long *g_word[kMaxDevices][2] = {};
+
+int device_word(int which, unsigned long long **word)
+{
+  int dev       = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return fail(CGB_ERR_ARGS, "device ordinal beyond the result-word table");
+  if (!g_word[dev][which] && cudaMalloc(&g_word[dev][which], sizeof(unsigned long long)) != cudaSuccess) {
+    g_word[dev][which] = nullptr;
+    cudaGetLastError();
+    return fail(CGB_ERR_NOMEM, "reduction result word");
+  }
+  *word = g_word[dev][which];
+  return CGB_OK;
+}
 
 // Bytes of static scratch one step of box b needs in the given arithmetic, and (base != null)
 // the Scratch pointers laid out from base, each array on a 256-byte boundary.
@@ -324,9 +351,9 @@ int cgb_calc_dt_gpu(const double *d_conserved, int nx, int ny, int nz, int n_gho
   b.dx = dx, b.dy = dy, b.dz = dz, b.density_floor = 0;
   if (b.mhd && !(ny > 1 && nz > 1)) return fail(CGB_ERR_ARGS, "MHD boxes are 3D");
   if (!(nx > 1 && ((ny == 1 && nz == 1) || (ny > 1 && nz > 1)))) return fail(CGB_ERR_ARGS, "1D or 3D boxes only");
-  static unsigned long long *d_dti = nullptr;
-  if (!d_dti && cudaMalloc(&d_dti, sizeof(unsigned long long)) != cudaSuccess)
-    return fail(CGB_ERR_NOMEM, "dt buffer");
+  unsigned long long *d_dti = nullptr;
+  int const rw               = device_word(0, &d_dti);
+  if (rw != CGB_OK) return rw;
   if (!g_dti_host && cudaMallocHost(&g_dti_host, sizeof(unsigned long long)) != cudaSuccess)
     return fail(CGB_ERR_NOMEM, "pinned dt buffer");
   cudaError_t e = b.mhd ? cgb::mhd_calc_dt(b, d_conserved, d_dti, g_stream)
@@ -381,9 +408,9 @@ int cgb_max_magnetic_divergence(const double *d_conserved, int nx, int ny, int n
   int const rc = make_box(b, nx, ny, nz, n_ghost, n_fields, dx, dy, dz, 0.0, g_scheme);
   if (rc != CGB_OK) return rc;
   if (ny < 2 || nz < 2) return fail(CGB_ERR_ARGS, "MHD boxes are 3D");
-  static unsigned long long *d_div = nullptr;
-  if (!d_div && cudaMalloc(&d_div, sizeof(unsigned long long)) != cudaSuccess)
-    return fail(CGB_ERR_NOMEM, "divergence buffer");
+  unsigned long long *d_div = nullptr;
+  int const rw               = device_word(1, &d_div);
+  if (rw != CGB_OK) return rw;
   if (!g_dti_host && cudaMallocHost(&g_dti_host, sizeof(unsigned long long)) != cudaSuccess)
     return fail(CGB_ERR_NOMEM, "pinned result buffer");
   cudaError_t e = cgb::mhd_max_divb(b, d_conserved, d_div, g_stream);

@@ -71,8 +71,9 @@ const char *cgb_version(void);
  * Same arguments and meaning; d_grav_potential, x/y/z_off, x/y/zbound, custom_grav and
  * host_grav_potential belong to the gravity build (out of scope) and must be NULL / 0
  * (non-zero custom_grav or a non-NULL potential returns CGB_ERR_UNSUPPORTED).
- * Scratch is allocated on the first call for a box shape and kept until
- * cgb_free_memory_vl_3d(); a call with a new shape reallocates it. */
+ * Scratch is allocated on the current device on the first call for a box shape and kept
+ * until cgb_free_memory_vl_3d(); a call with a new shape, or on another device, reallocates
+ * it (one scratch per process, as the reference's file-scope scratch). */
 int cgb_vl_algorithm_3d(double *d_conserved, double *d_grav_potential, int nx, int ny, int nz, int x_off, int y_off,
                         int z_off, int n_ghost, double dx, double dy, double dz, double xbound, double ybound,
                         double zbound, double dt, int n_fields, int custom_grav, double density_floor,
@@ -103,8 +104,9 @@ int cgb_vl_algorithm_3d_static(double *d_conserved, double *d_grav_potential, in
 int cgb_vl_algorithm_1d(double *d_conserved, int nx, int x_off, int n_ghost, double dx, double xbound, double dt,
                         int n_fields, int custom_grav);
 
-/* Replaces Free_Memory_VL_3D (VL_3D_cuda.cu:362-377).  Frees the library's scratch only:
- * unlike the reference it does not free the caller's d_conserved. */
+/* Replaces Free_Memory_VL_3D (VL_3D_cuda.cu:362-377).  Frees the library's scratch only,
+ * on the device that owns it whatever the current device: unlike the reference it does not
+ * free the caller's d_conserved. */
 int cgb_free_memory_vl_3d(void);
 
 /* Replaces Calc_dt_GPU (src/hydro/hydro_cuda.h:69-70, hydro_cuda.cu:562-597): writes the
