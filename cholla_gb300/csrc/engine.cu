@@ -27,10 +27,11 @@ struct cgb_box {
   double *dt_t = nullptr;  // device [dt, t]
   double t_end = 0.0;
   bool dti_valid = false;
-  // graph of one step (captured on first use per state pointer and stream)
+  // graph of one step (captured on first use per state pointer, stream and CFL number)
   cudaGraphExec_t graph = nullptr;
   double *graph_U = nullptr;
   cudaStream_t graph_stream = nullptr;
+  double graph_cfl = 0.0;  // the CFL number is baked into the captured dt launch
   bool use_graph = false;
   // timing: four events per timed step (before predictor, after predictor, after corrector,
   // after finalize), recorded on the launching stream and read back by cgb_box_kernel_times
@@ -190,7 +191,9 @@ int cgb_box_set_time(cgb_box *bx, double t, double t_end)
 {
   if (!bx) return box_fail(nullptr, CGB_ERR_ARGS, "null box");
   double h[2] = {0.0, t};
-  if (cudaMemcpy(bx->dt_t, h, 16, cudaMemcpyHostToDevice) != cudaSuccess)
+  // steps still queued on the box's stream read [dt, t]: let them finish before it is replaced
+  if (cudaStreamSynchronize(bx->last_stream) != cudaSuccess ||
+      cudaMemcpy(bx->dt_t, h, 16, cudaMemcpyHostToDevice) != cudaSuccess)
     return box_fail(bx, CGB_ERR_CUDA, "set_time copy");
   bx->t_end = t_end;
   if (bx->graph) {  // t_end is baked into the captured launch
@@ -245,7 +248,7 @@ int cgb_box_advance(cgb_box *bx, double *d_conserved, int n_steps, double c_cfl,
     bx->dti_valid = true;
   }
   bool const graph_ok = bx->use_graph && !bx->timing && st != nullptr;
-  if (graph_ok && (!bx->graph || bx->graph_U != d_conserved || bx->graph_stream != st)) {
+  if (graph_ok && (!bx->graph || bx->graph_U != d_conserved || bx->graph_stream != st || bx->graph_cfl != c_cfl)) {
     if (bx->graph) cudaGraphExecDestroy(bx->graph), bx->graph = nullptr;
     cudaGraph_t g;
     if ((e = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal)) != cudaSuccess)
@@ -259,6 +262,7 @@ int cgb_box_advance(cgb_box *bx, double *d_conserved, int n_steps, double c_cfl,
     if (e != cudaSuccess) return box_fail(bx, CGB_ERR_CUDA, cudaGetErrorString(e));
     bx->graph_U      = d_conserved;
     bx->graph_stream = st;
+    bx->graph_cfl    = c_cfl;
   }
   for (int i = 0; i < n_steps; i++) {
     if (graph_ok) {
