@@ -15,7 +15,7 @@ HERE = Path(__file__).resolve().parent
 LIBPATH = HERE / "_build" / "libcholla_oracle.so"
 
 PCM, PLMC, PPMC = 0, 1, 2
-HLLC, ROE, HLLD = 0, 1, 2
+HLLC, ROE, HLLD, HLL, EXACT = 0, 1, 2, 3, 4
 
 
 class orc_config(C.Structure):
@@ -50,6 +50,8 @@ def lib() -> C.CDLL:
             "orc_hllc": [P, _DP, _DP, _DP, C.c_int],
             "orc_roe": [P, _DP, _DP, _DP, C.c_int],
             "orc_hlld": [P, _DP, _DP, _DP, _DP, C.c_int],
+            "orc_hll": [P, _DP, _DP, _DP, C.c_int],
+            "orc_exact": [P, _DP, _DP, _DP, C.c_int],
             "orc_ct_electric_fields": [P, _DP, _DP, _DP, _DP, _DP],
             "orc_update_magnetic": [P, _DP, _DP, _DP, C.c_double],
             "orc_update_half": [P, _DP, _DP, _DP, _DP, _DP, C.c_double],

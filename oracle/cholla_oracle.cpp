@@ -1101,6 +1101,205 @@ void orc_roe(const orc_config *c, const double *QL, const double *QR, double *F,
   });
 }
 
+// src/riemann_solvers/hll_cuda.cu:19-268 Calculate_HLL_Fluxes_CUDA: the two-wave flux with
+// Davis's wave-speed estimates (the slower of the two left-going and the faster of the two
+// right-going acoustic speeds).  Interface states are conserved; every cell is computed.
+void orc_hll(const orc_config *c, const double *QL, const double *QR, double *F, int dir)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int o1, o2, o3;
+  perm(dir, o1, o2, o3);
+  double const gamma = g.gamma;
+  par_cells(g, [&](size_t tid) {
+    int const nq = 5 + g.ns + (g.de ? 1 : 0);
+    double ql[5 + MAXS + 1], qr[5 + MAXS + 1], fl[5 + MAXS + 1], fr[5 + MAXS + 1];
+    size_t idx[5 + MAXS + 1];
+    idx[0] = 0, idx[1] = (size_t)o1, idx[2] = (size_t)o2, idx[3] = (size_t)o3, idx[4] = 4;
+    for (int s = 0; s < g.ns; s++) idx[5 + s] = (size_t)(5 + s);
+    if (g.de) idx[nq - 1] = (size_t)g.fGE;
+    for (int k = 0; k < nq; k++) ql[k] = QL[idx[k] * n + tid], qr[k] = QR[idx[k] * n + tid];
+    auto side = [&](const double *q, double *f, double &vx, double &p) {
+      double const d = q[0];
+      vx             = q[1] / d;
+      double const vy = q[2] / d, vz = q[3] / d;
+      if (g.de) {
+        double const E_kin = 0.5 * d * (vx * vx + vy * vy + vz * vz);
+        p                  = pressure_from_de(q[4], q[4] - E_kin, q[nq - 1], gamma);
+      } else {
+        p = (q[4] - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (gamma - 1.0);
+      }
+      p    = fmax(p, TINY);
+      f[0] = q[1];
+      f[1] = q[1] * vx + p;
+      f[2] = q[2] * vx;
+      f[3] = q[3] * vx;
+      f[4] = (q[4] + p) * vx;
+      for (int k = 5; k < nq; k++) f[k] = q[k] * vx;  // scalars and the thermal energy advect
+    };
+    double vxl, pl, vxr, pr;
+    side(ql, fl, vxl, pl);
+    side(qr, fr, vxr, pr);
+    double const cfl = sqrt(gamma * pl / ql[0]), cfr = sqrt(gamma * pr / qr[0]);
+    double const Sl = fmin(vxr - cfr, vxl - cfl);
+    double const Sr = fmax(vxl + cfl, vxr + cfr);
+    for (int k = 0; k < nq; k++) {
+      double out;
+      if (Sl > 0.0) {
+        out = fl[k];
+      } else if (Sr < 0.0) {
+        out = fr[k];
+      } else {
+        out = ((Sr * fl[k]) - (Sl * fr[k]) + Sl * Sr * (qr[k] - ql[k])) / (Sr - Sl);
+      }
+      F[idx[k] * n + tid] = out;
+    }
+  });
+}
+
+// src/riemann_solvers/exact_cuda.cu:19-334 Calculate_Exact_Fluxes_CUDA: the exact Riemann
+// solution (Toro 2009, ch. 4) sampled on the interface, x/t = 0.  Star pressure from the
+// primitive-variable guess (two-shock correction when it is not positive), then Newton with a
+// relative tolerance of 1e-6 and at most 21 passes.  The reference evaluates its fractional
+// powers in single precision (powf), so this restatement does too: its results agree with the
+// reference's to single-precision rounding of those powers, not bit for bit.
+namespace
+{
+inline double fpow(double a, double b) { return (double)powf((float)a, (float)b); }
+
+void exact_pressure_function(double &f, double &fd, double p, double dk, double pk, double ck, double g)
+{
+  if (p <= pk) {  // rarefaction branch
+    f  = (2.0 / (g - 1.0)) * ck * (fpow(p / pk, (g - 1.0) / (2.0 * g)) - 1.0);
+    fd = (1.0 / (dk * ck)) * fpow(p / pk, -((g + 1.0) / (2.0 * g)));
+  } else {  // shock branch
+    double const bk = ((g - 1.0) / (g + 1.0)) * pk;
+    double const q  = sqrt(((2.0 / (g + 1.0)) / dk) / (bk + p));
+    f  = (p - pk) * q;
+    fd = (1.0 - 0.5 * (p - pk) / (bk + p)) * q;
+  }
+}
+
+void exact_star(double &pm, double &vm, double dl, double vl, double pl, double cl, double dr, double vr, double pr,
+                double cr, double g)
+{
+  double const tol = 1.0e-6;
+  double ppv       = 0.5 * (pl + pr) + 0.125 * (vl - vr) * (dl + dr) * (cl + cr);
+  if (ppv < 0.0) ppv = 0.0;
+  double const gl = sqrt((2.0 / ((g + 1.0) * dl)) / (((g - 1.0) / (g + 1.0)) * pl + ppv));
+  double const gr = sqrt((2.0 / ((g + 1.0) * dr)) / (((g - 1.0) / (g + 1.0)) * pr + ppv));
+  double pold     = (gl * pl + gr * pr - (vr - vl)) / (gl + gr);
+  if (pold < 0.0) pold = tol;
+  double fl = 0, fld = 0, fr = 0, frd = 0;
+  for (int it = 0; it <= 20; it++) {
+    exact_pressure_function(fl, fld, pold, dl, pl, cl, g);
+    exact_pressure_function(fr, frd, pold, dr, pr, cr, g);
+    pm                  = pold - (fl + fr + vr - vl) / (fld + frd);
+    double const change = 2.0 * fabs((pm - pold) / (pm + pold));
+    if (change <= tol) break;
+    if (pm < 0.0) pm = tol;
+    pold = pm;
+  }
+  vm = 0.5 * (vl + vr + fr - fl);
+}
+
+// the state on x/t = 0 of the wave pattern with star pressure pm and contact speed vm
+void exact_sample(double pm, double vm, double &d, double &v, double &p, double dl, double vl, double pl, double cl,
+                  double dr, double vr, double pr, double cr, double g)
+{
+  double const gm = (g - 1.0) / (g + 1.0);
+  if (vm >= 0) {  // left of the contact
+    if (pm <= pl) {  // left rarefaction
+      if (vl - cl >= 0) {
+        d = dl, v = vl, p = pl;
+      } else if (vm - cl * fpow(pm / pl, (g - 1.0) / (2.0 * g)) < 0) {
+        d = dl * fpow(pm / pl, 1.0 / g), v = vm, p = pm;
+      } else {  // inside the fan
+        double const c = (2.0 / (g + 1.0)) * (cl + ((g - 1.0) / 2.0) * vl);
+        v = c;
+        d = dl * fpow(c / cl, 2.0 / (g - 1.0));
+        p = pl * fpow(c / cl, 2.0 * g / (g - 1.0));
+      }
+    } else {  // left shock
+      double const sl = vl - cl * sqrt(((g + 1.0) / (2.0 * g)) * (pm / pl) + ((g - 1.0) / (2.0 * g)));
+      if (sl >= 0) {
+        d = dl, v = vl, p = pl;
+      } else {
+        d = dl * (pm / pl + gm) / ((pm / pl) * gm + 1.0), v = vm, p = pm;
+      }
+    }
+  } else {  // right of the contact
+    if (pm > pr) {  // right shock
+      double const sr = vr + cr * sqrt(((g + 1.0) / (2.0 * g)) * (pm / pr) + ((g - 1.0) / (2.0 * g)));
+      if (sr <= 0) {
+        d = dr, v = vr, p = pr;
+      } else {
+        d = dr * (pm / pr + gm) / ((pm / pr) * gm + 1.0), v = vm, p = pm;
+      }
+    } else {  // right rarefaction
+      if (vr + cr <= 0) {
+        d = dr, v = vr, p = pr;
+      } else if (vm + cr * fpow(pm / pr, (g - 1.0) / (2.0 * g)) >= 0) {
+        d = dr * fpow(pm / pr, 1.0 / g), v = vm, p = pm;
+      } else {  // inside the fan
+        double const c = (2.0 / (g + 1.0)) * (cr - ((g - 1.0) / 2.0) * vr);
+        v = -c;
+        d = dr * fpow(c / cr, 2.0 / (g - 1.0));
+        p = pr * fpow(c / cr, 2.0 * g / (g - 1.0));
+      }
+    }
+  }
+}
+}  // namespace
+
+void orc_exact(const orc_config *c, const double *QL, const double *QR, double *F, int dir)
+{
+  Grid g(c);
+  size_t const n = g.n;
+  int o1, o2, o3;
+  perm(dir, o1, o2, o3);
+  double const gamma = g.gamma;
+  par_cells(g, [&](size_t tid) {
+    auto load = [&](const double *Q, double &d, double &vx, double &vy, double &vz, double &p, double &ge,
+                    double *sc) {
+      d  = Q[tid];
+      vx = Q[(size_t)o1 * n + tid] / d;
+      vy = Q[(size_t)o2 * n + tid] / d;
+      vz = Q[(size_t)o3 * n + tid] / d;
+      double const E = Q[4 * n + tid];
+      ge             = 0.0;
+      if (g.de) {
+        double const E_kin = 0.5 * d * (vx * vx + vy * vy + vz * vz);
+        double const dge   = Q[(size_t)g.fGE * n + tid];
+        p                  = pressure_from_de(E, E - E_kin, dge, gamma);
+        ge                 = dge / d;
+      } else {
+        p = (E - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (gamma - 1.0);
+      }
+      p = fmax(p, TINY);
+      for (int s = 0; s < g.ns; s++) sc[s] = Q[(size_t)(5 + s) * n + tid] / d;
+    };
+    double dl, vxl, vyl, vzl, pl, gel, scl[MAXS];
+    double dr, vxr, vyr, vzr, pr, ger, scr[MAXS];
+    load(QL, dl, vxl, vyl, vzl, pl, gel, scl);
+    load(QR, dr, vxr, vyr, vzr, pr, ger, scr);
+    double const cl = sqrt(gamma * pl / dl), cr = sqrt(gamma * pr / dr);
+    double pm = 0, vm = 0, ds = 0, vs = 0, ps = 0;
+    exact_star(pm, vm, dl, vxl, pl, cl, dr, vxr, pr, cr, gamma);
+    exact_sample(pm, vm, ds, vs, ps, dl, vxl, pl, cl, dr, vxr, pr, cr, gamma);
+    F[tid]                  = ds * vs;
+    F[(size_t)o1 * n + tid] = ds * vs * vs + ps;
+    bool const left         = vs >= 0;  // the transverse velocities and passive quantities advect upwind
+    double const vy = left ? vyl : vyr, vz = left ? vzl : vzr;
+    F[(size_t)o2 * n + tid] = ds * vs * vy;
+    F[(size_t)o3 * n + tid] = ds * vs * vz;
+    for (int s = 0; s < g.ns; s++) F[(size_t)(5 + s) * n + tid] = ds * vs * (left ? scl[s] : scr[s]);
+    if (g.de) F[(size_t)g.fGE * n + tid] = ds * vs * (left ? gel : ger);
+    double const Es = (ps / (gamma - 1.0)) + 0.5 * ds * (vs * vs + vy * vy + vz * vz);
+    F[4 * n + tid]  = (Es + ps) * vs;
+  });
+}
+
 // src/riemann_solvers/hlld_cuda.cu:31-508 (mhd::Calculate_HLLD_Fluxes_CUDA and mhd::internal)
 namespace
 {
@@ -2025,6 +2224,14 @@ int orc_vl_step_3d(const orc_config *c, double *U, double dt)
       orc_roe(c, QLx.data(), QRx.data(), Fx.data(), 0);
       orc_roe(c, QLy.data(), QRy.data(), Fy.data(), 1);
       orc_roe(c, QLz.data(), QRz.data(), Fz.data(), 2);
+    } else if (c->solver == ORC_HLL) {
+      orc_hll(c, QLx.data(), QRx.data(), Fx.data(), 0);
+      orc_hll(c, QLy.data(), QRy.data(), Fy.data(), 1);
+      orc_hll(c, QLz.data(), QRz.data(), Fz.data(), 2);
+    } else if (c->solver == ORC_EXACT) {
+      orc_exact(c, QLx.data(), QRx.data(), Fx.data(), 0);
+      orc_exact(c, QLy.data(), QRy.data(), Fy.data(), 1);
+      orc_exact(c, QLz.data(), QRz.data(), Fz.data(), 2);
     } else {
       orc_hlld(c, QLx.data(), QRx.data(), Ub + (size_t)g.fB * n, Fx.data(), 0);
       orc_hlld(c, QLy.data(), QRy.data(), Ub + (size_t)(g.fB + 1) * n, Fy.data(), 1);
@@ -2079,6 +2286,10 @@ int orc_vl_step_1d(const orc_config *c, double *U, double dt)
   auto riemann = [&]() {
     if (c->solver == ORC_ROE) {
       orc_roe(c, QL.data(), QR.data(), F.data(), 0);
+    } else if (c->solver == ORC_HLL) {
+      orc_hll(c, QL.data(), QR.data(), F.data(), 0);
+    } else if (c->solver == ORC_EXACT) {
+      orc_exact(c, QL.data(), QR.data(), F.data(), 0);
     } else {
       orc_hllc(c, QL.data(), QR.data(), F.data(), 0);
     }

@@ -22,7 +22,7 @@ extern "C" {
 #endif
 
 enum { ORC_PCM = 0, ORC_PLMC = 1, ORC_PPMC = 2 };
-enum { ORC_HLLC = 0, ORC_ROE = 1, ORC_HLLD = 2 };
+enum { ORC_HLLC = 0, ORC_ROE = 1, ORC_HLLD = 2, ORC_HLL = 3, ORC_EXACT = 4 };
 
 typedef struct {
   int nx, ny, nz;     /* padded sizes (ghosts included) */
@@ -32,7 +32,7 @@ typedef struct {
   int de;             /* dual energy on */
   int mhd;            /* MHD (face-centred B, CT) */
   int recon;          /* ORC_PCM / ORC_PLMC / ORC_PPMC */
-  int solver;         /* ORC_HLLC / ORC_ROE / ORC_HLLD */
+  int solver;         /* ORC_HLLC / ORC_ROE / ORC_HLLD / ORC_HLL / ORC_EXACT */
   int density_floor_on;
   double gamma;
   double dx, dy, dz;
@@ -47,6 +47,10 @@ void orc_plmc(const orc_config *c, const double *U, double *QL, double *QR, int 
 void orc_hllc(const orc_config *c, const double *QL, const double *QR, double *F, int dir);
 void orc_roe(const orc_config *c, const double *QL, const double *QR, double *F, int dir);
 void orc_hlld(const orc_config *c, const double *QL, const double *QR, const double *Bface, double *F, int dir);
+/* hll_cuda.cu:19-268 and exact_cuda.cu:19-334 (hydro; the exact solver's fractional powers in
+ * single precision, as the reference's powf) */
+void orc_hll(const orc_config *c, const double *QL, const double *QR, double *F, int dir);
+void orc_exact(const orc_config *c, const double *QL, const double *QR, double *F, int dir);
 /* one CT slope at cell (x, y, z) (ct_electric_fields.h:66-120 _ctSlope) */
 double orc_ct_slope(const orc_config *c, const double *flux, const double *U, double flux_sign, int ct_dir, int cq1,
                     int cq2, int fq1, int fq2, int x, int y, int z);
