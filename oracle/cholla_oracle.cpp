@@ -1162,7 +1162,8 @@ void orc_hll(const orc_config *c, const double *QL, const double *QR, double *F,
 // primitive-variable guess (two-shock correction when it is not positive), then Newton with a
 // relative tolerance of 1e-6 and at most 21 passes.  The reference evaluates its fractional
 // powers in single precision (powf), so this restatement does too: its results agree with the
-// reference's to single-precision rounding of those powers, not bit for bit.
+// reference's to single-precision rounding of those powers, not bit for bit.  (The reference's
+// VL integrator itself does not compile with this solver selected: VL_3D_cuda.cu:149.)
 namespace
 {
 inline double fpow(double a, double b) { return (double)powf((float)a, (float)b); }

@@ -26,7 +26,7 @@ std::vector<CUmodule> g_mods;
 std::map<std::string, CUfunction> g_fn;
 bool g_de = false, g_mhd = false;
 int g_recon = 2;   // 1 PLMC, 2 PPMC
-int g_solver = 0;  // 0 HLLC, 1 ROE, 2 HLLD
+int g_solver = 0;  // 0 HLLC, 1 ROE, 2 HLLD, 3 HLL, 4 exact
 struct Scratch {
   size_t n = 0;
   int nf = 0;
@@ -108,6 +108,8 @@ const char *K_PCM1    = "_Z21PCM_Reconstruction_1DPdS_S_iidi";
 const char *K_HLLC    = "_Z26Calculate_HLLC_Fluxes_CUDAPdS_S_iiiidii";
 const char *K_ROE     = "_Z25Calculate_Roe_Fluxes_CUDAPdS_S_iiiidii";
 const char *K_HLLD    = "_ZN3mhd26Calculate_HLLD_Fluxes_CUDAEPKdS1_S1_Pdidii";
+const char *K_HLL     = "_Z25Calculate_HLL_Fluxes_CUDAPdS_S_iiiidii";
+const char *K_EXACT   = "_Z27Calculate_Exact_Fluxes_CUDAPdS_S_iiiidii";
 const char *K_CT      = "_ZN3mhd28Calculate_CT_Electric_FieldsEPKdS1_S1_S1_Pdiiii";
 const char *K_BUPD    = "_ZN3mhd24Update_Magnetic_Field_3DEPdS0_S0_iiiidddd";
 const char *K_DIVB    = "_ZN3mhd27calculateMagneticDivergenceEPKdPddddiiii";
@@ -133,7 +135,8 @@ int riemann(CUdeviceptr QL, CUdeviceptr QR, CUdeviceptr F, CUdeviceptr Bface, in
 {
   size_t const n = (size_t)nx * ny * nz;
   if (g_solver == 2) return launch(K_HLLD, n, QL, QR, Bface, F, (int)n, gamma, dir, nf);
-  return launch(g_solver == 1 ? K_ROE : K_HLLC, n, QL, QR, F, nx, ny, nz, ng, gamma, dir, nf);
+  const char *k = g_solver == 1 ? K_ROE : g_solver == 3 ? K_HLL : g_solver == 4 ? K_EXACT : K_HLLC;
+  return launch(k, n, QL, QR, F, nx, ny, nz, ng, gamma, dir, nf);
 }
 }  // namespace
 
@@ -158,7 +161,9 @@ int refh_init(const char *variant_dir, const char *variant)
   g_de     = v.find("_de") != std::string::npos;
   g_mhd    = v.rfind("mhd", 0) == 0;
   g_recon  = v.find("plmc") != std::string::npos ? 1 : 2;
-  g_solver = v.find("hlld") != std::string::npos ? 2 : v.find("roe") != std::string::npos ? 1 : 0;
+  auto has = [&v](const char *t) { return v.find(t) != std::string::npos; };
+  // "hllc" and "hlld" contain "hll": test them first
+  g_solver = has("hlld") ? 2 : has("roe") ? 1 : has("exact") ? 4 : (has("_hll") && !has("_hllc")) ? 3 : 0;
   DIR *dir = opendir(variant_dir);
   if (!dir) return err(std::string("no reference cubins at ") + variant_dir);
   while (dirent *e = readdir(dir)) {
