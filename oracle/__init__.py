@@ -14,7 +14,7 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIBPATH = HERE / "_build" / "libcholla_oracle.so"
 
-PCM, PLMC, PPMC = 0, 1, 2
+PCM, PLMC, PPMC, PLMP, PPMP = 0, 1, 2, 3, 4
 HLLC, ROE, HLLD, HLL, EXACT = 0, 1, 2, 3, 4
 
 
@@ -47,6 +47,8 @@ def lib() -> C.CDLL:
             "orc_pcm_3d": [P, _DP, _DP, _DP, _DP, _DP, _DP, _DP],
             "orc_ppmc_vl": [P, _DP, _DP, _DP, C.c_int],
             "orc_plmc": [P, _DP, _DP, _DP, C.c_int],
+            "orc_plmp": [P, _DP, _DP, _DP, C.c_int],
+            "orc_ppmp": [P, _DP, _DP, _DP, C.c_int],
             "orc_hllc": [P, _DP, _DP, _DP, C.c_int],
             "orc_roe": [P, _DP, _DP, _DP, C.c_int],
             "orc_hlld": [P, _DP, _DP, _DP, _DP, C.c_int],
@@ -63,6 +65,7 @@ def lib() -> C.CDLL:
             "orc_set_boundaries": [P, _DP, C.POINTER(C.c_int)],
             "orc_vl_step_3d": [P, _DP, C.c_double],
             "orc_vl_step_1d": [P, _DP, C.c_double],
+            "orc_vl_step_2d": [P, _DP, C.c_double],
             "orc_mt19937_uniform": [C.c_ulonglong, C.c_double, C.c_double, C.c_size_t, _DP],
             "orc_mt19937_32_uniform": [C.c_ulong, C.c_double, C.c_double, C.c_size_t, _DP],
             "orc_ppm_single_variable": [C.c_double] * 5 + [C.POINTER(C.c_double)] * 2,
@@ -143,6 +146,12 @@ def vl_step_3d(cfg: orc_config, U: np.ndarray, dt: float) -> None:
 
 def vl_step_1d(cfg: orc_config, U: np.ndarray, dt: float) -> None:
     rc = lib().orc_vl_step_1d(C.byref(cfg), U, dt)
+    if rc != 0:
+        raise ValueError("oracle rejected the configuration")
+
+
+def vl_step_2d(cfg: orc_config, U: np.ndarray, dt: float) -> None:
+    rc = lib().orc_vl_step_2d(C.byref(cfg), U, dt)
     if rc != 0:
         raise ValueError("oracle rejected the configuration")
 

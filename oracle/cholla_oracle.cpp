@@ -807,6 +807,131 @@ void orc_plmc(const orc_config *c, const double *U, double *QL, double *QR, int 
   });
 }
 
+}  // extern "C"
+
+// ---- primitive-limited reconstructions: PLMP and PPMP ----
+// src/reconstruction/plmp_cuda.cu:21-328 PLMP_cuda and ppmp_cuda.cu:28-683 PPMP_cuda as the VL
+// build compiles them (no half-step tracing, no flattening or steepening macros): every
+// primitive (density, the three velocities, pressure, scalars and GasEnergy per unit mass) is
+// limited on its own, with no characteristic projection.
+namespace
+{
+// One cell's primitives as both kernels load them (plmp_cuda.cu:108-133, ppmp_cuda.cu:155-180):
+// velocities by division, pressure from the total energy (dual energy: the select of
+// Get_Pressure_From_DE) floored at TINY; q = {d, v1, v2, v3, p, scalars..., ge}.
+struct PrimQ {
+  double q[5 + MAXS + 1];
+};
+
+PrimQ load_prim_q(const Grid &g, const double *U, size_t id, int o1, int o2, int o3)
+{
+  PrimQ s;
+  size_t const n = g.n;
+  double const d = U[id];
+  double const vx = U[(size_t)o1 * n + id] / d, vy = U[(size_t)o2 * n + id] / d, vz = U[(size_t)o3 * n + id] / d;
+  double p;
+  if (g.de) {
+    double const E    = U[4 * n + id];
+    double const Ekin = 0.5 * d * (vx * vx + vy * vy + vz * vz);
+    double const dge  = U[(size_t)g.fGE * n + id];
+    p                 = pressure_from_de(E, E - Ekin, dge, g.gamma);
+    s.q[5 + g.ns]     = dge / d;
+  } else {
+    p = (U[4 * n + id] - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (g.gamma - 1.0);
+  }
+  s.q[0] = d, s.q[1] = vx, s.q[2] = vy, s.q[3] = vz, s.q[4] = fmax(p, TINY);
+  for (int k = 0; k < g.ns; k++) s.q[5 + k] = U[(size_t)(5 + k) * n + id] / d;
+  return s;
+}
+
+// Van Leer-limited slope of a three-point stencil (plmp_cuda.cu:330-365 Interface_Values_PLM,
+// ppmp_cuda.cu:687-720 Calculate_Slope): monotonised central difference with the harmonic mean.
+inline double limited_slope(double qm, double q, double qp)
+{
+  double const dl = q - qm, dr = qp - q, dc = 0.5 * (qp - qm);
+  double const dg = (dl * dr > 0.0) ? 2.0 * dl * dr / (dl + dr) : 0.0;
+  double const a = fmin(fabs(dl), fabs(dr)), b = fmin(fabs(dc), fabs(dg));
+  return sgn_int(dc) * fmin(2.0 * a, b);
+}
+
+// Fryxell et al. (2000) parabola through cell i with the monotonicity constraints
+// (ppmp_cuda.cu:727-752 Interface_Values_PPM).
+void ppm_parabola(double qm, double q, double qp, double sm, double s0, double sp, double &L, double &R)
+{
+  L = 0.5 * (q + qm) - (1.0 / 6.0) * (s0 - sm);
+  R = 0.5 * (qp + q) - (1.0 / 6.0) * (sp - s0);
+  if ((R - q) * (q - L) <= 0) L = R = q;
+  if (6.0 * (R - L) * (q - 0.5 * (L + R)) > (R - L) * (R - L)) L = 3.0 * q - 2.0 * R;
+  if (6.0 * (R - L) * (q - 0.5 * (L + R)) < -(R - L) * (R - L)) R = 3.0 * q - 2.0 * L;
+  L = fmax(fmin(q, qm), L);
+  L = fmin(fmax(q, qm), L);
+  R = fmax(fmin(q, qp), R);
+  R = fmin(fmax(q, qp), R);
+}
+
+// order 1: PLMP (cells 1 .. n-3 along dir), order 2: PPMP (cells 2 .. n-4).  Writes the state on
+// the low side of cell i into QR at i-1 and the state on its high side into QL at i, as conserved
+// variables (plmp_cuda.cu:290-326, ppmp_cuda.cu:645-681).
+template <int order>
+void recon_primitive(const orc_config *c, const double *U, double *QL, double *QR, int dir)
+{
+  Grid g(c);
+  int o1, o2, o3;
+  perm(dir, o1, o2, o3);
+  int const ext   = dir == 0 ? g.nx : dir == 1 ? g.ny : g.nz;
+  size_t const st = dir == 0 ? 1 : dir == 1 ? (size_t)g.nx : (size_t)g.nx * g.ny;
+  int const nq    = 5 + g.ns + (g.de ? 1 : 0);
+  size_t const n  = g.n;
+  par_cells(g, [&](size_t id) {
+    int x, y, z;
+    g.xyz(id, x, y, z);
+    int const a = dir == 0 ? x : dir == 1 ? y : z;
+    if (a < order || a >= ext - order - 1) return;
+    PrimQ s[2 * order + 1];
+    for (int j = 0; j <= 2 * order; j++) s[j] = load_prim_q(g, U, id - order * st + j * st, o1, o2, o3);
+    double lo[5 + MAXS + 1], hi[5 + MAXS + 1];
+    for (int k = 0; k < nq; k++) {
+      if (order == 1) {
+        double const dm = limited_slope(s[0].q[k], s[1].q[k], s[2].q[k]);
+        lo[k]           = s[1].q[k] - 0.5 * dm;
+        hi[k]           = s[1].q[k] + 0.5 * dm;
+      } else {
+        double const sm = limited_slope(s[0].q[k], s[1].q[k], s[2].q[k]);
+        double const s0 = limited_slope(s[1].q[k], s[2].q[k], s[3].q[k]);
+        double const sp = limited_slope(s[2].q[k], s[3].q[k], s[4].q[k]);
+        ppm_parabola(s[1].q[k], s[2].q[k], s[3].q[k], sm, s0, sp, lo[k], hi[k]);
+      }
+    }
+    lo[0] = fmax(lo[0], TINY), hi[0] = fmax(hi[0], TINY);
+    lo[4] = fmax(lo[4], TINY), hi[4] = fmax(hi[4], TINY);
+    auto put = [&](double *Q, size_t at, const double *v) {
+      double const d        = v[0];
+      Q[at]                 = d;
+      Q[(size_t)o1 * n + at] = d * v[1];
+      Q[(size_t)o2 * n + at] = d * v[2];
+      Q[(size_t)o3 * n + at] = d * v[3];
+      Q[4 * n + at]         = v[4] / (g.gamma - 1.0) + 0.5 * d * (v[1] * v[1] + v[2] * v[2] + v[3] * v[3]);
+      for (int k = 0; k < g.ns; k++) Q[(size_t)(5 + k) * n + at] = d * v[5 + k];
+      if (g.de) Q[(size_t)g.fGE * n + at] = d * v[5 + g.ns];
+    };
+    put(QR, id - st, lo);
+    put(QL, id, hi);
+  });
+}
+}  // namespace
+
+void orc_plmp(const orc_config *c, const double *U, double *QL, double *QR, int dir)
+{
+  recon_primitive<1>(c, U, QL, QR, dir);
+}
+
+void orc_ppmp(const orc_config *c, const double *U, double *QL, double *QR, int dir)
+{
+  recon_primitive<2>(c, U, QL, QR, dir);
+}
+
+extern "C" {
+
 // src/riemann_solvers/hllc_cuda.cu:19-307 Calculate_HLLC_Fluxes_CUDA
 void orc_hllc(const orc_config *c, const double *QL, const double *QR, double *F, int dir)
 {
@@ -2032,6 +2157,14 @@ double orc_calc_dt(const orc_config *c, const double *U)
       P        = fmax(P, TINY);
       double const cs = sqrt(d_inv * gamma * P);
       m               = fmax(m, (fabs(vx) + cs) / dx);
+    } else if (g.nz == 1) {  // hydro_cuda.cu:473-512 Calc_dt_2D
+      if (!(x > ng - 1 && x < g.nx - ng && y > ng - 1 && y < g.ny - ng)) continue;
+      double const d = U[id], d_inv = 1.0 / d;
+      double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+      double P = (U[4 * n + id] - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (gamma - 1.0);
+      P        = fmax(P, TINY);
+      double const cs = sqrt(d_inv * gamma * P);
+      m               = fmax(m, fmax((fabs(vx) + cs) / dx, (fabs(vy) + cs) / dy));
     } else {
       if (!(x > ng - 1 && x < g.nx - ng && y > ng - 1 && y < g.ny - ng && z > ng - 1 && z < g.nz - ng)) continue;
       double const d = U[id], d_inv = 1.0 / d;
@@ -2209,6 +2342,7 @@ int orc_vl_step_3d(const orc_config *c, double *U, double dt)
   if (g.mhd && g.de) return -1;  // the reference's MHD+DE flux indexing is out of bounds
   if (g.mhd && c->solver != ORC_HLLD) return -1;
   if (!g.mhd && c->solver == ORC_HLLD) return -1;
+  if (g.mhd && (c->recon == ORC_PLMP || c->recon == ORC_PPMP)) return -1;  // hydro-only kernels
   if (g.ns > MAXS) return -1;
   size_t const n = g.n;
   std::vector<double> Uh((size_t)g.nf * n, 0.0);
@@ -2252,6 +2386,14 @@ int orc_vl_step_3d(const orc_config *c, double *U, double dt)
     orc_plmc(c, Uh.data(), QLx.data(), QRx.data(), 0);
     orc_plmc(c, Uh.data(), QLy.data(), QRy.data(), 1);
     orc_plmc(c, Uh.data(), QLz.data(), QRz.data(), 2);
+  } else if (c->recon == ORC_PLMP) {
+    orc_plmp(c, Uh.data(), QLx.data(), QRx.data(), 0);
+    orc_plmp(c, Uh.data(), QLy.data(), QRy.data(), 1);
+    orc_plmp(c, Uh.data(), QLz.data(), QRz.data(), 2);
+  } else if (c->recon == ORC_PPMP) {
+    orc_ppmp(c, Uh.data(), QLx.data(), QRx.data(), 0);
+    orc_ppmp(c, Uh.data(), QLy.data(), QRy.data(), 1);
+    orc_ppmp(c, Uh.data(), QLz.data(), QRz.data(), 2);
   } else {
     orc_ppmc_vl(c, Uh.data(), QLx.data(), QRx.data(), 0);
     orc_ppmc_vl(c, Uh.data(), QLy.data(), QRy.data(), 1);
@@ -2274,6 +2416,9 @@ int orc_vl_step_1d(const orc_config *c, double *U, double dt)
 {
   Grid g(c);
   if (g.mhd || g.ny != 1 || g.nz != 1 || c->solver == ORC_HLLD) return -1;
+  // VL_1D_cuda.cu:69-80 and :112-123 have Riemann branches for the exact solver, Roe and HLLC
+  // only: built with HLL, the 1D integrator computes no fluxes.
+  if (c->solver == ORC_HLL) return -1;
   size_t const n = g.n;
   std::vector<double> Uh((size_t)g.nf * n, 0.0), QL((size_t)g.nf * n, 0.0), QR((size_t)g.nf * n, 0.0),
       F((size_t)g.nf * n, 0.0);
@@ -2287,8 +2432,6 @@ int orc_vl_step_1d(const orc_config *c, double *U, double dt)
   auto riemann = [&]() {
     if (c->solver == ORC_ROE) {
       orc_roe(c, QL.data(), QR.data(), F.data(), 0);
-    } else if (c->solver == ORC_HLL) {
-      orc_hll(c, QL.data(), QR.data(), F.data(), 0);
     } else if (c->solver == ORC_EXACT) {
       orc_exact(c, QL.data(), QR.data(), F.data(), 0);
     } else {
@@ -2321,6 +2464,10 @@ int orc_vl_step_1d(const orc_config *c, double *U, double dt)
     pcm1(Uh.data());
   } else if (c->recon == ORC_PLMC) {
     orc_plmc(c, Uh.data(), QL.data(), QR.data(), 0);
+  } else if (c->recon == ORC_PLMP) {
+    orc_plmp(c, Uh.data(), QL.data(), QR.data(), 0);
+  } else if (c->recon == ORC_PPMP) {
+    orc_ppmp(c, Uh.data(), QL.data(), QR.data(), 0);
   } else {
     orc_ppmc_vl(c, Uh.data(), QL.data(), QR.data(), 0);
   }
@@ -2330,6 +2477,134 @@ int orc_vl_step_1d(const orc_config *c, double *U, double dt)
   if (g.de) {
     orc_de_select(c, U);
     orc_de_sync(c, U);
+  }
+  return 0;
+}
+
+// ---- the 2D VL step ----
+// src/integrators/VL_2D_cuda.cu:25-174 VL_Algorithm_2D_CUDA on an nx x ny grid (nz = 1), with
+// the 2D kernels of VL_2D_cuda.cu:176-258 and hydro_cuda.cu (Update_Conserved_Variables_2D,
+// the 2D dual-energy kernels).  The 2D integrator has no density floor and no HLL branch.
+int orc_vl_step_2d(const orc_config *c, double *U, double dt)
+{
+  Grid g(c);
+  if (g.mhd || g.nz != 1 || g.ny < 2 || g.ns > MAXS) return -1;
+  if (c->solver == ORC_HLLD || c->solver == ORC_HLL) return -1;
+  size_t const n = g.n;
+  int const nx = g.nx, ny = g.ny, ng = g.ng;
+  std::vector<double> Uh((size_t)g.nf * n, 0.0);
+  std::vector<double> QLx((size_t)g.nf * n, 0.0), QRx((size_t)g.nf * n, 0.0), QLy((size_t)g.nf * n, 0.0),
+      QRy((size_t)g.nf * n, 0.0), Qz((size_t)g.nf * n, 0.0);
+  std::vector<double> Fx((size_t)g.nf * n, 0.0), Fy((size_t)g.nf * n, 0.0);
+  auto riemann = [&]() {
+    if (c->solver == ORC_ROE) {
+      orc_roe(c, QLx.data(), QRx.data(), Fx.data(), 0);
+      orc_roe(c, QLy.data(), QRy.data(), Fy.data(), 1);
+    } else if (c->solver == ORC_EXACT) {
+      orc_exact(c, QLx.data(), QRx.data(), Fx.data(), 0);
+      orc_exact(c, QLy.data(), QRy.data(), Fy.data(), 1);
+    } else {
+      orc_hllc(c, QLx.data(), QRx.data(), Fx.data(), 0);
+      orc_hllc(c, QLy.data(), QRy.data(), Fy.data(), 1);
+    }
+  };
+  auto interior = [&](int x, int y) { return x > ng - 1 && x < nx - ng && y > ng - 1 && y < ny - ng; };
+  // pcm_cuda.cu:123-254 PCM_Reconstruction_2D: the 3D form's x and y faces on a one-cell-deep grid
+  orc_pcm_3d(c, U, QLx.data(), QRx.data(), QLy.data(), QRy.data(), Qz.data(), Qz.data());
+  riemann();
+  {  // VL_2D_cuda.cu:176-258 Update_Conserved_Variables_2D_half
+    double const hdt = 0.5 * dt, dtodx = hdt / c->dx, dtody = hdt / c->dy;
+    par_cells(g, [&](size_t id) {
+      int x, y, z;
+      g.xyz(id, x, y, z);
+      if (!(x > 0 && x < nx - 1 && y > 0 && y < ny - 1)) return;
+      size_t const imo = id - 1, jmo = id - nx, ipo = id + 1, jpo = id + nx;
+      double const d = U[id], d_inv = 1.0 / d;
+      double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+      double const P  = (U[4 * n + id] - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (g.gamma - 1.0);
+      auto upd        = [&](size_t f) {
+        return U[f * n + id] + dtodx * (Fx[f * n + imo] - Fx[f * n + id]) + dtody * (Fy[f * n + jmo] - Fy[f * n + id]);
+      };
+      for (int f = 0; f < 5 + g.ns; f++) Uh[(size_t)f * n + id] = upd((size_t)f);
+      if (g.de) {
+        double const vx_imo = U[n + imo] / U[imo], vx_ipo = U[n + ipo] / U[ipo];
+        double const vy_jmo = U[2 * n + jmo] / U[jmo], vy_jpo = U[2 * n + jpo] / U[jpo];
+        Uh[(size_t)g.fGE * n + id] =
+            upd((size_t)g.fGE) + 0.5 * P * (dtodx * (vx_imo - vx_ipo) + dtody * (vy_jmo - vy_jpo));
+      }
+    });
+  }
+  // VL_2D_cuda.cu:97-122 reconstructs U-half only for PLMP, PLMC, PPMP and PPMC: with PCM the
+  // corrector's Riemann solve reads the predictor's interface states of Un again.
+  if (c->recon != ORC_PCM) {
+    void (*recon)(const orc_config *, const double *, double *, double *, int) =
+        c->recon == ORC_PLMC ? orc_plmc : c->recon == ORC_PLMP ? orc_plmp : c->recon == ORC_PPMP ? orc_ppmp : orc_ppmc_vl;
+    recon(c, Uh.data(), QLx.data(), QRx.data(), 0);
+    recon(c, Uh.data(), QLy.data(), QRy.data(), 1);
+  }
+  riemann();
+  double const dtodx = dt / c->dx, dtody = dt / c->dy;
+  if (g.de) {  // hydro_cuda.cu:725-752 Partial_Update_Advected_Internal_Energy_2D (reads U only)
+    par_cells(g, [&](size_t id) {
+      int x, y, z;
+      g.xyz(id, x, y, z);
+      if (!interior(x, y)) return;
+      double const d = U[id], d_inv = 1.0 / d;
+      double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+      double const E = U[4 * n + id], GE = U[(size_t)g.fGE * n + id];
+      double const Ekin = 0.5 * d * (vx * vx + vy * vy + vz * vz);
+      double const P    = fmax(pressure_from_de(E, E - Ekin, GE, g.gamma), TINY);
+      size_t const imo = id - 1, ipo = id + 1, jmo = id - nx, jpo = id + nx;
+      double const vx_imo = U[n + imo] / U[imo], vx_ipo = U[n + ipo] / U[ipo];
+      double const vy_jmo = U[2 * n + jmo] / U[jmo], vy_jpo = U[2 * n + jpo] / U[jpo];
+      U[(size_t)g.fGE * n + id] += 0.5 * P * (dtodx * (vx_imo - vx_ipo) + dtody * (vy_jmo - vy_jpo));
+    });
+  }
+  // hydro_cuda.cu:87-170 Update_Conserved_Variables_2D: U += (x difference + y difference)
+  par_cells(g, [&](size_t id) {
+    int x, y, z;
+    g.xyz(id, x, y, z);
+    if (!interior(x, y)) return;
+    size_t const imo = id - 1, jmo = id - nx;
+    for (int f = 0; f < g.nf; f++) {
+      size_t const o = (size_t)f * n;
+      U[o + id] += dtodx * (Fx[o + imo] - Fx[o + id]) + dtody * (Fy[o + jmo] - Fy[o + id]);
+    }
+  });
+  if (g.de) {
+    // hydro_cuda.cu:880-933 Select_Internal_Energy_2D: neighbour maximum of E over the four
+    // face neighbours, indices clamped to the real cells
+    std::vector<double> GEsel(n, 0.0);
+    par_cells(g, [&](size_t id) {
+      int x, y, z;
+      g.xyz(id, x, y, z);
+      if (!interior(x, y)) return;
+      size_t const imo = (size_t)std::max(x - 1, ng) + (size_t)y * nx;
+      size_t const ipo = (size_t)std::min(x + 1, nx - ng - 1) + (size_t)y * nx;
+      size_t const jmo = (size_t)x + (size_t)std::max(y - 1, ng) * nx;
+      size_t const jpo = (size_t)x + (size_t)std::min(y + 1, ny - ng - 1) * nx;
+      double const d = U[id], d_inv = 1.0 / d;
+      double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+      double const E   = U[4 * n + id];
+      double const Uad = U[(size_t)g.fGE * n + id];
+      double const Utot = E - 0.5 * d * (vx * vx + vy * vy + vz * vz);
+      double Emax       = fmax(U[4 * n + imo], E);
+      Emax              = fmax(Emax, U[4 * n + ipo]);
+      Emax              = fmax(Emax, U[4 * n + jmo]);
+      Emax              = fmax(Emax, U[4 * n + jpo]);
+      double const Usel = (Utot / E > ETA_1 || Utot / Emax > ETA_2) ? Utot : Uad;
+      GEsel[id]         = fmax(Usel, TINY);
+    });
+    // hydro_cuda.cu:1035-1068 Sync_Energies_2D: E = kinetic + selected internal energy
+    par_cells(g, [&](size_t id) {
+      int x, y, z;
+      g.xyz(id, x, y, z);
+      if (!interior(x, y)) return;
+      U[(size_t)g.fGE * n + id] = GEsel[id];
+      double const d = U[id], d_inv = 1.0 / d;
+      double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
+      U[4 * n + id] = 0.5 * d * (vx * vx + vy * vy + vz * vz) + GEsel[id];
+    });
   }
   return 0;
 }

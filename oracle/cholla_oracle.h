@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-enum { ORC_PCM = 0, ORC_PLMC = 1, ORC_PPMC = 2 };
+enum { ORC_PCM = 0, ORC_PLMC = 1, ORC_PPMC = 2, ORC_PLMP = 3, ORC_PPMP = 4 };
 enum { ORC_HLLC = 0, ORC_ROE = 1, ORC_HLLD = 2, ORC_HLL = 3, ORC_EXACT = 4 };
 
 typedef struct {
@@ -31,7 +31,7 @@ typedef struct {
   int n_scalars;
   int de;             /* dual energy on */
   int mhd;            /* MHD (face-centred B, CT) */
-  int recon;          /* ORC_PCM / ORC_PLMC / ORC_PPMC */
+  int recon;          /* ORC_PCM / ORC_PLMC / ORC_PPMC / ORC_PLMP / ORC_PPMP */
   int solver;         /* ORC_HLLC / ORC_ROE / ORC_HLLD / ORC_HLL / ORC_EXACT */
   int density_floor_on;
   double gamma;
@@ -44,6 +44,9 @@ void orc_pcm_3d(const orc_config *c, const double *U, double *QLx, double *QRx, 
                 double *QLz, double *QRz);
 void orc_ppmc_vl(const orc_config *c, const double *U, double *QL, double *QR, int dir);
 void orc_plmc(const orc_config *c, const double *U, double *QL, double *QR, int dir);
+/* primitive-limited PLM / PPM (plmp_cuda.cu:21-365, ppmp_cuda.cu:28-752; hydro only) */
+void orc_plmp(const orc_config *c, const double *U, double *QL, double *QR, int dir);
+void orc_ppmp(const orc_config *c, const double *U, double *QL, double *QR, int dir);
 void orc_hllc(const orc_config *c, const double *QL, const double *QR, double *F, int dir);
 void orc_roe(const orc_config *c, const double *QL, const double *QR, double *F, int dir);
 void orc_hlld(const orc_config *c, const double *QL, const double *QR, const double *Bface, double *F, int dir);
@@ -141,6 +144,8 @@ void orc_t_hlld_double_star_fluxes(const double *dstar, double dstar_energy, con
 /* ---- the step: VL_Algorithm_3D_CUDA / VL_Algorithm_1D_CUDA ---- */
 int orc_vl_step_3d(const orc_config *c, double *U, double dt);
 int orc_vl_step_1d(const orc_config *c, double *U, double dt);
+/* src/integrators/VL_2D_cuda.cu:25-174 VL_Algorithm_2D_CUDA (nz = 1; hydro; no HLL or HLLD) */
+int orc_vl_step_2d(const orc_config *c, double *U, double dt);
 
 /* std::mt19937_64(seed) + std::uniform_real_distribution<double>(a, b), n draws: the input
  * generator of the reference's unit tests (e.g. src/reconstruction/ppmc_cuda_tests.cu:131-132) */

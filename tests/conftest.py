@@ -22,6 +22,24 @@ def oracle_lib():
 
 
 @pytest.fixture(scope="session")
+def ref_host(oracle_lib):
+    """The reference's own VL integrators compiled as host code (oracle/build_ref_host.sh), built
+    on first use where the reference source tree is present; the tests that need it skip
+    elsewhere."""
+    import subprocess
+
+    from oracle import ref_host
+
+    tree = Path(os.environ.get("CHOLLA_REFERENCE", "/root/reference"))
+    if tree.is_dir():
+        subprocess.run(["bash", str(ROOT / "oracle" / "build_ref_host.sh"), str(tree)], check=True,
+                       stdout=subprocess.DEVNULL)
+    if not ref_host.available("ppmc_hllc_de"):
+        pytest.skip("the reference source tree is absent: no host-compiled reference")
+    return ref_host
+
+
+@pytest.fixture(scope="session")
 def cuda():
     import torch
 

@@ -461,7 +461,7 @@ def hydro_system_cases(src_dir: Path) -> dict:
     its input file)."""
     raw = (src_dir / "system_tests/hydro_system_tests.cpp").read_text()
     out = {"linear_waves": {}, "source": "src/system_tests/hydro_system_tests.cpp:99-306"}
-    for recon in ("PCM", "PLMC", "PPMC"):
+    for recon in ("PCM", "PLMC", "PPMC", "PLMP", "PPMP"):
         src = re.sub(r"//[^\n]*", "", _preprocess(raw, {recon}))
         allowed = {k: float(v) for k, v in re.findall(r"double static constexpr (allowedL1Error|allowedError)\s*=\s*"
                                                       r"([-+0-9.eE]+)", src)}
