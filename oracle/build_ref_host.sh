@@ -13,9 +13,12 @@ CXX=${CXX:-g++}
 CUDA_HOME=${CUDA_HOME:-/usr/local/cuda}
 FLAGS="-std=c++17 -O2 -ffp-contract=off -fno-fast-math -fopenmp -fPIC -shared -w -I$CUDA_HOME/include -I$REF/src -include $HERE/ref_host_shim.h"
 COMMON="-DVL -DPRECISION=2 -DDENSITY_FLOOR -DTEMPERATURE_FLOOR"
-# The exact solver has no variant: the reference's VL integrators do not compile with -DEXACT
-# (integrators/VL_3D_cuda.cu:149 runs the argument n_cells into the kernel's name).
+# The exact-solver libraries hold its flux kernel but no integrator: the reference's VL
+# integrators do not compile with -DEXACT (integrators/VL_3D_cuda.cu:149 runs the argument
+# n_cells into the kernel's name).
 declare -A DEFS=(
+  [pcm_exact]="-DPCM -DEXACT"
+  [pcm_exact_de]="-DPCM -DEXACT -DDE"
   [ppmc_hllc_de]="-DPPMC -DHLLC -DDE"
   [ppmc_hllc]="-DPPMC -DHLLC"
   [ppmc_hllc_de_scalar]="-DPPMC -DHLLC -DDE -DSCALAR -DBASIC_SCALAR"

@@ -14,7 +14,10 @@
  *   refh_vl1d  VL_Algorithm_1D_CUDA   (src/integrators/VL_1D_cuda.cu:30)
  *   refh_plmp / refh_ppmp  PLMP_cuda / PPMP_cuda, one direction (reconstruction/plmp_cuda.cu:21,
  *              ppmp_cuda.cu:28), writing the interface arrays the caller passes
+ *   refh_riemann  one launch of the HLLC, Roe, HLL or exact flux kernel along a direction
  *   refh_scheme  which of the make.type macros this library was compiled with
+ * The library built with the exact solver has no integrator entry points: the reference's VL
+ * integrators do not compile with it (VL_3D_cuda.cu:149).
  * The state is updated in place in the reference's field-major layout.  The integrators keep
  * their scratch in file-scope globals that are allocated on the first call and never resized
  * (VL_3D_cuda.cu:58-133); each entry point here releases them after the step, so successive
@@ -30,9 +33,13 @@ Real gama;  // the reference's adiabatic index global (global.h:147), an argumen
 
 #include "global/global_cuda.cu"
 #include "hydro/hydro_cuda.cu"
-#include "integrators/VL_1D_cuda.cu"
-#include "integrators/VL_2D_cuda.cu"
-#include "integrators/VL_3D_cuda.cu"
+#ifndef EXACT  // the integrators do not compile with the exact solver (VL_3D_cuda.cu:149)
+  #include "integrators/VL_1D_cuda.cu"
+  #include "integrators/VL_2D_cuda.cu"
+  #include "integrators/VL_3D_cuda.cu"
+#else
+  #include "riemann_solvers/exact_cuda.cu"
+#endif
 #include "reconstruction/pcm_cuda.cu"
 #include "reconstruction/plmc_cuda.cu"
 #include "reconstruction/plmp_cuda.cu"
@@ -81,6 +88,7 @@ int launch_blocks(int n_cells) { return (n_cells + TPB - 1) / TPB; }
 
 extern "C" {
 
+#ifndef EXACT
 int refh_vl3d(double *U, int nx, int ny, int nz, int n_ghost, double dx, double dy, double dz, double dt, int n_fields,
               double gamma, double density_floor)
 {
@@ -101,6 +109,35 @@ int refh_vl1d(double *U, int nx, int n_ghost, double dx, double dt, int n_fields
 {
   gama = gamma;
   return guarded([&] { VL_Algorithm_1D_CUDA(U, nx, 0, n_ghost, dx, 0.0, dt, n_fields, 0); });
+}
+#endif
+
+// One launch of a Riemann solver kernel over the whole grid along dir: 0 HLLC
+// (hllc_cuda.cu:19), 1 Roe (roe_cuda.cu:19), 3 HLL (hll_cuda.cu:19), 4 exact (exact_cuda.cu:20,
+// in the library built with EXACT only).  Returns -2 for a solver this library lacks.
+int refh_riemann(int solver, double *QL, double *QR, double *F, int nx, int ny, int nz, int n_ghost, double gamma,
+                 int dir, int n_fields)
+{
+  auto run = [&](auto kernel) {
+    return guarded([&] {
+      hipLaunchKernelGGL(kernel, launch_blocks(nx * ny * nz), TPB, 0, 0, QL, QR, F, nx, ny, nz, n_ghost, gamma, dir,
+                         n_fields);
+    });
+  };
+  switch (solver) {
+    case 0:
+      return run(Calculate_HLLC_Fluxes_CUDA);
+    case 1:
+      return run(Calculate_Roe_Fluxes_CUDA);
+    case 3:
+      return run(Calculate_HLL_Fluxes_CUDA);
+#ifdef EXACT
+    case 4:
+      return run(Calculate_Exact_Fluxes_CUDA);
+#endif
+    default:
+      return -2;
+  }
 }
 
 int refh_plmp(double *U, double *QL, double *QR, int nx, int ny, int nz, int n_ghost, double dx, double dt,
@@ -129,7 +166,7 @@ int refh_ppmp(double *U, double *QL, double *QR, int nx, int ny, int nz, int n_g
 
 // Bit mask of the scheme macros: 1 DE, 2 MHD, 4 density floor, 8 scalar; the reconstruction
 // (0 PCM, 1 PLMC, 2 PPMC, 3 PLMP, 4 PPMP) in bits 8-11 and the solver (0 HLLC, 1 Roe, 2 HLLD,
-// 3 HLL) in bits 12-15.
+// 3 HLL, 4 exact) in bits 12-15.
 int refh_scheme(void)
 {
   int m = 0;
@@ -160,6 +197,8 @@ int refh_scheme(void)
   m |= 2 << 12;
 #elif defined(HLL)
   m |= 3 << 12;
+#elif defined(EXACT)
+  m |= 4 << 12;
 #endif
   return m;
 }

@@ -43,9 +43,11 @@ def lib(scheme: str, shape: tuple = ()) -> C.CDLL:
         copy = _tmp / f"{key}.so"
         shutil.copyfile(path(scheme), copy)
         h = C.CDLL(str(copy))
-        h.refh_vl3d.argtypes = [_DP] + [C.c_int] * 4 + [C.c_double] * 4 + [C.c_int, C.c_double, C.c_double]
-        h.refh_vl2d.argtypes = [_DP] + [C.c_int] * 3 + [C.c_double] * 3 + [C.c_int, C.c_double]
-        h.refh_vl1d.argtypes = [_DP, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double]
+        h.refh_riemann.argtypes = [C.c_int, _DP, _DP, _DP] + [C.c_int] * 4 + [C.c_double, C.c_int, C.c_int]
+        if hasattr(h, "refh_vl3d"):
+            h.refh_vl3d.argtypes = [_DP] + [C.c_int] * 4 + [C.c_double] * 4 + [C.c_int, C.c_double, C.c_double]
+            h.refh_vl2d.argtypes = [_DP] + [C.c_int] * 3 + [C.c_double] * 3 + [C.c_int, C.c_double]
+            h.refh_vl1d.argtypes = [_DP, C.c_int, C.c_int, C.c_double, C.c_double, C.c_int, C.c_double]
         for name in ("refh_plmp", "refh_ppmp"):
             getattr(h, name).argtypes = [_DP, _DP, _DP] + [C.c_int] * 4 + [C.c_double] * 3 + [C.c_int] * 2
         _libs[key] = h
@@ -71,6 +73,13 @@ def vl_step_2d(scheme: str, U: np.ndarray, nx, ny, n_ghost, dx, dy, dt, gamma) -
 def vl_step_1d(scheme: str, U: np.ndarray, nx, n_ghost, dx, dt, gamma) -> None:
     """VL_Algorithm_1D_CUDA (integrators/VL_1D_cuda.cu:30)."""
     _check(lib(scheme, (nx,)).refh_vl1d(U, nx, n_ghost, dx, dt, U.size // nx, gamma), "VL 1D step")
+
+
+def riemann(scheme: str, solver: int, QL: np.ndarray, QR: np.ndarray, F: np.ndarray, nx, ny, nz, n_ghost, gamma,
+            direction) -> None:
+    """One launch of a flux kernel (0 HLLC, 1 Roe, 3 HLL, 4 exact) along `direction`."""
+    _check(lib(scheme, (nx, ny, nz)).refh_riemann(solver, QL, QR, F, nx, ny, nz, n_ghost, gamma, direction,
+                                                  QL.size // (nx * ny * nz)), "Riemann solver")
 
 
 def reconstruct(scheme: str, kind: str, U: np.ndarray, QL: np.ndarray, QR: np.ndarray, nx, ny, nz, n_ghost, dx, dt,
