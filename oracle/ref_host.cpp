@@ -15,6 +15,7 @@
  *   refh_plmp / refh_ppmp  PLMP_cuda / PPMP_cuda, one direction (reconstruction/plmp_cuda.cu:21,
  *              ppmp_cuda.cu:28), writing the interface arrays the caller passes
  *   refh_riemann  one launch of the HLLC, Roe, HLL or exact flux kernel along a direction
+ *   refh_set_ghost_cells  SetGhostCells, the ghost fill of one face (grid/cuda_boundaries.cu:151)
  *   refh_scheme  which of the make.type macros this library was compiled with
  * The library built with the exact solver has no integrator entry points: the reference's VL
  * integrators do not compile with it (VL_3D_cuda.cu:149).
@@ -32,6 +33,7 @@ Real gama;  // the reference's adiabatic index global (global.h:147), an argumen
 [[noreturn]] void chexit(int code) { throw std::runtime_error("chexit " + std::to_string(code)); }
 
 #include "global/global_cuda.cu"
+#include "grid/cuda_boundaries.cu"
 #include "hydro/hydro_cuda.cu"
 #ifndef EXACT  // the integrators do not compile with the exact solver (VL_3D_cuda.cu:149)
   #include "integrators/VL_1D_cuda.cu"
@@ -162,6 +164,17 @@ int refh_ppmp(double *U, double *QL, double *QR, int nx, int ny, int nz, int n_g
       (void)n_fields;
   return -2;  // PPMP_cuda is compiled only with the PPMP macro (ppmp_cuda.cu:4)
 #endif
+}
+
+// SetGhostCells (grid/cuda_boundaries.cu:151-159) for one face dir over the ghost slab of
+// isize x jsize x ksize cells starting at (imin, jmin, kmin), the extents the reference's
+// Grid3D::Set_Boundary_Extents gives (grid/boundary_conditions.cpp:419-493).
+int refh_set_ghost_cells(double *U, int nx, int ny, int nz, int n_fields, int n_ghost, const int *flags, int isize,
+                         int jsize, int ksize, int imin, int jmin, int kmin, int dir)
+{
+  int f[6] = {flags[0], flags[1], flags[2], flags[3], flags[4], flags[5]};
+  return guarded(
+      [&] { SetGhostCells(U, nx, ny, nz, n_fields, nx * ny * nz, n_ghost, f, isize, jsize, ksize, imin, jmin, kmin, dir); });
 }
 
 // Bit mask of the scheme macros: 1 DE, 2 MHD, 4 density floor, 8 scalar; the reconstruction

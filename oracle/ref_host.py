@@ -43,6 +43,7 @@ def lib(scheme: str, shape: tuple = ()) -> C.CDLL:
         copy = _tmp / f"{key}.so"
         shutil.copyfile(path(scheme), copy)
         h = C.CDLL(str(copy))
+        h.refh_set_ghost_cells.argtypes = [_DP] + [C.c_int] * 5 + [C.POINTER(C.c_int)] + [C.c_int] * 7
         h.refh_riemann.argtypes = [C.c_int, _DP, _DP, _DP] + [C.c_int] * 4 + [C.c_double, C.c_int, C.c_int]
         if hasattr(h, "refh_vl3d"):
             h.refh_vl3d.argtypes = [_DP] + [C.c_int] * 4 + [C.c_double] * 4 + [C.c_int, C.c_double, C.c_double]
@@ -80,6 +81,25 @@ def riemann(scheme: str, solver: int, QL: np.ndarray, QR: np.ndarray, F: np.ndar
     """One launch of a flux kernel (0 HLLC, 1 Roe, 3 HLL, 4 exact) along `direction`."""
     _check(lib(scheme, (nx, ny, nz)).refh_riemann(solver, QL, QR, F, nx, ny, nz, n_ghost, gamma, direction,
                                                   QL.size // (nx * ny * nz)), "Riemann solver")
+
+
+def set_boundaries(scheme: str, U: np.ndarray, nx, ny, nz, n_ghost, flags) -> None:
+    """Grid3D::Set_Boundaries_Grid's ghost fill: SetGhostCells for faces 0-5 in turn
+    (grid/boundary_conditions.cpp:104-116), over the ghost slabs of Set_Boundary_Extents
+    (:419-493), on the faces whose axis has more than one cell."""
+    h = lib(scheme, (nx, ny, nz))
+    fl = (C.c_int * 6)(*flags)
+    jl, ju = (n_ghost, ny - n_ghost) if ny > 1 else (0, ny)
+    kl, ku = (n_ghost, nz - n_ghost) if nz > 1 else (0, nz)
+    slabs = [((0, n_ghost), (jl, ju), (kl, ku)), ((nx - n_ghost, nx), (jl, ju), (kl, ku)),
+             ((0, nx), (0, n_ghost), (kl, ku)), ((0, nx), (ny - n_ghost, ny), (kl, ku)),
+             ((0, nx), (0, ny), (0, n_ghost)), ((0, nx), (0, ny), (nz - n_ghost, nz))]
+    for face, ext in enumerate((nx, nx, ny, ny, nz, nz)):
+        if ext <= 1:
+            continue
+        (i0, i1), (j0, j1), (k0, k1) = slabs[face]
+        _check(h.refh_set_ghost_cells(U, nx, ny, nz, U.size // (nx * ny * nz), n_ghost, fl, i1 - i0, j1 - j0, k1 - k0,
+                                      i0, j0, k0, face), "ghost fill")
 
 
 def reconstruct(scheme: str, kind: str, U: np.ndarray, QL: np.ndarray, QR: np.ndarray, nx, ny, nz, n_ghost, dx, dt,

@@ -12,6 +12,7 @@ cells to be equal bit for bit:
 * single launches of the primitive-limited reconstructions PLMP_cuda and PPMP_cuda along each
   direction (every interface value they write);
 * single launches of the HLLC, Roe, HLL and exact flux kernels on random interface states;
+* the ghost fill (SetGhostCells per face) for periodic, reflective, outflow and mixed faces;
 * a full linear-sound-wave crossing in the PPMP build (214 steps), the case where the reference
   misses its own largest-error bound.
 
@@ -198,3 +199,41 @@ def test_riemann_kernel_matches_reference(oracle_lib, ref_host, solver, de):
         ref_host.riemann(scheme, getattr(o, solver), QL, QR, Fr, n, n, n, ng, GAMMA, direction)
         assert np.count_nonzero(Fr) > 0.5 * Fr.size
         assert _same(Fo, Fr), (direction, np.abs(Fo - Fr).max(axis=1))
+
+
+@pytest.mark.parametrize("flags", [(1,) * 6, (2,) * 6, (3,) * 6, (3, 2, 1, 1, 2, 3)])
+@pytest.mark.parametrize("name", ["ppmc_hllc_de", "mhd_plmc_hlld"])
+def test_ghost_fill_matches_reference(oracle_lib, ref_host, name, flags):
+    """The ghost fill between steps (SetGhostCellsKernel, grid/cuda_boundaries.cu:71-149):
+    periodic (1), reflective (2) and outflow (3, with the hydro build's diode on the normal
+    momentum) faces on a random box whose ghost cells start random; every cell compared, ghosts
+    included.  The MHD build copies without the diode."""
+    o = oracle_lib
+    mhd = name.startswith("mhd")
+    rng = np.random.default_rng(sum(flags) + 7 * mhd)
+    nx, ny, nz, ng = 10 + 8, 9 + 8, 8 + 8, 4
+    nf = 8 if mhd else 6
+    U = rng.uniform(-1.0, 1.0, (nf, nz, ny, nx))
+    U[0] = rng.uniform(0.5, 2.0, (nz, ny, nx))
+    U[4] = rng.uniform(5.0, 9.0, (nz, ny, nx))
+    cfg = o.config(nx, ny, nz, ng, nf, de=not mhd, mhd=mhd, recon=o.PLMC if mhd else o.PPMC,
+                   solver=o.HLLD if mhd else o.HLLC, gamma=GAMMA)
+    Uo, Ur = U.reshape(nf, -1).copy(), U.reshape(nf, -1).copy()
+    o.set_boundaries(cfg, Uo, flags)
+    ref_host.set_boundaries(name, Ur, nx, ny, nz, ng, flags)
+    assert not np.array_equal(Uo, U.reshape(nf, -1))
+    assert _same(Uo, Ur), np.abs(Uo - Ur).max(axis=1)
+
+
+def test_ghost_fill_1d_matches_reference(oracle_lib, ref_host):
+    from cholla_gb300 import ics
+
+    o = oracle_lib
+    U, dx = ics.sod_1d(100, 4, GAMMA)
+    U[1] = np.linspace(-1.0, 1.0, U.shape[1])  # inflow at both ends: the diode acts
+    nf, N = U.shape
+    cfg = o.config(N, 1, 1, 4, nf, gamma=GAMMA, dx=dx)
+    Uo, Ur = np.ascontiguousarray(U), np.ascontiguousarray(U).copy()
+    o.set_boundaries(cfg, Uo.reshape(-1), (3, 3, 0, 0, 0, 0))
+    ref_host.set_boundaries("ppmc_hllc", Ur.reshape(-1), N, 1, 1, 4, (3, 3, 0, 0, 0, 0))
+    assert _same(Uo, Ur)
