@@ -16,6 +16,7 @@
  *              ppmp_cuda.cu:28), writing the interface arrays the caller passes
  *   refh_riemann  one launch of the HLLC, Roe, HLL or exact flux kernel along a direction
  *   refh_set_ghost_cells  SetGhostCells, the ghost fill of one face (grid/cuda_boundaries.cu:151)
+ *   refh_temperature_floor  Apply_Temperature_Floor (hydro/hydro_cuda.cu:1103)
  *   refh_scheme  which of the make.type macros this library was compiled with
  * The library built with the exact solver has no integrator entry points: the reference's VL
  * integrators do not compile with it (VL_3D_cuda.cu:149).
@@ -175,6 +176,12 @@ int refh_set_ghost_cells(double *U, int nx, int ny, int nz, int n_fields, int n_
   int f[6] = {flags[0], flags[1], flags[2], flags[3], flags[4], flags[5]};
   return guarded(
       [&] { SetGhostCells(U, nx, ny, nz, n_fields, nx * ny * nz, n_ghost, f, isize, jsize, ksize, imin, jmin, kmin, dir); });
+}
+
+// Apply_Temperature_Floor (hydro/hydro_cuda.cu:1103-1153): the internal-energy floor U_floor.
+int refh_temperature_floor(double *U, int nx, int ny, int nz, int n_ghost, int n_fields, double U_floor)
+{
+  return guarded([&] { Apply_Temperature_Floor(U, nx, ny, nz, n_ghost, n_fields, U_floor); });
 }
 
 // Bit mask of the scheme macros: 1 DE, 2 MHD, 4 density floor, 8 scalar; the reconstruction

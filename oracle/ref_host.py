@@ -44,6 +44,7 @@ def lib(scheme: str, shape: tuple = ()) -> C.CDLL:
         shutil.copyfile(path(scheme), copy)
         h = C.CDLL(str(copy))
         h.refh_set_ghost_cells.argtypes = [_DP] + [C.c_int] * 5 + [C.POINTER(C.c_int)] + [C.c_int] * 7
+        h.refh_temperature_floor.argtypes = [_DP] + [C.c_int] * 5 + [C.c_double]
         h.refh_riemann.argtypes = [C.c_int, _DP, _DP, _DP] + [C.c_int] * 4 + [C.c_double, C.c_int, C.c_int]
         if hasattr(h, "refh_vl3d"):
             h.refh_vl3d.argtypes = [_DP] + [C.c_int] * 4 + [C.c_double] * 4 + [C.c_int, C.c_double, C.c_double]
@@ -100,6 +101,12 @@ def set_boundaries(scheme: str, U: np.ndarray, nx, ny, nz, n_ghost, flags) -> No
         (i0, i1), (j0, j1), (k0, k1) = slabs[face]
         _check(h.refh_set_ghost_cells(U, nx, ny, nz, U.size // (nx * ny * nz), n_ghost, fl, i1 - i0, j1 - j0, k1 - k0,
                                       i0, j0, k0, face), "ghost fill")
+
+
+def temperature_floor(scheme: str, U: np.ndarray, nx, ny, nz, n_ghost, U_floor) -> None:
+    """Apply_Temperature_Floor (hydro/hydro_cuda.cu:1103)."""
+    _check(lib(scheme, (nx, ny, nz)).refh_temperature_floor(U, nx, ny, nz, n_ghost, U.size // (nx * ny * nz),
+                                                            U_floor), "temperature floor")
 
 
 def reconstruct(scheme: str, kind: str, U: np.ndarray, QL: np.ndarray, QR: np.ndarray, nx, ny, nz, n_ghost, dx, dt,

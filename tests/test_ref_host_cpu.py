@@ -13,6 +13,7 @@ cells to be equal bit for bit:
   direction (every interface value they write);
 * single launches of the HLLC, Roe, HLL and exact flux kernels on random interface states;
 * the ghost fill (SetGhostCells per face) for periodic, reflective, outflow and mixed faces;
+* the temperature floor (Apply_Temperature_Floor) with and without dual energy;
 * a full linear-sound-wave crossing in the PPMP build (214 steps), the case where the reference
   misses its own largest-error bound.
 
@@ -236,4 +237,22 @@ def test_ghost_fill_1d_matches_reference(oracle_lib, ref_host):
     Uo, Ur = np.ascontiguousarray(U), np.ascontiguousarray(U).copy()
     o.set_boundaries(cfg, Uo.reshape(-1), (3, 3, 0, 0, 0, 0))
     ref_host.set_boundaries("ppmc_hllc", Ur.reshape(-1), N, 1, 1, 4, (3, 3, 0, 0, 0, 0))
+    assert _same(Uo, Ur)
+
+
+@pytest.mark.parametrize("name", ["ppmc_hllc", "ppmc_hllc_de"])
+def test_temperature_floor_matches_reference(oracle_lib, ref_host, name):
+    """Apply_Temperature_Floor (hydro_cuda.cu:1103-1153) with a floor that about half the cells
+    are under: both the total energy and, with dual energy, GasEnergy are raised there."""
+    o = oracle_lib
+    de = name.endswith("_de")
+    U = _hydro_box(12, 4, de, 0)
+    nf, N = U.shape[0], U.shape[1]
+    cfg = o.config(N, N, N, 4, nf, de=de, gamma=GAMMA)
+    Uo, Ur = U.reshape(nf, -1).copy(), U.reshape(nf, -1).copy()
+    eint = (U[4] - 0.5 * (U[1] ** 2 + U[2] ** 2 + U[3] ** 2) / U[0]).ravel()
+    floor = float(np.median(eint))
+    o.temperature_floor(cfg, Uo, floor)
+    ref_host.temperature_floor(name, Ur, N, N, N, 4, floor)
+    assert not np.array_equal(Uo, U.reshape(nf, -1))
     assert _same(Uo, Ur)
