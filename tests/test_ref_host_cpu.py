@@ -174,7 +174,8 @@ def test_ppmp_sound_wave_crossing_matches_reference(oracle_lib, ref_host):
 @pytest.mark.parametrize("solver", ["HLLC", "ROE", "HLL", "EXACT"])
 def test_riemann_kernel_matches_reference(oracle_lib, ref_host, solver, de):
     """One launch of each hydro flux kernel on seeded random interface states (density 0.1-10,
-    velocities within +-3, pressure 0.05-10), every direction.  The exact solver's kernel is
+    velocities within +-1, pressure 1-10: strong jumps, but no state pair that opens a vacuum,
+    where the reference's exact solver prints a message), every direction.  The exact solver's kernel is
     built on its own (its integrators do not compile); both sides evaluate its single-precision
     powf on the host, so they agree bit for bit but only approximate the GPU's powf."""
     o = oracle_lib
@@ -186,8 +187,8 @@ def test_riemann_kernel_matches_reference(oracle_lib, ref_host, solver, de):
 
     def states():
         d = rng.uniform(0.1, 10.0, size)
-        v = rng.uniform(-3.0, 3.0, (3, size))
-        p = rng.uniform(0.05, 10.0, size)
+        v = rng.uniform(-1.0, 1.0, (3, size))
+        p = rng.uniform(1.0, 10.0, size)
         E = p / (GAMMA - 1.0) + 0.5 * d * (v ** 2).sum(axis=0)
         fields = [d, d * v[0], d * v[1], d * v[2], E] + ([p / (GAMMA - 1.0)] if de else [])
         return np.ascontiguousarray(np.stack(fields))
