@@ -21,8 +21,8 @@ CGB_ERR_NONFINITE = 4
 CGB_ERR_TIMEOUT = 5
 CGB_ERR_UNSUPPORTED = 6
 
-PCM, PLMC, PPMC = 0, 1, 2
-HLLC, ROE, HLLD = 0, 1, 2
+PCM, PLMC, PPMC, PLMP, PPMP = 0, 1, 2, 3, 4
+HLLC, ROE, HLLD, HLL, EXACT = 0, 1, 2, 3, 4
 FP64, MIXED, FP64_FAST = 0, 1, 2
 
 

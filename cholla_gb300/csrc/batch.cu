@@ -177,6 +177,11 @@ int cgb_batch_create(cgb_batch **out, const cgb_scheme *scheme, double c_cfl, vo
   if (!out || !scheme) return bfail(CGB_ERR_ARGS, "null argument");
   *out                 = nullptr;
   cgb_scheme const &s = *scheme;
+  if (s.reconstruction < CGB_PCM || s.reconstruction > CGB_PPMP || s.riemann_solver < CGB_HLLC ||
+      s.riemann_solver > CGB_EXACT)
+    return bfail(CGB_ERR_ARGS, "bad reconstruction or riemann solver");
+  if (s.reconstruction >= CGB_PLMP || s.riemann_solver >= CGB_HLL)
+    return bfail(CGB_ERR_UNSUPPORTED, "PLMP, PPMP, HLL and the exact solver are not built in this library");
   if (s.mhd || s.riemann_solver == CGB_HLLD) return bfail(CGB_ERR_UNSUPPORTED, "batches are hydro only");
   if (s.precision != CGB_MIXED && s.precision != CGB_FP64_FAST)
     return bfail(CGB_ERR_UNSUPPORTED, "batches run the fast FP64 or the mixed-precision form");

@@ -101,8 +101,12 @@ int ensure_slot(int nx, int ny, int nz, int nf, int mhd)
 
 int check_scheme(const cgb_scheme &s)
 {
-  if (s.reconstruction < CGB_PCM || s.reconstruction > CGB_PPMC) return fail(CGB_ERR_ARGS, "bad reconstruction");
-  if (s.riemann_solver < CGB_HLLC || s.riemann_solver > CGB_HLLD) return fail(CGB_ERR_ARGS, "bad riemann solver");
+  if (s.reconstruction < CGB_PCM || s.reconstruction > CGB_PPMP) return fail(CGB_ERR_ARGS, "bad reconstruction");
+  if (s.riemann_solver < CGB_HLLC || s.riemann_solver > CGB_EXACT) return fail(CGB_ERR_ARGS, "bad riemann solver");
+  if (s.reconstruction == CGB_PLMP || s.reconstruction == CGB_PPMP)
+    return fail(CGB_ERR_UNSUPPORTED, "the primitive-limited PLMP / PPMP reconstructions are not built in this library");
+  if (s.riemann_solver == CGB_HLL || s.riemann_solver == CGB_EXACT)
+    return fail(CGB_ERR_UNSUPPORTED, "the HLL and exact Riemann solvers are not built in this library");
   if (s.n_scalars < 0 || s.n_scalars > cgb::NS_MAX) return fail(CGB_ERR_ARGS, "n_scalars must be 0..2");
   if (!(s.gamma > 1.0)) return fail(CGB_ERR_ARGS, "gamma must exceed 1");
   if (s.mhd && s.riemann_solver != CGB_HLLD) return fail(CGB_ERR_ARGS, "MHD needs the HLLD solver");

@@ -29,8 +29,8 @@ def _ptr(a) -> int:
     return a.data_ptr()
 
 
-_RECON = {"PCM": L.PCM, "PLMC": L.PLMC, "PPMC": L.PPMC}
-_SOLVER = {"HLLC": L.HLLC, "ROE": L.ROE, "HLLD": L.HLLD}
+_RECON = {"PCM": L.PCM, "PLMC": L.PLMC, "PPMC": L.PPMC, "PLMP": L.PLMP, "PPMP": L.PPMP}
+_SOLVER = {"HLLC": L.HLLC, "ROE": L.ROE, "HLLD": L.HLLD, "HLL": L.HLL, "EXACT": L.EXACT}
 _PREC = {"fp64": L.FP64, "mixed": L.MIXED, "fp64_fast": L.FP64_FAST}
 
 
@@ -55,7 +55,7 @@ class Scheme:
 
     def n_ghost(self) -> int:
         """Ghost layers the reference uses for this scheme (src/grid/grid3D.cpp:53-76)."""
-        g = {"PCM": 2, "PLMC": 3, "PPMC": 4}[self.reconstruction]
+        g = {"PCM": 2, "PLMC": 3, "PPMC": 4, "PLMP": 3, "PPMP": 4}[self.reconstruction]
         return g + (1 if self.mhd else 0)
 
     def to_c(self) -> L.cgb_scheme:

@@ -31,14 +31,21 @@ extern "C" {
 #define CGB_ERR_TIMEOUT     5  /* a bounded device wait ran out */
 #define CGB_ERR_UNSUPPORTED 6  /* option combination not built */
 
-/* reconstruction (builds/make.type.*: -DPCM / -DPLMC / -DPPMC) */
+/* reconstruction (builds/make.type.*: -DPCM / -DPLMC / -DPPMC; -DPLMP / -DPPMP are the
+   primitive-limited forms of src/reconstruction/plmp_cuda.cu and ppmp_cuda.cu, which
+   cgb_set_scheme rejects with CGB_ERR_UNSUPPORTED: their kernels are not built yet) */
 #define CGB_PCM  0
 #define CGB_PLMC 1
 #define CGB_PPMC 2
-/* Riemann solver (-DHLLC / -DROE / -DHLLD) */
-#define CGB_HLLC 0
-#define CGB_ROE  1
-#define CGB_HLLD 2
+#define CGB_PLMP 3
+#define CGB_PPMP 4
+/* Riemann solver (-DHLLC / -DROE / -DHLLD; -DHLL and -DEXACT, src/riemann_solvers/hll_cuda.cu
+   and exact_cuda.cu, are rejected with CGB_ERR_UNSUPPORTED: not built yet) */
+#define CGB_HLLC  0
+#define CGB_ROE   1
+#define CGB_HLLD  2
+#define CGB_HLL   3
+#define CGB_EXACT 4
 /* arithmetic */
 #define CGB_FP64      0 /* FP64 in the reference's operation order: bit-exact with its -fmad=false build */
 #define CGB_MIXED     1 /* FP32 reconstruction and fluxes, FP64 state accumulation, energy recovery and dt */
