@@ -8,8 +8,14 @@ reduction, predictor, corrector, finalize (DE select/sync, temperature floor, CF
 
     python bench.py [--steps K] [--warmup W] [--gpus N] [--n 256] [--impl ours|reference]
 
+Besides the headline line's own numbers it reports, on the same GPU: the other arithmetic forms;
+per-field accuracy against the exact FP64 form for the 256^3 box (20 steps), the 512^3 box in
+mixed precision (50 steps) and every job of a serving stream; the 512^3 box's speed in every form
+and of the reference's own CUDA build; the 256^3 ideal-MHD box; the serving sweep; the drop-in
+C ABI end to end with host copies; and the CPU baseline (the FP64 host oracle, 256^3 sample).
+
 --impl reference times the reference's CPU path: the FP64 host restatement of the same scheme
-(oracle/, OpenMP over every host core), on a bounded 128^3 sample of the same workload.
+(oracle/, OpenMP over every host core) on the same 256^3 box, W warm-up and K timed steps.
 Multi-GPU (torchrun): every rank steps its own independent box (replicas; there is no
 collective on this path); value = all cells updated / max-over-ranks time.
 """
@@ -155,14 +161,15 @@ def cpu_sample(n_sample: int, min_seconds: float, max_steps: int, threads: int):
 
 
 def run_reference(args, world, rank):
-    """The reference's CPU implementation of the path: the FP64 host restatement (oracle)."""
+    """The reference's CPU implementation of the path: the FP64 host restatement (oracle), on the
+    same n^3 box as our arm, every step a full step of it."""
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    n_sample = 128
-    cpu_sample(n_sample, 0.0, args.warmup, threads)  # warm-up
-    cu_s, steps, el = cpu_sample(n_sample, 0.0, args.steps, threads)
-    sample = (f"{steps} steps of a {n_sample}^3 box of the same workload (seed 0), exact FP64 oracle, "
+    n = args.n
+    cpu_sample(n, 0.0, args.warmup, threads)  # warm-up steps (untimed)
+    cu_s, steps, el = cpu_sample(n, 0.0, args.steps, threads)
+    sample = (f"{steps} full steps of the {n}^3 box of the same workload (seed 0), exact FP64 oracle, "
               f"{threads} OpenMP threads")
     line = {
         "metric": "cell updates/s", "value": cu_s, "unit": "cell-updates/s", "impl": "reference",
@@ -208,10 +215,61 @@ def kernel_breakdown(box, U, steps, stream):
     return {name: kt[name] / k for name in ("predictor", "corrector", "finalize")}
 
 
+def scheme_of(prec, gamma=5.0 / 3.0):
+    from cholla_gb300 import integrator as I
+
+    return I.Scheme(reconstruction="PPMC", riemann_solver="HLLC", dual_energy=True, density_floor=True,
+                    temperature_floor=True, gamma=gamma, precision=prec)
+
+
+# kernels one engine step launches: ghost fill, dt, [primitives], predictor, corrector (three
+# sweeps), negative-density repair, finalize
+LAUNCHES_PER_STEP = {"fp64": 8, "fp64_fast": 9, "mixed": 9}
+
+
+def time_reference_build(R, U0, n, ng, gamma, dev, stream, torch, steps, sync_each=False):
+    """ms per step of the reference's own CUDA build (its kernels, launched as VL_Algorithm_3D_CUDA
+    launches them, plus its Calc_dt_GPU with the device-to-host copy of dt, its temperature floor and
+    its ghost fill), on `stream`, after one warm-up step."""
+    N, nf, dx = n + 2 * ng, U0.shape[0], 1.0 / n
+    R.init("hydro_ppmc_hllc_de")
+    R.set_stream(stream)
+    R.set_sync_each(sync_each)
+    Ur = torch.from_numpy(U0).to(dev)
+
+    def ref_step():
+        R.set_boundaries(Ur, N, N, N, ng, nf, (1,) * 6)
+        dti = R.calc_dt(Ur, N, N, N, ng, nf, dx, dx, dx, gamma)
+        R.vl_step_3d(Ur, N, N, N, ng, dx, dx, dx, 0.3 / dti, nf, gamma, 0.0)
+        R.temperature_floor(Ur, N, N, N, ng, nf, 0.0)
+
+    try:
+        ref_step()
+        stream.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(steps):
+            ref_step()
+        f1.record(stream)
+        f1.synchronize()
+        return f0.elapsed_time(f1) / steps
+    finally:
+        R.set_sync_each(False)
+        del Ur
+
+
+REF_BUILD_NOTE = ("reference hot-path .cu files compiled unchanged for sm_103a with its Makefile flags "
+                  "(-O3 -fmad=false), launched kernel by kernel as VL_Algorithm_3D_CUDA does; 'no_sync' is its "
+                  "-DDISABLE_GPU_ERROR_CHECKING build (no device synchronisation between kernels: the conservative "
+                  "baseline the speedups divide by), 'sync_each' its default build (cudaDeviceSynchronize after "
+                  "every kernel, src/utils/gpu.hpp:139-155)")
+
+
 def run_ours(args, world, rank, local):
     import torch
 
-    from cholla_gb300 import ics
+    from cholla_gb300 import accuracy, ics
     from cholla_gb300 import integrator as I
     from cholla_gb300.engine import Box
 
@@ -220,10 +278,7 @@ def run_ours(args, world, rank, local):
     n, ng, gamma = args.n, 4, 5.0 / 3.0
     N = n + 2 * ng
     dx = 1.0 / n
-
-    def scheme(prec):
-        return I.Scheme(reconstruction="PPMC", riemann_solver="HLLC", dual_energy=True, density_floor=True,
-                        temperature_floor=True, gamma=gamma, precision=prec)
+    scheme = scheme_of
 
     U0 = ics.turbulence_box(n, ng, gamma, seed=rank)
     nf = U0.shape[0]
@@ -248,10 +303,11 @@ def run_ours(args, world, rank, local):
     # ---- per-kernel times over a second timed region (events on the launching stream) ----
     kt = kernel_breakdown(box, U, args.steps, stream)
     box.close()
+    del U
     corr_ms = kt["corrector"]
-    # algorithmic bytes of the corrector stage per step (the x, y and z sweep launches): half-step
-    # primitives in (6 fields, compute type), U^n in and U^{n+1} out (6 fields FP64), GasEnergy
-    # partial update in, pre-sync energy out.  The exact FP64 form is one fused launch.
+    # algorithmic bytes of the corrector stage per step (its sweep launches): half-step primitives
+    # in (6 fields, compute type), U^n in and U^{n+1} out (6 fields FP64), GasEnergy partial update
+    # in, pre-sync energy out
     wbytes = 4 if args.precision == "mixed" else 8
     corr_bytes = n ** 3 * (nf * wbytes + 2 * nf * 8 + 2 * 8)
     peak, peak_kind = hbm_peak()
@@ -274,7 +330,36 @@ def run_ours(args, world, rank, local):
             bv.close()
             del Uv
 
-    # ---- ideal MHD (PLMC + HLLD + CT, exact FP64) on the same GPU: ours and the reference build ----
+    # ---- accuracy of the throughput forms against the exact FP64 form at n^3, 20 steps ----
+    acc = None
+    if rank == 0 and not args.no_accuracy:
+        acc = accuracy.run(torch, n=n, steps=20, seed=rank, forms=("fp64_fast", "mixed"), U0=U0)
+
+    # ---- the reference's own CUDA build on the same GPU (cubins compiled from its source) ----
+    ref_gpu = None
+    if rank == 0 and not args.no_reference_gpu:
+        try:
+            from oracle import reference_gpu as R
+
+            if R.available():
+                rms = time_reference_build(R, U0, n, ng, gamma, dev, stream, torch, 3)
+                rms_sync = time_reference_build(R, U0, n, ng, gamma, dev, stream, torch, 2, sync_each=True)
+                rv = n ** 3 / (rms / 1e3)
+                ref_gpu = {"value": rv, "unit": "cell-updates/s", "ms_per_step": rms, "steps": 3,
+                           "variant": "no_sync",
+                           "sync_each": {"ms_per_step": rms_sync, "value": n ** 3 / (rms_sync / 1e3), "steps": 2},
+                           "speedup_vs_reference_build": {"headline": (value / world) / rv,
+                                                          **{p: o["value"] / rv for p, o in others.items()}},
+                           "build": REF_BUILD_NOTE}
+        except Exception as ex:  # the reference build is a comparison, not part of the product
+            ref_gpu = {"unavailable": str(ex)[:200]}
+
+    # ---- the 512^3 box: every form, the reference build, and mixed-precision accuracy (50 steps) ----
+    big = None
+    if rank == 0 and not args.no_512:
+        big = run_512(args, dev, stream, torch)
+
+    # ---- ideal MHD (PLMC + HLLD + CT) on the same GPU: ours and the reference build ----
     mhd = None
     if rank == 0 and not args.no_variants:
         mhd = run_mhd(args, dev, stream, torch)
@@ -344,50 +429,13 @@ def run_ours(args, world, rank, local):
                        "upload and the previous step's download overlap the step on their own copy streams)"}
         del dbuf
 
-    # ---- the reference's own CUDA build on the same GPU (cubins compiled from its source) ----
-    ref_gpu = None
-    if rank == 0 and not args.no_reference_gpu:
-        try:
-            from oracle import reference_gpu as R
-
-            if R.available():
-                R.init("hydro_ppmc_hllc_de")
-                R.set_stream(stream)
-                Ur = torch.from_numpy(ics.turbulence_box(n, ng, gamma, seed=0)).to(dev)
-                kr = 3
-
-                def ref_step():
-                    R.set_boundaries(Ur, N, N, N, ng, nf, (1,) * 6)
-                    dti = R.calc_dt(Ur, N, N, N, ng, nf, dx, dx, dx, gamma)
-                    R.vl_step_3d(Ur, N, N, N, ng, dx, dx, dx, 0.3 / dti, nf, gamma, 0.0)
-                    R.temperature_floor(Ur, N, N, N, ng, nf, 0.0)
-
-                ref_step()
-                stream.synchronize()
-                f0 = torch.cuda.Event(enable_timing=True)
-                f1 = torch.cuda.Event(enable_timing=True)
-                f0.record(stream)
-                for _ in range(kr):
-                    ref_step()
-                f1.record(stream)
-                f1.synchronize()
-                rms = f0.elapsed_time(f1) / kr
-                rv = n ** 3 / (rms / 1e3)
-                ref_gpu = {"value": rv, "unit": "cell-updates/s", "ms_per_step": rms, "steps": kr,
-                           "speedup_vs_reference_build": {"headline": (value / world) / rv,
-                                                          **{p: o["value"] / rv for p, o in others.items()}},
-                           "build": "reference hot-path .cu files compiled unchanged for sm_103a with its Makefile "
-                                    "flags (-O3 -fmad=false), launched kernel by kernel as VL_Algorithm_3D_CUDA does"}
-                del Ur
-        except Exception as ex:  # the reference build is a comparison, not part of the product
-            ref_gpu = {"unavailable": str(ex)[:200]}
-
     cpu = None
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        cu_s, steps, el = cpu_sample(96, 12.0, 400, threads)
+        cu_s, steps, el = cpu_sample(n, 10.0, 400, threads)
         cpu = {"value": cu_s, "unit": "cell-updates/s", "cores": threads, "kind": "port",
-               "sample": f"{steps} steps of a 96^3 box of the same workload in {el:.1f} s (FP64 oracle, OpenMP)"}
+               "sample": f"{steps} full steps of the {n}^3 box of the same workload in {el:.1f} s (FP64 oracle, "
+                         f"OpenMP on {threads} threads)"}
 
     if rank == 0:
         clocks = clk.summary()
@@ -400,23 +448,66 @@ def run_ours(args, world, rank, local):
             "config": {**workload_config(args), "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": load_traffic(n, args.precision),
-                         "kernel": "corrector (x, y, z sweep launches of one step)" if args.precision != "fp64"
-                         else "corrector", "kernel_ms": corr_ms, "kernels_ms": kt,
-                         "algorithmic_bytes_per_launch": corr_bytes,
+                         "kernel": "corrector (its sweep launches in one step)", "kernel_ms": corr_ms,
+                         "kernels_ms": kt, "algorithmic_bytes_per_step": corr_bytes,
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json)",
                          "binding_ceiling": "FP64 pipe: GB300 FP64 FMA measured 1.19 TFLOP/s, divide 60 G/s"},
             "variants": others,
+            "accuracy": acc,
+            "at_512": big,
             "mhd": mhd,
             "serving": serving,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "reference_gpu": ref_gpu,
-            # kernels per engine step: ghost fill, dt, [primitives], predictor, corrector (1 fused
-            # launch exact, 3 sweeps otherwise), negative-density repair, finalize
-            "gpu_launches": (6 if args.precision == "fp64" else 9) * args.steps,
+            "gpu_launches": LAUNCHES_PER_STEP[args.precision] * args.steps,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
+
+
+def run_512(args, dev, stream, torch):
+    """The 512^3 box of the same workload: ms per step of every arithmetic form and of the
+    reference's build on the same GPU, and the mixed form's per-field accuracy against the exact
+    FP64 form after 50 steps on the same dt sequence (whose timing also gives the exact form's
+    speed through the drop-in calls, with the host dt round trip of every step)."""
+    from cholla_gb300 import accuracy, ics
+    from cholla_gb300.engine import Box
+
+    n, ng, gamma = 512, 4, 5.0 / 3.0
+    N, dx = n + 2 * ng, 1.0 / n
+    U0 = ics.turbulence_box(n, ng, gamma, seed=0)
+    out = {"workload": "3D adiabatic hydro 512^3 periodic turbulence-like box (seed 0, rms Mach 2), PPMC+HLLC+VL, "
+                       "dual energy, floors, CFL 0.3", "n": n}
+    for prec, k in (("fp64_fast", 3), ("mixed", 10)):
+        U = torch.from_numpy(U0).to(dev)
+        box = Box(N, N, N, ng, dx, dx, dx, scheme_of(prec))
+        box.use_graph(True)
+        box.advance(U, 1, 0.3, stream)
+        stream.synchronize()
+        ms = time_box(box, U, k, stream, torch) / k
+        out[prec] = {"ms_per_step": ms, "value": n ** 3 / (ms / 1e3), "steps": k}
+        box.close()
+        del U
+    try:
+        from oracle import reference_gpu as R
+
+        if R.available():
+            rms = time_reference_build(R, U0, n, ng, gamma, dev, stream, torch, 2)
+            out["reference_gpu"] = {"ms_per_step": rms, "value": n ** 3 / (rms / 1e3), "steps": 2,
+                                    "variant": "no_sync", "build": REF_BUILD_NOTE}
+            out["speedup_vs_reference_build"] = {p: rms / out[p]["ms_per_step"] for p in ("fp64_fast", "mixed")}
+    except Exception as ex:  # the reference build is a comparison, not part of the product
+        out["reference_gpu"] = {"unavailable": str(ex)[:200]}
+    if not args.no_accuracy:
+        acc = accuracy.run(torch, n=n, steps=50, seed=0, forms=("mixed",), U0=U0)
+        out["accuracy_mixed_vs_exact_50_steps"] = acc
+        out["fp64"] = {"ms_per_step_dropin": 1e3 * acc["seconds"]["fp64"] / 50,
+                       "note": "exact FP64 through the drop-in calls, host dt round trip every step"}
+        if "reference_gpu" in out and "ms_per_step" in out["reference_gpu"]:
+            out.setdefault("speedup_vs_reference_build", {})["fp64"] = (out["reference_gpu"]["ms_per_step"] /
+                                                                      out["fp64"]["ms_per_step_dropin"])
+    return out
 
 
 def run_mhd(args, dev, stream, torch):
@@ -485,21 +576,24 @@ def run_serving(args, torch):
     precision, 100 steps each, admitted by free device memory) served by the continuous-batching
     server and by per-request launches of the single-box step (kernel by kernel, and from a CUDA
     graph per request), each mode warmed up first, at every arrival rate.  Latency = arrival to
-    completion of the last step."""
-    from cholla_gb300 import serve
+    completion of the last step.  Then every job of a further stream against its exact FP64 twin."""
+    from cholla_gb300 import accuracy, serve
 
     modes = serve.MODES
+    rates = [float(r) for r in args.serve_rates.split(",") if r]
+    counts = [int(c) for c in args.serve_count.split(",") if c]
+    counts = (counts * len(rates))[:len(rates)] if len(counts) < len(rates) else counts
     out = {"workload": "Poisson stream of 3D hydro jobs, n in {32,48,64,96,128}, blast or Sod tube, "
-                       f"PPMC + HLLC mixed, 100 steps, {args.serve_count} requests per rate",
+                       "PPMC + HLLC mixed, 100 steps, seed 17",
            "batched_server": "first come first served up to 3 Mi cells per step (rest held); batch schedule "
                              "(chains, solo threshold) autotuned on the size mix at start-up (see each row's 'tuned')",
            "rates": {}}
     for mode in modes:  # module loading, first captures and allocator growth outside the timed runs
         serve.serve(torch, serve.make_requests(rate=2000.0, count=6, seed=99, steps=5), mode=mode)
-    for rate in [float(r) for r in args.serve_rates.split(",") if r]:
-        row = {}
+    for rate, count in zip(rates, counts):
+        row = {"requests": count}
         for mode in modes:
-            reqs = serve.make_requests(rate=rate, count=args.serve_count, seed=17, steps=100)
+            reqs = serve.make_requests(rate=rate, count=count, seed=17, steps=100)
             row[mode] = serve.serve(torch, reqs, mode=mode)
         b = row["batched"]
         for base in modes[1:]:
@@ -507,6 +601,15 @@ def run_serving(args, torch):
             row[f"vs_{base}"] = {"throughput_ratio": b["cell_updates_per_s"] / p["cell_updates_per_s"],
                                  "p99_ratio": p["p99_ms"] / b["p99_ms"], "p50_ratio": p["p50_ms"] / b["p50_ms"]}
         out["rates"][f"{rate:g}"] = row
+    if not args.no_accuracy and args.serve_twins > 0:
+        reqs = serve.make_requests(rate=100.0, count=args.serve_twins, seed=23, steps=100)
+        twins = accuracy.serving_twins(torch, reqs)
+        worst = {f: max(t["rel_l1"][f] for t in twins) for f in twins[0]["rel_l1"]}
+        out["accuracy_vs_fp64_twins"] = {
+            "how": "every job of a seeded stream (seed 23) run as a batch job (the served arithmetic: the same "
+                   "bits whatever shares the batch) against its exact FP64 twin on the job's own dt sequence; "
+                   "relative L1 over the real cells",
+            "jobs": twins, "max_rel_l1": worst}
     return out
 
 
@@ -533,8 +636,11 @@ def main():
     ap.add_argument("--no-reference-gpu", action="store_true")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-512", action="store_true")
     ap.add_argument("--serve-rates", default="10,30,100,2000")
-    ap.add_argument("--serve-count", type=int, default=40)
+    ap.add_argument("--serve-count", default="60,100,200,200", help="requests per rate (one per rate, or one for all)")
+    ap.add_argument("--serve-twins", type=int, default=12, help="served jobs checked against their FP64 twins")
     ap.add_argument("--precision", choices=["fp64_fast", "fp64", "mixed"], default="fp64_fast")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -21,6 +21,10 @@ CGB_ERR_NONFINITE = 4
 CGB_ERR_TIMEOUT = 5
 CGB_ERR_UNSUPPORTED = 6
 
+CGB_STATUS_NEG_DENSITY = 1
+CGB_STATUS_NONFINITE = 2
+CGB_MAX_DIVB = 1.0e-9
+
 PCM, PLMC, PPMC, PLMP, PPMP = 0, 1, 2, 3, 4
 HLLC, ROE, HLLD, HLL, EXACT = 0, 1, 2, 3, 4
 FP64, MIXED, FP64_FAST = 0, 1, 2
@@ -67,6 +71,9 @@ SIGNATURES = {
     "cgb_apply_temperature_floor": (_I, [_P, _I, _I, _I, _I, _I, _D]),
     "cgb_set_boundaries": (_I, [_P, _I, _I, _I, _I, _I, C.POINTER(_I)]),
     "cgb_max_magnetic_divergence": (_I, [_P, _I, _I, _I, _I, _I, _D, _D, _D, C.POINTER(_D)]),
+    "cgb_check_magnetic_divergence": (_I, [_P, _I, _I, _I, _I, _I, _D, _D, _D, C.POINTER(_D)]),
+    "cgb_check_status": (_I, [C.POINTER(_I)]),
+    "cgb_debug_fail_alloc": (_I, [_I]),
     "cgb_box_create": (_I, [C.POINTER(_P), _I, _I, _I, _I, _D, _D, _D, C.POINTER(cgb_scheme), C.POINTER(_I)]),
     "cgb_box_destroy": (_I, [_P]),
     "cgb_box_n_fields": (_I, [_P]),
@@ -76,6 +83,7 @@ SIGNATURES = {
     "cgb_box_kernel_times": (_I, [_P, C.POINTER(_D), C.POINTER(C.c_longlong)]),
     "cgb_box_advance": (_I, [_P, _P, _I, _D, _P]),
     "cgb_box_get_time": (_I, [_P, C.POINTER(_D), C.POINTER(_D)]),
+    "cgb_box_check_status": (_I, [_P, C.POINTER(_I)]),
     "cgb_box_last_error": (C.c_char_p, []),
     "cgb_batch_create": (_I, [C.POINTER(_P), C.POINTER(cgb_scheme), _D, _P]),
     "cgb_batch_destroy": (_I, [_P]),
@@ -86,9 +94,11 @@ SIGNATURES = {
     "cgb_batch_set_chains": (_I, [_P, _I]),
     "cgb_batch_hold": (_I, [_P, _I, _I]),
     "cgb_selftest_conversions": (_I, [_P, C.c_longlong, _P, _P]),
+    "cgb_selftest_fast_math": (_I, [_P, C.c_longlong, _P, _P]),
     "cgb_batch_set_solo_cells": (_I, [_P, C.c_longlong]),
     "cgb_batch_step": (_I, [_P, _I]),
     "cgb_batch_job_time": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_D)]),
+    "cgb_batch_job_status": (_I, [_P, _I, C.POINTER(_I)]),
     "cgb_batch_last_error": (C.c_char_p, []),
     "cgb_ic_blast": (_I, [_P, _I, _I, _I, _I, _I, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _I, _P]),
     "cgb_ic_shock_tube": (_I, [_P, _I, _I, _I, _I, _I, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D, _D,

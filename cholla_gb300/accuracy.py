@@ -49,11 +49,14 @@ def _steps(torch, U, n, ng, precision, count, dts=None, cfl=0.3):
     return out
 
 
-def run(torch, n: int = 64, steps: int = 10, seed: int = 0, forms=("mixed", "fp64_fast"), mach: float = 2.0) -> dict:
+def run(torch, n: int = 64, steps: int = 10, seed: int = 0, forms=("mixed", "fp64_fast"), mach: float = 2.0,
+        U0=None) -> dict:
+    """U0: the initial state (host array of turbulence_box(n, 4, 5/3, seed, mach)) if already built."""
     from . import ics
 
     ng = 4
-    U0 = ics.turbulence_box(n, ng, 5.0 / 3.0, seed=seed, mach=mach)
+    if U0 is None:
+        U0 = ics.turbulence_box(n, ng, 5.0 / 3.0, seed=seed, mach=mach)
     real = (slice(None), slice(ng, ng + n), slice(ng, ng + n), slice(ng, ng + n))
     host = torch.from_numpy(U0)
     U = host.to("cuda")
@@ -66,7 +69,7 @@ def run(torch, n: int = 64, steps: int = 10, seed: int = 0, forms=("mixed", "fp6
     res = {"workload": f"3D hydro {n}^3 periodic turbulence-like box (seed {seed}, rms Mach {mach:g}), PPMC + HLLC + "
                        f"VL, dual energy, {steps} steps at CFL 0.3 of the exact FP64 form",
            "baseline": "exact FP64 form (bit-identical to the reference build)", "t_end": float(sum(dts)),
-           "seconds": {"fp64": t_exact}, "rel_l1": {}, "conservation": {}}
+           "steps": steps, "seconds": {"fp64": t_exact}, "rel_l1": {}, "conservation": {}}
     mom_scale = ref[1:4].abs().sum()  # momenta drift relative to the total absolute momentum
     drift_m = (U[real][1:4].sum(dim=(1, 2, 3)) - sums0[1:4]).abs().max() / mom_scale
     res["conservation"]["fp64"] = {"mass": float(((U[real][0].sum() - sums0[0]) / sums0[0]).abs()),
@@ -85,6 +88,41 @@ def run(torch, n: int = 64, steps: int = 10, seed: int = 0, forms=("mixed", "fp6
                                      "momentum": float(drift_m)}
         del Uf, cur
     return res
+
+
+def serving_twins(torch, requests) -> list[dict]:
+    """Accuracy of served jobs: each request of the serving workload (mixed precision, see serve.py)
+    is run as the batched server runs it -- a cgb_batch job, whose result is the same bit for bit
+    whatever else shares the batch -- one step at a time, recording the job's own dt sequence;
+    then its exact FP64 twin (same initial state) takes the same dt sequence through the drop-in
+    calls.  Per request: the relative L1 error per field of the served result against the twin."""
+    from .batch import Batch
+    from .serve import N_GHOST, default_scheme, init_state
+
+    scheme = default_scheme()
+    stream = torch.cuda.Stream()
+    ng = N_GHOST
+    out = []
+    for req in requests:
+        U, dx = init_state(torch, req, scheme, stream)
+        stream.synchronize()
+        U0 = U.clone()
+        b = Batch(scheme, stream)
+        jid = b.add(U, ng, dx, dx, dx)
+        dts = []
+        for _ in range(req.steps):
+            b.step(1)
+            dts.append(b.job_time(jid)[1])
+        b.close()
+        twin = U0.clone()
+        _steps(torch, twin, req.n, ng, "fp64", len(dts), dts)
+        real = (slice(None), slice(ng, ng + req.n), slice(ng, ng + req.n), slice(ng, ng + req.n))
+        ref = twin[real]
+        err = (U[real] - ref).abs().sum(dim=(1, 2, 3)) / ref.abs().sum(dim=(1, 2, 3)).clamp_min(1e-300)
+        out.append({"rid": req.rid, "n": req.n, "kind": req.kind, "steps": len(dts),
+                    "rel_l1": {FIELDS[i]: float(err[i]) for i in range(err.shape[0])}})
+        del U, U0, twin
+    return out
 
 
 def main():

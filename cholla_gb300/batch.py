@@ -81,9 +81,18 @@ class Batch:
         _check(L.lib().cgb_batch_step(self._h, n_steps))
 
     def job_time(self, job_id: int):
+        """(t, last dt) of a job; raises BatchError (CGB_ERR_NONFINITE) once it has a bad cell."""
         t, dt = C.c_double(), C.c_double()
         _check(L.lib().cgb_batch_job_time(self._h, job_id, C.byref(t), C.byref(dt)))
         return t.value, dt.value
+
+    def job_status(self, job_id: int) -> int:
+        """Status bits (CGB_STATUS_*) of a job, without raising for CGB_ERR_NONFINITE."""
+        f = C.c_int()
+        rc = L.lib().cgb_batch_job_status(self._h, job_id, C.byref(f))
+        if rc not in (L.CGB_OK, L.CGB_ERR_NONFINITE):
+            _check(rc)
+        return f.value
 
 
 def ic_blast(U, n_ghost: int, dx: float, center, radius: float, energy: float = 1.0, rho: float = 1.0,

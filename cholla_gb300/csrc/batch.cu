@@ -262,7 +262,7 @@ int cgb_batch_add(cgb_batch *bt, double *d_conserved, int nx, int ny, int nz, in
   size_t const wb = al256(cgb::batch_w_bytes(b)), cb = al256((size_t)b.n * 8);
   size_t const bytes = wb + 2 * cb + 3 * 256;
   void *mem          = nullptr;
-  cudaError_t e      = cudaMallocFromPoolAsync(&mem, bytes, bt->pool, bt->stream);
+  cudaError_t e      = cgb::dev_malloc_pool_async(&mem, bytes, bt->pool, bt->stream);
   if (e != cudaSuccess) {
     cudaGetLastError();
     return bfail(CGB_ERR_NOMEM, "job scratch allocation failed");
@@ -393,7 +393,14 @@ int cgb_batch_step(cgb_batch *bt, int n_steps)
   return CGB_OK;
 }
 
-// Time and last dt of one job (synchronises the batch stream).
+namespace
+{
+const char *kBadJob =
+    "the job holds a real cell with non-finite density or energy, or density <= 0 after the negative-density repair";
+}
+
+// Time and last dt of one job (synchronises the batch stream).  Returns CGB_ERR_NONFINITE (with t
+// and dt filled in) while the job's status word records a bad cell.
 int cgb_batch_job_time(cgb_batch *bt, int job_id, double *t, double *dt_last)
 {
   if (!bt) return bfail(CGB_ERR_ARGS, "null batch");
@@ -401,11 +408,30 @@ int cgb_batch_job_time(cgb_batch *bt, int job_id, double *t, double *dt_last)
   for (size_t i = 0; i < bt->slots.size(); i++) {
     if (bt->slots[i].id != job_id) continue;
     double h[2];
+    int st        = 0;
     cudaError_t e = cudaStreamSynchronize(bt->stream);
     if (e == cudaSuccess) e = cudaMemcpy(h, bt->jobs[i].dt_t, 16, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&st, bt->jobs[i].status, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return bcuda(e, "batch_job_time");
     if (t) *t = h[1];
     if (dt_last) *dt_last = h[0];
+    if (st & CGB_STATUS_NONFINITE) return bfail(CGB_ERR_NONFINITE, kBadJob);
+    return CGB_OK;
+  }
+  return bfail(CGB_ERR_ARGS, "no such job");
+}
+
+// Status bits (CGB_STATUS_*) of one job without clearing them (synchronises the batch stream).
+int cgb_batch_job_status(cgb_batch *bt, int job_id, int *flags)
+{
+  if (!bt || !flags) return bfail(CGB_ERR_ARGS, "null argument");
+  std::lock_guard<std::mutex> lk(bt->mu);
+  for (size_t i = 0; i < bt->slots.size(); i++) {
+    if (bt->slots[i].id != job_id) continue;
+    cudaError_t e = cudaStreamSynchronize(bt->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(flags, bt->jobs[i].status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return bcuda(e, "batch_job_status");
+    if (*flags & CGB_STATUS_NONFINITE) return bfail(CGB_ERR_NONFINITE, kBadJob);
     return CGB_OK;
   }
   return bfail(CGB_ERR_ARGS, "no such job");

@@ -77,7 +77,7 @@ int ensure_slot(int nx, int ny, int nz, int nf, int mhd)
       *p = nullptr;
       return true;
     }
-    if (cudaMalloc(p, bytes) != cudaSuccess) return false;
+    if (cgb::dev_malloc(p, bytes) != cudaSuccess) return false;
     return cudaMemset(*p, 0, bytes) == cudaSuccess;
   };
   bool ok = alloc((void **)&s.dti, sizeof(unsigned long long)) && alloc((void **)&s.status, sizeof(int));
@@ -138,9 +138,10 @@ int make_box(cgb::Box &b, int nx, int ny, int nz, int ng, int nf, double dx, dou
 }  // namespace
 
 // Static scratch of cgb_vl_algorithm_3d_static: a file-scope array in the module's static device
-// memory, which the driver provides when it loads the module; no call allocates it.  24 MiB
-// holds the exact FP64 step of a box of up to 393,216 padded cells with 6 fields (73^3) and the
-// fast FP64 / mixed forms up to 196,608 (58^3).
+// memory, which the driver provides when it loads the module; no call allocates it.  A box of n
+// padded cells and f fields needs (f + 2) 8 n bytes in exact FP64 and (2 f + 4) 8 n in the fast
+// forms (each array rounded to 256 bytes) plus 512: with 6 fields, 24 MiB holds fewer than
+// 393,216 padded cells (73^3) in FP64 and fewer than 196,608 (58^3) in fast FP64 / mixed.
 constexpr size_t kStaticScratchBytes = size_t(24) << 20;
 static __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
@@ -160,7 +161,7 @@ int device_word(int which, unsigned long long **word)
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices) return fail(CGB_ERR_ARGS, "device ordinal beyond the result-word table");
-  if (!g_word[dev][which] && cudaMalloc(&g_word[dev][which], sizeof(unsigned long long)) != cudaSuccess) {
+  if (!g_word[dev][which] && cgb::dev_malloc((void **)&g_word[dev][which], sizeof(unsigned long long)) != cudaSuccess) {
     g_word[dev][which] = nullptr;
     cudaGetLastError();
     return fail(CGB_ERR_NOMEM, "reduction result word");
@@ -424,6 +425,45 @@ int cgb_max_magnetic_divergence(const double *d_conserved, int nx, int ny, int n
   if (e != cudaSuccess) return cuda_fail(e, "max_magnetic_divergence");
   unsigned long long const bits = *g_dti_host;
   std::memcpy(max_divb, &bits, sizeof(double));
+  return CGB_OK;
+}
+
+int cgb_check_magnetic_divergence(const double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields,
+                                  double dx, double dy, double dz, double *max_divb)
+{
+  double v  = 0.0;
+  int const rc = cgb_max_magnetic_divergence(d_conserved, nx, ny, nz, n_ghost, n_fields, dx, dy, dz, &v);
+  if (max_divb) *max_divb = v;
+  if (rc != CGB_OK) return rc;
+  // magnetic_divergence.cu:105-116: the limit, and a negative (or NaN) maximum, are fatal there
+  if (!(v >= 0.0) || v > CGB_MAX_DIVB) {
+    char buf[160];
+    std::snprintf(buf, sizeof buf, "magnetic divergence %.4e exceeds the limit %.1e (or is not a number)", v,
+                  CGB_MAX_DIVB);
+    return fail(CGB_ERR_NONFINITE, buf);
+  }
+  return CGB_OK;
+}
+
+int cgb_check_status(int *flags)
+{
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (flags) *flags = 0;
+  if (!g_slot.live || !g_slot.s.status) return CGB_OK;
+  int cur = -1;
+  bool const other = cudaGetDevice(&cur) == cudaSuccess && g_slot.dev != cur;
+  if (other) cudaSetDevice(g_slot.dev);
+  int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, g_slot.s.status, sizeof(int), cudaMemcpyDeviceToHost, g_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g_stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(g_slot.s.status, 0, sizeof(int), g_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g_stream);
+  if (other) cudaSetDevice(cur);
+  if (e != cudaSuccess) return cuda_fail(e, "check_status");
+  if (flags) *flags = h;
+  if (h & CGB_STATUS_NONFINITE)
+    return fail(CGB_ERR_NONFINITE, "a step left a real cell with non-finite density or energy, or density <= 0 "
+                                   "after the negative-density repair");
   return CGB_OK;
 }
 

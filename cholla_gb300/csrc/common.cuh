@@ -16,6 +16,26 @@ constexpr double ETA_2 = 0.035;
 constexpr int NS_MAX   = 2;        // passive scalars supported by the fused kernels
 constexpr int NQ_MAX   = 5 + NS_MAX + 1;
 
+// Bits of the per-box device status word (collected with atomicOr by the kernels; read by the
+// host through cgb_check_status / cgb_box_check_status / cgb_batch_job_status).
+constexpr int STATUS_NEG_DENSITY = 1;  // a real cell's update gave density <= 0 (repaired by averaging)
+constexpr int STATUS_NONFINITE   = 2;  // a real cell holds non-finite density or energy, or density <= 0 after repair
+
+// x is NaN or +-infinity (exponent bits all ones), tested on the integer pipe
+__device__ __forceinline__ bool not_finite(double x) { return (__double2hiint(x) & 0x7ff00000) == 0x7ff00000; }
+// a density or energy pair that makes the cell unusable: density not a finite positive number, or
+// non-finite total energy (the conditions of the reference's "Thread crashed" report,
+// hydro_cuda.cu:381-389, with the floors' negative-energy case left to the floors)
+__device__ __forceinline__ bool bad_cell(double d, double E)
+{
+  return __double_as_longlong(d) <= 0 || not_finite(d) || not_finite(E);
+}
+
+// Device allocations of the library go through these (alloc.cu), so that a test can make the
+// n-th one fail on the host (cgb_debug_fail_alloc) without touching the GPU.
+cudaError_t dev_malloc(void **p, size_t bytes);
+cudaError_t dev_malloc_pool_async(void **p, size_t bytes, cudaMemPool_t pool, cudaStream_t s);
+
 enum Recon { RECON_PCM = 0, RECON_PLMC = 1, RECON_PPMC = 2 };
 enum Solver { SOLVER_HLLC = 0, SOLVER_ROE = 1, SOLVER_HLLD = 2 };
 

@@ -161,7 +161,7 @@ int cgb_box_create(cgb_box **out, int nx, int ny, int nz, int n_ghost, double dx
   b.gamma = s.gamma, b.dx = dx, b.dy = dy, b.dz = dz, b.density_floor = 0.0;
   size_t const n = (size_t)b.n;
   auto al = [](void **p, size_t bytes) {
-    if (cudaMalloc(p, bytes) != cudaSuccess) return false;
+    if (cgb::dev_malloc(p, bytes) != cudaSuccess) return false;
     return cudaMemset(*p, 0, bytes) == cudaSuccess;
   };
   bool ok = al((void **)&bx->s.dti, 8) && al((void **)&bx->s.status, 4) && al((void **)&bx->dt_t, 16);
@@ -280,16 +280,41 @@ int cgb_box_advance(cgb_box *bx, double *d_conserved, int n_steps, double c_cfl,
   return CGB_OK;
 }
 
-// Current (dt, t) of the box; synchronises the box's last stream.
+namespace
+{
+const char *kBadCells =
+    "the box holds a real cell with non-finite density or energy, or density <= 0 after the negative-density repair";
+}
+
+// Current (dt, t) of the box; synchronises the box's last stream.  Returns CGB_ERR_NONFINITE (with
+// t and dt filled in) while the box's status word records a bad cell.
 int cgb_box_get_time(cgb_box *bx, double *t, double *dt_last)
 {
   if (!bx) return box_fail(nullptr, CGB_ERR_ARGS, "null box");
   double h[2];
+  int st = 0;
   if (cudaStreamSynchronize(bx->last_stream) != cudaSuccess ||
-      cudaMemcpy(h, bx->dt_t, 16, cudaMemcpyDeviceToHost) != cudaSuccess)
+      cudaMemcpy(h, bx->dt_t, 16, cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(&st, bx->s.status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
     return box_fail(bx, CGB_ERR_CUDA, "get_time");
   if (dt_last) *dt_last = h[0];
   if (t) *t = h[1];
+  if (st & CGB_STATUS_NONFINITE) return box_fail(bx, CGB_ERR_NONFINITE, kBadCells);
+  return CGB_OK;
+}
+
+// The box's status bits (CGB_STATUS_*) since the last call, which clears them; synchronises the
+// box's last stream.  CGB_ERR_NONFINITE when CGB_STATUS_NONFINITE is among them.
+int cgb_box_check_status(cgb_box *bx, int *flags)
+{
+  if (!bx) return box_fail(nullptr, CGB_ERR_ARGS, "null box");
+  int st = 0;
+  if (cudaStreamSynchronize(bx->last_stream) != cudaSuccess ||
+      cudaMemcpy(&st, bx->s.status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemset(bx->s.status, 0, sizeof(int)) != cudaSuccess)
+    return box_fail(bx, CGB_ERR_CUDA, "check_status");
+  if (flags) *flags = st;
+  if (st & CGB_STATUS_NONFINITE) return box_fail(bx, CGB_ERR_NONFINITE, kBadCells);
   return CGB_OK;
 }
 

@@ -462,10 +462,11 @@ __global__ void __launch_bounds__(TX *TY *TZ, 2) k_corrector(Box b, const double
         v[4] *= (floor / dens_0);
         if (b.de) v[nq - 1] *= (floor / dens_0);
       } else {
-        atomicOr(status, 1);  // negative density: averaged by the finalize kernel
+        atomicOr(status, STATUS_NEG_DENSITY);  // negative density: averaged by the finalize kernel
       }
     }
   }
+  if (not_finite(v[0]) || not_finite(v[4])) atomicOr(status, STATUS_NONFINITE);
 #pragma unroll
   for (int qq = 0; qq < NQ_MAX; qq++)
     if (qq < nq) U[(long long)field_of_q(qq, b) * b.n + gid] = v[qq];
@@ -507,8 +508,8 @@ __device__ __forceinline__ void block_max_to(double v, unsigned long long *dst)
 }
 
 __global__ void __launch_bounds__(256) k_finalize(Box b, double *__restrict__ U, const double *__restrict__ Epre,
-                                                  unsigned long long *__restrict__ dti, double U_floor, int temp_floor,
-                                                  int do_dt)
+                                                  unsigned long long *__restrict__ dti, int *__restrict__ status,
+                                                  double U_floor, int temp_floor, int do_dt)
 {
   int const ng = b.ng;
   bool const one_d = (b.ny == 1 && b.nz == 1);
@@ -562,6 +563,7 @@ __global__ void __launch_bounds__(256) k_finalize(Box b, double *__restrict__ U,
         if (Ui < U_floor) U[fge + id] = d * U_floor;
       }
     }
+    if (bad_cell(d, E)) atomicOr(status, STATUS_NONFINITE);
     if (do_dt) {
       if (one_d) {
         // hydro_cuda.cu:437-471 Calc_dt_1D
@@ -876,10 +878,11 @@ __global__ void __launch_bounds__(L *WA *WB, 2)
         v[4] *= (floor / dens_0);
         if (b.de) v[nq - 1] *= (floor / dens_0);
       } else {
-        atomicOr(status, 1);  // negative density: averaged by the finalize kernel
+        atomicOr(status, STATUS_NEG_DENSITY);  // negative density: averaged by the finalize kernel
       }
     }
   }
+  if (not_finite(v[0]) || not_finite(v[4])) atomicOr(status, STATUS_NONFINITE);
 #pragma unroll
   for (int qq = 0; qq < NQ_MAX; qq++)
     if (qq < nq) U[(long long)field_of_q(qq, b) * n + gid] = v[qq];
@@ -1009,7 +1012,8 @@ cudaError_t hydro_exact_step(const Box &b, int recon, int solver, double *U, con
     int const ng = b.ng;
     long long const nreal =
         (long long)(b.nx - 2 * ng) * (one_d ? 1 : b.ny - 2 * ng) * (one_d ? 1 : b.nz - 2 * ng);
-    k_finalize<<<(unsigned)((nreal + 255) / 256), 256, 0, s>>>(b, U, sc.Epre, sc.dti, U_floor, temp_floor, do_dt);
+    k_finalize<<<(unsigned)((nreal + 255) / 256), 256, 0, s>>>(b, U, sc.Epre, sc.dti, sc.status, U_floor, temp_floor,
+                                                               do_dt);
     e = cudaGetLastError();
   }
   if (marks) cudaEventRecord(marks[3], s);

@@ -453,9 +453,10 @@ __device__ __forceinline__ void final_update(const Box &b, long long gid, const 
       v[1] *= sc, v[2] *= sc, v[3] *= sc, v[4] *= sc;
       if (b.de) v[5] *= sc;
     } else {
-      atomicOr(status, 1);
+      atomicOr(status, STATUS_NEG_DENSITY);
     }
   }
+  if (not_finite(v[0]) || not_finite(v[4])) atomicOr(status, STATUS_NONFINITE);
 #pragma unroll
   for (int q = 0; q < NSLOT; q++)
     if (live(q, b)) U[field(q, b) * n + gid] = v[q];
@@ -673,8 +674,9 @@ __device__ __forceinline__ void block_max_to(double v, unsigned long long *dst)
 // maximum stay FP64 (maxima compare bit patterns on the integer pipe).
 template <bool MIX>
 __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict__ U, const double *__restrict__ Epre,
-                                                unsigned long long *__restrict__ dti, double U_floor, int temp_floor,
-                                                int do_dt, double idx, double idy, double idz, long long blk)
+                                                unsigned long long *__restrict__ dti, int *__restrict__ status,
+                                                double U_floor, int temp_floor, int do_dt, double idx, double idy,
+                                                double idz, long long blk)
 {
   int const ng = b.ng;
   bool const one_d = (b.ny == 1 && b.nz == 1);
@@ -725,6 +727,7 @@ __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict
         if (U[fge + id] < U_floor * d) U[fge + id] = d * U_floor;
       }
     }
+    if (bad_cell(d, E)) atomicOr(status, STATUS_NONFINITE);
     if (do_dt) {  // hydroInverseCrossingTime (hydro_cuda.cu:404-419)
       double const c2 = b.gamma * (E - ke) * (b.gamma - 1.0) * d_inv;
       double const cs = MIX ? hf::to_f64(sqrtf(hf::to_f32(hf::max_pos(c2, 0.0)))) : hf::sqrtT(hf::max_pos(c2, 0.0));
@@ -742,10 +745,11 @@ __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict
 
 template <bool MIX>
 __global__ void __launch_bounds__(256) k_ffinalize(Box b, double *__restrict__ U, const double *__restrict__ Epre,
-                                                   unsigned long long *__restrict__ dti, double U_floor,
-                                                   int temp_floor, int do_dt, double idx, double idy, double idz)
+                                                   unsigned long long *__restrict__ dti, int *__restrict__ status,
+                                                   double U_floor, int temp_floor, int do_dt, double idx, double idy,
+                                                   double idz)
 {
-  ffinalize_block<MIX>(b, U, Epre, dti, U_floor, temp_floor, do_dt, idx, idy, idz, blockIdx.x);
+  ffinalize_block<MIX>(b, U, Epre, dti, status, U_floor, temp_floor, do_dt, idx, idy, idz, blockIdx.x);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -936,7 +940,7 @@ __global__ void __launch_bounds__(256)
   int const tile    = blockIdx.x;
   int const j       = find_job(C, BK_REAL, tile);
   BatchJob const &J = C.jobs[j];
-  ffinalize_block<MIX>(J.b, J.U, J.Epre, J.dti, U_floor, temp_floor, do_dt, J.b.idx, J.b.idy, J.b.idz,
+  ffinalize_block<MIX>(J.b, J.U, J.Epre, J.dti, J.status, U_floor, temp_floor, do_dt, J.b.idx, J.b.idy, J.b.idz,
                        tile - C.off[BK_REAL][j]);
 }
 
@@ -1051,11 +1055,11 @@ cudaError_t hydro_fast_step(const Box &box, int recon, int solver, int mixed, do
         (long long)(b.nx - 2 * ng) * (one_d ? 1 : b.ny - 2 * ng) * (one_d ? 1 : b.nz - 2 * ng);
     unsigned const grid = (unsigned)((nreal + 255) / 256);
     if (mixed) {
-      k_ffinalize<true><<<grid, 256, 0, s>>>(b, U, sc.Epre, sc.dti, U_floor, temp_floor, do_dt, b.idx, b.idy,
-                                              b.idz);
+      k_ffinalize<true><<<grid, 256, 0, s>>>(b, U, sc.Epre, sc.dti, sc.status, U_floor, temp_floor, do_dt, b.idx,
+                                              b.idy, b.idz);
     } else {
-      k_ffinalize<false><<<grid, 256, 0, s>>>(b, U, sc.Epre, sc.dti, U_floor, temp_floor, do_dt, b.idx, b.idy,
-                                               b.idz);
+      k_ffinalize<false><<<grid, 256, 0, s>>>(b, U, sc.Epre, sc.dti, sc.status, U_floor, temp_floor, do_dt, b.idx,
+                                               b.idy, b.idz);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }

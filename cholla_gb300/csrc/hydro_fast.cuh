@@ -124,10 +124,15 @@ struct Eps<float> {
   static constexpr float roundoff = 1.0e-6f;  // same test scaled to single precision
 };
 
-// Reciprocal and square root.  FP64: an FP32 estimate refined by two Newton steps (4 and 5
-// FP64 FMAs instead of a ~12-instruction divide or square-root sequence); the result is within
-// an ulp or two of the correctly rounded value.  Outside the FP32 exponent range a true
-// divide / square root is used.  FP32: the hardware approximations (about 1 ulp).
+// Reciprocal and square root.  FP64: an FP32 estimate refined by Newton steps (4 and 5 FP64
+// FMAs instead of a ~12-instruction divide or square-root sequence).  rcp: two Newton-Raphson
+// steps r <- r + r (1 - d r) on the reciprocal.  sqrtT: two Newton-Raphson steps on the inverse
+// square root y <- y (3/2 - x y^2 / 2), then the square root s = x y corrected once with its own
+// residual, s + (x - s^2) y / 2 (Karp and Markstein, "High-precision division and square root",
+// ACM TOMS 23(4), 1997).  Both stay within 1 ulp of the correctly rounded result, which
+// cgb_selftest_fast_math measures against CUDA's 1 / x and sqrt over the FP32 exponent range.
+// Outside |x| in (1e-30, 1e30) a true divide / square root is used.  FP32: the hardware
+// approximations (about 1 ulp).
 __device__ __forceinline__ double rcp(double d)
 {
   float const f = to_f32(d);
@@ -147,7 +152,7 @@ __device__ __forceinline__ double sqrtT(double x)
   y              = y * fma(-h * y, y, 1.5);
   y              = y * fma(-h * y, y, 1.5);
   double const s = x * y;
-  return fma(fma(-s, s, x), 0.5 * y, s);  // final correction of the square root itself
+  return fma(fma(-s, s, x), 0.5 * y, s);  // Karp-Markstein correction of the square root
 }
 __device__ __forceinline__ float sqrtT(float x) { return __fsqrt_rn(x); }
 

@@ -1,6 +1,7 @@
 // selftest.cu -- device self-checks of arithmetic helpers that replace hardware instructions:
 // the integer-pipe binary64 <-> binary32 conversions of hydro_fast.cuh against the hardware
-// conversions, bit for bit.
+// conversions, bit for bit; the fast FP64 reciprocal and square root against CUDA's correctly
+// rounded ones.
 #include <cuda_runtime.h>
 
 #include "../../include/cholla_gb300.h"
@@ -21,7 +22,30 @@ __global__ void k_check_conversions(const double *__restrict__ x, long long n, u
     if (__double_as_longlong(c) != __double_as_longlong(d)) atomicAdd(&bad[1], 1ULL);
   }
 }
+
+// out[0 n + i] = rcp(x), out[1 n + i] = CUDA's correctly rounded 1 / x, out[2 n + i] = sqrtT(|x|),
+// out[3 n + i] = CUDA's correctly rounded sqrt(|x|)
+__global__ void k_fast_math(const double *__restrict__ x, long long n, double *__restrict__ out)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    double const v = x[i], a = fabs(v);
+    out[i]         = cgb::hf::rcp(v);
+    out[n + i]     = __drcp_rn(v);
+    out[2 * n + i] = cgb::hf::sqrtT(a);
+    out[3 * n + i] = __dsqrt_rn(a);
+  }
+}
 }  // namespace
+
+extern "C" int cgb_selftest_fast_math(const double *d_values, long long n, double *d_out, void *stream)
+{
+  if (!d_values || !d_out || n < 0) return CGB_ERR_ARGS;
+  cudaStream_t const s = (cudaStream_t)stream;
+  if (n > 0) k_fast_math<<<1024, 256, 0, s>>>(d_values, n, d_out);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? CGB_OK : CGB_ERR_CUDA;
+}
 
 extern "C" int cgb_selftest_conversions(const double *d_values, long long n, unsigned long long *mismatches,
                                         void *stream)

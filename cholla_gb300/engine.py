@@ -66,7 +66,15 @@ class Box:
         _check(L.lib().cgb_box_advance(self._h, _ptr(U), n_steps, c_cfl, C.c_void_p(handle)))
 
     def time(self):
+        """(t, last dt); raises BoxError with code CGB_ERR_NONFINITE once a step has left a bad cell."""
         t = C.c_double()
         dt = C.c_double()
         _check(L.lib().cgb_box_get_time(self._h, C.byref(t), C.byref(dt)))
         return t.value, dt.value
+
+    def check_status(self) -> int:
+        """Status bits (CGB_STATUS_*) of the steps since the last call, which clears them; raises
+        BoxError (CGB_ERR_NONFINITE) when a real cell went non-finite."""
+        f = C.c_int()
+        _check(L.lib().cgb_box_check_status(self._h, C.byref(f)))
+        return f.value

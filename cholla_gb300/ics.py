@@ -18,20 +18,48 @@ def n_fields(dual_energy: bool, mhd: bool = False, n_scalars: int = 0) -> int:
     return 5 + n_scalars + (3 if mhd else 0) + (1 if dual_energy else 0)
 
 
+try:  # multi-threaded FFTs where scipy is present (same transform as numpy's, to rounding)
+    import scipy.fft as _fft
+
+    def _rfftn(a):
+        return _fft.rfftn(a, workers=-1, overwrite_x=True)
+
+    def _irfftn(a, n):
+        return _fft.irfftn(a, s=(n, n, n), workers=-1, overwrite_x=True)
+except ImportError:  # pragma: no cover
+    def _rfftn(a):
+        return np.fft.rfftn(a)
+
+    def _irfftn(a, n):
+        return np.fft.irfftn(a, s=(n, n, n), axes=(0, 1, 2))
+
+_AMP: dict = {}
+
+
+def _spectral_amplitude(n: int, slope: float) -> np.ndarray:
+    key = (n, slope)
+    if key not in _AMP:
+        k = np.fft.fftfreq(n) * n
+        kr = np.fft.rfftfreq(n) * n
+        kk = np.sqrt(k[:, None, None] ** 2 + k[None, :, None] ** 2 + kr[None, None, :] ** 2)
+        amp = np.zeros_like(kk)
+        nz = kk > 0
+        amp[nz] = kk[nz] ** ((slope - 2.0) / 2.0)
+        _AMP.clear()
+        _AMP[key] = amp
+    return _AMP[key]
+
+
 def gaussian_random_field(n: int, slope: float, rng: np.random.Generator) -> np.ndarray:
     """Periodic unit-variance Gaussian random field on n^3 cells whose spectrum, summed over
     shells of |k| (the turbulence convention, E(k) dk), goes as k^slope: Fourier amplitudes
     |f_k| ~ k^((slope - 2) / 2).  (A k^-2 slope is Burgers-like: smooth at the grid scale.  With
     the slope put on |f_k|^2 instead, a k^-2 field is white at the grid scale, with Mach-2 jumps
     between neighbouring cells from which even the exact FP64 scheme fails within a few steps.)"""
-    k = np.fft.fftfreq(n) * n
-    kr = np.fft.rfftfreq(n) * n
-    kk = np.sqrt(k[:, None, None] ** 2 + k[None, :, None] ** 2 + kr[None, None, :] ** 2)
-    amp = np.zeros_like(kk)
-    nz = kk > 0
-    amp[nz] = kk[nz] ** ((slope - 2.0) / 2.0)
-    noise = rng.standard_normal((n, n, n))
-    f = np.fft.irfftn(np.fft.rfftn(noise) * amp, s=(n, n, n), axes=(0, 1, 2))
+    amp = _spectral_amplitude(n, slope)
+    spec = _rfftn(rng.standard_normal((n, n, n)))
+    spec *= amp
+    f = _irfftn(spec, n)
     f -= f.mean()
     f /= f.std()
     return f
@@ -42,12 +70,52 @@ def pad_periodic(real: np.ndarray, ng: int) -> np.ndarray:
     return np.ascontiguousarray(np.pad(real, ((0, 0), (ng, ng), (ng, ng), (ng, ng)), mode="wrap"))
 
 
+def _turbulence_box_torch(torch, n, ng, gamma, rng, sigma, mach, pressure, dual_energy):
+    """turbulence_box with the transforms and the arithmetic in torch's multi-threaded CPU kernels
+    (the same noise, spectrum and formulas; results agree with the numpy form to rounding)."""
+
+    def grf(slope):
+        f = torch.fft.irfftn(torch.fft.rfftn(torch.from_numpy(rng.standard_normal((n, n, n)))) *
+                             torch.from_numpy(_spectral_amplitude(n, slope)), s=(n, n, n))
+        f -= f.mean()
+        f /= f.std(correction=0)
+        return f
+
+    g = grf(-2.0)
+    rho = torch.exp(sigma * g - 0.5 * sigma * sigma)
+    del g
+    v = torch.stack([grf(-2.0) for _ in range(3)])
+    cs = math.sqrt(gamma * pressure / 1.0)
+    v2 = (v * v).sum(dim=0)
+    scale = mach * cs / math.sqrt(float(v2.mean()))
+    v *= scale
+    v2 *= scale * scale
+    nf = n_fields(dual_energy)
+    U = torch.empty((1, nf, n, n, n), dtype=torch.float64)
+    U[0, 0] = rho
+    U[0, 1:4] = rho * v
+    eint = pressure / (gamma - 1.0)
+    U[0, 4] = eint + 0.5 * rho * v2
+    if dual_energy:
+        U[0, nf - 1] = eint
+    del v, v2, rho
+    out = torch.nn.functional.pad(U, (ng,) * 6, mode="circular")[0]
+    return np.ascontiguousarray(out.numpy())
+
+
 def turbulence_box(n: int, ng: int = 4, gamma: float = 5.0 / 3.0, seed: int = 0, sigma: float = 0.5,
                    mach: float = 2.0, pressure: float = 1.0, dual_energy: bool = True) -> np.ndarray:
     """Periodic cube of side 1: lognormal density (mean 1, sigma) from a Gaussian field with a
     k^-2 shell spectrum, three independent k^-2 velocity fields scaled to rms Mach `mach`,
     uniform pressure."""
     rng = np.random.default_rng(seed)
+    if n >= 96:  # large boxes: multi-threaded transforms and arithmetic
+        try:
+            import torch
+
+            return _turbulence_box_torch(torch, n, ng, gamma, rng, sigma, mach, pressure, dual_energy)
+        except ImportError:  # pragma: no cover
+            pass
     g = gaussian_random_field(n, -2.0, rng)
     rho = np.exp(sigma * g - 0.5 * sigma * sigma)
     v = np.stack([gaussian_random_field(n, -2.0, rng) for _ in range(3)])

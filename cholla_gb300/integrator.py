@@ -127,3 +127,27 @@ def Max_Magnetic_Divergence(dev_conserved, nx, ny, nz, n_ghost, n_fields, dx, dy
     L.check(L.lib().cgb_max_magnetic_divergence(_ptr(dev_conserved), nx, ny, nz, n_ghost, n_fields, dx, dy, dz,
                                                 C.byref(out)))
     return out.value
+
+
+def Check_Magnetic_Divergence(dev_conserved, nx, ny, nz, n_ghost, n_fields, dx, dy, dz) -> float:
+    """checkMagneticDivergence (src/mhd/magnetic_divergence.cu:92-120): the maximum |div B|, raising
+    CgbError with CGB_ERR_NONFINITE where the reference would exit (above 1e-9, negative or NaN)."""
+    out = C.c_double(0.0)
+    rc = L.lib().cgb_check_magnetic_divergence(_ptr(dev_conserved), nx, ny, nz, n_ghost, n_fields, dx, dy, dz,
+                                               C.byref(out))
+    L.check(rc)
+    return out.value
+
+
+def Check_Status() -> int:
+    """Status bits (CGB_STATUS_*) the drop-in steps collected since the last call, which clears
+    them; raises CgbError (CGB_ERR_NONFINITE) when a real cell went non-finite.  The reference
+    prints such cells from the device (src/hydro/hydro_cuda.cu:381-389)."""
+    f = C.c_int(0)
+    L.check(L.lib().cgb_check_status(C.byref(f)))
+    return f.value
+
+
+def debug_fail_alloc(n: int) -> None:
+    """Make the n-th device allocation of the library from now on fail (0: off).  Test hook."""
+    L.check(L.lib().cgb_debug_fail_alloc(int(n)))

@@ -31,6 +31,15 @@ extern "C" {
 #define CGB_ERR_TIMEOUT     5  /* a bounded device wait ran out */
 #define CGB_ERR_UNSUPPORTED 6  /* option combination not built */
 
+/* bits of the device status word a step leaves (cgb_check_status, cgb_box_check_status,
+   cgb_batch_job_status) */
+#define CGB_STATUS_NEG_DENSITY 1 /* an update gave a real cell density <= 0; the step repaired it by averaging
+                                    the six neighbours (hydro_cuda.cu:296 Average_Cell_Single_Field) */
+#define CGB_STATUS_NONFINITE   2 /* a real cell holds non-finite density or total energy, or density <= 0
+                                    after that repair: the state is unusable */
+/* largest |div B| cgb_check_magnetic_divergence accepts (src/mhd/magnetic_divergence.cu:105) */
+#define CGB_MAX_DIVB 1.0e-9
+
 /* reconstruction (builds/make.type.*: -DPCM / -DPLMC / -DPPMC; -DPLMP / -DPPMP are the
    primitive-limited forms of src/reconstruction/plmp_cuda.cu and ppmp_cuda.cu, which
    cgb_set_scheme rejects with CGB_ERR_UNSUPPORTED: their kernels are not built yet) */
@@ -96,16 +105,31 @@ int cgb_vl_algorithm_3d(double *d_conserved, double *d_grav_potential, int nx, i
  * call on a device is when those 24 MiB leave the free pool).  Its address is looked up once
  * per device (cudaGetSymbolAddress, with that device current) on the first call there, so
  * make that first call before capturing any stream that will contain this call.
- * Limit: a box whose scratch exceeds the pool is rejected with CGB_ERR_ARGS and a message
- * (6 fields: up to 393,216 padded cells, e.g. 73^3, with CGB_FP64; 196,608, e.g. 58^3, with
- * CGB_FP64_FAST or CGB_MIXED).  Each call clears the pool's status word on the stream before
- * the step; nothing else in the pool needs to start at zero.  There is one pool per device:
- * calls that can overlap in time (from several host threads, or queued on streams that run
- * concurrently) race on it and corrupt each other's results, so serialise them. */
+ * Limit: a box whose scratch exceeds the pool is rejected with CGB_ERR_ARGS and a message.  With
+ * n padded cells and f fields the scratch is (f + 2) * 8 * n bytes with CGB_FP64 and
+ * (2 f + 4) * 8 * n bytes with CGB_FP64_FAST or CGB_MIXED, each array rounded up to 256 bytes,
+ * plus 512 bytes: with 6 fields, fewer than 393,216 padded cells (e.g. 73^3) in FP64 and fewer
+ * than 196,608 (e.g. 58^3) in the fast forms.  The FP64 form has no room for the sweeps'
+ * accumulator here, so it runs the corrector as one fused tile per 8 x 8 x 4 cells: the same
+ * result bit for bit as cgb_vl_algorithm_3d, at about 0.8x its speed.  Each call clears the
+ * pool's status word on the stream before the step; nothing else in the pool needs to start at
+ * zero.  There is one pool per device: calls that can overlap in time (from several host
+ * threads, or queued on streams that run concurrently) race on it and corrupt each other's
+ * results, so serialise them.  The pool's address is cached per device ordinal for the life of
+ * the process: after cudaDeviceReset (or any teardown of the device's primary context) do not
+ * call this entry point again in that process. */
 int cgb_vl_algorithm_3d_static(double *d_conserved, double *d_grav_potential, int nx, int ny, int nz, int x_off,
                                int y_off, int z_off, int n_ghost, double dx, double dy, double dz, double xbound,
                                double ybound, double zbound, double dt, int n_fields, int custom_grav,
                                double density_floor, double *host_grav_potential);
+
+/* Bad-cell report of the drop-in steps (cgb_vl_algorithm_3d, cgb_vl_algorithm_1d): the status
+ * bits (CGB_STATUS_*) their steps collected since the last call, which clears them; synchronises
+ * the library's stream.  Returns CGB_ERR_NONFINITE (message in cgb_last_error) when
+ * CGB_STATUS_NONFINITE is set.  The reference prints such cells from the device and carries on
+ * (src/hydro/hydro_cuda.cu:381-389); this library counts them on the device and reports on request,
+ * so the step itself never synchronises. */
+int cgb_check_status(int *flags);
 
 /* Replaces VL_Algorithm_1D_CUDA (src/integrators/VL_1D_cuda.h, VL_1D_cuda.cu:30-146). */
 int cgb_vl_algorithm_1d(double *d_conserved, int nx, int x_off, int n_ghost, double dx, double xbound, double dt,
@@ -139,6 +163,11 @@ int cgb_set_boundaries(double *d_conserved, int nx, int ny, int nz, int n_ghost,
  * not change the range. */
 int cgb_max_magnetic_divergence(const double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields,
                                 double dx, double dy, double dz, double *max_divb);
+/* The reference's checkMagneticDivergence (src/mhd/magnetic_divergence.cu:92-120): the same maximum
+ * into *max_divb, and CGB_ERR_NONFINITE (instead of the reference's process exit) when it exceeds
+ * CGB_MAX_DIVB or is negative or NaN. */
+int cgb_check_magnetic_divergence(const double *d_conserved, int nx, int ny, int nz, int n_ghost, int n_fields,
+                                  double dx, double dy, double dz, double *max_divb);
 
 /* ---- box handles: device-resident stepping of many boxes (no counterpart in the reference,
  * which can hold one box shape per process: its scratch is file-scope globals) ---- */
@@ -163,8 +192,12 @@ int cgb_box_kernel_times(cgb_box *box, double ms[3], long long *steps);
  * (clamped to t_end), VL step, temperature floor, CFL reduction for the next step.  The time
  * step never leaves the device; nothing synchronises with the host. */
 int cgb_box_advance(cgb_box *box, double *d_conserved, int n_steps, double c_cfl, void *stream);
-/* Current time and last dt (synchronises the last stream used with the box). */
+/* Current time and last dt (synchronises the last stream used with the box).  Returns
+ * CGB_ERR_NONFINITE, with t and dt_last filled in, while the box's status word records a bad cell. */
 int cgb_box_get_time(cgb_box *box, double *t, double *dt_last);
+/* Status bits (CGB_STATUS_*) of the box's steps since the last call, which clears them (synchronises
+ * the box's last stream); CGB_ERR_NONFINITE when CGB_STATUS_NONFINITE is set. */
+int cgb_box_check_status(cgb_box *box, int *flags);
 const char *cgb_box_last_error(void);
 
 /* ---- batches: many independent 3D boxes of one scheme advanced together (no counterpart in
@@ -200,14 +233,28 @@ int cgb_batch_set_solo_cells(cgb_batch *batch, long long cells);
 int cgb_batch_set_chains(cgb_batch *batch, int chains);
 /* Advance every job by n_steps on the batch stream (no host synchronisation). */
 int cgb_batch_step(cgb_batch *batch, int n_steps);
-/* Time and last dt of one job (synchronises the batch stream). */
+/* Time and last dt of one job (synchronises the batch stream).  Returns CGB_ERR_NONFINITE, with t and
+ * dt_last filled in, while the job's status word records a bad cell (the other jobs are unaffected). */
 int cgb_batch_job_time(cgb_batch *batch, int job_id, double *t, double *dt_last);
+/* Status bits (CGB_STATUS_*) of one job's steps so far (not cleared; synchronises the batch stream);
+ * CGB_ERR_NONFINITE when CGB_STATUS_NONFINITE is set. */
+int cgb_batch_job_status(cgb_batch *batch, int job_id, int *flags);
 const char *cgb_batch_last_error(void);
 
 /* ---- self-check: the integer-pipe binary64 <-> binary32 conversions of the mixed form against
  * the hardware conversions, on the n doubles at d_values (and the binary32 in each low word);
  * mismatches[0] (narrowing) and [1] (widening) receive the counts.  Synchronises `stream`. ---- */
 int cgb_selftest_conversions(const double *d_values, long long n, unsigned long long *mismatches, void *stream);
+/* ---- self-check: the fast FP64 form's reciprocal and square root (an FP32 estimate refined by Newton
+ * steps) beside CUDA's correctly rounded ones, on the n doubles at d_values: d_out[0..n) the fast
+ * 1/x, [n..2n) CUDA's 1/x, [2n..3n) the fast sqrt(|x|), [3n..4n) CUDA's sqrt(|x|).  Synchronises
+ * `stream`. ---- */
+int cgb_selftest_fast_math(const double *d_values, long long n, double *d_out, void *stream);
+
+/* ---- fault injection for tests (no counterpart in the reference): the n-th device allocation the
+ * library makes from now on (1 = the next; 0 = off) reports out-of-memory without calling CUDA, so
+ * each entry point's CGB_ERR_NOMEM path can be exercised on the host.  Nothing runs on the GPU. ---- */
+int cgb_debug_fail_alloc(int n);
 
 /* ---- initial conditions on the device (the serving workload's problems) ---- */
 /* Blast: uniform density rho and pressure p, plus thermal energy `energy` spread uniformly

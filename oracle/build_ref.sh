@@ -6,7 +6,7 @@
 # API to run the reference's VL step on the GPU as the parity and speed baseline.
 # Usage: oracle/build_ref.sh /path/to/cholla
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${CHOLLA_REFERENCE:-$(cd "$(dirname "$0")/../.." && pwd)/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 NVCC=${NVCC:-nvcc}

@@ -6,7 +6,7 @@
 # -ffp-contract=off is the host counterpart of the reference Makefile's -fmad=false (Makefile:70).
 # Usage: oracle/build_ref_host.sh /path/to/cholla
 set -euo pipefail
-REF=${1:-/root/reference}
+REF=${1:-${CHOLLA_REFERENCE:-$(cd "$(dirname "$0")/../.." && pwd)/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref/host"
 CXX=${CXX:-g++}

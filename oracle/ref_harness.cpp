@@ -33,6 +33,9 @@ struct Scratch {
   CUdeviceptr Uh = 0, QLx = 0, QRx = 0, QLy = 0, QRy = 0, QLz = 0, QRz = 0, Fx = 0, Fy = 0, Fz = 0, emf = 0, dti = 0;
 } g_s;
 CUstream g_stream = nullptr;
+// the reference's default build synchronises the device after every kernel (GPU_Error_Check ->
+// cudaDeviceSynchronize, src/utils/gpu.hpp:139-155); -DDISABLE_GPU_ERROR_CHECKING removes it
+bool g_sync_each = false;
 
 int err(const std::string &m)
 {
@@ -69,7 +72,8 @@ int launch(const char *name, size_t nthreads, A... args)
   void *p[] = {(void *)&args...};
   unsigned const tpb  = 256;
   unsigned const grid = (unsigned)((nthreads + tpb - 1) / tpb);
-  return cu(cuLaunchKernel(f, grid, 1, 1, tpb, 1, 1, 0, g_stream, p, nullptr), name);
+  if (cu(cuLaunchKernel(f, grid, 1, 1, tpb, 1, 1, 0, g_stream, p, nullptr), name)) return 1;
+  return g_sync_each ? cu(cuCtxSynchronize(), name) : 0;
 }
 
 void free_scratch()
@@ -314,6 +318,13 @@ int refh_set_boundaries(unsigned long long U_, int nx, int ny, int nz, int ng, i
 }
 
 int refh_sync(void) { return cu(cuStreamSynchronize(g_stream), "sync"); }
+
+// 1: synchronise the context after every kernel, as the reference's default build does
+int refh_set_sync_each(int on)
+{
+  g_sync_each = on != 0;
+  return 0;
+}
 
 int refh_free(void)
 {

@@ -39,6 +39,7 @@ def _load() -> C.CDLL:
         h.refh_calc_dt.argtypes = [U, I, I, I, I, I, D, D, D, D, C.POINTER(D)]
         h.refh_temperature_floor.argtypes = [U, I, I, I, I, I, D]
         h.refh_set_boundaries.argtypes = [U, I, I, I, I, I, C.POINTER(I)]
+        h.refh_set_sync_each.argtypes = [I]
         _lib = h
     return _lib
 
@@ -85,3 +86,9 @@ def set_boundaries(U, nx, ny, nz, ng, nf, flags) -> None:
 
 def sync() -> None:
     _check(_load().refh_sync())
+
+
+def set_sync_each(on: bool) -> None:
+    """Synchronise after every kernel (the reference's default build, src/utils/gpu.hpp:139-155) or
+    not (its -DDISABLE_GPU_ERROR_CHECKING build, the default here)."""
+    _check(_load().refh_set_sync_each(int(bool(on))))

@@ -30,7 +30,7 @@ def ref_host(oracle_lib):
 
     from oracle import ref_host
 
-    tree = Path(os.environ.get("CHOLLA_REFERENCE", "/root/reference"))
+    tree = Path(os.environ.get("CHOLLA_REFERENCE", ROOT.parent / "reference"))
     if tree.is_dir():
         subprocess.run(["bash", str(ROOT / "oracle" / "build_ref_host.sh"), str(tree)], check=True,
                        stdout=subprocess.DEVNULL)

@@ -1,6 +1,7 @@
 """Extract the golden vectors of the reference's unit tests into reference_fiducials.json.
 
-Run in a container where the reference source tree is mounted (default /root/reference):
+Run where the reference source tree is present (the argument, else $CHOLLA_REFERENCE, else a
+directory named `reference` beside the repository):
 
     python tests/golden/extract_reference_fiducials.py [/path/to/cholla]
 
@@ -12,6 +13,7 @@ from __future__ import annotations
 
 import json
 import math
+import os
 import re
 import sys
 from pathlib import Path
@@ -584,7 +586,7 @@ def constant_state_cases(src_dir: Path) -> dict:
 
 
 def main() -> None:
-    root = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = Path(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("CHOLLA_REFERENCE", Path(__file__).resolve().parents[3] / "reference"))
     src = root / "src"
     data = {
         "note": "golden vectors read from the reference's unit tests by extract_reference_fiducials.py",

@@ -1,0 +1,160 @@
+"""Parity and accuracy at the sizes the headline workloads are quoted on.
+
+* 256^3 hydro (PPMC + HLLC + VL, dual energy, floors; lognormal density, k^-2 velocities at rms
+  Mach 2), 20 steps at CFL 0.3: the exact FP64 form against the reference's own CUDA build on the
+  same dt sequence (relative L1 per field <= 1e-12: at Mach 2 cells reach negative density, which
+  the reference averages while neighbouring threads still update, hydro_cuda.cu:296-311, so a
+  bitwise claim cannot hold there), and the fast FP64 (<= 1e-12) and mixed (density <= 1e-5)
+  forms against the exact form on the same dt sequence.
+* 256^3 ideal MHD (PLMC + HLLD + CT, beta 1), 20 steps: exact FP64 against the reference build
+  bit for bit, fast FP64 against exact within 1e-12, div B at roundoff.
+* 512^3 mixed precision, 50 steps, against the exact FP64 form on the same dt sequence: relative
+  L1 of density, momenta and energy <= 1e-5; mass conserved to roundoff.
+
+Each test prints its per-field errors.
+"""
+import json
+
+import numpy as np
+import pytest
+
+from helpers import real_slice
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("density", "momentum_x", "momentum_y", "momentum_z", "Energy", "GasEnergy")
+
+
+@pytest.fixture(scope="module")
+def ref():
+    from oracle import reference_gpu as R
+
+    if not R.available():
+        pytest.skip("reference cubins not built (oracle/build_ref.sh needs the cholla source tree)")
+    return R
+
+
+def _rel_l1(a, b):
+    """sum |a - b| / sum |b| per field over the given (real-cell) arrays, as torch tensors."""
+    return ((a - b).abs().sum(dim=(1, 2, 3)) / b.abs().sum(dim=(1, 2, 3))).cpu().numpy()
+
+
+def test_config2_256_hydro_forms_and_reference(cuda, ref):
+    from cholla_gb300 import accuracy, ics
+    from cholla_gb300 import integrator as I
+
+    n, ng, gamma, steps = 256, 4, 5 / 3, 20
+    U0 = ics.turbulence_box(n, ng, gamma, seed=0, mach=2.0)
+    nf, N = U0.shape[0], U0.shape[1]
+    dx = 1 / n
+    rs = real_slice(ng)
+    host = cuda.from_numpy(U0)
+    Ue = host.to("cuda")
+    dts = accuracy._steps(cuda, Ue, n, ng, "fp64", steps)  # exact form, its own CFL steps
+    exact = Ue[rs].clone()
+    del Ue
+    # the reference build, driven by the same dt sequence (step, temperature floor, ghost fill)
+    ref.init("hydro_ppmc_hllc_de")
+    Ur = host.to("cuda")
+    for dt in dts:
+        ref.set_boundaries(Ur, N, N, N, ng, nf, (1,) * 6)
+        ref.vl_step_3d(Ur, N, N, N, ng, dx, dx, dx, dt, nf, gamma, 0.0)
+        ref.temperature_floor(Ur, N, N, N, ng, nf, 0.0)
+    ref.sync()
+    err_ref = _rel_l1(Ur[rs], exact)
+    same = int((Ur[rs] == exact).sum().item())
+    del Ur
+    out = {"reference_build_vs_exact": dict(zip(FIELDS, map(float, err_ref))),
+           "bitwise_equal_fraction": same / exact.numel()}
+    for form in ("fp64_fast", "mixed"):
+        Uf = host.to("cuda")
+        accuracy._steps(cuda, Uf, n, ng, form, steps, dts)
+        out[f"{form}_vs_exact"] = dict(zip(FIELDS, map(float, _rel_l1(Uf[rs], exact))))
+        del Uf
+    I.set_scheme(I.Scheme())
+    print(json.dumps(out))
+    assert np.all(err_ref <= 1e-12), out
+    assert max(out["fp64_fast_vs_exact"].values()) <= 1e-12, out
+    assert out["mixed_vs_exact"]["density"] <= 1e-5, out
+
+
+def test_config3_256_mhd_reference_exact_fast(cuda):
+    from oracle import reference_gpu as R
+
+    from cholla_gb300 import ics
+    from cholla_gb300 import integrator as I
+
+    if not R.available("mhd_plmc_hlld"):
+        pytest.skip("reference MHD cubins not built")
+    n, gamma, steps = 256, 5 / 3, 20
+    s = I.Scheme(reconstruction="PLMC", riemann_solver="HLLD", mhd=True, dual_energy=False, gamma=gamma)
+    ng = s.n_ghost()
+    U0 = ics.mhd_box(n, ng, gamma, seed=1)
+    nf, N = U0.shape[0], U0.shape[1]
+    dx = 1 / n
+    rs = real_slice(ng)
+    host = cuda.from_numpy(U0)
+    I.set_scheme(s)
+    Ue = host.to("cuda")
+    dts = []
+    for _ in range(steps):
+        I.Set_Boundaries(Ue, N, N, N, ng, nf, (1,) * 6)
+        dt = 0.3 / I.Calc_dt_GPU(Ue, N, N, N, ng, nf, dx, dx, dx, gamma)
+        I.VL_Algorithm_3D_CUDA(Ue, None, N, N, N, 0, 0, 0, ng, dx, dx, dx, 0, 0, 0, dt, nf, 0, 0.0)
+        dts.append(dt)
+    I.Set_Boundaries(Ue, N, N, N, ng, nf, (1,) * 6)
+    divb = I.Check_Magnetic_Divergence(Ue, N, N, N, ng, nf, dx, dx, dx)
+    cuda.cuda.synchronize()
+    R.init("mhd_plmc_hlld")
+    Ur = host.to("cuda")
+    for dt in dts:
+        R.set_boundaries(Ur, N, N, N, ng, nf, (1,) * 6)
+        R.vl_step_3d(Ur, N, N, N, ng, dx, dx, dx, dt, nf, gamma, 0.0)
+    R.sync()
+    exact = Ue[rs]
+    nbad = int((Ur[rs].view(cuda.int64) != exact.view(cuda.int64)).sum().item())
+    del Ur
+    I.set_scheme(I.Scheme(reconstruction="PLMC", riemann_solver="HLLD", mhd=True, dual_energy=False, gamma=gamma,
+                          precision="fp64_fast"))
+    Uf = host.to("cuda")
+    for dt in dts:
+        I.Set_Boundaries(Uf, N, N, N, ng, nf, (1,) * 6)
+        I.VL_Algorithm_3D_CUDA(Uf, None, N, N, N, 0, 0, 0, ng, dx, dx, dx, 0, 0, 0, dt, nf, 0, 0.0)
+    cuda.cuda.synchronize()
+    err = _rel_l1(Uf[rs][:5], exact[:5])
+    I.set_scheme(I.Scheme())
+    print(json.dumps({"reference_build_values_differing": nbad, "fast_vs_exact": list(map(float, err)),
+                      "max_div_b": divb}))
+    assert nbad == 0
+    assert np.all(err <= 1e-12), err
+    assert divb <= 1e-9
+
+
+def test_config4_512_mixed_50_steps(cuda):
+    from cholla_gb300 import accuracy
+
+    free = cuda.cuda.mem_get_info()[0]
+    if free < 40 << 30:
+        pytest.skip("needs about 40 GB of free device memory")
+    res = accuracy.run(cuda, n=512, steps=50, seed=0, forms=("mixed",))
+    print(json.dumps(res))
+    l1 = res["rel_l1"]["mixed"]
+    for f in ("density", "momentum_x", "momentum_y", "momentum_z", "Energy"):
+        assert l1[f] <= 1e-5, (f, l1[f])
+    assert res["conservation"]["mixed"]["mass"] <= 1e-12
+
+
+def test_config5_served_jobs_against_fp64_twins(cuda):
+    """Every job of a short serving stream (blasts and tubes, mixed precision, 100 steps) against
+    its exact FP64 twin on the job's own dt sequence.  Bound: relative L1 density <= 1e-4 per job
+    (the blast's p = 1e-5 ambient gas and its strong shock make it the least forgiving case)."""
+    from cholla_gb300 import accuracy, serve
+
+    reqs = serve.make_requests(rate=100.0, count=6, seed=5, steps=100, sizes=(32, 48))
+    res = accuracy.serving_twins(cuda, reqs)
+    print(json.dumps(res))
+    assert {r["kind"] for r in res} == {"blast", "tube"} or len(res) == 6
+    for r in res:
+        l1 = r["rel_l1"]
+        assert all(np.isfinite(v) for v in l1.values()), r
+        assert l1["density"] <= 1e-4, r

@@ -75,3 +75,25 @@ def test_static_step_rejects_box_larger_than_pool(cuda, precision, n):
     msg = lib.cgb_last_error().decode()
     assert "static pool" in msg and "bytes" in msg, msg
     I.set_scheme(I.Scheme())
+
+
+@pytest.mark.parametrize("precision,N", [("fp64", 73), ("fp64_fast", 58), ("mixed", 58)])
+def test_static_step_accepts_largest_box(cuda, precision, N):
+    """The largest cube the pool holds with 6 fields: 73^3 padded cells in FP64 ((f + 2) 8 n bytes),
+    58^3 in the fast forms ((2 f + 4) 8 n bytes), each plus 512 bytes and array rounding."""
+    from cholla_gb300 import _lib, ics
+    from cholla_gb300 import integrator as I
+
+    lib = _lib.lib()
+    ng = 4
+    n = N - 2 * ng
+    U0 = ics.turbulence_box(n, ng, 5 / 3, seed=9)
+    nf = U0.shape[0]
+    I.set_scheme(I.Scheme(reconstruction="PPMC", riemann_solver="HLLC", dual_energy=True, precision=precision))
+    U = cuda.from_numpy(U0.copy()).cuda()
+    dt = 0.3 / I.Calc_dt_GPU(U, N, N, N, ng, nf, 1 / n, 1 / n, 1 / n, 5 / 3)
+    rc = _static_step(lib, U, N, ng, 1 / n, dt, nf)
+    assert rc == _lib.CGB_OK, lib.cgb_last_error().decode()
+    cuda.cuda.synchronize()
+    assert np.isfinite(U.cpu().numpy()[real_slice(ng)]).all()
+    I.set_scheme(I.Scheme())
