@@ -25,6 +25,10 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relax
 # same MHD source with contraction: the fast FP64 form).
 PER_FILE = {
     "hydro_exact.cu": ["-fmad=false"],
+    "hydro_exact_hllc.cu": ["-fmad=false"],
+    "hydro_exact_roe.cu": ["-fmad=false"],
+    "hydro_exact_hll.cu": ["-fmad=false"],
+    "hydro_exact_exact.cu": ["-fmad=false"],
     "mhd_exact.cu": ["-fmad=false"],
 }
 

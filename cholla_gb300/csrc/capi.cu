@@ -103,10 +103,10 @@ int check_scheme(const cgb_scheme &s)
 {
   if (s.reconstruction < CGB_PCM || s.reconstruction > CGB_PPMP) return fail(CGB_ERR_ARGS, "bad reconstruction");
   if (s.riemann_solver < CGB_HLLC || s.riemann_solver > CGB_EXACT) return fail(CGB_ERR_ARGS, "bad riemann solver");
-  if (s.reconstruction == CGB_PLMP || s.reconstruction == CGB_PPMP)
-    return fail(CGB_ERR_UNSUPPORTED, "the primitive-limited PLMP / PPMP reconstructions are not built in this library");
-  if (s.riemann_solver == CGB_HLL || s.riemann_solver == CGB_EXACT)
-    return fail(CGB_ERR_UNSUPPORTED, "the HLL and exact Riemann solvers are not built in this library");
+  if ((s.reconstruction == CGB_PLMP || s.reconstruction == CGB_PPMP || s.riemann_solver == CGB_HLL ||
+       s.riemann_solver == CGB_EXACT) &&
+      s.precision != CGB_FP64)
+    return fail(CGB_ERR_UNSUPPORTED, "PLMP, PPMP, HLL and the exact solver are built in the exact FP64 form (CGB_FP64) only");
   if (s.n_scalars < 0 || s.n_scalars > cgb::NS_MAX) return fail(CGB_ERR_ARGS, "n_scalars must be 0..2");
   if (!(s.gamma > 1.0)) return fail(CGB_ERR_ARGS, "gamma must exceed 1");
   if (s.mhd && s.riemann_solver != CGB_HLLD) return fail(CGB_ERR_ARGS, "MHD needs the HLLD solver");
@@ -115,6 +115,18 @@ int check_scheme(const cgb_scheme &s)
     return fail(CGB_ERR_UNSUPPORTED, "MHD with dual energy is not supported (the reference indexes past its flux arrays)");
   if (s.precision < CGB_FP64 || s.precision > CGB_FP64_FAST) return fail(CGB_ERR_ARGS, "bad precision");
   return CGB_OK;
+}
+
+// ghost layers the reconstruction's stencil needs (the reference's n_ghost, grid3D.cpp:53-76)
+int ghosts_needed(const cgb_scheme &s)
+{
+  switch (s.reconstruction) {
+    case CGB_PPMC:
+    case CGB_PPMP: return 4;
+    case CGB_PLMC:
+    case CGB_PLMP: return 3;
+    default: return 2;
+  }
 }
 
 int expected_fields(const cgb_scheme &s) { return 5 + s.n_scalars + (s.mhd ? 3 : 0) + (s.dual_energy ? 1 : 0); }
@@ -257,8 +269,7 @@ int cgb_vl_algorithm_3d(double *d_conserved, double *d_grav_potential, int nx, i
   cgb::Box b;
   int rc = make_box(b, nx, ny, nz, n_ghost, n_fields, dx, dy, dz, density_floor, g_scheme);
   if (rc != CGB_OK) return rc;
-  int const H = (g_scheme.reconstruction == CGB_PPMC ? 4 : g_scheme.reconstruction == CGB_PLMC ? 3 : 2) +
-                (g_scheme.mhd ? 1 : 0);
+  int const H = ghosts_needed(g_scheme) + (g_scheme.mhd ? 1 : 0);
   if (n_ghost < H) return fail(CGB_ERR_ARGS, "n_ghost too small for the reconstruction");
   if (g_scheme.mhd && g_scheme.precision == CGB_MIXED)
     return fail(CGB_ERR_UNSUPPORTED, "the MHD step is built in exact and fast FP64 only");
@@ -291,7 +302,7 @@ int cgb_vl_algorithm_3d_static(double *d_conserved, double *d_grav_potential, in
   cgb::Box b;
   int rc = make_box(b, nx, ny, nz, n_ghost, n_fields, dx, dy, dz, density_floor, g_scheme);
   if (rc != CGB_OK) return rc;
-  int const H = g_scheme.reconstruction == CGB_PPMC ? 4 : g_scheme.reconstruction == CGB_PLMC ? 3 : 2;
+  int const H = ghosts_needed(g_scheme);
   if (n_ghost < H) return fail(CGB_ERR_ARGS, "n_ghost too small for the reconstruction");
   if (g_scheme.mhd) return fail(CGB_ERR_UNSUPPORTED, "the static-pool step is hydro only");
   size_t const need = static_layout(b, g_scheme.precision, nullptr, nullptr);
@@ -322,6 +333,8 @@ int cgb_vl_algorithm_1d(double *d_conserved, int nx, int x_off, int n_ghost, dou
   if (!d_conserved) return fail(CGB_ERR_ARGS, "null d_conserved");
   if (custom_grav) return fail(CGB_ERR_UNSUPPORTED, "gravity source terms are not part of this library");
   if (g_scheme.mhd) return fail(CGB_ERR_UNSUPPORTED, "the 1D integrator is hydro only");
+  if (g_scheme.riemann_solver == CGB_HLL)
+    return fail(CGB_ERR_UNSUPPORTED, "the reference's 1D integrator has no HLL branch (VL_1D_cuda.cu)");
   if (nx < 2 * n_ghost + 1) return fail(CGB_ERR_ARGS, "1D step needs at least one real cell");
   cgb::Box b;
   int rc = make_box(b, nx, 1, 1, n_ghost, n_fields, dx, dx, dx, 0.0, g_scheme);

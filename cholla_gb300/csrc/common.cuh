@@ -36,8 +36,9 @@ __device__ __forceinline__ bool bad_cell(double d, double E)
 cudaError_t dev_malloc(void **p, size_t bytes);
 cudaError_t dev_malloc_pool_async(void **p, size_t bytes, cudaMemPool_t pool, cudaStream_t s);
 
-enum Recon { RECON_PCM = 0, RECON_PLMC = 1, RECON_PPMC = 2 };
-enum Solver { SOLVER_HLLC = 0, SOLVER_ROE = 1, SOLVER_HLLD = 2 };
+// the values of the C ABI's CGB_PCM .. CGB_PPMP and CGB_HLLC .. CGB_EXACT
+enum Recon { RECON_PCM = 0, RECON_PLMC = 1, RECON_PPMC = 2, RECON_PLMP = 3, RECON_PPMP = 4 };
+enum Solver { SOLVER_HLLC = 0, SOLVER_ROE = 1, SOLVER_HLLD = 2, SOLVER_HLL = 3, SOLVER_EXACT = 4 };
 
 // Everything a kernel needs to know about one padded box.  Passed by value.
 struct Box {

@@ -135,15 +135,21 @@ int cgb_box_create(cgb_box **out, int nx, int ny, int nz, int n_ghost, double dx
   if (s.reconstruction < CGB_PCM || s.reconstruction > CGB_PPMP || s.riemann_solver < CGB_HLLC ||
       s.riemann_solver > CGB_EXACT)
     return box_fail(nullptr, CGB_ERR_ARGS, "bad reconstruction or riemann solver");
-  if (s.reconstruction >= CGB_PLMP || s.riemann_solver >= CGB_HLL)
-    return box_fail(nullptr, CGB_ERR_UNSUPPORTED, "PLMP, PPMP, HLL and the exact solver are not built in this library");
+  if ((s.reconstruction >= CGB_PLMP || s.riemann_solver >= CGB_HLL) && s.precision != CGB_FP64)
+    return box_fail(nullptr, CGB_ERR_UNSUPPORTED,
+                    "PLMP, PPMP, HLL and the exact solver are built in the exact FP64 form (CGB_FP64) only");
   if (s.precision < CGB_FP64 || s.precision > CGB_FP64_FAST) return box_fail(nullptr, CGB_ERR_ARGS, "bad precision");
   if (s.n_scalars < 0 || s.n_scalars > cgb::NS_MAX || !(s.gamma > 1.0) || (s.riemann_solver == CGB_HLLD) != (s.mhd != 0))
     return box_fail(nullptr, CGB_ERR_ARGS, "bad scheme (MHD goes with HLLD and only with it)");
   if (s.mhd && (s.precision == CGB_MIXED || s.dual_energy || ny < 2 || nz < 2))
     return box_fail(nullptr, CGB_ERR_UNSUPPORTED, "MHD boxes are 3D, exact or fast FP64, without dual energy");
   bool const one_d = ny == 1 && nz == 1;
-  int const H = (s.reconstruction == CGB_PPMC ? 4 : s.reconstruction == CGB_PLMC ? 3 : 2) + (s.mhd ? 1 : 0);
+  if (one_d && s.riemann_solver == CGB_HLL)
+    return box_fail(nullptr, CGB_ERR_UNSUPPORTED, "the reference's 1D integrator has no HLL branch (VL_1D_cuda.cu)");
+  int const H = (s.reconstruction == CGB_PPMC || s.reconstruction == CGB_PPMP   ? 4
+                 : s.reconstruction == CGB_PLMC || s.reconstruction == CGB_PLMP ? 3
+                                                                                : 2) +
+                (s.mhd ? 1 : 0);
   if (n_ghost < H || nx < 2 * n_ghost + 1 || (!one_d && (ny < 2 * n_ghost + 1 || nz < 2 * n_ghost + 1)))
     return box_fail(nullptr, CGB_ERR_ARGS, "box too small for the reconstruction stencil");
   if (!(dx > 0 && dy > 0 && dz > 0)) return box_fail(nullptr, CGB_ERR_ARGS, "cell sizes must be positive");

@@ -1,0 +1,12 @@
+// hydro_exact_exact.cu -- the exact FP64 predictor + corrector with the exact Riemann solver
+// (instantiated here alone; the kernels are in hydro_exact_step.cuh).  Built with -fmad=false.
+#include "hydro_exact_step.cuh"
+
+namespace cgb
+{
+cudaError_t exact_step_exact(const Box &b, int recon, double *U, const Scratch &sc, double dt, const double *dtp,
+                  cudaStream_t s, cudaEvent_t *marks)
+{
+  return exact_solver_step<SOLVER_EXACT>(b, recon, U, sc, dt, dtp, s, marks);
+}
+}  // namespace cgb

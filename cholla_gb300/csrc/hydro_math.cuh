@@ -529,5 +529,321 @@ __device__ __forceinline__ void roe(const double *qL, const double *qR, double *
   if (de) f[5 + ns] = (f[0] >= 0.0) ? f[0] * gel : f[0] * ger;
 }
 
+// ---- primitive-limited reconstructions (the VL build of plmp_cuda.cu:21-328 and
+// ppmp_cuda.cu:28-683: no half-step tracing, no flattening or steepening): every primitive is
+// limited on its own, with no characteristic projection ----
+
+__device__ __forceinline__ int sgn_int(double x) { return (x < 0) ? -1 : 1; }  // global_cuda.h:41-48
+
+// One cell's primitives as PLMP_cuda / PPMP_cuda load them (plmp_cuda.cu:108-133,
+// ppmp_cuda.cu:155-180) from a rotated conserved state: velocities by division, the kinetic
+// energy summed in the sweep's order, pressure from the total energy (dual energy: the select of
+// Get_Pressure_From_DE) floored at TINY, scalars and GasEnergy per unit mass.
+__device__ __forceinline__ Prim load_prim_plm(const double *q, int ns, int de, double gamma)
+{
+  Prim P;
+  P.d   = q[0];
+  P.vn  = q[1] / P.d;
+  P.vt1 = q[2] / P.d;
+  P.vt2 = q[3] / P.d;
+  P.ge  = 0.0;
+  double p;
+  if (de) {
+    double const E    = q[4];
+    double const Ekin = 0.5 * P.d * (P.vn * P.vn + P.vt1 * P.vt1 + P.vt2 * P.vt2);
+    double const dge  = q[5 + ns];
+    p                 = pressure_de(E, E - Ekin, dge, gamma);
+    P.ge              = dge / P.d;
+  } else {
+    p = (q[4] - 0.5 * P.d * (P.vn * P.vn + P.vt1 * P.vt1 + P.vt2 * P.vt2)) * (gamma - 1.0);
+  }
+  P.p = fmax(p, TINY);
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++) P.sc[k] = (k < ns) ? q[5 + k] / P.d : 0.0;
+  return P;
+}
+
+// Van Leer-limited slope of a three-point stencil (plmp_cuda.cu:330-365 Interface_Values_PLM,
+// ppmp_cuda.cu:687-720 Calculate_Slope): monotonised central difference with the harmonic mean.
+__device__ __forceinline__ double limited_slope(double qm, double q, double qp)
+{
+  double const dl = q - qm, dr = qp - q, dc = 0.5 * (qp - qm);
+  double const dg = (dl * dr > 0.0) ? 2.0 * dl * dr / (dl + dr) : 0.0;
+  double const a = fmin(fabs(dl), fabs(dr)), b = fmin(fabs(dc), fabs(dg));
+  return sgn_int(dc) * fmin(2.0 * a, b);
+}
+
+// Fryxell et al. (2000) parabola through cell i with its monotonicity constraints
+// (ppmp_cuda.cu:727-752 Interface_Values_PPM): L at the cell's low face, R at its high face.
+__device__ __forceinline__ void ppm_parabola(double qm, double q, double qp, double sm, double s0, double sp,
+                                             double &L, double &R)
+{
+  L = 0.5 * (q + qm) - (1.0 / 6.0) * (s0 - sm);
+  R = 0.5 * (qp + q) - (1.0 / 6.0) * (sp - s0);
+  if ((R - q) * (q - L) <= 0) L = R = q;
+  if (6.0 * (R - L) * (q - 0.5 * (L + R)) > (R - L) * (R - L)) L = 3.0 * q - 2.0 * R;
+  if (6.0 * (R - L) * (q - 0.5 * (L + R)) < -(R - L) * (R - L)) R = 3.0 * q - 2.0 * L;
+  L = fmax(fmin(q, qm), L);
+  L = fmin(fmax(q, qm), L);
+  R = fmax(fmin(q, qp), R);
+  R = fmin(fmax(q, qp), R);
+}
+
+// the primitive slots of a Prim as one indexable list: 0 d, 1 vn, 2 vt1, 3 vt2, 4 p, 5.. scalars, last ge
+__device__ __forceinline__ double prim_slot(const Prim &s, int k, int ns)
+{
+  if (k == 0) return s.d;
+  if (k == 1) return s.vn;
+  if (k == 2) return s.vt1;
+  if (k == 3) return s.vt2;
+  if (k == 4) return s.p;
+#pragma unroll
+  for (int j = 0; j < NS_MAX; j++)
+    if (k == 5 + j && j < ns) return s.sc[j];
+  return s.ge;
+}
+
+// Interface primitives (v: d, v1, v2, v3, p, scalars, ge) -> rotated conserved state, as
+// plmp_cuda.cu:290-326 / ppmp_cuda.cu:645-681 write them.
+__device__ __forceinline__ void plm_put(const double *v, double *q, int ns, int de, double gamma)
+{
+  double const d = v[0];
+  q[0]           = d;
+  q[1]           = d * v[1];
+  q[2]           = d * v[2];
+  q[3]           = d * v[3];
+  q[4]           = v[4] / (gamma - 1.0) + 0.5 * d * (v[1] * v[1] + v[2] * v[2] + v[3] * v[3]);
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++)
+    if (k < ns) q[5 + k] = d * v[5 + k];
+  if (de) q[5 + ns] = d * v[5 + ns];
+}
+
+// PLMP (ORDER 1, stencil c[0..2], centre c[1]) or PPMP (ORDER 2, stencil c[0..4], centre c[2])
+// for one cell: qL = the state at its high face, qR = the state at its low face (rotated conserved).
+template <int ORDER>
+__device__ __forceinline__ void plmp_ppmp_cell(const Prim *c, int ns, int de, double gamma, double *qL, double *qR)
+{
+  int const nq = 5 + ns + (de ? 1 : 0);
+  double lo[NQ_MAX], hi[NQ_MAX];
+#pragma unroll
+  for (int k = 0; k < NQ_MAX; k++) {
+    lo[k] = hi[k] = 0.0;
+    if (k < nq) {
+      if (ORDER == 1) {
+        double const q  = prim_slot(c[1], k, ns);
+        double const dm = limited_slope(prim_slot(c[0], k, ns), q, prim_slot(c[2], k, ns));
+        lo[k]           = q - 0.5 * dm;
+        hi[k]           = q + 0.5 * dm;
+      } else {
+        double const q0 = prim_slot(c[0], k, ns), q1 = prim_slot(c[1], k, ns), q2 = prim_slot(c[2], k, ns);
+        double const q3 = prim_slot(c[3], k, ns), q4 = prim_slot(c[4], k, ns);
+        double const sm = limited_slope(q0, q1, q2);
+        double const s0 = limited_slope(q1, q2, q3);
+        double const sp = limited_slope(q2, q3, q4);
+        ppm_parabola(q1, q2, q3, sm, s0, sp, lo[k], hi[k]);
+      }
+    }
+  }
+  lo[0] = fmax(lo[0], TINY), hi[0] = fmax(hi[0], TINY);
+  lo[4] = fmax(lo[4], TINY), hi[4] = fmax(hi[4], TINY);
+  plm_put(hi, qL, ns, de, gamma);
+  plm_put(lo, qR, ns, de, gamma);
+}
+
+// hll_cuda.cu:19-268 Calculate_HLL_Fluxes_CUDA: two-wave flux with Davis's wave speeds, from
+// rotated conserved interface states.
+__device__ __forceinline__ void hll(const double *qL, const double *qR, double *f, int ns, int de, double gamma)
+{
+  int const nq = 5 + ns + (de ? 1 : 0);
+  double fl[NQ_MAX], fr[NQ_MAX];
+  auto side = [&](const double *q, double *fo, double &vx, double &p) {
+    double const d  = q[0];
+    vx              = q[1] / d;
+    double const vy = q[2] / d, vz = q[3] / d;
+    if (de) {
+      double const E_kin = 0.5 * d * (vx * vx + vy * vy + vz * vz);
+      p                  = pressure_de(q[4], q[4] - E_kin, q[5 + ns], gamma);
+    } else {
+      p = (q[4] - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (gamma - 1.0);
+    }
+    p     = fmax(p, TINY);
+    fo[0] = q[1];
+    fo[1] = q[1] * vx + p;
+    fo[2] = q[2] * vx;
+    fo[3] = q[3] * vx;
+    fo[4] = (q[4] + p) * vx;
+#pragma unroll
+    for (int k = 5; k < NQ_MAX; k++) fo[k] = (k < nq) ? q[k] * vx : 0.0;  // scalars, thermal energy advect
+  };
+  double vxl, pl, vxr, pr;
+  side(qL, fl, vxl, pl);
+  side(qR, fr, vxr, pr);
+  double const cfl = sqrt(gamma * pl / qL[0]), cfr = sqrt(gamma * pr / qR[0]);
+  double const Sl = fmin(vxr - cfr, vxl - cfl);
+  double const Sr = fmax(vxl + cfl, vxr + cfr);
+#pragma unroll
+  for (int k = 0; k < NQ_MAX; k++) {
+    if (k < nq) {
+      if (Sl > 0.0) {
+        f[k] = fl[k];
+      } else if (Sr < 0.0) {
+        f[k] = fr[k];
+      } else {
+        f[k] = ((Sr * fl[k]) - (Sl * fr[k]) + Sl * Sr * (qR[k] - qL[k])) / (Sr - Sl);
+      }
+    }
+  }
+}
+
+// ---- exact_cuda.cu:19-334 Calculate_Exact_Fluxes_CUDA: the exact Riemann solution (Toro ch. 4)
+// sampled at x/t = 0, star pressure by Newton from the primitive-variable guess.  The reference
+// evaluates its fractional powers in single precision (powf on double arguments); so does this.
+__device__ __forceinline__ double fpow(double a, double b) { return (double)powf((float)a, (float)b); }
+
+__device__ __forceinline__ void exact_pressure_function(double &f, double &fd, double p, double dk, double pk,
+                                                        double ck, double g)
+{
+  if (p <= pk) {  // rarefaction
+    f  = (2.0 / (g - 1.0)) * ck * (fpow(p / pk, (g - 1.0) / (2.0 * g)) - 1.0);
+    fd = (1.0 / (dk * ck)) * fpow(p / pk, -((g + 1.0) / (2.0 * g)));
+  } else {  // shock
+    double const bk = ((g - 1.0) / (g + 1.0)) * pk;
+    double const q  = sqrt(((2.0 / (g + 1.0)) / dk) / (bk + p));
+    f  = (p - pk) * q;
+    fd = (1.0 - 0.5 * (p - pk) / (bk + p)) * q;
+  }
+}
+
+__device__ __forceinline__ void exact_star(double &pm, double &vm, double dl, double vl, double pl, double cl,
+                                           double dr, double vr, double pr, double cr, double g)
+{
+  double const tol = 1.0e-6;
+  double ppv       = 0.5 * (pl + pr) + 0.125 * (vl - vr) * (dl + dr) * (cl + cr);
+  if (ppv < 0.0) ppv = 0.0;
+  double const gl = sqrt((2.0 / ((g + 1.0) * dl)) / (((g - 1.0) / (g + 1.0)) * pl + ppv));
+  double const gr = sqrt((2.0 / ((g + 1.0) * dr)) / (((g - 1.0) / (g + 1.0)) * pr + ppv));
+  double pold     = (gl * pl + gr * pr - (vr - vl)) / (gl + gr);
+  if (pold < 0.0) pold = tol;
+  double fl = 0, fld = 0, fr = 0, frd = 0;
+  for (int it = 0; it <= 20; it++) {  // at most 21 Newton passes: the loop always ends
+    exact_pressure_function(fl, fld, pold, dl, pl, cl, g);
+    exact_pressure_function(fr, frd, pold, dr, pr, cr, g);
+    pm                  = pold - (fl + fr + vr - vl) / (fld + frd);
+    double const change = 2.0 * fabs((pm - pold) / (pm + pold));
+    if (change <= tol) break;
+    if (pm < 0.0) pm = tol;
+    pold = pm;
+  }
+  vm = 0.5 * (vl + vr + fr - fl);
+}
+
+__device__ __forceinline__ void exact_sample(double pm, double vm, double &d, double &v, double &p, double dl,
+                                             double vl, double pl, double cl, double dr, double vr, double pr,
+                                             double cr, double g)
+{
+  double const gm = (g - 1.0) / (g + 1.0);
+  if (vm >= 0) {
+    if (pm <= pl) {  // left rarefaction
+      if (vl - cl >= 0) {
+        d = dl, v = vl, p = pl;
+      } else if (vm - cl * fpow(pm / pl, (g - 1.0) / (2.0 * g)) < 0) {
+        d = dl * fpow(pm / pl, 1.0 / g), v = vm, p = pm;
+      } else {
+        double const c = (2.0 / (g + 1.0)) * (cl + ((g - 1.0) / 2.0) * vl);
+        v = c;
+        d = dl * fpow(c / cl, 2.0 / (g - 1.0));
+        p = pl * fpow(c / cl, 2.0 * g / (g - 1.0));
+      }
+    } else {  // left shock
+      double const sl = vl - cl * sqrt(((g + 1.0) / (2.0 * g)) * (pm / pl) + ((g - 1.0) / (2.0 * g)));
+      if (sl >= 0) {
+        d = dl, v = vl, p = pl;
+      } else {
+        d = dl * (pm / pl + gm) / ((pm / pl) * gm + 1.0), v = vm, p = pm;
+      }
+    }
+  } else {
+    if (pm > pr) {  // right shock
+      double const sr = vr + cr * sqrt(((g + 1.0) / (2.0 * g)) * (pm / pr) + ((g - 1.0) / (2.0 * g)));
+      if (sr <= 0) {
+        d = dr, v = vr, p = pr;
+      } else {
+        d = dr * (pm / pr + gm) / ((pm / pr) * gm + 1.0), v = vm, p = pm;
+      }
+    } else {  // right rarefaction
+      if (vr + cr <= 0) {
+        d = dr, v = vr, p = pr;
+      } else if (vm + cr * fpow(pm / pr, (g - 1.0) / (2.0 * g)) >= 0) {
+        d = dr * fpow(pm / pr, 1.0 / g), v = vm, p = pm;
+      } else {
+        double const c = (2.0 / (g + 1.0)) * (cr - ((g - 1.0) / 2.0) * vr);
+        v = -c;
+        d = dr * fpow(c / cr, 2.0 / (g - 1.0));
+        p = pr * fpow(c / cr, 2.0 * g / (g - 1.0));
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void exact(const double *qL, const double *qR, double *f, int ns, int de, double gamma)
+{
+  auto load = [&](const double *q, double &d, double &vx, double &vy, double &vz, double &p, double &ge,
+                  double *sc) {
+    d  = q[0];
+    vx = q[1] / d;
+    vy = q[2] / d;
+    vz = q[3] / d;
+    double const E = q[4];
+    ge             = 0.0;
+    if (de) {
+      double const E_kin = 0.5 * d * (vx * vx + vy * vy + vz * vz);
+      double const dge   = q[5 + ns];
+      p                  = pressure_de(E, E - E_kin, dge, gamma);
+      ge                 = dge / d;
+    } else {
+      p = (E - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (gamma - 1.0);
+    }
+    p = fmax(p, TINY);
+#pragma unroll
+    for (int k = 0; k < NS_MAX; k++) sc[k] = (k < ns) ? q[5 + k] / d : 0.0;
+  };
+  double dl, vxl, vyl, vzl, pl, gel, scl[NS_MAX];
+  double dr, vxr, vyr, vzr, pr, ger, scr[NS_MAX];
+  load(qL, dl, vxl, vyl, vzl, pl, gel, scl);
+  load(qR, dr, vxr, vyr, vzr, pr, ger, scr);
+  double const cl = sqrt(gamma * pl / dl), cr = sqrt(gamma * pr / dr);
+  double pm = 0, vm = 0, ds = 0, vs = 0, ps = 0;
+  exact_star(pm, vm, dl, vxl, pl, cl, dr, vxr, pr, cr, gamma);
+  exact_sample(pm, vm, ds, vs, ps, dl, vxl, pl, cl, dr, vxr, pr, cr, gamma);
+  f[0]            = ds * vs;
+  f[1]            = ds * vs * vs + ps;
+  bool const left = vs >= 0;  // transverse velocities and passive quantities advect upwind
+  double const vy = left ? vyl : vyr, vz = left ? vzl : vzr;
+  f[2] = ds * vs * vy;
+  f[3] = ds * vs * vz;
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++)
+    if (k < ns) f[5 + k] = ds * vs * (left ? scl[k] : scr[k]);
+  if (de) f[5 + ns] = ds * vs * (left ? gel : ger);
+  double const Es = (ps / (gamma - 1.0)) + 0.5 * ds * (vs * vs + vy * vy + vz * vz);
+  f[4]            = (Es + ps) * vs;
+}
+
+// flux of one face with the scheme's solver (SOLVER_* of common.cuh)
+template <int SOLVER>
+__device__ __forceinline__ void riemann(const double *qL, const double *qR, double *f, int ns, int de, double gamma)
+{
+  if (SOLVER == SOLVER_ROE) {
+    roe(qL, qR, f, ns, de, gamma);
+  } else if (SOLVER == SOLVER_HLL) {
+    hll(qL, qR, f, ns, de, gamma);
+  } else if (SOLVER == SOLVER_EXACT) {
+    exact(qL, qR, f, ns, de, gamma);
+  } else {
+    hllc(qL, qR, f, ns, de, gamma);
+  }
+}
+
 }  // namespace hx
 }  // namespace cgb

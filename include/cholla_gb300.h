@@ -40,16 +40,17 @@ extern "C" {
 /* largest |div B| cgb_check_magnetic_divergence accepts (src/mhd/magnetic_divergence.cu:105) */
 #define CGB_MAX_DIVB 1.0e-9
 
-/* reconstruction (builds/make.type.*: -DPCM / -DPLMC / -DPPMC; -DPLMP / -DPPMP are the
-   primitive-limited forms of src/reconstruction/plmp_cuda.cu and ppmp_cuda.cu, which
-   cgb_set_scheme rejects with CGB_ERR_UNSUPPORTED: their kernels are not built yet) */
+/* reconstruction (builds/make.type.*: -DPCM / -DPLMC / -DPPMC / -DPLMP / -DPPMP; PLMP and PPMP are
+   the primitive-limited forms of src/reconstruction/plmp_cuda.cu and ppmp_cuda.cu, built in the
+   exact FP64 form only: other precisions are rejected with CGB_ERR_UNSUPPORTED) */
 #define CGB_PCM  0
 #define CGB_PLMC 1
 #define CGB_PPMC 2
 #define CGB_PLMP 3
 #define CGB_PPMP 4
-/* Riemann solver (-DHLLC / -DROE / -DHLLD; -DHLL and -DEXACT, src/riemann_solvers/hll_cuda.cu
-   and exact_cuda.cu, are rejected with CGB_ERR_UNSUPPORTED: not built yet) */
+/* Riemann solver (-DHLLC / -DROE / -DHLLD / -DHLL / -DEXACT; HLL and EXACT, src/riemann_solvers/
+   hll_cuda.cu and exact_cuda.cu, are built in the exact FP64 form only, and HLL not in 1D, where the
+   reference's VL_1D integrator has no HLL branch) */
 #define CGB_HLLC  0
 #define CGB_ROE   1
 #define CGB_HLLD  2
@@ -61,8 +62,8 @@ extern "C" {
 #define CGB_FP64_FAST 2 /* FP64 with reciprocal forms, per-cell primitives and FMA (not bit-exact) */
 
 typedef struct {
-  int reconstruction;    /* CGB_PCM / CGB_PLMC / CGB_PPMC */
-  int riemann_solver;    /* CGB_HLLC / CGB_ROE / CGB_HLLD */
+  int reconstruction;    /* CGB_PCM / CGB_PLMC / CGB_PPMC / CGB_PLMP / CGB_PPMP */
+  int riemann_solver;    /* CGB_HLLC / CGB_ROE / CGB_HLLD / CGB_HLL / CGB_EXACT */
   int dual_energy;       /* -DDE: GasEnergy is the last field */
   int mhd;               /* -DMHD: face-centred Bx, By, Bz follow the scalars; needs CGB_HLLD */
   int n_scalars;         /* -DSCALAR: passive scalars after Energy (0..2) */

@@ -25,7 +25,7 @@ CUcontext g_ctx = nullptr;
 std::vector<CUmodule> g_mods;
 std::map<std::string, CUfunction> g_fn;
 bool g_de = false, g_mhd = false;
-int g_recon = 2;   // 1 PLMC, 2 PPMC
+int g_recon = 2;   // 1 PLMC, 2 PPMC, 3 PLMP, 4 PPMP
 int g_solver = 0;  // 0 HLLC, 1 ROE, 2 HLLD, 3 HLL, 4 exact
 struct Scratch {
   size_t n = 0;
@@ -121,6 +121,8 @@ const char *K_HALF3   = "_Z34Update_Conserved_Variables_3D_halfPdS_S_S_S_iiiiddd
 const char *K_HALF1   = "_Z34Update_Conserved_Variables_1D_halfPdS_S_iidddi";
 const char *K_PPMC    = "_Z7PPMC_VLPdS_S_iiidi";
 const char *K_PLMC    = "_Z9PLMC_cudaPdS_S_iiidddii";
+const char *K_PLMP    = "_Z9PLMP_cudaPdS_S_iiiidddii";
+const char *K_PPMP    = "_Z9PPMP_cudaPdS_S_iiiidddii";
 const char *K_DEP3    = "_Z42Partial_Update_Advected_Internal_Energy_3DPdS_S_S_S_S_S_iiiidddddi";
 const char *K_DEP1    = "_Z42Partial_Update_Advected_Internal_Energy_1DPdS_S_iidddi";
 const char *K_UPD3    = "_Z29Update_Conserved_Variables_3DPdS_S_S_S_S_S_S_S_S_iiiiiiiddddddddiidS_";
@@ -164,8 +166,8 @@ int refh_init(const char *variant_dir, const char *variant)
   std::string v(variant);
   g_de     = v.find("_de") != std::string::npos;
   g_mhd    = v.rfind("mhd", 0) == 0;
-  g_recon  = v.find("plmc") != std::string::npos ? 1 : 2;
   auto has = [&v](const char *t) { return v.find(t) != std::string::npos; };
+  g_recon  = has("plmc") ? 1 : has("plmp") ? 3 : has("ppmp") ? 4 : 2;
   // "hllc" and "hlld" contain "hll": test them first
   g_solver = has("hlld") ? 2 : has("roe") ? 1 : has("exact") ? 4 : (has("_hll") && !has("_hllc")) ? 3 : 0;
   DIR *dir = opendir(variant_dir);
@@ -214,6 +216,9 @@ int refh_vl_step_3d(unsigned long long U_, int nx, int ny, int nz, int ng, doubl
   for (int d = 0; d < 3; d++) {
     if (g_recon == 2) {
       if (launch(K_PPMC, n, s.Uh, QL[d], QR[d], nx, ny, nz, gamma, d)) return 1;
+    } else if (g_recon >= 3) {
+      if (launch(g_recon == 3 ? K_PLMP : K_PPMP, n, s.Uh, QL[d], QR[d], nx, ny, nz, ng, dd[d], dt, gamma, d, nf))
+        return 1;
     } else {
       if (launch(K_PLMC, n, s.Uh, QL[d], QR[d], nx, ny, nz, dd[d], dt, gamma, d, nf)) return 1;
     }
@@ -250,6 +255,9 @@ int refh_vl_step_1d(unsigned long long U_, int nx, int ng, double dx, double dt,
   if (launch(K_HALF1, n, U, s.Uh, s.Fx, nx, ng, dx, 0.5 * dt, gamma, nf)) return 1;
   if (g_recon == 2) {
     if (launch(K_PPMC, n, s.Uh, s.QLx, s.QRx, nx, one, one, gamma, 0)) return 1;
+  } else if (g_recon >= 3) {
+    if (launch(g_recon == 3 ? K_PLMP : K_PPMP, n, s.Uh, s.QLx, s.QRx, nx, one, one, ng, dx, dt, gamma, 0, nf))
+      return 1;
   } else {
     if (launch(K_PLMC, n, s.Uh, s.QLx, s.QRx, nx, one, one, dx, dt, gamma, 0, nf)) return 1;
   }

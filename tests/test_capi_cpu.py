@@ -56,9 +56,11 @@ def test_scheme_round_trip_and_validation(lib):
     with pytest.raises(_lib.CgbError):
         I.set_scheme(I.Scheme(gamma=1.0))
     for recon, solver in (("PLMP", "HLLC"), ("PPMP", "HLLC"), ("PPMC", "HLL"), ("PPMC", "EXACT")):
-        with pytest.raises(_lib.CgbError) as e:  # make.type options whose kernels are not built
-            I.set_scheme(I.Scheme(reconstruction=recon, riemann_solver=solver))
-        assert e.value.code == _lib.CGB_ERR_UNSUPPORTED
+        I.set_scheme(I.Scheme(reconstruction=recon, riemann_solver=solver))  # built in the exact FP64 form
+        for prec in ("fp64_fast", "mixed"):  # not in the throughput forms
+            with pytest.raises(_lib.CgbError) as e:
+                I.set_scheme(I.Scheme(reconstruction=recon, riemann_solver=solver, precision=prec))
+            assert e.value.code == _lib.CGB_ERR_UNSUPPORTED
     bad = I.Scheme().to_c()
     bad.reconstruction = 7
     assert _lib.lib().cgb_set_scheme(bad) == _lib.CGB_ERR_ARGS
