@@ -66,6 +66,7 @@ SIGNATURES = {
     "cgb_vl_algorithm_3d_static": (_I, [_P, _P, _I, _I, _I, _I, _I, _I, _I, _D, _D, _D, _D, _D, _D, _D, _I, _I, _D,
                                         _P]),
     "cgb_vl_algorithm_1d": (_I, [_P, _I, _I, _I, _D, _D, _D, _I, _I]),
+    "cgb_vl_algorithm_2d": (_I, [_P, _I, _I, _I, _I, _I, _D, _D, _D, _D, _D, _I, _I]),
     "cgb_free_memory_vl_3d": (_I, []),
     "cgb_calc_dt_gpu": (_I, [_P, _I, _I, _I, _I, _I, _D, _D, _D, _D, C.POINTER(_D)]),
     "cgb_apply_temperature_floor": (_I, [_P, _I, _I, _I, _I, _I, _D]),

@@ -90,12 +90,18 @@ def run(torch, n: int = 64, steps: int = 10, seed: int = 0, forms=("mixed", "fp6
     return res
 
 
-def serving_twins(torch, requests) -> list[dict]:
+def serving_twins(torch, requests, sensitivity: bool = True) -> list[dict]:
     """Accuracy of served jobs: each request of the serving workload (mixed precision, see serve.py)
     is run as the batched server runs it -- a cgb_batch job, whose result is the same bit for bit
     whatever else shares the batch -- one step at a time, recording the job's own dt sequence;
     then its exact FP64 twin (same initial state) takes the same dt sequence through the drop-in
-    calls.  Per request: the relative L1 error per field of the served result against the twin."""
+    calls.  Per request: the relative L1 error per field of the served result against the twin.
+
+    With `sensitivity`, a second exact FP64 run on the same dt sequence starts from the initial
+    state with every density raised by one unit in the last place: its distance from the twin is
+    how much this problem itself amplifies a rounding-sized perturbation in FP64, the scale against
+    which the served result's error is read (a blast or tube that wraps around the periodic box
+    amplifies rounding by orders of magnitude whatever the arithmetic)."""
     from .batch import Batch
     from .serve import N_GHOST, default_scheme, init_state
 
@@ -118,9 +124,18 @@ def serving_twins(torch, requests) -> list[dict]:
         _steps(torch, twin, req.n, ng, "fp64", len(dts), dts)
         real = (slice(None), slice(ng, ng + req.n), slice(ng, ng + req.n), slice(ng, ng + req.n))
         ref = twin[real]
-        err = (U[real] - ref).abs().sum(dim=(1, 2, 3)) / ref.abs().sum(dim=(1, 2, 3)).clamp_min(1e-300)
-        out.append({"rid": req.rid, "n": req.n, "kind": req.kind, "steps": len(dts),
-                    "rel_l1": {FIELDS[i]: float(err[i]) for i in range(err.shape[0])}})
+        den = ref.abs().sum(dim=(1, 2, 3)).clamp_min(1e-300)
+        err = (U[real] - ref).abs().sum(dim=(1, 2, 3)) / den
+        rec = {"rid": req.rid, "n": req.n, "kind": req.kind, "steps": len(dts),
+               "rel_l1": {FIELDS[i]: float(err[i]) for i in range(err.shape[0])}}
+        if sensitivity:
+            pert = U0.clone()
+            pert[0] = torch.nextafter(pert[0], torch.full_like(pert[0], float("inf")))
+            _steps(torch, pert, req.n, ng, "fp64", len(dts), dts)
+            sen = (pert[real] - ref).abs().sum(dim=(1, 2, 3)) / den
+            rec["fp64_one_ulp_sensitivity"] = {FIELDS[i]: float(sen[i]) for i in range(sen.shape[0])}
+            del pert
+        out.append(rec)
         del U, U0, twin
     return out
 

@@ -29,6 +29,7 @@ PER_FILE = {
     "hydro_exact_roe.cu": ["-fmad=false"],
     "hydro_exact_hll.cu": ["-fmad=false"],
     "hydro_exact_exact.cu": ["-fmad=false"],
+    "hydro_2d.cu": ["-fmad=false"],
     "mhd_exact.cu": ["-fmad=false"],
 }
 

@@ -348,6 +348,32 @@ int cgb_vl_algorithm_1d(double *d_conserved, int nx, int x_off, int n_ghost, dou
   return CGB_OK;
 }
 
+int cgb_vl_algorithm_2d(double *d_conserved, int nx, int ny, int x_off, int y_off, int n_ghost, double dx, double dy,
+                        double xbound, double ybound, double dt, int n_fields, int custom_grav)
+{
+  (void)x_off, (void)y_off, (void)xbound, (void)ybound;
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (!d_conserved) return fail(CGB_ERR_ARGS, "null d_conserved");
+  if (custom_grav) return fail(CGB_ERR_UNSUPPORTED, "gravity source terms are not part of this library");
+  if (g_scheme.mhd) return fail(CGB_ERR_UNSUPPORTED, "the 2D integrator is hydro only");
+  if (g_scheme.riemann_solver == CGB_HLL)
+    return fail(CGB_ERR_UNSUPPORTED, "the reference's 2D integrator has no HLL branch (VL_2D_cuda.cu)");
+  if (g_scheme.precision != CGB_FP64)
+    return fail(CGB_ERR_UNSUPPORTED, "the 2D step is built in the exact FP64 form (CGB_FP64) only");
+  if (nx < 2 * n_ghost + 1 || ny < 2 * n_ghost + 1) return fail(CGB_ERR_ARGS, "2D step needs real cells in x and y");
+  cgb::Box b;
+  int rc = make_box(b, nx, ny, 1, n_ghost, n_fields, dx, dy, dx, 0.0, g_scheme);
+  if (rc != CGB_OK) return rc;
+  b.floor_on = 0;  // the 2D updates apply no density floor (VL_2D_cuda.cu:176-258, hydro_cuda.cu:87-170)
+  if (n_ghost < ghosts_needed(g_scheme)) return fail(CGB_ERR_ARGS, "n_ghost too small for the reconstruction");
+  rc = ensure_slot(nx, ny, 1, n_fields, 0);
+  if (rc != CGB_OK) return rc;
+  cudaError_t e = cgb::hydro_step(b, g_scheme.reconstruction, g_scheme.riemann_solver, CGB_FP64, d_conserved,
+                                  g_slot.s, dt, nullptr, 0.0, 0, 0, g_stream);
+  if (e != cudaSuccess) return cuda_fail(e, "vl_algorithm_2d");
+  return CGB_OK;
+}
+
 int cgb_free_memory_vl_3d(void)
 {
   std::lock_guard<std::mutex> lk(g_mu);
@@ -368,7 +394,8 @@ int cgb_calc_dt_gpu(const double *d_conserved, int nx, int ny, int nz, int n_gho
   b.de = s.dual_energy, b.mhd = s.mhd, b.floor_on = 0, b.n = (long long)nx * ny * nz, b.gamma = gamma;
   b.dx = dx, b.dy = dy, b.dz = dz, b.density_floor = 0;
   if (b.mhd && !(ny > 1 && nz > 1)) return fail(CGB_ERR_ARGS, "MHD boxes are 3D");
-  if (!(nx > 1 && ((ny == 1 && nz == 1) || (ny > 1 && nz > 1)))) return fail(CGB_ERR_ARGS, "1D or 3D boxes only");
+  if (!(nx > 1 && ((ny == 1 && nz == 1) || ny > 1))) return fail(CGB_ERR_ARGS, "1D, 2D (nz = 1) or 3D boxes only");
+  if (b.mhd && nz == 1) return fail(CGB_ERR_ARGS, "MHD boxes are 3D");
   unsigned long long *d_dti = nullptr;
   int const rw               = device_word(0, &d_dti);
   if (rw != CGB_OK) return rw;

@@ -143,14 +143,17 @@ int cgb_box_create(cgb_box **out, int nx, int ny, int nz, int n_ghost, double dx
     return box_fail(nullptr, CGB_ERR_ARGS, "bad scheme (MHD goes with HLLD and only with it)");
   if (s.mhd && (s.precision == CGB_MIXED || s.dual_energy || ny < 2 || nz < 2))
     return box_fail(nullptr, CGB_ERR_UNSUPPORTED, "MHD boxes are 3D, exact or fast FP64, without dual energy");
-  bool const one_d = ny == 1 && nz == 1;
-  if (one_d && s.riemann_solver == CGB_HLL)
-    return box_fail(nullptr, CGB_ERR_UNSUPPORTED, "the reference's 1D integrator has no HLL branch (VL_1D_cuda.cu)");
+  bool const one_d = ny == 1 && nz == 1, two_d = nz == 1 && ny > 1;
+  if ((one_d || two_d) && s.riemann_solver == CGB_HLL)
+    return box_fail(nullptr, CGB_ERR_UNSUPPORTED, "the reference's 1D and 2D integrators have no HLL branch");
+  if (two_d && (s.precision != CGB_FP64 || s.mhd))
+    return box_fail(nullptr, CGB_ERR_UNSUPPORTED, "2D boxes are hydro, exact FP64 form only");
   int const H = (s.reconstruction == CGB_PPMC || s.reconstruction == CGB_PPMP   ? 4
                  : s.reconstruction == CGB_PLMC || s.reconstruction == CGB_PLMP ? 3
                                                                                 : 2) +
                 (s.mhd ? 1 : 0);
-  if (n_ghost < H || nx < 2 * n_ghost + 1 || (!one_d && (ny < 2 * n_ghost + 1 || nz < 2 * n_ghost + 1)))
+  if (n_ghost < H || nx < 2 * n_ghost + 1 ||
+      (!one_d && (ny < 2 * n_ghost + 1 || (!two_d && nz < 2 * n_ghost + 1))))
     return box_fail(nullptr, CGB_ERR_ARGS, "box too small for the reconstruction stencil");
   if (!(dx > 0 && dy > 0 && dz > 0)) return box_fail(nullptr, CGB_ERR_ARGS, "cell sizes must be positive");
   for (int i = 0; i < 6; i++)
@@ -162,7 +165,7 @@ int cgb_box_create(cgb_box **out, int nx, int ny, int nz, int n_ghost, double dx
   b.nx = nx, b.ny = ny, b.nz = nz, b.ng = n_ghost, b.ns = s.n_scalars;
   b.de = s.dual_energy ? 1 : 0, b.mhd = s.mhd ? 1 : 0;
   b.nf = 5 + s.n_scalars + b.de + 3 * b.mhd;
-  b.floor_on = one_d ? 0 : (s.density_floor ? 1 : 0);
+  b.floor_on = (one_d || two_d) ? 0 : (s.density_floor ? 1 : 0);  // the 1D and 2D updates have no density floor
   b.n = (long long)nx * ny * nz;
   b.gamma = s.gamma, b.dx = dx, b.dy = dy, b.dz = dz, b.density_floor = 0.0;
   size_t const n = (size_t)b.n;

@@ -9,6 +9,8 @@
 //                            reduction on the new state (hydro_cuda.cu:949-1099, 1117-1153, 514-597)
 //
 // Interface states and fluxes never leave the SM.
+#include <cfloat>
+
 #include "common.cuh"
 #include "hydro_math.cuh"
 #include "kernels.h"
@@ -44,6 +46,17 @@ __device__ __forceinline__ double hydro_inverse_crossing_time(double E, double d
   return m;
 }
 
+// hydro_cuda.cu:473-512 Calc_dt_2D: the pressure floored at TINY, the larger of the two crossing rates
+__device__ __forceinline__ double hydro_inverse_crossing_time_2d(double E, double d, double d_inv, double vx,
+                                                                 double vy, double vz, double dx, double dy,
+                                                                 double gamma)
+{
+  double P = (E - 0.5 * d * (vx * vx + vy * vy + vz * vz)) * (gamma - 1.0);
+  P        = fmax(P, TINY);
+  double const cs = sqrt(d_inv * gamma * P);
+  return fmax(-DBL_MAX, fmax((fabs(vx) + cs) / dx, (fabs(vy) + cs) / dy));
+}
+
 __device__ __forceinline__ void block_max_to(double v, unsigned long long *dst)
 {
   // values are >= 0 (or -DBL_MAX for threads without a cell): compare as ordered bit patterns
@@ -67,15 +80,15 @@ __global__ void __launch_bounds__(256) k_finalize(Box b, double *__restrict__ U,
                                                   double U_floor, int temp_floor, int do_dt)
 {
   int const ng = b.ng;
-  bool const one_d = (b.ny == 1 && b.nz == 1);
-  int const rx = b.nx - 2 * ng, ry = one_d ? 1 : b.ny - 2 * ng, rz = one_d ? 1 : b.nz - 2 * ng;
+  bool const one_d = (b.ny == 1 && b.nz == 1), two_d = (b.nz == 1 && b.ny > 1);
+  int const rx = b.nx - 2 * ng, ry = one_d ? 1 : b.ny - 2 * ng, rz = b.nz == 1 ? 1 : b.nz - 2 * ng;
   long long const nreal = (long long)rx * ry * rz;
   long long const r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   double m = -1.0;
   if (r < nreal) {
     int const x = (int)(r % rx) + ng;
     int const y = one_d ? 0 : (int)((r / rx) % ry) + ng;
-    int const z = one_d ? 0 : (int)(r / ((long long)rx * ry)) + ng;
+    int const z = b.nz == 1 ? 0 : (int)(r / ((long long)rx * ry)) + ng;
     long long const n = b.n, id = b.id(x, y, z);
     double const d = U[id], d_inv = 1.0 / d;
     double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
@@ -88,6 +101,11 @@ __global__ void __launch_bounds__(256) k_finalize(Box b, double *__restrict__ U,
         int const imo = max(x - 1, ng), ipo = min(x + 1, b.nx - ng - 1);
         Emax = fmax(Epre[imo], E);
         Emax = fmax(Emax, Epre[ipo]);
+      } else if (two_d) {  // hydro_cuda.cu:880-933 Select_Internal_Energy_2D
+        Emax = fmax(Epre[b.id(max(x - 1, ng), y, 0)], E);
+        Emax = fmax(Emax, Epre[b.id(min(x + 1, b.nx - ng - 1), y, 0)]);
+        Emax = fmax(Emax, Epre[b.id(x, max(y - 1, ng), 0)]);
+        Emax = fmax(Emax, Epre[b.id(x, min(y + 1, b.ny - ng - 1), 0)]);
       } else {
         Emax = fmax(Epre[b.id(max(x - 1, ng), y, z)], E);
         Emax = fmax(Emax, Epre[b.id(min(x + 1, b.nx - ng - 1), y, z)]);
@@ -126,6 +144,8 @@ __global__ void __launch_bounds__(256) k_finalize(Box b, double *__restrict__ U,
         P        = fmax(P, TINY);
         double const cs = sqrt(d_inv * b.gamma * P);
         m               = fmax(-1.0, (fabs(vx) + cs) / b.dx);
+      } else if (two_d) {
+        m = hydro_inverse_crossing_time_2d(E, d, d_inv, vx, vy, vz, b.dx, b.dy, b.gamma);
       } else {
         m = hydro_inverse_crossing_time(E, d, d_inv, vx, vy, vz, b.dx, b.dy, b.dz, b.gamma);
       }
@@ -156,15 +176,15 @@ __global__ void k_negative_density_average(Box b, double *__restrict__ U)
 __global__ void __launch_bounds__(256) k_calc_dt(Box b, const double *__restrict__ U, unsigned long long *__restrict__ dti)
 {
   int const ng = b.ng;
-  bool const one_d = (b.ny == 1 && b.nz == 1);
-  int const rx = b.nx - 2 * ng, ry = one_d ? 1 : b.ny - 2 * ng, rz = one_d ? 1 : b.nz - 2 * ng;
+  bool const one_d = (b.ny == 1 && b.nz == 1), two_d = (b.nz == 1 && b.ny > 1);
+  int const rx = b.nx - 2 * ng, ry = one_d ? 1 : b.ny - 2 * ng, rz = b.nz == 1 ? 1 : b.nz - 2 * ng;
   long long const nreal = (long long)rx * ry * rz;
   double m = -1.0;
   for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < nreal;
        r += (long long)gridDim.x * blockDim.x) {
     int const x = (int)(r % rx) + ng;
     int const y = one_d ? 0 : (int)((r / rx) % ry) + ng;
-    int const z = one_d ? 0 : (int)(r / ((long long)rx * ry)) + ng;
+    int const z = b.nz == 1 ? 0 : (int)(r / ((long long)rx * ry)) + ng;
     long long const n = b.n, id = b.id(x, y, z);
     double const d = U[id], d_inv = 1.0 / d;
     double const vx = U[n + id] * d_inv, vy = U[2 * n + id] * d_inv, vz = U[3 * n + id] * d_inv;
@@ -174,6 +194,8 @@ __global__ void __launch_bounds__(256) k_calc_dt(Box b, const double *__restrict
       P        = fmax(P, TINY);
       double const cs = sqrt(d_inv * b.gamma * P);
       m               = fmax(m, (fabs(vx) + cs) / b.dx);
+    } else if (two_d) {
+      m = fmax(m, hydro_inverse_crossing_time_2d(E, d, d_inv, vx, vy, vz, b.dx, b.dy, b.gamma));
     } else {
       m = fmax(m, hydro_inverse_crossing_time(E, d, d_inv, vx, vy, vz, b.dx, b.dy, b.dz, b.gamma));
     }
@@ -213,16 +235,21 @@ cudaError_t hydro_exact_step(const Box &b, int recon, int solver, double *U, con
                              const double *dt_dev, double U_floor, int temp_floor, int do_dt, cudaStream_t s,
                              cudaEvent_t *marks)
 {
-  bool const one_d = (b.ny == 1 && b.nz == 1);
+  bool const one_d = (b.ny == 1 && b.nz == 1), two_d = (b.nz == 1 && b.ny > 1);
+  if (b.nz < 2 * b.ng + 1) temp_floor = 0;  // the reference's temperature floor acts in 3D only
   cudaError_t e;
-  switch (solver) {
+  if (two_d) {
+    e = hydro_2d_step(b, recon, solver, U, sc, dt, dt_dev, s);
+  } else {
+    switch (solver) {
     case SOLVER_ROE: e = exact_step_roe(b, recon, U, sc, dt, dt_dev, s, marks); break;
     case SOLVER_HLL: e = exact_step_hll(b, recon, U, sc, dt, dt_dev, s, marks); break;
     case SOLVER_EXACT: e = exact_step_exact(b, recon, U, sc, dt, dt_dev, s, marks); break;
     default: e = exact_step_hllc(b, recon, U, sc, dt, dt_dev, s, marks); break;
+    }
   }
   if (e != cudaSuccess) return e;
-  if (b.floor_on && !one_d) {
+  if (b.floor_on && !one_d && !two_d) {
     k_negative_density_average<<<152 * 4, 256, 0, s>>>(b, U);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
@@ -274,8 +301,11 @@ cudaError_t negative_density_average(const Box &b, double *U, cudaStream_t s)
   return cudaGetLastError();
 }
 
+// Temperature_Floor_Kernel acts on cells whose x, y and z all lie in the real range
+// (hydro_cuda.cu:1130-1131), so on a 1D or 2D box (extent 1 in z) it changes nothing; neither does this.
 cudaError_t hydro_temperature_floor(const Box &b, double *U, double U_floor, cudaStream_t s)
 {
+  if (b.nz < 2 * b.ng + 1) return cudaSuccess;
   k_temperature_floor<<<152 * 8, 256, 0, s>>>(b, U, U_floor);
   return cudaGetLastError();
 }

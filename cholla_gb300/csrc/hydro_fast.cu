@@ -1036,6 +1036,7 @@ cudaError_t hydro_fast_step(const Box &box, int recon, int solver, int mixed, do
 {
   Box const b = with_inverses(box);
   bool const one_d = (b.ny == 1 && b.nz == 1);
+  if (b.nz < 2 * b.ng + 1) temp_floor = 0;  // the reference's temperature floor acts in 3D only
   cudaError_t e;
   if (mixed) {
     e = one_d ? launch_fast<float, 128, 1, 1>(b, recon, solver, U, sc, dt, dt_dev, s, marks)

@@ -15,6 +15,10 @@ namespace cgb
 cudaError_t hydro_exact_step(const Box &b, int recon, int solver, double *U, const Scratch &sc, double dt,
                              const double *dt_dev, double U_floor, int temp_floor, int do_dt, cudaStream_t s,
                              cudaEvent_t *marks = nullptr);
+// The VL step of a 2D box (nz = 1) in exact FP64, predictor and corrector (hydro_2d.cu); the caller
+// runs the finalize pass.  sc.W holds the predictor's fluxes for the PCM corrector (2 nf fields).
+cudaError_t hydro_2d_step(const Box &b, int recon, int solver, double *U, const Scratch &sc, double dt,
+                          const double *dt_dev, cudaStream_t s);
 // dt_t[0] = C_cfl / max_dti (clamped so that t does not pass t_end when t_end > 0), dt_t[1] += dt_t[0]
 cudaError_t cfl_dt(const unsigned long long *dti, double *dt_t, double c_cfl, double t_end, cudaStream_t s);
 // Fast FP64 (mixed = 0) or mixed-precision (mixed = 1) step (hydro_fast.cu).  sc.W holds the

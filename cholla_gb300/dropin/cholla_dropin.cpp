@@ -1,8 +1,8 @@
 // cholla_dropin.cpp -- link-time replacement of Cholla's VL integrator entry points.
 //
 // A Cholla build adds this file (and links libchollagb) in place of the objects of
-// src/integrators/VL_3D_cuda.cu and VL_1D_cuda.cu.  The functions below have the exact C++
-// signatures the rest of Cholla calls (src/integrators/VL_3D_cuda.h:9-13, VL_1D_cuda.h,
+// src/integrators/VL_3D_cuda.cu, VL_2D_cuda.cu and VL_1D_cuda.cu.  The functions below have the exact
+// C++ signatures the rest of Cholla calls (src/integrators/VL_3D_cuda.h:9-13, VL_2D_cuda.h:9-12, VL_1D_cuda.h,
 // src/hydro/hydro_cuda.h:69-70, 90), so Grid3D::Execute_Hydro_Integrator, Calc_Inverse_Timestep
 // and Update_Hydro_Grid need no change.  The compile-time scheme macros of the Cholla build
 // (builds/make.type.*) and its global adiabatic index `gama` become the library's run-time
@@ -40,6 +40,10 @@ void configure()
   s.reconstruction = CGB_PPMC;
 #elif defined(PLMC)
   s.reconstruction = CGB_PLMC;
+#elif defined(PPMP)
+  s.reconstruction = CGB_PPMP;
+#elif defined(PLMP)
+  s.reconstruction = CGB_PLMP;
 #else
   s.reconstruction = CGB_PCM;
 #endif
@@ -47,6 +51,10 @@ void configure()
   s.riemann_solver = CGB_HLLD;
 #elif defined(ROE)
   s.riemann_solver = CGB_ROE;
+#elif defined(HLL)
+  s.riemann_solver = CGB_HLL;
+#elif defined(EXACT)
+  s.riemann_solver = CGB_EXACT;
 #else
   s.riemann_solver = CGB_HLLC;
 #endif
@@ -100,6 +108,17 @@ void VL_Algorithm_1D_CUDA(Real *d_conserved, int nx, int x_off, int n_ghost, Rea
 }
 
 void Free_Memory_VL_1D() { check(cgb_free_memory_vl_3d(), "Free_Memory_VL_1D"); }
+
+void VL_Algorithm_2D_CUDA(Real *d_conserved, int nx, int ny, int x_off, int y_off, int n_ghost, Real dx, Real dy,
+                          Real xbound, Real ybound, Real dt, int n_fields, int custom_grav)
+{
+  configure();
+  check(cgb_vl_algorithm_2d(d_conserved, nx, ny, x_off, y_off, n_ghost, dx, dy, xbound, ybound, dt, n_fields,
+                            custom_grav),
+        "VL_Algorithm_2D_CUDA");
+}
+
+void Free_Memory_VL_2D() { check(cgb_free_memory_vl_3d(), "Free_Memory_VL_2D"); }
 
 // Calc_dt_GPU and Apply_Temperature_Floor are defined in src/hydro/hydro_cuda.cu next to
 // kernels other files still use; build these replacements only once those two definitions

@@ -96,6 +96,12 @@ def VL_Algorithm_1D_CUDA(d_conserved, nx, x_off, n_ghost, dx, xbound, dt, n_fiel
                                         custom_grav))
 
 
+def VL_Algorithm_2D_CUDA(d_conserved, nx, ny, x_off, y_off, n_ghost, dx, dy, xbound, ybound, dt, n_fields,
+                         custom_grav=0) -> None:
+    L.check(L.lib().cgb_vl_algorithm_2d(_ptr(d_conserved), nx, ny, x_off, y_off, n_ghost, dx, dy, xbound, ybound,
+                                        dt, n_fields, custom_grav))
+
+
 def Free_Memory_VL_3D() -> None:
     L.check(L.lib().cgb_free_memory_vl_3d())
 

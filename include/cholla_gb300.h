@@ -136,6 +136,13 @@ int cgb_check_status(int *flags);
 int cgb_vl_algorithm_1d(double *d_conserved, int nx, int x_off, int n_ghost, double dx, double xbound, double dt,
                         int n_fields, int custom_grav);
 
+/* Replaces VL_Algorithm_2D_CUDA (src/integrators/VL_2D_cuda.h:9-10, VL_2D_cuda.cu:25-174): one VL step of
+ * an nx x ny padded box (one cell deep), in place.  As the reference's 2D integrator: no density floor,
+ * no HLL solver, and with PCM the corrector reuses the predictor's fluxes of Uⁿ.  Exact FP64 form only;
+ * custom_grav must be 0.  Scratch is shared with cgb_vl_algorithm_3d (same rules). */
+int cgb_vl_algorithm_2d(double *d_conserved, int nx, int ny, int x_off, int y_off, int n_ghost, double dx, double dy,
+                        double xbound, double ybound, double dt, int n_fields, int custom_grav);
+
 /* Replaces Free_Memory_VL_3D (VL_3D_cuda.cu:362-377).  Frees the library's scratch only,
  * on the device that owns it whatever the current device: unlike the reference it does not
  * free the caller's d_conserved. */

@@ -102,6 +102,9 @@ int ensure_scratch(size_t n, int nf)
     free_scratch();
     return err("reference scratch allocation failed");
   }
+  // the zeroing above runs on the legacy stream, which a non-blocking caller stream does not wait
+  // for: finish it before any kernel of that stream touches the scratch
+  if (cu(cuCtxSynchronize(), "scratch zeroing")) return 1;
   g_s.n  = n;
   g_s.nf = nf;
   return 0;

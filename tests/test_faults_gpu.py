@@ -148,7 +148,7 @@ def test_injected_allocation_failures(cuda):
     try:
         # box creation makes several allocations: fail each in turn
         free0 = cuda.cuda.mem_get_info()[0]
-        for k in range(1, 8):
+        for k in range(1, 16):
             I.debug_fail_alloc(k)
             try:
                 b = Box(N, N, N, NG, dx, dx, dx, _scheme("fp64_fast"))
