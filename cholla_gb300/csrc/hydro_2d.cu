@@ -170,33 +170,40 @@ __global__ void __launch_bounds__(T2 *T2) k2_corr(Box b, const double *__restric
     using S = C2<RECON>;
     constexpr int H = S::H, B = S::B;
     extern __shared__ double smem2[];
-    double *Ps  = smem2;            // [nq][NB] primitives, canonical velocity order
+    double *Ps  = smem2;            // [nq][NB] primitives, rotated for the current sweep
     double *QLs = Ps + nq * S::NB;  // [nq][NR] rotated conserved states of one direction
     double *QRs = QLs + nq * S::NR;
     double *Fs  = QRs + nq * S::NR;  // [nq][NF]
-    for (int p = t; p < S::NB; p += NT) {
-      int const cx = clamp2(x0 - H + p % B, 1, b.nx - 2), cy = clamp2(y0 - H + p / B, 1, b.ny - 2);
-      long long const gid = b.id(cx, cy, 0);
-      double q[NQ_MAX];
-#pragma unroll
-      for (int k = 0; k < NQ_MAX; k++)
-        if (k < nq) q[k] = Uh[(long long)field_of_q2(k, b) * n + gid];
-      hx::Prim const P = (RECON == RECON_PLMP || RECON == RECON_PPMP) ? hx::load_prim_plm(q, b.ns, b.de, b.gamma)
-                                                                      : hx::load_prim(q, b.ns, b.de, b.gamma);
-      Ps[0 * S::NB + p] = P.d;
-      Ps[1 * S::NB + p] = P.vn;  // x velocity (canonical: the load above is unrotated)
-      Ps[2 * S::NB + p] = P.vt1;
-      Ps[3 * S::NB + p] = P.vt2;
-      Ps[4 * S::NB + p] = P.p;
-#pragma unroll
-      for (int k = 0; k < NS_MAX; k++)
-        if (k < b.ns) Ps[(5 + k) * S::NB + p] = P.sc[k];
-      if (b.de) Ps[(5 + b.ns) * S::NB + p] = P.ge;
-    }
-    __syncthreads();
 #pragma unroll
     for (int dir = 0; dir < 2; dir++) {
       int const st = dir == 0 ? 1 : B;
+      int const o1 = dir + 1, o2 = (dir + 1) % 3 + 1, o3 = (dir + 2) % 3 + 1;
+      // U½ -> primitives in this sweep's rotated order (the reference's reconstruction kernels
+      // load them per direction, and the kinetic energy's rounding depends on the order)
+      for (int p = t; p < S::NB; p += NT) {
+        int const cx = clamp2(x0 - H + p % B, 1, b.nx - 2), cy = clamp2(y0 - H + p / B, 1, b.ny - 2);
+        long long const gid = b.id(cx, cy, 0);
+        double q[NQ_MAX];
+#pragma unroll
+        for (int k = 0; k < NQ_MAX; k++) {
+          if (k < nq) {
+            int const src = k == 1 ? o1 : k == 2 ? o2 : k == 3 ? o3 : field_of_q2(k, b);
+            q[k]          = Uh[(long long)src * n + gid];
+          }
+        }
+        hx::Prim const P = (RECON == RECON_PLMP || RECON == RECON_PPMP) ? hx::load_prim_plm(q, b.ns, b.de, b.gamma)
+                                                                        : hx::load_prim(q, b.ns, b.de, b.gamma);
+        Ps[0 * S::NB + p] = P.d;
+        Ps[1 * S::NB + p] = P.vn;
+        Ps[2 * S::NB + p] = P.vt1;
+        Ps[3 * S::NB + p] = P.vt2;
+        Ps[4 * S::NB + p] = P.p;
+#pragma unroll
+        for (int k = 0; k < NS_MAX; k++)
+          if (k < b.ns) Ps[(5 + k) * S::NB + p] = P.sc[k];
+        if (b.de) Ps[(5 + b.ns) * S::NB + p] = P.ge;
+      }
+      __syncthreads();
       // reconstructed cell r: position a = -1 .. T2 along the sweep, line l across it
       for (int r = t; r < S::NR; r += NT) {
         int const a = r % (T2 + 2) - 1, l = r / (T2 + 2);
@@ -204,12 +211,10 @@ __global__ void __launch_bounds__(T2 *T2) k2_corr(Box b, const double *__restric
         auto prim_at = [&](int off) {
           int const pi = base + off * st;
           hx::Prim P;
-          P.d = Ps[pi];
-          double const vx = Ps[S::NB + pi], vy = Ps[2 * S::NB + pi], vz = Ps[3 * S::NB + pi];
-          // rotate the velocities to (normal, t1, t2): (x, y, z) along x, (y, z, x) along y
-          P.vn  = dir == 0 ? vx : vy;
-          P.vt1 = dir == 0 ? vy : vz;
-          P.vt2 = dir == 0 ? vz : vx;
+          P.d   = Ps[pi];
+          P.vn  = Ps[S::NB + pi];
+          P.vt1 = Ps[2 * S::NB + pi];
+          P.vt2 = Ps[3 * S::NB + pi];
           P.p   = Ps[4 * S::NB + pi];
 #pragma unroll
           for (int k = 0; k < NS_MAX; k++) P.sc[k] = (k < b.ns) ? Ps[(5 + k) * S::NB + pi] : 0.0;
@@ -263,7 +268,6 @@ __global__ void __launch_bounds__(T2 *T2) k2_corr(Box b, const double *__restric
         int const a = dir == 0 ? ti : tj, l = dir == 0 ? tj : ti;
         int const fm = a + (T2 + 1) * l;
         double const k = dir == 0 ? dtodx : dtody;
-        int const o1 = dir + 1, o2 = (dir + 1) % 3 + 1, o3 = (dir + 2) % 3 + 1;
 #pragma unroll
         for (int q = 0; q < NQ_MAX; q++) {
           if (q < nq) {

@@ -260,7 +260,7 @@ cudaError_t hydro_exact_step(const Box &b, int recon, int solver, double *U, con
     }
     int const ng = b.ng;
     long long const nreal =
-        (long long)(b.nx - 2 * ng) * (one_d ? 1 : b.ny - 2 * ng) * (one_d ? 1 : b.nz - 2 * ng);
+        (long long)(b.nx - 2 * ng) * (one_d ? 1 : b.ny - 2 * ng) * (b.nz == 1 ? 1 : b.nz - 2 * ng);
     k_finalize<<<(unsigned)((nreal + 255) / 256), 256, 0, s>>>(b, U, sc.Epre, sc.dti, sc.status, U_floor, temp_floor,
                                                                do_dt);
     e = cudaGetLastError();
