@@ -603,201 +603,6 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
   }
 }
 
-// ------------------------------------------------------------------------------------------
-// Warp-per-pencil sweeps.  A warp owns one pencil segment at a time: lane l holds cell c = l - 1
-// of the segment (c = -1 .. 30), reconstructs it from its stencil in shared memory, takes the
-// face between cells c - 1 and c from its own low-face state and lane l - 1's high-face state
-// (a shuffle), and updates cell c (lanes 1 .. 30) from its own face flux and lane l + 1's.  The
-// interface states and fluxes never leave registers, and no block-wide barrier separates the
-// phases: only the cooperative load of the block's 32 pencils is followed by one __syncthreads.
-// Every lane does useful work in every phase (30 updated cells, 31 faces, 32 reconstructions per
-// 32 lanes), where the block-phased sweeps ran each phase's last few items as a second, nearly
-// empty pass behind a barrier.  A block is 8 warps over 32 neighbouring pencils (32 x-adjacent
-// pencils for the y and z sweeps, so the loads are coalesced along x; 32 y-adjacent x-pencils for
-// the x sweep, each loaded along its own contiguous row).
-// ------------------------------------------------------------------------------------------
-constexpr int WSL = 30;  // cells updated per pencil segment
-constexpr int WSP = 32;  // pencils per block
-constexpr int WSW = 8;   // warps per block
-// resident blocks per SM the register budget targets (FP32 / FP64 compute): the FP32 PPMC + HLLC
-// lane needs about 80 registers, so 4 blocks (64 registers) spill several hundred bytes per thread
-#ifndef CGB_WS_MINB_F32
-#define CGB_WS_MINB_F32 3
-#endif
-#ifndef CGB_WS_MINB_F64
-#define CGB_WS_MINB_F64 2
-#endif
-
-template <int DIR, int RECON>
-struct WSweep {
-  static constexpr int H  = FHalo<RECON>::H;
-  static constexpr int LA = WSL + 2 * H;  // loaded cells per pencil
-  // shared layout: y and z sweeps [slot][a][pencil] with the pencil row padded to 33 (a warp reads
-  // one pencil at 32 different a: distinct banks); x sweep [slot][pencil][a] with rows of LA + 1
-  static constexpr int ROW = DIR == 0 ? LA + 1 : WSP + 1;
-  static constexpr int PER_SLOT = DIR == 0 ? WSP * (LA + 1) : LA * (WSP + 1);
-  __device__ static int at(int a, int pencil) { return DIR == 0 ? a + ROW * pencil : pencil + ROW * a; }
-};
-
-template <typename T>
-__device__ __forceinline__ hf::Prim<T> shfl_up_prim(const hf::Prim<T> &s, int ns, int de)
-{
-  hf::Prim<T> o;
-  o.d   = __shfl_up_sync(0xffffffffu, s.d, 1);
-  o.vn  = __shfl_up_sync(0xffffffffu, s.vn, 1);
-  o.vt1 = __shfl_up_sync(0xffffffffu, s.vt1, 1);
-  o.vt2 = __shfl_up_sync(0xffffffffu, s.vt2, 1);
-  o.p   = __shfl_up_sync(0xffffffffu, s.p, 1);
-  o.ge  = de ? __shfl_up_sync(0xffffffffu, s.ge, 1) : T(0);
-#pragma unroll
-  for (int k = 0; k < NS_MAX; k++) o.sc[k] = (k < ns) ? __shfl_up_sync(0xffffffffu, s.sc[k], 1) : T(0);
-  return o;
-}
-
-template <typename T, int DIR, int RECON, int SOLVER, bool FIRST, bool FINAL>
-__device__ __forceinline__ void wsweep_tile(const Box &b, const T *__restrict__ W, T *__restrict__ dU,
-                                            double *__restrict__ U, const double *__restrict__ GEp,
-                                            double *__restrict__ Epre, int *__restrict__ status, double dt,
-                                            const double *__restrict__ dtp, int seg, int pg, int pc)
-{
-  using S = WSweep<DIR, RECON>;
-  constexpr int H = S::H, LA = S::LA;
-  constexpr int o1 = DIR + 1, o2 = (DIR + 1) % 3 + 1, o3 = (DIR + 2) % 3 + 1;
-  if (dtp) dt = *dtp;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *Ps = reinterpret_cast<T *>(smem_raw);  // [slot][PER_SLOT]
-  int const ns_ = nslot(b), ng = b.ng;
-  long long const n = b.n;
-  int const rx = b.nx - 2 * ng, ry = b.ny - 2 * ng, rz = b.nz - 2 * ng;
-  int const ra = DIR == 0 ? rx : DIR == 1 ? ry : rz;  // real cells along the sweep
-  int const rp = DIR == 0 ? ry : rx;                  // real extent of the pencil index
-  int const a0 = seg * WSL;                           // first updated cell of the segment
-  int const p0 = pg * WSP;                            // first pencil of the block
-  int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // global cell of segment position a (sweep coordinate a0 + a - H) on pencil p, clamped to the
-  // cells the predictor wrote (1 .. n - 2): positions past the box feed only discarded faces
-  auto gid_of = [&](int a, int p) -> long long {
-    int const g = ng + a0 + a - H, q = ng + min(p0 + p, rp - 1), c2 = ng + pc;
-    int gx, gy, gz;
-    if (DIR == 0) {
-      gx = g, gy = q, gz = c2;
-    } else if (DIR == 1) {
-      gy = g, gx = q, gz = c2;
-    } else {
-      gz = g, gx = q, gy = c2;
-    }
-    return b.id(clampi(gx, 1, b.nx - 2), clampi(gy, 1, b.ny - 2), clampi(gz, 1, b.nz - 2));
-  };
-  // 1. load the block's 32 pencil segments of W½, rotated to (d, vn, vt1, vt2, p, ge, scalars)
-  if (DIR == 0) {  // each warp loads the x rows of its own pencils
-    for (int p = warp; p < WSP; p += WSW)
-      for (int a = lane; a < LA; a += 32) {
-        long long const gid = gid_of(a, p);
-        for (int q = 0; q < ns_; q++) Ps[q * S::PER_SLOT + S::at(a, p)] = W[(long long)rot(q, o1, o2, o3) * n + gid];
-      }
-    __syncwarp();
-  } else {  // lanes run along x: coalesced
-    for (int i = threadIdx.x; i < WSP * LA; i += WSW * 32) {
-      int const p = i % WSP, a = i / WSP;
-      long long const gid = gid_of(a, p);
-      for (int q = 0; q < ns_; q++) Ps[q * S::PER_SLOT + S::at(a, p)] = W[(long long)rot(q, o1, o2, o3) * n + gid];
-    }
-    __syncthreads();
-  }
-  T const dtod = narrow<T>(dt * (DIR == 0 ? b.idx : DIR == 1 ? b.idy : b.idz));
-  int const c  = lane - 1;  // this lane's cell in the segment
-  bool const upd = lane >= 1 && lane <= WSL && a0 + c < ra;
-  for (int p = warp; p < WSP; p += WSW) {
-    if (p0 + p >= rp) break;  // pencils past the box (uniform per warp)
-    int const ac = c + H;     // segment position of this lane's cell
-    auto prim = [&](int k) { return prim_at(Ps, S::PER_SLOT, S::at(ac + k, p), b); };
-    hf::Prim<T> Lf, Rf;  // states at the cell's high (Lf) and low (Rf) faces
-    if (RECON == RECON_PPMC) {
-      hf::ppmc_cell(prim(-2), prim(-1), prim(0), prim(1), prim(2), b.ns, b.de, (T)b.gamma, Lf, Rf);
-    } else if (RECON == RECON_PLMC) {
-      hf::plmc_cell(prim(-1), prim(0), prim(1), b.ns, b.de, (T)b.gamma, Lf, Rf);
-    } else {
-      Lf = Rf = prim(0);
-    }
-    hf::Prim<T> const Lm = shfl_up_prim(Lf, b.ns, b.de);  // high-face state of cell c - 1
-    T f[NSLOT];
-    riemann<T, SOLVER>(Lm, Rf, f, b);  // flux at the low face of cell c (lane 0: unused)
-    T fr[NSLOT];
-#pragma unroll
-    for (int q = 0; q < NSLOT; q++) fr[q] = __shfl_down_sync(0xffffffffu, live(q, b) ? f[q] : T(0), 1);
-    if (!upd) continue;
-    int const q0 = ng + min(p0 + p, rp - 1), g = ng + a0 + c, c2 = ng + pc;
-    long long const gid = DIR == 0 ? b.id(g, q0, c2) : DIR == 1 ? b.id(q0, g, c2) : b.id(q0, c2, g);
-    Acc<T> acc[NSLOT];
-#pragma unroll
-    for (int q = 0; q < NSLOT; q++) {
-      int const qq = q == 1 ? o1 : q == 2 ? o2 : q == 3 ? o3 : q;  // rotated momenta back to x, y, z
-      if (live(q, b)) acc[qq] = flux_diff(dtod, f[q], fr[q]);
-    }
-    Acc<T> *__restrict__ dA = reinterpret_cast<Acc<T> *>(dU);
-    if (!FIRST) {
-#pragma unroll
-      for (int q = 0; q < NSLOT; q++)
-        if (live(q, b)) acc[q] = acc_add(dA[(long long)q * n + gid], acc[q]);
-    }
-    if constexpr (!FINAL) {
-#pragma unroll
-      for (int q = 0; q < NSLOT; q++)
-        if (live(q, b)) dA[(long long)q * n + gid] = acc[q];
-    } else {
-      double inc[NSLOT];
-#pragma unroll
-      for (int q = 0; q < NSLOT; q++) inc[q] = live(q, b) ? acc_value(acc[q]) : 0.0;
-      final_update(b, gid, inc, U, GEp, Epre, status);
-    }
-  }
-}
-
-template <typename T, int DIR, int RECON, int SOLVER, bool FIRST, bool FINAL>
-__global__ void __launch_bounds__(WSW * 32, sizeof(T) == 4 ? CGB_WS_MINB_F32 : CGB_WS_MINB_F64)
-    k_wsweep(Box b, const T *__restrict__ W, T *__restrict__ dU, double *__restrict__ U, const double *__restrict__ GEp,
-             double *__restrict__ Epre, int *__restrict__ status, double dt, const double *__restrict__ dtp)
-{
-  wsweep_tile<T, DIR, RECON, SOLVER, FIRST, FINAL>(b, W, dU, U, GEp, Epre, status, dt, dtp, blockIdx.x, blockIdx.y,
-                                                   blockIdx.z);
-}
-
-// grid of a warp sweep: (segments along the sweep, pencil groups, the remaining axis)
-template <int DIR>
-__host__ __device__ inline void wsweep_grid(const Box &b, int &gs, int &gp, int &gc)
-{
-  int const rx = b.nx - 2 * b.ng, ry = b.ny - 2 * b.ng, rz = b.nz - 2 * b.ng;
-  int const ra = DIR == 0 ? rx : DIR == 1 ? ry : rz, rp = DIR == 0 ? ry : rx, rc = DIR == 2 ? ry : rz;
-  gs = (ra + WSL - 1) / WSL, gp = (rp + WSP - 1) / WSP, gc = rc;
-}
-
-template <typename T, int DIR, bool FIRST, bool FINAL>
-cudaError_t launch_wsweep(const Box &b, int recon, int solver, const T *Wh, T *dU, double *U, const Scratch &sc,
-                          double dt, const double *dtp, cudaStream_t s)
-{
-  int gs, gp, gc;
-  wsweep_grid<DIR>(b, gs, gp, gc);
-  void (*k)(Box, const T *, T *, double *, const double *, double *, int *, double, const double *);
-  size_t per_slot;
-#define CGB_PICK(R)                                                                                        \
-  per_slot = WSweep<DIR, R>::PER_SLOT;                                                                     \
-  k        = (solver == SOLVER_ROE) ? k_wsweep<T, DIR, R, SOLVER_ROE, FIRST, FINAL>                          \
-                                    : k_wsweep<T, DIR, R, SOLVER_HLLC, FIRST, FINAL>;
-  if (recon == RECON_PPMC) {
-    CGB_PICK(RECON_PPMC)
-  } else if (recon == RECON_PLMC) {
-    CGB_PICK(RECON_PLMC)
-  } else {
-    CGB_PICK(RECON_PCM)
-  }
-#undef CGB_PICK
-  size_t const sm = sizeof(T) * (size_t)nslot(b) * per_slot;
-  cudaError_t e   = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-  if (e != cudaSuccess) return e;
-  k<<<dim3(gs, gp, gc), WSW * 32, sm, s>>>(b, Wh, dU, U, sc.GEp, sc.Epre, sc.status, dt, dtp);
-  return cudaGetLastError();
-}
-
 // Mixed-precision sweeps are latency-bound (FP32 reconstruction chains, FMA pipe under 20% at
 // two blocks per SM): five resident blocks per SM (51 registers, spills to L1) take the 256^3
 // corrector from 6.8 to 4.1 ms (two: 6.8, three: 5.2, four: 4.3, six: 4.07).  The FP64 sweeps
@@ -864,9 +669,9 @@ __device__ __forceinline__ void block_max_to(double v, unsigned long long *dst)
   }
 }
 
-// MIX: the mixed-precision form takes the sound speed's square root in FP32 and the
-// reciprocal of the density with one Newton step; the selection, sync, floor and the
-// maximum stay FP64 (maxima compare bit patterns on the integer pipe).
+// MIX: the mixed-precision form takes the reciprocal of the density with one Newton step and each
+// cell's crossing rate in FP32; the total-minus-kinetic energy, the selection, sync, floor and the
+// maximum over the box stay FP64 (maxima compare bit patterns on the integer pipe).
 template <bool MIX>
 __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict__ U, const double *__restrict__ Epre,
                                                 unsigned long long *__restrict__ dti, int *__restrict__ status,
@@ -923,9 +728,24 @@ __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict
       }
     }
     if (bad_cell(d, E)) atomicOr(status, STATUS_NONFINITE);
-    if (do_dt) {  // hydroInverseCrossingTime (hydro_cuda.cu:404-419)
+    if (do_dt && MIX) {
+      // the crossing rate of the cell in FP32 from its FP64 thermal energy (E - ke); the maximum
+      // over the box, which sets dt, stays FP64
+      float const idf = hf::to_f32(d_inv), g = (float)b.gamma;
+      float const c2  = g * (g - 1.0f) * hf::to_f32(E - ke) * idf;
+      float const cs  = sqrtf(fmaxf(c2, 0.0f));
+      float const ax  = fabsf(hf::to_f32(mx) * idf) + cs;
+      float mf;
+      if (one_d) {
+        mf = ax * (float)idx;
+      } else {
+        float const ay = fabsf(hf::to_f32(my) * idf) + cs, az = fabsf(hf::to_f32(mz) * idf) + cs;
+        mf = fmaxf(fmaxf(ax * (float)idx, ay * (float)idy), az * (float)idz);
+      }
+      m = hf::to_f64(mf);
+    } else if (do_dt) {  // hydroInverseCrossingTime (hydro_cuda.cu:404-419)
       double const c2 = b.gamma * (E - ke) * (b.gamma - 1.0) * d_inv;
-      double const cs = MIX ? hf::to_f64(sqrtf(hf::to_f32(hf::max_pos(c2, 0.0)))) : hf::sqrtT(hf::max_pos(c2, 0.0));
+      double const cs = hf::sqrtT(hf::max_pos(c2, 0.0));
       double const ax = fabs(mx * d_inv) + cs;
       if (one_d) {
         m = ax * idx;
@@ -984,9 +804,9 @@ cudaError_t launch_fast(const Box &b, int recon, int solver, double *U, const Sc
   if (b.ny == 1 && b.nz == 1) {
     e = launch_sweep<T, 0, 128, 1, 1, true, true>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
   } else {
-    e = launch_wsweep<T, 0, true, false>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
-    if (e == cudaSuccess) e = launch_wsweep<T, 1, false, false>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
-    if (e == cudaSuccess) e = launch_wsweep<T, 2, false, true>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
+    e = launch_sweep<T, 0, SXL, SXA, SXB, true, false>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
+    if (e == cudaSuccess) e = launch_sweep<T, 1, SYL, SYA, SYB, false, false>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
+    if (e == cudaSuccess) e = launch_sweep<T, 2, SYL, SYA, SYB, false, true>(b, recon, solver, Wh, Wn, U, sc, dt, dtp, s);
   }
   if (e != cudaSuccess) return e;
   if (marks) cudaEventRecord(marks[2], s);

@@ -123,6 +123,8 @@ def test_dropin_shim_exports_the_reference_symbols(tmp_path):
         "_Z17Free_Memory_VL_3Dv",
         "_Z20VL_Algorithm_1D_CUDAPdiiidddii",
         "_Z17Free_Memory_VL_1Dv",
+        "_Z20VL_Algorithm_2D_CUDAPdiiiiidddddii",  # VL_2D_cuda.h:9-12
+        "_Z17Free_Memory_VL_2Dv",
         "_Z11Calc_dt_GPUPdiiiiidddd",
         "_Z23Apply_Temperature_FloorPdiiiiid",
     }
