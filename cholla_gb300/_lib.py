@@ -23,6 +23,7 @@ CGB_ERR_UNSUPPORTED = 6
 
 CGB_STATUS_NEG_DENSITY = 1
 CGB_STATUS_NONFINITE = 2
+CGB_STATUS_TIMEOUT = 4
 CGB_MAX_DIVB = 1.0e-9
 
 PCM, PLMC, PPMC, PLMP, PPMP = 0, 1, 2, 3, 4
@@ -96,6 +97,8 @@ SIGNATURES = {
     "cgb_batch_hold": (_I, [_P, _I, _I]),
     "cgb_selftest_conversions": (_I, [_P, C.c_longlong, _P, _P]),
     "cgb_selftest_fast_math": (_I, [_P, C.c_longlong, _P, _P]),
+    "cgb_selftest_tma_timeout": (_I, [_P, C.c_uint, _P]),
+    "cgb_set_tma": (_I, [_I]),
     "cgb_batch_set_solo_cells": (_I, [_P, C.c_longlong]),
     "cgb_batch_step": (_I, [_P, _I]),
     "cgb_batch_job_time": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_D)]),

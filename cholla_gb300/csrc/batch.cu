@@ -398,6 +398,7 @@ namespace
 {
 const char *kBadJob =
     "the job holds a real cell with non-finite density or energy, or density <= 0 after the negative-density repair";
+const char *kTimedOut = "a bounded device wait for a TMA copy ran out; a step of the job left a tile undone";
 }
 
 // Time and last dt of one job (synchronises the batch stream).  Returns CGB_ERR_NONFINITE (with t
@@ -416,6 +417,7 @@ int cgb_batch_job_time(cgb_batch *bt, int job_id, double *t, double *dt_last)
     if (e != cudaSuccess) return bcuda(e, "batch_job_time");
     if (t) *t = h[1];
     if (dt_last) *dt_last = h[0];
+    if (st & CGB_STATUS_TIMEOUT) return bfail(CGB_ERR_TIMEOUT, kTimedOut);
     if (st & CGB_STATUS_NONFINITE) return bfail(CGB_ERR_NONFINITE, kBadJob);
     return CGB_OK;
   }
@@ -432,6 +434,7 @@ int cgb_batch_job_status(cgb_batch *bt, int job_id, int *flags)
     cudaError_t e = cudaStreamSynchronize(bt->stream);
     if (e == cudaSuccess) e = cudaMemcpy(flags, bt->jobs[i].status, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return bcuda(e, "batch_job_status");
+    if (*flags & CGB_STATUS_TIMEOUT) return bfail(CGB_ERR_TIMEOUT, kTimedOut);
     if (*flags & CGB_STATUS_NONFINITE) return bfail(CGB_ERR_NONFINITE, kBadJob);
     return CGB_OK;
   }

@@ -501,6 +501,8 @@ int cgb_check_status(int *flags)
   if (other) cudaSetDevice(cur);
   if (e != cudaSuccess) return cuda_fail(e, "check_status");
   if (flags) *flags = h;
+  if (h & CGB_STATUS_TIMEOUT)
+    return fail(CGB_ERR_TIMEOUT, "a bounded device wait for a TMA copy ran out; the step left a tile undone");
   if (h & CGB_STATUS_NONFINITE)
     return fail(CGB_ERR_NONFINITE, "a step left a real cell with non-finite density or energy, or density <= 0 "
                                    "after the negative-density repair");

@@ -20,6 +20,7 @@ constexpr int NQ_MAX   = 5 + NS_MAX + 1;
 // host through cgb_check_status / cgb_box_check_status / cgb_batch_job_status).
 constexpr int STATUS_NEG_DENSITY = 1;  // a real cell's update gave density <= 0 (repaired by averaging)
 constexpr int STATUS_NONFINITE   = 2;  // a real cell holds non-finite density or energy, or density <= 0 after repair
+// (bit 4, STATUS_TMA_TIMEOUT in tma.cuh: a bounded wait for a TMA copy ran out and a tile was left undone)
 
 // x is NaN or +-infinity (exponent bits all ones), tested on the integer pipe
 __device__ __forceinline__ bool not_finite(double x) { return (__double2hiint(x) & 0x7ff00000) == 0x7ff00000; }

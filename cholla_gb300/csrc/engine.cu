@@ -293,6 +293,7 @@ namespace
 {
 const char *kBadCells =
     "the box holds a real cell with non-finite density or energy, or density <= 0 after the negative-density repair";
+const char *kTimeout = "a bounded device wait for a TMA copy ran out; a step left a tile undone";
 }
 
 // Current (dt, t) of the box; synchronises the box's last stream.  Returns CGB_ERR_NONFINITE (with
@@ -308,6 +309,7 @@ int cgb_box_get_time(cgb_box *bx, double *t, double *dt_last)
     return box_fail(bx, CGB_ERR_CUDA, "get_time");
   if (dt_last) *dt_last = h[0];
   if (t) *t = h[1];
+  if (st & CGB_STATUS_TIMEOUT) return box_fail(bx, CGB_ERR_TIMEOUT, kTimeout);
   if (st & CGB_STATUS_NONFINITE) return box_fail(bx, CGB_ERR_NONFINITE, kBadCells);
   return CGB_OK;
 }
@@ -323,6 +325,7 @@ int cgb_box_check_status(cgb_box *bx, int *flags)
       cudaMemset(bx->s.status, 0, sizeof(int)) != cudaSuccess)
     return box_fail(bx, CGB_ERR_CUDA, "check_status");
   if (flags) *flags = st;
+  if (st & CGB_STATUS_TIMEOUT) return box_fail(bx, CGB_ERR_TIMEOUT, kTimeout);
   if (st & CGB_STATUS_NONFINITE) return box_fail(bx, CGB_ERR_NONFINITE, kBadCells);
   return CGB_OK;
 }

@@ -17,6 +17,7 @@
 #include "ghost.cuh"
 #include "hydro_fast.cuh"
 #include "kernels.h"
+#include "tma.cuh"
 
 namespace cgb
 {
@@ -27,7 +28,26 @@ constexpr int NSLOT = 6 + NS_MAX;
 // tiles of the 3D step (single boxes and batches alike): predictor 8 x 8 x 4 cells; corrector
 // sweeps along x over 64 x 2 x 2 cells, along y and z over 32 x 8 x 1
 constexpr int PTX = 8, PTY = 8, PTZ = 4;
-constexpr int SXL = 64, SXA = 2, SXB = 2, SYL = 32, SYA = 8, SYB = 1;
+// (compile-time tunables: the tile shapes and the resident blocks per SM the sweeps' register
+// budget targets, FP32 and FP64 compute)
+#ifndef CGB_SWEEP_XL  // x sweep: cells per pencil, pencils along y and along z
+#define CGB_SWEEP_XL 64
+#define CGB_SWEEP_XA 2
+#define CGB_SWEEP_XB 2
+#endif
+#ifndef CGB_SWEEP_YL  // y and z sweeps: cells per pencil, x-adjacent pencils, pencils across
+#define CGB_SWEEP_YL 32
+#define CGB_SWEEP_YA 8
+#define CGB_SWEEP_YB 1
+#endif
+#ifndef CGB_SWEEP_MINB_F32
+#define CGB_SWEEP_MINB_F32 5
+#endif
+#ifndef CGB_SWEEP_MINB_F64
+#define CGB_SWEEP_MINB_F64 2
+#endif
+constexpr int SXL = CGB_SWEEP_XL, SXA = CGB_SWEEP_XA, SXB = CGB_SWEEP_XB;
+constexpr int SYL = CGB_SWEEP_YL, SYA = CGB_SWEEP_YA, SYB = CGB_SWEEP_YB;
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
@@ -158,20 +178,6 @@ __device__ __forceinline__ hf::Prim<T> prim_at(const T *P, int stride, int i, co
 #pragma unroll
   for (int k = 0; k < NS_MAX; k++) s.sc[k] = (k < b.ns) ? P[(6 + k) * stride + i] : T(0);
   return s;
-}
-
-template <typename T>
-__device__ __forceinline__ void prim_put(T *P, int stride, int i, const hf::Prim<T> &s, const Box &b)
-{
-  P[0 * stride + i] = s.d;
-  P[1 * stride + i] = s.vn;
-  P[2 * stride + i] = s.vt1;
-  P[3 * stride + i] = s.vt2;
-  P[4 * stride + i] = s.p;
-  if (b.de) P[5 * stride + i] = s.ge;
-#pragma unroll
-  for (int k = 0; k < NS_MAX; k++)
-    if (k < b.ns) P[(6 + k) * stride + i] = s.sc[k];
 }
 
 template <typename T, int SOLVER>
@@ -354,11 +360,20 @@ struct FHalo {
 // A sweep block: CS = WA * WB pencils of L cells along the sweep direction DIR.  Arrays in
 // shared memory are [slot][pencil position, pencil]; along x the position is fastest (the x
 // pencils are contiguous in HBM), along y and z the pencil index is (WA consecutive x cells).
+// Threads of a sweep block: one per reconstructed cell (L + 2 per pencil; PCM: one per face,
+// L + 1), rounded up to whole warps, so that the reconstruction and Riemann phases each take one
+// pass; the update phase uses the first L * CS of them, one per updated cell.
+__host__ __device__ constexpr int sweep_threads(int L, int CS, int recon)
+{
+  return ((recon == RECON_PCM ? L + 1 : L + 2) * CS + 31) / 32 * 32;
+}
+
 template <int DIR, int L, int WA, int WB, int RECON>
 struct Sweep {
   static constexpr int H  = FHalo<RECON>::H;
   static constexpr int CS = WA * WB;
-  static constexpr int NT = L * CS;  // one thread per updated cell
+  static constexpr int NU = L * CS;  // updated cells
+  static constexpr int NT = sweep_threads(L, CS, RECON);
   static constexpr int LA = L + 2 * H, LR = L + 2, LF = L + 1;
   static constexpr int NP = LA * CS, NR = LR * CS, NF = LF * CS;
   // P (loaded primitives), QL and QR (face states); the fluxes reuse P once it is consumed
@@ -366,6 +381,20 @@ struct Sweep {
   static constexpr int PER_Q = RECON == RECON_PCM ? NP + NF : NP + 2 * NR;
   static constexpr int STRIDE = DIR == 0 ? 1 : CS;
   __device__ static int at(int a, int c, int len) { return DIR == 0 ? a + len * c : c + CS * a; }
+  // TMA staging of P (y and z sweeps need WB == 1): the box of one slot lands as rows along x,
+  // padded so that its first x can be rounded down to a 16-byte boundary (offset 0 .. E - 1):
+  // x sweep CS rows of LAP cells, y and z sweeps LA rows of WAP cells
+  template <typename T>
+  struct Tma {
+    static constexpr int E   = 16 / (int)sizeof(T);
+    static constexpr int LAP = (LA + 2 * E - 2) / E * E;
+    static constexpr int WAP = (WA + 2 * E - 2) / E * E;
+    static constexpr int NPT = DIR == 0 ? LAP * CS : WAP * LA;
+    static constexpr int ROW = DIR == 0 ? LAP : WAP;
+    static constexpr int NPS = ((NPT > NP ? NPT : NP) + 31) / 32 * 32;  // slot stride, whole 128 bytes
+    static constexpr int PER_Q = RECON == RECON_PCM ? NPS + NF : NPS + 2 * NR;
+    static constexpr bool ok = DIR == 0 || WB == 1;
+  };
   __device__ static void split(int i, int len, int &a, int &c)
   {
     if (DIR == 0) {
@@ -467,21 +496,28 @@ __device__ __forceinline__ void final_update(const Box &b, long long gid, const 
 // difference dt/dx (F(i-1/2) - F(i+1/2)) per cell.  Not FINAL: the difference is added to the
 // accumulator dU (the x sweep starts it).  FINAL (the last sweep): Uⁿ⁺¹ = Uⁿ + (dU + the
 // difference) in FP64 in place, density floor, Epre = pre-sync total energy.
-template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
+// With TMA (single boxes): the P boxes are copied by the Tensor Memory Accelerator from the tensor
+// map `map` of W (4D: x, y, z, slot), one copy per slot issued by thread 0 and counted on an
+// mbarrier; without, every thread loads its share of the P array.
+template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL, bool TMA = false>
 __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ W, T *__restrict__ dU,
                                             double *__restrict__ U, const double *__restrict__ GEp,
                                             double *__restrict__ Epre, int *__restrict__ status, double dt,
-                                            const double *__restrict__ dtp, int bx_, int by_, int bz_)
+                                            const double *__restrict__ dtp, int bx_, int by_, int bz_,
+                                            const CUtensorMap *map = nullptr)
 {
-  using S = Sweep<DIR, L, WA, WB, RECON>;
+  using S  = Sweep<DIR, L, WA, WB, RECON>;
+  using TM = typename S::template Tma<T>;
+  static_assert(!TMA || TM::ok, "TMA staging of the y and z sweeps needs WB == 1");
   constexpr int H  = S::H;
   constexpr int NT = S::NT;
+  constexpr int PS = TMA ? TM::NPS : S::NP;  // P elements per slot
   constexpr int o1 = DIR + 1, o2 = (DIR + 1) % 3 + 1, o3 = (DIR + 2) % 3 + 1;
   if (dtp) dt = *dtp;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int const ns_ = nslot(b);
   T *Ps  = reinterpret_cast<T *>(smem_raw);
-  T *QLs = Ps + ns_ * S::NP;
+  T *QLs = Ps + ns_ * PS;
   T *QRs = QLs + ns_ * S::NR;
   T *Fs  = RECON == RECON_PCM ? QLs : Ps;
 
@@ -511,36 +547,78 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
   };
 
   int const t = threadIdx.x;
-  // Positions past the box (a partial tile) read the nearest cell the predictor wrote (1 .. n-2;
-  // the outermost layer of W½ stays zero), so their discarded states stay physical and off the
-  // slow paths.  No real cell's stencil reaches the outermost layer.
-  for (int p = t; p < S::NP; p += NT) {
-    int a, c, gx, gy, gz;
-    S::split(p, S::LA, a, c);
-    cell(a - H, c, gx, gy, gz);
-    long long const gid = b.id(clampi(gx, 1, b.nx - 2), one_d ? 0 : clampi(gy, 1, b.ny - 2),
-                               one_d ? 0 : clampi(gz, 1, b.nz - 2));
-    for (int q = 0; q < ns_; q++) Ps[q * S::NP + p] = W[(long long)rot(q, o1, o2, o3) * n + gid];
+  // P index of sweep position a on pencil c, and the step between neighbouring positions
+  int off = 0;  // TMA: the box's first x lies `off` cells before the block's first needed x
+  auto pidx = [&](int a, int c) -> int {
+    if constexpr (TMA) return DIR == 0 ? (a + off) + TM::ROW * c : (c + off) + TM::ROW * a;
+    return S::at(a, c, S::LA);
+  };
+  constexpr int STR = TMA ? (DIR == 0 ? 1 : TM::ROW) : S::STRIDE;
+  if constexpr (TMA) {
+    // Every position a used face needs lies in 1 .. n-2 whatever the tile, so the unclamped boxes
+    // give those positions exactly what the plain load gives them; positions past the array (a
+    // partial tile) read zeros and feed only faces the tile skips.
+    __shared__ uint64_t bar;
+    int const xs = DIR == 0 ? a0 + ng - H : ca0 + ng;  // first needed x
+    off          = xs % TM::E;
+    if (t == 0) {
+      mbar_init(&bar, 1);
+      fence_mbar_init();
+    }
+    __syncthreads();
+    if (t == 0) {
+      mbar_arrive_expect_tx(&bar, (unsigned)(ns_ * TM::NPT * (int)sizeof(T)));
+      int const xa = xs - off, s0 = a0 + ng - H;
+      for (int q = 0; q < ns_; q++) {
+        int const w = rot(q, o1, o2, o3);
+        if (DIR == 0)
+          tma_load_4d(Ps + q * PS, map, &bar, xa, ca0 + ng, cb0 + ng, w);
+        else if (DIR == 1)
+          tma_load_4d(Ps + q * PS, map, &bar, xa, s0, cb0 + ng, w);
+        else
+          tma_load_4d(Ps + q * PS, map, &bar, xa, cb0 + ng, s0, w);
+      }
+    }
+    bool const ok = __syncthreads_and(mbar_wait(&bar, 0));
+    if (!ok) {  // a copy never completed: leave the tile undone, reported through the status word
+      if (t == 0) {
+        atomicOr(status, STATUS_TMA_TIMEOUT);
+        mbar_wait(&bar, 0);  // bounded: let a late copy land before the block's shared memory goes
+      }
+      return;
+    }
+  } else {
+    // Positions past the box (a partial tile) read the nearest cell the predictor wrote (1 .. n-2;
+    // the outermost layer of W½ stays zero), so their discarded states stay physical and off the
+    // slow paths.  No real cell's stencil reaches the outermost layer.
+    for (int p = t; p < S::NP; p += NT) {
+      int a, c, gx, gy, gz;
+      S::split(p, S::LA, a, c);
+      cell(a - H, c, gx, gy, gz);
+      long long const gid = b.id(clampi(gx, 1, b.nx - 2), one_d ? 0 : clampi(gy, 1, b.ny - 2),
+                                 one_d ? 0 : clampi(gz, 1, b.nz - 2));
+      for (int q = 0; q < ns_; q++) Ps[q * S::NP + p] = W[(long long)rot(q, o1, o2, o3) * n + gid];
+    }
+    __syncthreads();
   }
-  __syncthreads();
   if (RECON != RECON_PCM) {
     for (int r = t; r < S::NR; r += NT) {
       int a, c;
       S::split(r, S::LR, a, c);
       if (a > lim + 1 || !pencil_in(c)) continue;  // cell a0 + a - 1 feeds no real face
-      int const base = S::at(a - 1 + H, c, S::LA);
-      constexpr int st = S::STRIDE;
-      hf::Prim<T> Lf, Rf;
+      int const base = pidx(a - 1 + H, c);
+      // the stencil is read from shared memory variable by variable and each face value written
+      // back as soon as it is known (a handful of live registers instead of five whole cells)
+      auto ld  = [&](int j, int q) { return Ps[q * PS + base + j * STR]; };
+      auto out = [&](int q, T l, T rr) {
+        QLs[q * S::NR + r] = l;
+        QRs[q * S::NR + r] = rr;
+      };
       if (RECON == RECON_PPMC) {
-        hf::ppmc_cell(prim_at(Ps, S::NP, base - 2 * st, b), prim_at(Ps, S::NP, base - st, b), prim_at(Ps, S::NP, base, b),
-                      prim_at(Ps, S::NP, base + st, b), prim_at(Ps, S::NP, base + 2 * st, b), b.ns, b.de, (T)b.gamma, Lf,
-                      Rf);
+        hf::ppmc_cell<T>(ld, out, b.ns, b.de, (T)b.gamma);
       } else {
-        hf::plmc_cell(prim_at(Ps, S::NP, base - st, b), prim_at(Ps, S::NP, base, b), prim_at(Ps, S::NP, base + st, b),
-                      b.ns, b.de, (T)b.gamma, Lf, Rf);
+        hf::plmc_cell<T>(ld, out, b.ns, b.de, (T)b.gamma);
       }
-      prim_put(QLs, S::NR, r, Lf, b);
-      prim_put(QRs, S::NR, r, Rf, b);
     }
     __syncthreads();
   }
@@ -550,9 +628,9 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
     if (a > lim || !pencil_in(c)) continue;
     hf::Prim<T> Lf, Rf;
     if (RECON == RECON_PCM) {
-      int const pl = S::at(a - 1 + H, c, S::LA);
-      Lf = prim_at(Ps, S::NP, pl, b);
-      Rf = prim_at(Ps, S::NP, pl + S::STRIDE, b);
+      int const pl = pidx(a - 1 + H, c);
+      Lf = prim_at(Ps, PS, pl, b);
+      Rf = prim_at(Ps, PS, pl + STR, b);
     } else {
       Lf = prim_at(QLs, S::NR, S::at(a, c, S::LR), b);
       Rf = prim_at(QRs, S::NR, S::at(a + 1, c, S::LR), b);
@@ -565,6 +643,7 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
   }
   __syncthreads();
 
+  if (t >= S::NU) return;  // the threads beyond the updated cells only reconstructed and solved
   int a, c, gx, gy, gz;
   S::split(t, L, a, c);
   cell(a, c, gx, gy, gz);
@@ -603,12 +682,11 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
   }
 }
 
-// Mixed-precision sweeps are latency-bound (FP32 reconstruction chains, FMA pipe under 20% at
-// two blocks per SM): five resident blocks per SM (51 registers, spills to L1) take the 256^3
-// corrector from 6.8 to 4.1 ms (two: 6.8, three: 5.2, four: 4.3, six: 4.07).  The FP64 sweeps
-// are FP64-pipe bound at two.
+// Mixed-precision sweeps are latency-bound (FP32 reconstruction chains): more resident blocks
+// per SM hide more of it (CGB_SWEEP_MINB_F32); the FP64 sweeps are FP64-pipe bound.
 template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
-__global__ void __launch_bounds__(L *WA *WB, sizeof(T) == 4 ? 5 : 2)
+__global__ void __launch_bounds__(sweep_threads(L, WA *WB, RECON), sizeof(T) == 4 ? CGB_SWEEP_MINB_F32
+                                                                                     : CGB_SWEEP_MINB_F64)
     k_fsweep(Box b, const T *__restrict__ W, T *__restrict__ dU, double *__restrict__ U,
              const double *__restrict__ GEp, double *__restrict__ Epre, int *__restrict__ status, double dt,
              const double *__restrict__ dtp)
@@ -617,10 +695,73 @@ __global__ void __launch_bounds__(L *WA *WB, sizeof(T) == 4 ? 5 : 2)
                                                               blockIdx.y, blockIdx.z);
 }
 
+// the same sweep with its P boxes staged by the TMA unit from the tensor map of W½
+template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
+__global__ void __launch_bounds__(sweep_threads(L, WA *WB, RECON), sizeof(T) == 4 ? CGB_SWEEP_MINB_F32
+                                                                                     : CGB_SWEEP_MINB_F64)
+    k_fsweep_tma(Box b, const T *__restrict__ W, T *__restrict__ dU, double *__restrict__ U,
+                 const double *__restrict__ GEp, double *__restrict__ Epre, int *__restrict__ status, double dt,
+                 const double *__restrict__ dtp, const __grid_constant__ CUtensorMap map)
+{
+  fsweep_tile<T, DIR, L, WA, WB, RECON, SOLVER, FIRST, FINAL, true>(b, W, dU, U, GEp, Epre, status, dt, dtp,
+                                                                    blockIdx.x, blockIdx.y, blockIdx.z, &map);
+}
+
+#ifndef CGB_SWEEP_TMA
+#define CGB_SWEEP_TMA 1  // stage the 3D sweeps' tiles with the TMA unit where W½ allows a tensor map
+#endif
+int g_sweep_tma = CGB_SWEEP_TMA;  // run-time switch (cgb_set_tma)
+
+template <typename T, int DIR, int L, int WA, int WB, bool FIRST, bool FINAL>
+cudaError_t launch_sweep_tma(const Box &b, int recon, int solver, const T *Wh, T *dU, double *U, const Scratch &sc,
+                             double dt, const double *dtp, cudaStream_t s, bool &launched)
+{
+  launched = false;
+  if (!g_sweep_tma || (DIR != 0 && WB != 1)) return cudaSuccess;
+  int const rx = b.nx - 2 * b.ng, ry = b.ny - 2 * b.ng, rz = b.nz - 2 * b.ng;
+  int const ra = DIR == 0 ? rx : DIR == 1 ? ry : rz, rb = DIR == 0 ? ry : rx, rc = DIR == 2 ? ry : rz;
+  dim3 grid((ra + L - 1) / L, (rb + WA - 1) / WA, (rc + WB - 1) / WB);
+  void (*k)(Box, const T *, T *, double *, const double *, double *, int *, double, const double *, CUtensorMap);
+  size_t per_q;
+  int bx, by, bz;
+#define CGB_PICK(R)                                                                                        \
+  {                                                                                                        \
+    using TM = typename Sweep<DIR, L, WA, WB, R>::template Tma<T>;                                         \
+    per_q    = TM::PER_Q;                                                                                  \
+    bx       = DIR == 0 ? TM::LAP : TM::WAP;                                                               \
+    by       = DIR == 0 ? WA : DIR == 1 ? Sweep<DIR, L, WA, WB, R>::LA : 1;                                \
+    bz       = DIR == 0 ? WB : DIR == 1 ? 1 : Sweep<DIR, L, WA, WB, R>::LA;                                \
+    k = (solver == SOLVER_ROE) ? k_fsweep_tma<T, DIR, L, WA, WB, R, SOLVER_ROE, FIRST, FINAL>               \
+                               : k_fsweep_tma<T, DIR, L, WA, WB, R, SOLVER_HLLC, FIRST, FINAL>;             \
+  }
+  if (recon == RECON_PPMC) {
+    CGB_PICK(RECON_PPMC)
+  } else if (recon == RECON_PLMC) {
+    CGB_PICK(RECON_PLMC)
+  } else {
+    CGB_PICK(RECON_PCM)
+  }
+#undef CGB_PICK
+  CUtensorMap map;
+  if (!tma_encode_4d(&map, Wh, (int)sizeof(T), b.nx, b.ny, b.nz, nslot(b), bx, by, bz)) return cudaSuccess;
+  size_t const sm = sizeof(T) * (size_t)nslot(b) * per_q;
+  cudaError_t e   = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+  if (e != cudaSuccess) return e;
+  k<<<grid, sweep_threads(L, WA * WB, recon), sm, s>>>(b, Wh, dU, U, sc.GEp, sc.Epre, sc.status, dt, dtp, map);
+  launched = true;
+  return cudaGetLastError();
+}
+
 template <typename T, int DIR, int L, int WA, int WB, bool FIRST, bool FINAL>
 cudaError_t launch_sweep(const Box &b, int recon, int solver, const T *Wh, T *dU, double *U, const Scratch &sc,
                          double dt, const double *dtp, cudaStream_t s)
 {
+  if (!(b.ny == 1 && b.nz == 1)) {
+    bool launched = false;
+    cudaError_t const e =
+        launch_sweep_tma<T, DIR, L, WA, WB, FIRST, FINAL>(b, recon, solver, Wh, dU, U, sc, dt, dtp, s, launched);
+    if (e != cudaSuccess || launched) return e;
+  }
   // real cells along the sweep (ra) and across it (rb: the WA axis, rc: the WB axis)
   bool const one_d = (b.ny == 1 && b.nz == 1);
   int const rx = b.nx - 2 * b.ng, ry = one_d ? 1 : b.ny - 2 * b.ng, rz = one_d ? 1 : b.nz - 2 * b.ng;
@@ -645,7 +786,7 @@ cudaError_t launch_sweep(const Box &b, int recon, int solver, const T *Wh, T *dU
   size_t const sm = sizeof(T) * (size_t)nslot(b) * per_q;
   cudaError_t e   = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k<<<grid, L * WA * WB, sm, s>>>(b, Wh, dU, U, sc.GEp, sc.Epre, sc.status, dt, dtp);
+  k<<<grid, sweep_threads(L, WA * WB, recon), sm, s>>>(b, Wh, dU, U, sc.GEp, sc.Epre, sc.status, dt, dtp);
   return cudaGetLastError();
 }
 
@@ -910,7 +1051,9 @@ __global__ void __launch_bounds__(PTX *PTY *PTZ, sizeof(T) == 4 ? 4 : 2)
 }
 
 template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
-__global__ void __launch_bounds__(L *WA *WB, sizeof(T) == 4 ? 5 : 2) kb_sweep(const __grid_constant__ BatchChunk C)
+__global__ void __launch_bounds__(sweep_threads(L, WA *WB, RECON), sizeof(T) == 4 ? CGB_SWEEP_MINB_F32
+                                                                                     : CGB_SWEEP_MINB_F64)
+    kb_sweep(const __grid_constant__ BatchChunk C)
 {
   int const kind    = BK_SWX + DIR;
   int const tile    = blockIdx.x;
@@ -979,7 +1122,7 @@ cudaError_t launch_batch_sweep(const BatchChunk &C, int recon, int solver, int n
   size_t const sm = sizeof(T) * (size_t)nsl * per_q;
   cudaError_t e   = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
-  k<<<C.total[BK_SWX + DIR], L * WA * WB, sm, s>>>(C);
+  k<<<C.total[BK_SWX + DIR], sweep_threads(L, WA * WB, recon), sm, s>>>(C);
   return cudaGetLastError();
 }
 
@@ -1041,6 +1184,9 @@ cudaError_t batch_chunk_step(const BatchChunk &C, int recon, int solver, int mix
                : launch_core<double>(C, recon, solver, nsl, U_floor, temp_floor, s);
 }
 
+
+void set_sweep_tma(int enable) { g_sweep_tma = enable ? 1 : 0; }
+int sweep_tma() { return g_sweep_tma; }
 
 // bytes of W scratch the fast paths need: primitives of Uⁿ and of U½ (8 bytes covers both types)
 size_t fast_scratch_bytes(const Box &b) { return 2 * (size_t)nslot(b) * (size_t)b.n * sizeof(double); }

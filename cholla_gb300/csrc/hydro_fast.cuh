@@ -258,43 +258,49 @@ __device__ __forceinline__ void ppmc_char(const T (&d)[5], const T (&vn)[5], con
 // differences across the stencil still exceed 32 sound speeds (cold or near-vacuum gas) the
 // projected variables' +-d dv/(2cs) terms would cancel away most FP32 digits, so that cell's
 // characteristic part is evaluated in FP64 from the same FP32 inputs.
-template <typename T>
-__device__ __forceinline__ void ppmc_cell(const Prim<T> &cm2, const Prim<T> &cm1, const Prim<T> &c, const Prim<T> &cp1,
-                                          const Prim<T> &cp2, int ns, int de, T gamma, Prim<T> &L, Prim<T> &R)
+// Streamed: ld(j, s) returns slot s (0 d, 1 vn, 2 vt1, 3 vt2, 4 p, 5 GasEnergy, 6.. scalars) of
+// the stencil cell j (-2 .. 2) and st(s, L, R) takes the cell's high-face (L) and low-face (R)
+// values of slot s, one variable at a time, so that no more than one variable's stencil is live.
+template <typename T, typename LD, typename ST>
+__device__ __forceinline__ void ppmc_cell(LD ld, ST st, int ns, int de, T gamma)
 {
-  T const d[5] = {cm2.d, cm1.d, c.d, cp1.d, cp2.d};
-  T const v[5] = {cm2.vn, cm1.vn, c.vn, cp1.vn, cp2.vn};
-  T const p[5] = {cm2.p, cm1.p, c.p, cp1.p, cp2.p};
-  if constexpr (std::is_same<T, float>::value) {
-    float const cs = sqrtT(gamma * c.p * rcp(c.d));
-    float const dv = fmax(fmax(fabs(cm2.vn - c.vn), fabs(cm1.vn - c.vn)), fmax(fabs(cp1.vn - c.vn), fabs(cp2.vn - c.vn)));
-    if (kWideFallback && !(dv <= 32.0f * cs)) {
-      double const dw[5] = {d[0], d[1], d[2], d[3], d[4]};
-      double const vw[5] = {v[0], v[1], v[2], v[3], v[4]};
-      double const pw[5] = {p[0], p[1], p[2], p[3], p[4]};
-      double Ld, Lvn, Lp, Rd, Rvn, Rp;
-      ppmc_char<double>(dw, vw, pw, (double)gamma, 0.0, Ld, Lvn, Lp, Rd, Rvn, Rp);
-      L.d = (float)Ld, L.vn = (float)Lvn, L.p = (float)Lp, R.d = (float)Rd, R.vn = (float)Rvn, R.p = (float)Rp;
-    } else {
-      ppmc_char<float>(d, v, p, gamma, c.vn, L.d, L.vn, L.p, R.d, R.vn, R.p);
-    }
-  } else {
-    ppmc_char<T>(d, v, p, gamma, T(0), L.d, L.vn, L.p, R.d, R.vn, R.p);
-  }
-  ppm1(cm2.vt1, cm1.vt1, c.vt1, cp1.vt1, cp2.vt1, L.vt1, R.vt1);
-  ppm1(cm2.vt2, cm1.vt2, c.vt2, cp1.vt2, cp2.vt2, L.vt2, R.vt2);
-  L.ge = R.ge = T(0);
-  if (de) ppm1(cm2.ge, cm1.ge, c.ge, cp1.ge, cp2.ge, L.ge, R.ge);
-#pragma unroll
-  for (int k = 0; k < NS_MAX; k++) {
-    L.sc[k] = R.sc[k] = T(0);
-    if (k < ns) ppm1(cm2.sc[k], cm1.sc[k], c.sc[k], cp1.sc[k], cp2.sc[k], L.sc[k], R.sc[k]);
-  }
   T const tiny = T(TINY);
-  R.d = max_pos(R.d, tiny);
-  L.d = max_pos(L.d, tiny);
-  R.p = max_pos(R.p, tiny);
-  L.p = max_pos(L.p, tiny);
+  {
+    T const d[5] = {ld(-2, 0), ld(-1, 0), ld(0, 0), ld(1, 0), ld(2, 0)};
+    T const v[5] = {ld(-2, 1), ld(-1, 1), ld(0, 1), ld(1, 1), ld(2, 1)};
+    T const p[5] = {ld(-2, 4), ld(-1, 4), ld(0, 4), ld(1, 4), ld(2, 4)};
+    T Ld, Lvn, Lp, Rd, Rvn, Rp;
+    if constexpr (std::is_same<T, float>::value) {
+      float const cs = sqrtT(gamma * p[2] * rcp(d[2]));
+      float const dv = fmax(fmax(fabs(v[0] - v[2]), fabs(v[1] - v[2])), fmax(fabs(v[3] - v[2]), fabs(v[4] - v[2])));
+      if (kWideFallback && !(dv <= 32.0f * cs)) {
+        double const dw[5] = {d[0], d[1], d[2], d[3], d[4]};
+        double const vw[5] = {v[0], v[1], v[2], v[3], v[4]};
+        double const pw[5] = {p[0], p[1], p[2], p[3], p[4]};
+        double a, b, c, e, f, g;
+        ppmc_char<double>(dw, vw, pw, (double)gamma, 0.0, a, b, c, e, f, g);
+        Ld = (float)a, Lvn = (float)b, Lp = (float)c, Rd = (float)e, Rvn = (float)f, Rp = (float)g;
+      } else {
+        ppmc_char<float>(d, v, p, gamma, v[2], Ld, Lvn, Lp, Rd, Rvn, Rp);
+      }
+    } else {
+      ppmc_char<T>(d, v, p, gamma, T(0), Ld, Lvn, Lp, Rd, Rvn, Rp);
+    }
+    st(0, max_pos(Ld, tiny), max_pos(Rd, tiny));
+    st(1, Lvn, Rvn);
+    st(4, max_pos(Lp, tiny), max_pos(Rp, tiny));
+  }
+  auto plain = [&](int s) {
+    T L, R;
+    ppm1(ld(-2, s), ld(-1, s), ld(0, s), ld(1, s), ld(2, s), L, R);
+    st(s, L, R);
+  };
+  plain(2);
+  plain(3);
+  if (de) plain(5);
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++)
+    if (k < ns) plain(6 + k);
 }
 
 template <typename T>
@@ -343,64 +349,56 @@ __device__ __forceinline__ void plmc_char(const T (&d)[3], const T (&vn)[3], con
 
 // PLMC_cuda for one cell (VL, no characteristic tracing).  In FP32 a cell whose normal-velocity
 // differences exceed 32 sound speeds takes its characteristic part in FP64 (see ppmc_cell).
-template <typename T>
-__device__ __forceinline__ void plmc_cell(const Prim<T> &cm, const Prim<T> &c, const Prim<T> &cp, int ns, int de,
-                                          T gamma, Prim<T> &L, Prim<T> &R)
+// Streamed like ppmc_cell: ld(j, s) for the stencil cells j = -1 .. 1, st(s, L, R) per variable.
+template <typename T, typename LD, typename ST>
+__device__ __forceinline__ void plmc_cell(LD ld, ST st, int ns, int de, T gamma)
 {
-  T const d[3] = {cm.d, c.d, cp.d}, v[3] = {cm.vn, c.vn, cp.vn}, p[3] = {cm.p, c.p, cp.p};
-  T hd, hn, hp;
-  if constexpr (std::is_same<T, float>::value) {
-    float const cs = sqrtT(gamma * c.p * rcp(c.d));
-    if (kWideFallback && !(fmax(fabs(c.vn - cm.vn), fabs(cp.vn - c.vn)) <= 32.0f * cs)) {
-      double const dw[3] = {d[0], d[1], d[2]}, vw[3] = {v[0], v[1], v[2]}, pw[3] = {p[0], p[1], p[2]};
-      double a, b, e;
-      plmc_char<double>(dw, vw, pw, (double)gamma, a, b, e);
-      hd = (float)a, hn = (float)b, hp = (float)e;
-    } else {
-      plmc_char<float>(d, v, p, gamma, hd, hn, hp);
-    }
-  } else {
-    plmc_char<T>(d, v, p, gamma, hd, hn, hp);
-  }
-  T const dL1 = c.vt1 - cm.vt1, dR1 = cp.vt1 - c.vt1, dC1 = T(0.5) * (cp.vt1 - cm.vt1);
-  T const dL2 = c.vt2 - cm.vt2, dR2 = cp.vt2 - c.vt2, dC2 = T(0.5) * (cp.vt2 - cm.vt2);
-  T const m2 = plm_mono(dL1, dR1, dC1, plm_vl(dL1, dR1)), m3 = plm_mono(dL2, dR2, dC2, plm_vl(dL2, dR2));
-  L.d = c.d + hd, R.d = c.d - hd;
-  L.vn = c.vn + hn, R.vn = c.vn - hn;
-  L.vt1 = c.vt1 + T(0.5) * m2, R.vt1 = c.vt1 - T(0.5) * m2;
-  L.vt2 = c.vt2 + T(0.5) * m3, R.vt2 = c.vt2 - T(0.5) * m3;
-  L.p = c.p + hp, R.p = c.p - hp;
+  // each interface value within the range of its two cells (Plm_Limit_Interfaces)
   auto lim = [](T &l, T &r, T vm, T vi, T vp) {
     r = fmin(fmax(vi, vm), fmax(fmin(vi, vm), r));
     l = fmin(fmax(vi, vp), fmax(fmin(vi, vp), l));
   };
-  lim(L.d, R.d, cm.d, c.d, cp.d);
-  lim(L.vn, R.vn, cm.vn, c.vn, cp.vn);
-  lim(L.vt1, R.vt1, cm.vt1, c.vt1, cp.vt1);
-  lim(L.vt2, R.vt2, cm.vt2, c.vt2, cp.vt2);
-  lim(L.p, R.p, cm.p, c.p, cp.p);
-  L.ge = R.ge = T(0);
-  if (de) {
-    T const dL = c.ge - cm.ge, dR = cp.ge - c.ge;
-    T const h  = T(0.5) * plm_mono(dL, dR, T(0.5) * (cp.ge - cm.ge), plm_vl(dL, dR));
-    L.ge = c.ge + h, R.ge = c.ge - h;
-    lim(L.ge, R.ge, cm.ge, c.ge, cp.ge);
-  }
-#pragma unroll
-  for (int k = 0; k < NS_MAX; k++) {
-    L.sc[k] = R.sc[k] = T(0);
-    if (k < ns) {
-      T const dL = c.sc[k] - cm.sc[k], dR = cp.sc[k] - c.sc[k];
-      T const h  = T(0.5) * plm_mono(dL, dR, T(0.5) * (cp.sc[k] - cm.sc[k]), plm_vl(dL, dR));
-      L.sc[k] = c.sc[k] + h, R.sc[k] = c.sc[k] - h;
-      lim(L.sc[k], R.sc[k], cm.sc[k], c.sc[k], cp.sc[k]);
-    }
-  }
   T const tiny = T(TINY);
-  R.d = max_pos(R.d, tiny);
-  L.d = max_pos(L.d, tiny);
-  R.p = max_pos(R.p, tiny);
-  L.p = max_pos(L.p, tiny);
+  {
+    T const d[3] = {ld(-1, 0), ld(0, 0), ld(1, 0)}, v[3] = {ld(-1, 1), ld(0, 1), ld(1, 1)};
+    T const p[3] = {ld(-1, 4), ld(0, 4), ld(1, 4)};
+    T hd, hn, hp;
+    if constexpr (std::is_same<T, float>::value) {
+      float const cs = sqrtT(gamma * p[1] * rcp(d[1]));
+      if (kWideFallback && !(fmax(fabs(v[1] - v[0]), fabs(v[2] - v[1])) <= 32.0f * cs)) {
+        double const dw[3] = {d[0], d[1], d[2]}, vw[3] = {v[0], v[1], v[2]}, pw[3] = {p[0], p[1], p[2]};
+        double a, b, e;
+        plmc_char<double>(dw, vw, pw, (double)gamma, a, b, e);
+        hd = (float)a, hn = (float)b, hp = (float)e;
+      } else {
+        plmc_char<float>(d, v, p, gamma, hd, hn, hp);
+      }
+    } else {
+      plmc_char<T>(d, v, p, gamma, hd, hn, hp);
+    }
+    T Ld = d[1] + hd, Rd = d[1] - hd, Lv = v[1] + hn, Rv = v[1] - hn, Lp = p[1] + hp, Rp = p[1] - hp;
+    lim(Ld, Rd, d[0], d[1], d[2]);
+    lim(Lv, Rv, v[0], v[1], v[2]);
+    lim(Lp, Rp, p[0], p[1], p[2]);
+    st(0, max_pos(Ld, tiny), max_pos(Rd, tiny));
+    st(1, Lv, Rv);
+    st(4, max_pos(Lp, tiny), max_pos(Rp, tiny));
+  }
+  // monotonised slopes of the other variables, each on its own
+  auto plain = [&](int s) {
+    T const cm = ld(-1, s), c = ld(0, s), cp = ld(1, s);
+    T const dL = c - cm, dR = cp - c;
+    T const h  = T(0.5) * plm_mono(dL, dR, T(0.5) * (cp - cm), plm_vl(dL, dR));
+    T L = c + h, R = c - h;
+    lim(L, R, cm, c, cp);
+    st(s, L, R);
+  };
+  plain(2);
+  plain(3);
+  if (de) plain(5);
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++)
+    if (k < ns) plain(6 + k);
 }
 
 // u / e > eta without the division, keeping the quotient's sign behaviour: the total energy

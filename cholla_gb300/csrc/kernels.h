@@ -26,6 +26,9 @@ cudaError_t cfl_dt(const unsigned long long *dti, double *dt_t, double c_cfl, do
 cudaError_t hydro_fast_step(const Box &b, int recon, int solver, int mixed, double *U, const Scratch &sc, double dt,
                             const double *dt_dev, double U_floor, int temp_floor, int do_dt, cudaStream_t s,
                             cudaEvent_t *marks = nullptr);
+// TMA staging of the fast forms' 3D corrector sweeps (on by default; off: plain loads, same results)
+void set_sweep_tma(int enable);
+int sweep_tma();
 // Average_Cell_Single_Field of the density for real cells left with negative density
 cudaError_t negative_density_average(const Box &b, double *U, cudaStream_t s);
 cudaError_t hydro_calc_dt(const Box &b, const double *U, unsigned long long *dti, cudaStream_t s);

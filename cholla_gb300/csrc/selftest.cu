@@ -6,6 +6,8 @@
 
 #include "../../include/cholla_gb300.h"
 #include "hydro_fast.cuh"
+#include "kernels.h"
+#include "tma.cuh"
 
 namespace
 {
@@ -35,7 +37,37 @@ __global__ void k_fast_math(const double *__restrict__ x, long long n, double *_
     out[3 * n + i] = __dsqrt_rn(a);
   }
 }
+
+// an mbarrier that expects 16 bytes which no copy delivers: every thread's bounded wait runs out
+__global__ void k_tma_timeout(int *__restrict__ status, unsigned limit)
+{
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    cgb::mbar_init(&bar, 1);
+    cgb::fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) cgb::mbar_arrive_expect_tx(&bar, 16);
+  bool const ok = __syncthreads_and(cgb::mbar_wait(&bar, 0, limit));
+  if (!ok && threadIdx.x == 0) atomicOr(status, cgb::STATUS_TMA_TIMEOUT);
+}
 }  // namespace
+
+extern "C" int cgb_selftest_tma_timeout(int *d_status, unsigned limit, void *stream)
+{
+  if (!d_status) return CGB_ERR_ARGS;
+  cudaStream_t const s = (cudaStream_t)stream;
+  k_tma_timeout<<<1, 64, 0, s>>>(d_status, limit);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? CGB_OK : CGB_ERR_CUDA;
+}
+
+extern "C" int cgb_set_tma(int enable)
+{
+  cgb::set_sweep_tma(enable);
+  return CGB_OK;
+}
 
 extern "C" int cgb_selftest_fast_math(const double *d_values, long long n, double *d_out, void *stream)
 {

@@ -37,6 +37,8 @@ extern "C" {
                                     the six neighbours (hydro_cuda.cu:296 Average_Cell_Single_Field) */
 #define CGB_STATUS_NONFINITE   2 /* a real cell holds non-finite density or total energy, or density <= 0
                                     after that repair: the state is unusable */
+#define CGB_STATUS_TIMEOUT     4 /* a bounded device wait (a TMA copy into shared memory) ran out and its
+                                    tile was left undone: the state is unusable (CGB_ERR_TIMEOUT) */
 /* largest |div B| cgb_check_magnetic_divergence accepts (src/mhd/magnetic_divergence.cu:105) */
 #define CGB_MAX_DIVB 1.0e-9
 
@@ -258,6 +260,13 @@ int cgb_selftest_conversions(const double *d_values, long long n, unsigned long 
  * 1/x, [n..2n) CUDA's 1/x, [2n..3n) the fast sqrt(|x|), [3n..4n) CUDA's sqrt(|x|).  Synchronises
  * `stream`. ---- */
 int cgb_selftest_fast_math(const double *d_values, long long n, double *d_out, void *stream);
+/* ---- self-check of the bounded waits: a kernel whose mbarrier expects bytes that no copy delivers
+ * waits `limit` polls, gives up, and writes CGB_STATUS_TIMEOUT to *d_status (device int); no copy is
+ * ever issued, so nothing is left in flight.  Synchronises `stream`. ---- */
+int cgb_selftest_tma_timeout(int *d_status, unsigned limit, void *stream);
+/* ---- TMA staging of the fast forms' 3D corrector sweeps: on (1, default) or off (0: every thread
+ * loads its share of the tile).  The results are the same bit for bit either way. ---- */
+int cgb_set_tma(int enable);
 
 /* ---- fault injection for tests (no counterpart in the reference): the n-th device allocation the
  * library makes from now on (1 = the next; 0 = off) reports out-of-memory without calling CUDA, so
