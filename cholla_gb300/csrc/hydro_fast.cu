@@ -516,7 +516,11 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
   if (dtp) dt = *dtp;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int const ns_ = nslot(b);
-  T *Ps  = reinterpret_cast<T *>(smem_raw);
+  // a TMA tile copy writes to a 128-byte-aligned shared address: the P slots start at the first
+  // 128-byte boundary of the dynamic shared memory (its launch adds 128 bytes for this), and every
+  // slot spans whole 128 bytes (Tma::NPS)
+  unsigned const pad = TMA ? (128u - (smem_u32(smem_raw) & 127u)) & 127u : 0u;
+  T *Ps  = reinterpret_cast<T *>(smem_raw + pad);
   T *QLs = Ps + ns_ * PS;
   T *QRs = QLs + ns_ * S::NR;
   T *Fs  = RECON == RECON_PCM ? QLs : Ps;
@@ -559,13 +563,23 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
     // give those positions exactly what the plain load gives them; positions past the array (a
     // partial tile) read zeros and feed only faces the tile skips.
     __shared__ uint64_t bar;
+    __shared__ int aligned;
     int const xs = DIR == 0 ? a0 + ng - H : ca0 + ng;  // first needed x
     off          = xs % TM::E;
     if (t == 0) {
-      mbar_init(&bar, 1);
-      fence_mbar_init();
+      // self-check before any copy: destinations on 128 bytes, the box's x on 16 bytes, the
+      // mbarrier on 8; a failure skips the tile and records it instead of issuing the copy
+      aligned = (smem_u32(Ps) & 127u) == 0 && ((PS * (int)sizeof(T)) & 127) == 0 && (xs - off) % TM::E == 0 &&
+                (smem_u32(&bar) & 7u) == 0;
+      if (aligned) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+      } else {
+        atomicOr(status, STATUS_TMA_TIMEOUT);
+      }
     }
     __syncthreads();
+    if (!aligned) return;  // block-uniform
     if (t == 0) {
       mbar_arrive_expect_tx(&bar, (unsigned)(ns_ * TM::NPT * (int)sizeof(T)));
       int const xa = xs - off, s0 = a0 + ng - H;
@@ -744,7 +758,7 @@ cudaError_t launch_sweep_tma(const Box &b, int recon, int solver, const T *Wh, T
 #undef CGB_PICK
   CUtensorMap map;
   if (!tma_encode_4d(&map, Wh, (int)sizeof(T), b.nx, b.ny, b.nz, nslot(b), bx, by, bz)) return cudaSuccess;
-  size_t const sm = sizeof(T) * (size_t)nslot(b) * per_q;
+  size_t const sm = sizeof(T) * (size_t)nslot(b) * per_q + 128;  // + room to start P on 128 bytes
   cudaError_t e   = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
   if (e != cudaSuccess) return e;
   k<<<grid, sweep_threads(L, WA * WB, recon), sm, s>>>(b, Wh, dU, U, sc.GEp, sc.Epre, sc.status, dt, dtp, map);
