@@ -571,36 +571,29 @@ def run_mhd(args, dev, stream, torch):
 
 
 def run_serving(args, torch):
-    """Batched serving workload: a seeded Poisson stream of independent 3D hydro jobs (sizes
+    """Batched serving workload: seeded Poisson streams of independent 3D hydro jobs (sizes
     uniform over 32^3 .. 128^3, Sedov-like blast or randomly oriented Sod tube, PPMC + HLLC mixed
     precision, 100 steps each, admitted by free device memory) served by the continuous-batching
     server and by per-request launches of the single-box step (kernel by kernel, and from a CUDA
-    graph per request), each mode warmed up first, at every arrival rate.  Latency = arrival to
-    completion of the last step.  Then every job of a further stream against its exact FP64 twin."""
+    graph per request), each mode warmed up first, at every arrival rate: one seed below 100 req/s,
+    every seed of --serve-seeds from 100 req/s up.  Latency = arrival to completion of the last step.
+    Then every job of a further stream against its exact FP64 twin."""
     from cholla_gb300 import accuracy, serve
 
-    modes = serve.MODES
     rates = [float(r) for r in args.serve_rates.split(",") if r]
     counts = [int(c) for c in args.serve_count.split(",") if c]
     counts = (counts * len(rates))[:len(rates)] if len(counts) < len(rates) else counts
-    out = {"workload": "Poisson stream of 3D hydro jobs, n in {32,48,64,96,128}, blast or Sod tube, "
-                       "PPMC + HLLC mixed, 100 steps, seed 17",
+    seeds = [int(x) for x in args.serve_seeds.split(",") if x]
+    out = {"workload": "Poisson streams of 3D hydro jobs, n in {32,48,64,96,128}, blast or Sod tube, "
+                       "PPMC + HLLC mixed, 100 steps",
            "batched_server": "first come first served up to 3 Mi cells per step (rest held); batch schedule "
-                             "(chains, solo threshold) autotuned on the size mix at start-up (see each row's 'tuned')",
+                             "(chains, solo threshold, sweep tile set) autotuned on the size mix at start-up",
+           "ratios": "vs_<mode>: [min, mean, max] over seeds of batched/per-request throughput and of "
+                     "per-request/batched p99 (above 1: the batched server is ahead)",
            "rates": {}}
-    for mode in modes:  # module loading, first captures and allocator growth outside the timed runs
-        serve.serve(torch, serve.make_requests(rate=2000.0, count=6, seed=99, steps=5), mode=mode)
     for rate, count in zip(rates, counts):
-        row = {"requests": count}
-        for mode in modes:
-            reqs = serve.make_requests(rate=rate, count=count, seed=17, steps=100)
-            row[mode] = serve.serve(torch, reqs, mode=mode)
-        b = row["batched"]
-        for base in modes[1:]:
-            p = row[base]
-            row[f"vs_{base}"] = {"throughput_ratio": b["cell_updates_per_s"] / p["cell_updates_per_s"],
-                                 "p99_ratio": p["p99_ms"] / b["p99_ms"], "p50_ratio": p["p50_ms"] / b["p50_ms"]}
-        out["rates"][f"{rate:g}"] = row
+        row = serve.sweep(torch, [rate], [count], seeds if rate >= 100 else seeds[:1])
+        out["rates"].update(row)
     if not args.no_accuracy and args.serve_twins > 0:
         reqs = serve.make_requests(rate=100.0, count=args.serve_twins, seed=23, steps=100)
         twins = accuracy.serving_twins(torch, reqs)
@@ -640,6 +633,7 @@ def main():
     ap.add_argument("--no-512", action="store_true")
     ap.add_argument("--serve-rates", default="10,30,100,2000")
     ap.add_argument("--serve-count", default="60,100,200,200", help="requests per rate (one per rate, or one for all)")
+    ap.add_argument("--serve-seeds", default="17,18,19", help="request-stream seeds of the rates from 100 req/s up")
     ap.add_argument("--serve-twins", type=int, default=12, help="served jobs checked against their FP64 twins")
     ap.add_argument("--precision", choices=["fp64_fast", "fp64", "mixed"], default="fp64_fast")
     args = ap.parse_args()

@@ -74,6 +74,10 @@ class Batch:
         """Spread the jobs over at least `chains` parallel chains of launches (same results)."""
         _check(L.lib().cgb_batch_set_chains(self._h, int(chains)))
 
+    def set_tiles(self, tile_set: int) -> None:
+        """Sweep tile set (0 or 1) of the jobs that share the batched kernels."""
+        _check(L.lib().cgb_batch_set_tiles(self._h, int(tile_set)))
+
     def __len__(self) -> int:
         return int(L.lib().cgb_batch_n_jobs(self._h))
 

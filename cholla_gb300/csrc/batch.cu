@@ -36,6 +36,7 @@ struct cgb_batch {
   int next_id = 1;
   bool dirty  = true;                   // the job set changed since the graph was captured
   int chains  = 1;                      // at least this many chains of launches
+  int tiles   = 0;                      // sweep tile set of the shared-kernel chains (0 / 1)
   long long solo_cells = 2LL << 20;     // jobs of at least this many padded cells run solo
   cudaGraphExec_t graph = nullptr;
   std::vector<cudaStream_t> aux;        // capture streams of chunks 1, 2, ...
@@ -69,7 +70,7 @@ double job_work(const cgb::BatchJob &J) { return (double)J.b.n; }
 // The batch's jobs as chunks of at most BATCH_CHUNK jobs with per-kind tile offsets, at least
 // `chains` of them (each chunk is a chain of launches; the chains run side by side), filled
 // largest job first into the chunk with the least work so far.
-std::vector<cgb::BatchChunk> build_chunks(const std::vector<cgb::BatchJob> &jobs, int chains)
+std::vector<cgb::BatchChunk> build_chunks(const std::vector<cgb::BatchJob> &jobs, int chains, int set)
 {
   size_t const nj = jobs.size();
   size_t nc       = (nj + cgb::BATCH_CHUNK - 1) / cgb::BATCH_CHUNK;
@@ -92,7 +93,7 @@ std::vector<cgb::BatchChunk> build_chunks(const std::vector<cgb::BatchJob> &jobs
   for (auto &C : out) {
     for (int j = 0; j < C.njobs; j++) {
       int tiles[cgb::BK_NUM];
-      cgb::batch_tiles(C.jobs[j].b, tiles);
+      cgb::batch_tiles(C.jobs[j].b, tiles, set);
       for (int k = 0; k < cgb::BK_NUM; k++) {
         C.off[k][j] = C.total[k];
         C.total[k] += tiles[k];
@@ -114,7 +115,7 @@ cudaError_t make_plan(cgb_batch &bt)
     else
       shared.push_back(bt.jobs[i]);
   }
-  bt.plan.chunks  = build_chunks(shared, bt.chains);
+  bt.plan.chunks  = build_chunks(shared, bt.chains, bt.tiles);
   size_t const nc = bt.plan.chunks.size() + bt.plan.solo.size();
   cudaError_t e;
   while (bt.aux.size() + 1 < nc) {
@@ -147,7 +148,7 @@ cudaError_t launch_plan(cgb_batch &bt)
     cudaStream_t const st = c ? bt.aux[c - 1] : bt.stream;
     if (c < chunks.size()) {
       e = cgb::batch_chunk_step(chunks[c], s.reconstruction, s.riemann_solver, mixed, s.dual_energy, s.n_scalars,
-                                bt.c_cfl, s.U_floor, s.temperature_floor, st);
+                                bt.c_cfl, s.U_floor, s.temperature_floor, bt.tiles, st);
       continue;
     }
     size_t const i         = bt.plan.solo[c - chunks.size()];
@@ -158,7 +159,7 @@ cudaError_t launch_plan(cgb_batch &bt)
     if (e == cudaSuccess) e = cgb::cfl_dt(J.dti, J.dt_t, bt.c_cfl, J.t_end, st);
     if (e == cudaSuccess)
       e = cgb::hydro_step(J.b, s.reconstruction, s.riemann_solver, s.precision, J.U, sc, 0.0, J.dt_t, s.U_floor,
-                          s.temperature_floor, 1, st);
+                          s.temperature_floor, 1, st, nullptr, 1);
   }
   for (size_t c = 1; c < nc && e == cudaSuccess; c++) {
     e = cudaEventRecord(bt.ev[c], bt.aux[c - 1]);
@@ -353,6 +354,17 @@ int cgb_batch_set_chains(cgb_batch *bt, int chains)
   std::lock_guard<std::mutex> lk(bt->mu);
   if (chains != bt->chains) bt->dirty = true;
   bt->chains = chains;
+  return CGB_OK;
+}
+
+// Sweep tile set of the shared-kernel chains: 0 or 1 (two compiled shapes; they agree to the
+// rounding of the compiler's contractions).  Takes effect at the next step.
+int cgb_batch_set_tiles(cgb_batch *bt, int set)
+{
+  if (!bt || set < 0 || set > 1) return bfail(CGB_ERR_ARGS, "tile set must be 0 or 1");
+  std::lock_guard<std::mutex> lk(bt->mu);
+  if (set != bt->tiles) bt->dirty = true;
+  bt->tiles = set;
   return CGB_OK;
 }
 

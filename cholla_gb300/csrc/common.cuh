@@ -57,6 +57,9 @@ struct Box {
   // used by the fast / mixed forms only, set on the host by with_inverses(): 1/dx, 1/dy, 1/dz
   // and 1/(gamma - 1), so that no kernel thread divides by them
   double idx, idy, idz, ig1;
+  // binary32 roundings of gamma, gamma - 1 and 1/(gamma - 1) for the mixed form, also set by
+  // with_inverses() (a per-thread conversion would issue on the FP64 pipe)
+  float gf, gm1f, ig1f;
   __host__ __device__ long long id(int x, int y, int z) const
   {
     return (long long)x + (long long)y * nx + (long long)z * nx * ny;
@@ -70,6 +73,7 @@ struct Box {
 inline Box with_inverses(Box b)
 {
   b.idx = 1.0 / b.dx, b.idy = 1.0 / b.dy, b.idz = 1.0 / b.dz, b.ig1 = 1.0 / (b.gamma - 1.0);
+  b.gf = (float)b.gamma, b.gm1f = (float)(b.gamma - 1.0), b.ig1f = (float)b.ig1;
   return b;
 }
 

@@ -118,7 +118,7 @@ cudaError_t one_step(cgb_box *bx, double *U, double c_cfl, cudaStream_t st, bool
     return cudaSuccess;
   }
   return cgb::hydro_step(bx->b, bx->scheme.reconstruction, bx->scheme.riemann_solver, bx->scheme.precision, U, bx->s,
-                         0.0, bx->dt_t, bx->scheme.U_floor, bx->scheme.temperature_floor, 1, st, m);
+                         0.0, bx->dt_t, bx->scheme.U_floor, bx->scheme.temperature_floor, 1, st, m, 1);
 }
 }  // namespace
 
@@ -173,7 +173,7 @@ int cgb_box_create(cgb_box **out, int nx, int ny, int nz, int n_ghost, double dx
     if (cgb::dev_malloc(p, bytes) != cudaSuccess) return false;
     return cudaMemset(*p, 0, bytes) == cudaSuccess;
   };
-  bool ok = al((void **)&bx->s.dti, 8) && al((void **)&bx->s.status, 4) && al((void **)&bx->dt_t, 16);
+  bool ok = al((void **)&bx->s.dti, 8) && al((void **)&bx->s.status, 8) && al((void **)&bx->dt_t, 16);
   if (ok && b.mhd) {
     ok = al((void **)&bx->s.mhd, cgb::mhd_scratch_doubles(b) * 8);
   } else if (ok) {
@@ -261,6 +261,10 @@ int cgb_box_advance(cgb_box *bx, double *d_conserved, int n_steps, double c_cfl,
       return box_fail(bx, CGB_ERR_CUDA, cudaGetErrorString(e));
     bx->dti_valid = true;
   }
+  // the state may have changed since the last call: the first step forms every cell's primitives
+  // (status[1], the fast forms' carried-primitives flag, set again by each step's finalize)
+  if (!bx->b.mhd && (e = cudaMemsetAsync(bx->s.status + 1, 0, sizeof(int), st)) != cudaSuccess)
+    return box_fail(bx, CGB_ERR_CUDA, cudaGetErrorString(e));
   bool const graph_ok = bx->use_graph && !bx->timing && st != nullptr;
   if (graph_ok && (!bx->graph || bx->graph_U != d_conserved || bx->graph_stream != st || bx->graph_cfl != c_cfl)) {
     if (bx->graph) cudaGraphExecDestroy(bx->graph), bx->graph = nullptr;

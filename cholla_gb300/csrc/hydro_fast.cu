@@ -26,28 +26,49 @@ namespace
 
 constexpr int NSLOT = 6 + NS_MAX;
 // tiles of the 3D step (single boxes and batches alike): predictor 8 x 8 x 4 cells; corrector
-// sweeps along x over 64 x 2 x 2 cells, along y and z over 32 x 8 x 1
+// sweeps along x over 30 x 2 x 4 cells, along y and z over 30 x 8 x 1.  Measured at 256^3 on
+// GB300 (PPMC + HLLC, dual energy): against 64 x 2 x 2 / 32 x 8 x 1 the sweeps take 1 % less in
+// the mixed form and 2 % less in the fast FP64 form; 6 / 3 resident blocks target 1 % less than
+// 5 / 2 in the mixed form.
 constexpr int PTX = 8, PTY = 8, PTZ = 4;
 // (compile-time tunables: the tile shapes and the resident blocks per SM the sweeps' register
 // budget targets, FP32 and FP64 compute)
 #ifndef CGB_SWEEP_XL  // x sweep: cells per pencil, pencils along y and along z
-#define CGB_SWEEP_XL 64
+#define CGB_SWEEP_XL 30
 #define CGB_SWEEP_XA 2
-#define CGB_SWEEP_XB 2
+#define CGB_SWEEP_XB 4
 #endif
 #ifndef CGB_SWEEP_YL  // y and z sweeps: cells per pencil, x-adjacent pencils, pencils across
-#define CGB_SWEEP_YL 32
+#define CGB_SWEEP_YL 30
 #define CGB_SWEEP_YA 8
 #define CGB_SWEEP_YB 1
 #endif
 #ifndef CGB_SWEEP_MINB_F32
-#define CGB_SWEEP_MINB_F32 5
+#define CGB_SWEEP_MINB_F32 6
 #endif
 #ifndef CGB_SWEEP_MINB_F64
-#define CGB_SWEEP_MINB_F64 2
+#define CGB_SWEEP_MINB_F64 3
 #endif
 constexpr int SXL = CGB_SWEEP_XL, SXA = CGB_SWEEP_XA, SXB = CGB_SWEEP_XB;
 constexpr int SYL = CGB_SWEEP_YL, SYA = CGB_SWEEP_YA, SYB = CGB_SWEEP_YB;
+// the batches' second tile set (cgb_batch_set_tiles; the autotuner picks between the two)
+#ifndef CGB_SWEEP_ALT_XL
+#define CGB_SWEEP_ALT_XL 64
+#define CGB_SWEEP_ALT_XA 2
+#define CGB_SWEEP_ALT_XB 2
+#define CGB_SWEEP_ALT_YL 32
+#define CGB_SWEEP_ALT_YA 8
+#define CGB_SWEEP_ALT_YB 1
+#endif
+template <int SET>
+struct TileSet {
+  static constexpr int XL = SXL, XA = SXA, XB = SXB, YL = SYL, YA = SYA, YB = SYB;
+};
+template <>
+struct TileSet<1> {
+  static constexpr int XL = CGB_SWEEP_ALT_XL, XA = CGB_SWEEP_ALT_XA, XB = CGB_SWEEP_ALT_XB;
+  static constexpr int YL = CGB_SWEEP_ALT_YL, YA = CGB_SWEEP_ALT_YA, YB = CGB_SWEEP_ALT_YB;
+};
 
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
@@ -125,43 +146,86 @@ __device__ __forceinline__ double widen(T a)
     return a;
 }
 
+// gamma and 1/(gamma - 1) in the compute type
+template <typename T>
+__device__ __forceinline__ T gamma_of(const Box &b)
+{
+  if constexpr (std::is_same<T, float>::value)
+    return b.gf;
+  else
+    return b.gamma;
+}
+template <typename T>
+__device__ __forceinline__ T ig1_of(const Box &b)
+{
+  if constexpr (std::is_same<T, float>::value)
+    return b.ig1f;
+  else
+    return b.ig1;
+}
+
+// 1/d of a cell: an FP32 estimate refined by one Newton step in the mixed form (whose primitives
+// are rounded to FP32) and by two (hf::rcp) in the fast FP64 form
+template <bool MIX>
+__device__ __forceinline__ double inv_density(double d)
+{
+  if constexpr (MIX)
+    return rcp_nr<1>(d);
+  else
+    return hf::rcp(d);
+}
+// kinetic energy (mx^2 + my^2 + mz^2) / 2d from 1/d, every FP64 operation explicitly rounded:
+// the primitives of a cell then come out bit for bit alike in every kernel that forms them (the
+// finalize writes the next step's primitives of the real cells, k_fprims those of the ghosts)
+__device__ __forceinline__ double kinetic(double mx, double my, double mz, double id)
+{
+  return __dmul_rn(__dmul_rn(0.5, __fma_rn(mz, mz, __fma_rn(my, my, __dmul_rn(mx, mx)))), id);
+}
+
 // Primitives (T) of one cell from its FP64 conserved state q (slots), pressure recovered in
 // FP64 (Load_Data, reconstruction.h:139-212; Get_Pressure_From_DE, hydro_utilities.h:136-151).
 template <typename T>
 __device__ __forceinline__ void prim_from_cons(const double *q, const Box &b, T *w)
 {
-  bool const mix  = std::is_same<T, float>::value;
-  double const d  = q[0];
-  double const id = mix ? rcp_nr<1>(d) : 1.0 / d;
-  double const ke  = 0.5 * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) * id;
-  double const eth = q[4] - ke;
-  double p;
+  constexpr bool mix = std::is_same<T, float>::value;
+  double const d     = q[0];
+  double const id    = inv_density<mix>(d);
+  double const eth   = __dsub_rn(q[4], kinetic(q[1], q[2], q[3], id));
+  double p           = eth;
   if (b.de) {
-    p    = hf::ratio_gt(eth, q[4], ETA_1) ? eth : q[5];
-    p    = hf::max_pos(p * (b.gamma - 1.0), TINY);
-    w[5] = narrow<T>(q[5] * id);
+    p = hf::ratio_gt(eth, q[4], ETA_1) ? eth : q[5];
+    if constexpr (mix) {  // the thermal energy is selected in FP64; its scalings need not be
+      w[5] = hf::to_f32(q[5]) * hf::to_f32(id);
+    } else {
+      p    = hf::max_pos(__dmul_rn(p, __dsub_rn(b.gamma, 1.0)), TINY);
+      w[5] = __dmul_rn(q[5], id);
+    }
   } else {
-    p    = hf::max_pos((b.gamma - 1.0) * eth, TINY);
+    if constexpr (!mix) p = hf::max_pos(__dmul_rn(__dsub_rn(b.gamma, 1.0), eth), TINY);
     w[5] = T(0);
   }
   w[0] = narrow<T>(d);
-  if (mix) {
+  if constexpr (mix) {
     float const idf = hf::to_f32(id);
-    w[1] = (T)(hf::to_f32(q[1]) * idf);
-    w[2] = (T)(hf::to_f32(q[2]) * idf);
-    w[3] = (T)(hf::to_f32(q[3]) * idf);
+    w[1] = hf::to_f32(q[1]) * idf;
+    w[2] = hf::to_f32(q[2]) * idf;
+    w[3] = hf::to_f32(q[3]) * idf;
+    // p holds the FP64 thermal energy (the DE selection or E - ke): the pressure in FP32, floored
+    // at TINY (a NaN stays NaN, for the bad-cell checks downstream)
+    float const pf = hf::to_f32(p) * b.gm1f;
+    w[4]           = pf < (float)TINY ? (float)TINY : pf;
   } else {
-    w[1] = (T)(q[1] * id);
-    w[2] = (T)(q[2] * id);
-    w[3] = (T)(q[3] * id);
+    w[1] = __dmul_rn(q[1], id);
+    w[2] = __dmul_rn(q[2], id);
+    w[3] = __dmul_rn(q[3], id);
+    w[4] = p;
   }
-  w[4] = narrow<T>(p);
 #pragma unroll
   for (int k = 0; k < NS_MAX; k++) {
-    if constexpr (std::is_same<T, float>::value)
+    if constexpr (mix)
       w[6 + k] = (k < b.ns) ? hf::to_f32(q[6 + k]) * hf::to_f32(id) : 0.f;
     else
-      w[6 + k] = (k < b.ns) ? q[6 + k] * id : 0.0;
+      w[6 + k] = (k < b.ns) ? __dmul_rn(q[6 + k], id) : 0.0;
   }
 }
 
@@ -184,9 +248,9 @@ template <typename T, int SOLVER>
 __device__ __forceinline__ void riemann(const hf::Prim<T> &L, const hf::Prim<T> &R, T *f, const Box &b)
 {
   if (SOLVER == SOLVER_ROE) {
-    hf::roe(L, R, f, b.ns, b.de, (T)b.gamma, (T)b.ig1);
+    hf::roe(L, R, f, b.ns, b.de, gamma_of<T>(b), ig1_of<T>(b));
   } else {
-    hf::hllc(L, R, f, b.ns, b.de, (T)b.gamma, (T)b.ig1);
+    hf::hllc(L, R, f, b.ns, b.de, gamma_of<T>(b), ig1_of<T>(b));
   }
 }
 
@@ -206,11 +270,43 @@ __device__ __forceinline__ void fprims_cell(const Box &b, const double *__restri
     if (live(s, b)) Wn[(long long)s * n + i] = w[s];
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) k_fprims(Box b, const double *__restrict__ U, T *__restrict__ Wn)
+// real cells of a 3D box and the i-th of its ghost cells (0 <= i < n - real): the two z slabs,
+// then the two y slabs between them, then the two x slabs of the remaining rows
+__host__ __device__ __forceinline__ long long real_count(const Box &b)
 {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < b.n; i += (long long)gridDim.x * blockDim.x)
-    fprims_cell(b, U, Wn, i);
+  return (long long)(b.nx - 2 * b.ng) * (b.ny - 2 * b.ng) * (b.nz - 2 * b.ng);
+}
+__device__ __forceinline__ long long ghost_cell(const Box &b, long long i)
+{
+  long long const nx = b.nx, ny = b.ny, ng = b.ng, plane = nx * ny;
+  if (i < 2 * ng * plane) {
+    long long z = i / plane;
+    if (z >= ng) z += b.nz - 2 * ng;
+    return z * plane + (i - (i / plane) * plane);
+  }
+  i -= 2 * ng * plane;
+  long long const band = 2 * ng * nx;  // the two y slabs of one z plane
+  if (i < band * (b.nz - 2 * ng)) {
+    long long const z = i / band, r = i - z * band, yy = r / nx;
+    long long const y = yy >= ng ? yy + ny - 2 * ng : yy;
+    return (r - yy * nx) + nx * y + plane * (z + ng);
+  }
+  i -= band * (b.nz - 2 * ng);
+  long long const row = i / (2 * ng), xx = i - row * 2 * ng, my = ny - 2 * ng;
+  long long const x = xx >= ng ? xx + nx - 2 * ng : xx;
+  return x + nx * (row % my + ng) + plane * (row / my + ng);
+}
+
+// carry != null and *carry != 0: the previous step's finalize wrote the primitives of the real
+// cells (3D boxes stepped by the engine or a batch), so only the ghost shell is formed here
+template <typename T>
+__global__ void __launch_bounds__(256) k_fprims(Box b, const double *__restrict__ U, T *__restrict__ Wn,
+                                                const int *__restrict__ carry)
+{
+  bool const ghosts     = carry && *carry;
+  long long const count = ghosts ? b.n - real_count(b) : b.n;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (long long)gridDim.x * blockDim.x)
+    fprims_cell(b, U, Wn, ghosts ? ghost_cell(b, i) : i);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -239,6 +335,11 @@ __device__ __forceinline__ void fpred_tile(const Box &b, const double *__restric
   int const y0 = HY ? 1 + by_ * TY : 0;
   int const z0 = HZ ? 1 + bz_ * TZ : 0;
   long long const n = b.n;
+  // dt/2dx, dt/2dy, dt/2dz: formed once per block (FP64 products)
+  __shared__ T sdt[3];
+  if (threadIdx.x == 0) {
+    sdt[0] = narrow<T>(0.5 * dt * b.idx), sdt[1] = narrow<T>(0.5 * dt * b.idy), sdt[2] = narrow<T>(0.5 * dt * b.idz);
+  }
 
   for (int t = threadIdx.x; t < NB; t += NT) {
     int const bx = t % BX, by = (t / BX) % BY, bz = t / (BX * BY);
@@ -293,7 +394,7 @@ __device__ __forceinline__ void fpred_tile(const Box &b, const double *__restric
   int const fx = i + (TX + 1) * (j + TY * k);
   int const fy = i + TX * (j + (TY + 1) * k);
   int const fz = i + TX * (j + TY * k);
-  T const dtodx = narrow<T>(0.5 * dt * b.idx), dtody = narrow<T>(0.5 * dt * b.idy), dtodz = narrow<T>(0.5 * dt * b.idz);
+  T const dtodx = sdt[0], dtody = sdt[1], dtodz = sdt[2];
   double q[NSLOT];
 #pragma unroll
   for (int s = 0; s < NSLOT; s++) {
@@ -565,7 +666,7 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
     __shared__ uint64_t bar;
     __shared__ int aligned;
     int const xs = DIR == 0 ? a0 + ng - H : ca0 + ng;  // first needed x
-    off          = xs % TM::E;
+    off          = (xs % TM::E + TM::E) % TM::E;  // 0 .. E - 1 (the box may start left of x = 0)
     if (t == 0) {
       // self-check before any copy: destinations on 128 bytes, the box's x on 16 bytes, the
       // mbarrier on 8; a failure skips the tile and records it instead of issuing the copy
@@ -629,9 +730,9 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
         QRs[q * S::NR + r] = rr;
       };
       if (RECON == RECON_PPMC) {
-        hf::ppmc_cell<T>(ld, out, b.ns, b.de, (T)b.gamma);
+        hf::ppmc_cell<T>(ld, out, b.ns, b.de, gamma_of<T>(b));
       } else {
-        hf::plmc_cell<T>(ld, out, b.ns, b.de, (T)b.gamma);
+        hf::plmc_cell<T>(ld, out, b.ns, b.de, gamma_of<T>(b));
       }
     }
     __syncthreads();
@@ -827,17 +928,25 @@ __device__ __forceinline__ void block_max_to(double v, unsigned long long *dst)
 // MIX: the mixed-precision form takes the reciprocal of the density with one Newton step and each
 // cell's crossing rate in FP32; the total-minus-kinetic energy, the selection, sync, floor and the
 // maximum over the box stay FP64 (maxima compare bit patterns on the integer pipe).
+// Wout != null: also write the primitives of the updated real cells (the next step's Wⁿ, in the
+// compute type) and set status[1], which tells the next step's k_fprims to form only the ghosts'.
 template <bool MIX>
 __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict__ U, const double *__restrict__ Epre,
                                                 unsigned long long *__restrict__ dti, int *__restrict__ status,
                                                 double U_floor, int temp_floor, int do_dt, double idx, double idy,
-                                                double idz, long long blk)
+                                                double idz, long long blk, void *__restrict__ Wout = nullptr)
 {
   int const ng = b.ng;
   bool const one_d = (b.ny == 1 && b.nz == 1);
   int const rx = b.nx - 2 * ng, ry = one_d ? 1 : b.ny - 2 * ng, rz = one_d ? 1 : b.nz - 2 * ng;
   long long const nreal = (long long)rx * ry * rz;
   long long const r     = blk * blockDim.x + threadIdx.x;
+  // binary32 1/dx, 1/dy, 1/dz of the mixed form's crossing rate, converted once per block
+  __shared__ float sid[3];
+  if (MIX && do_dt) {
+    if (threadIdx.x == 0) sid[0] = (float)idx, sid[1] = (float)idy, sid[2] = (float)idz;
+    __syncthreads();
+  }
   double m = -1.0;
   if (r < nreal) {
     int x, y, z;
@@ -846,10 +955,11 @@ __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict
     y = one_d ? 0 : y + ng;
     z = one_d ? 0 : z + ng;
     long long const n = b.n, id = b.id(x, y, z);
-    double const d = U[id], d_inv = MIX ? rcp_nr<1>(d) : hf::rcp(d);
+    double const d = U[id], d_inv = inv_density<MIX>(d);
     double const mx = U[n + id], my = U[2 * n + id], mz = U[3 * n + id];
-    double const ke = 0.5 * (mx * mx + my * my + mz * mz) * d_inv;
+    double const ke = kinetic(mx, my, mz, d_inv);
     double E        = U[4 * n + id];
+    double ge       = 0.0;  // GasEnergy after the sync and the floor (dual energy)
     if (b.de) {
       long long const fge = (long long)(b.nf - 1) * n;
       // the maxima run on the integer pipe (max_ord), which the FP64-bound finalize leaves idle
@@ -869,6 +979,7 @@ __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict
       double Ui   = (hf::ratio_gt(ut, E, ETA_1) || hf::ratio_gt(ut, Emax, ETA_2)) ? ut : U[fge + id];
       Ui          = hf::max_pos(Ui, TINY);
       U[fge + id] = Ui;
+      ge          = Ui;
       E           = ke + Ui;  // Sync_Energies_3D (hydro_cuda.cu:1070-1099)
       U[4 * n + id] = E;
     }
@@ -877,25 +988,37 @@ __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict
         E             = ke + d * U_floor;
         U[4 * n + id] = E;
       }
-      if (b.de) {
-        long long const fge = (long long)(b.nf - 1) * n;
-        if (U[fge + id] < U_floor * d) U[fge + id] = d * U_floor;
+      if (b.de && ge < U_floor * d) {
+        ge                                 = d * U_floor;
+        U[(long long)(b.nf - 1) * n + id] = ge;
       }
     }
     if (bad_cell(d, E)) atomicOr(status, STATUS_NONFINITE);
+    if (Wout) {  // the next step's primitives, from the values just stored
+      using T = typename std::conditional<MIX, float, double>::type;
+      double q[NSLOT];
+      q[0] = d, q[1] = mx, q[2] = my, q[3] = mz, q[4] = E, q[5] = ge;
+#pragma unroll
+      for (int k = 0; k < NS_MAX; k++) q[6 + k] = k < b.ns ? U[(long long)(5 + k) * n + id] : 0.0;
+      T w[NSLOT];
+      prim_from_cons<T>(q, b, w);
+#pragma unroll
+      for (int sl = 0; sl < NSLOT; sl++)
+        if (live(sl, b)) static_cast<T *>(Wout)[(long long)sl * n + id] = w[sl];
+    }
     if (do_dt && MIX) {
       // the crossing rate of the cell in FP32 from its FP64 thermal energy (E - ke); the maximum
       // over the box, which sets dt, stays FP64
-      float const idf = hf::to_f32(d_inv), g = (float)b.gamma;
+      float const idf = hf::to_f32(d_inv), g = b.gf;
       float const c2  = g * (g - 1.0f) * hf::to_f32(E - ke) * idf;
       float const cs  = sqrtf(fmaxf(c2, 0.0f));
       float const ax  = fabsf(hf::to_f32(mx) * idf) + cs;
       float mf;
       if (one_d) {
-        mf = ax * (float)idx;
+        mf = ax * sid[0];
       } else {
         float const ay = fabsf(hf::to_f32(my) * idf) + cs, az = fabsf(hf::to_f32(mz) * idf) + cs;
-        mf = fmaxf(fmaxf(ax * (float)idx, ay * (float)idy), az * (float)idz);
+        mf = fmaxf(fmaxf(ax * sid[0], ay * sid[1]), az * sid[2]);
       }
       m = hf::to_f64(mf);
     } else if (do_dt) {  // hydroInverseCrossingTime (hydro_cuda.cu:404-419)
@@ -910,6 +1033,7 @@ __device__ __forceinline__ void ffinalize_block(const Box &b, double *__restrict
       }
     }
   }
+  if (Wout && blk == 0 && threadIdx.x == 0) status[1] = 1;
   if (do_dt) block_max_to(m, dti);
 }
 
@@ -917,9 +1041,9 @@ template <bool MIX>
 __global__ void __launch_bounds__(256) k_ffinalize(Box b, double *__restrict__ U, const double *__restrict__ Epre,
                                                    unsigned long long *__restrict__ dti, int *__restrict__ status,
                                                    double U_floor, int temp_floor, int do_dt, double idx, double idy,
-                                                   double idz)
+                                                   double idz, void *__restrict__ Wout)
 {
-  ffinalize_block<MIX>(b, U, Epre, dti, status, U_floor, temp_floor, do_dt, idx, idy, idz, blockIdx.x);
+  ffinalize_block<MIX>(b, U, Epre, dti, status, U_floor, temp_floor, do_dt, idx, idy, idz, blockIdx.x, Wout);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -934,7 +1058,7 @@ size_t fpred_smem(const Box &b)
 
 template <typename T, int TX, int TY, int TZ>
 cudaError_t launch_fast(const Box &b, int recon, int solver, double *U, const Scratch &sc, double dt,
-                        const double *dtp, cudaStream_t s, cudaEvent_t *marks)
+                        const double *dtp, cudaStream_t s, cudaEvent_t *marks, const int *carry)
 {
   T *Wn = (T *)sc.W;
   T *Wh = half_prims(Wn, b);
@@ -943,7 +1067,7 @@ cudaError_t launch_fast(const Box &b, int recon, int solver, double *U, const Sc
   {
     long long blocks = (b.n + 255) / 256;
     if (blocks > 152 * 16) blocks = 152 * 16;
-    k_fprims<T><<<(unsigned)blocks, 256, 0, s>>>(b, U, Wn);
+    k_fprims<T><<<(unsigned)blocks, 256, 0, s>>>(b, U, Wn, carry);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
   {
@@ -1043,7 +1167,11 @@ __global__ void __launch_bounds__(256) kb_prims(const __grid_constant__ BatchChu
   int const j        = find_job(C, BK_CELLS, tile);
   BatchJob const &J  = C.jobs[j];
   long long const id = (long long)(tile - C.off[BK_CELLS][j]) * 256 + threadIdx.x;
-  if (id < J.b.n) fprims_cell<T>(J.b, J.U, (T *)J.W, id);
+  if (J.status[1]) {  // the real cells' primitives are current: the ghost shell only
+    if (id < J.b.n - real_count(J.b)) fprims_cell<T>(J.b, J.U, (T *)J.W, ghost_cell(J.b, id));
+  } else if (id < J.b.n) {
+    fprims_cell<T>(J.b, J.U, (T *)J.W, id);
+  }
 }
 
 // FP32 tiles: four resident blocks per SM (64 registers), the single-box predictor's occupancy
@@ -1113,7 +1241,7 @@ __global__ void __launch_bounds__(256)
   int const j       = find_job(C, BK_REAL, tile);
   BatchJob const &J = C.jobs[j];
   ffinalize_block<MIX>(J.b, J.U, J.Epre, J.dti, J.status, U_floor, temp_floor, do_dt, J.b.idx, J.b.idy, J.b.idz,
-                       tile - C.off[BK_REAL][j]);
+                       tile - C.off[BK_REAL][j], MIX ? J.W : nullptr);
 }
 
 template <typename T, int DIR, int L, int WA, int WB, bool FIRST, bool FINAL>
@@ -1141,7 +1269,7 @@ cudaError_t launch_batch_sweep(const BatchChunk &C, int recon, int solver, int n
 }
 
 // primitives, predictor, x/y/z sweeps, negative-density repair and finalize of one chunk
-template <typename T>
+template <typename T, int SET>
 cudaError_t launch_core(const BatchChunk &C, int recon, int solver, int nsl, double U_floor, int temp_floor,
                         cudaStream_t s)
 {
@@ -1157,9 +1285,13 @@ cudaError_t launch_core(const BatchChunk &C, int recon, int solver, int nsl, dou
     k<<<C.total[BK_PRED], PTX * PTY * PTZ, sm, s>>>(C);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }
-  if ((e = launch_batch_sweep<T, 0, SXL, SXA, SXB, true, false>(C, recon, solver, nsl, s)) != cudaSuccess) return e;
-  if ((e = launch_batch_sweep<T, 1, SYL, SYA, SYB, false, false>(C, recon, solver, nsl, s)) != cudaSuccess) return e;
-  if ((e = launch_batch_sweep<T, 2, SYL, SYA, SYB, false, true>(C, recon, solver, nsl, s)) != cudaSuccess) return e;
+  using TS = TileSet<SET>;
+  if ((e = launch_batch_sweep<T, 0, TS::XL, TS::XA, TS::XB, true, false>(C, recon, solver, nsl, s)) != cudaSuccess)
+    return e;
+  if ((e = launch_batch_sweep<T, 1, TS::YL, TS::YA, TS::YB, false, false>(C, recon, solver, nsl, s)) != cudaSuccess)
+    return e;
+  if ((e = launch_batch_sweep<T, 2, TS::YL, TS::YA, TS::YB, false, true>(C, recon, solver, nsl, s)) != cudaSuccess)
+    return e;
   kb_negavg<<<C.total[BK_REAL], 256, 0, s>>>(C);
   constexpr bool MIX = std::is_same<T, float>::value;
   kb_final<MIX><<<C.total[BK_REAL], 256, 0, s>>>(C, U_floor, temp_floor, 1);
@@ -1168,25 +1300,35 @@ cudaError_t launch_core(const BatchChunk &C, int recon, int solver, int nsl, dou
 
 }  // namespace
 
-void batch_tiles(const Box &b, int tiles[BK_NUM])
+template <int SET>
+void batch_tiles_set(const Box &b, int tiles[BK_NUM])
 {
+  using TS = TileSet<SET>;
   int a, c, d;
   tiles[BK_CELLS] = (int)((b.n + 255) / 256);
   pred_grid(b, a, c, d);
   tiles[BK_PRED] = a * c * d;
-  sweep_grid<0, SXL, SXA, SXB>(b, a, c, d);
+  sweep_grid<0, TS::XL, TS::XA, TS::XB>(b, a, c, d);
   tiles[BK_SWX] = a * c * d;
-  sweep_grid<1, SYL, SYA, SYB>(b, a, c, d);
+  sweep_grid<1, TS::YL, TS::YA, TS::YB>(b, a, c, d);
   tiles[BK_SWY] = a * c * d;
-  sweep_grid<2, SYL, SYA, SYB>(b, a, c, d);
+  sweep_grid<2, TS::YL, TS::YA, TS::YB>(b, a, c, d);
   tiles[BK_SWZ] = a * c * d;
   tiles[BK_REAL] = (int)((real_cells(b) + 255) / 256);
+}
+
+void batch_tiles(const Box &b, int tiles[BK_NUM], int set)
+{
+  if (set == 1)
+    batch_tiles_set<1>(b, tiles);
+  else
+    batch_tiles_set<0>(b, tiles);
 }
 
 size_t batch_w_bytes(const Box &b) { return 2 * (size_t)nslot(b) * (size_t)b.n * sizeof(double); }
 
 cudaError_t batch_chunk_step(const BatchChunk &C, int recon, int solver, int mixed, int de, int ns, double c_cfl,
-                             double U_floor, int temp_floor, cudaStream_t s)
+                             double U_floor, int temp_floor, int set, cudaStream_t s)
 {
   if (C.njobs <= 0) return cudaSuccess;
   int const nsl = ns > 0 ? 6 + ns : 5 + (de ? 1 : 0);
@@ -1194,8 +1336,11 @@ cudaError_t batch_chunk_step(const BatchChunk &C, int recon, int solver, int mix
   kb_cfl<<<1, BATCH_CHUNK, 0, s>>>(C, c_cfl);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return mixed ? launch_core<float>(C, recon, solver, nsl, U_floor, temp_floor, s)
-               : launch_core<double>(C, recon, solver, nsl, U_floor, temp_floor, s);
+  if (set == 1)
+    return mixed ? launch_core<float, 1>(C, recon, solver, nsl, U_floor, temp_floor, s)
+                 : launch_core<double, 1>(C, recon, solver, nsl, U_floor, temp_floor, s);
+  return mixed ? launch_core<float, 0>(C, recon, solver, nsl, U_floor, temp_floor, s)
+               : launch_core<double, 0>(C, recon, solver, nsl, U_floor, temp_floor, s);
 }
 
 
@@ -1207,18 +1352,25 @@ size_t fast_scratch_bytes(const Box &b) { return 2 * (size_t)nslot(b) * (size_t)
 
 cudaError_t hydro_fast_step(const Box &box, int recon, int solver, int mixed, double *U, const Scratch &sc, double dt,
                             const double *dt_dev, double U_floor, int temp_floor, int do_dt, cudaStream_t s,
-                            cudaEvent_t *marks)
+                            cudaEvent_t *marks, int carry)
 {
   Box const b = with_inverses(box);
   bool const one_d = (b.ny == 1 && b.nz == 1);
   if (b.nz < 2 * b.ng + 1) temp_floor = 0;  // the reference's temperature floor acts in 3D only
+  // Primitives carried from the finalize to the next step: mixed form, 3D boxes whose finalize runs.
+  // The finalize already holds 1/d and the kinetic energy, so the carry saves the U loads and the
+  // FP64 work of a separate primitives pass over the real cells (256^3 mixed: 5.73 -> 5.63 ms per
+  // step).  In the fast FP64 form the primitives' own FP64 products dominate, and moving them into
+  // the FP64-bound finalize measured no gain (107.9 -> 108.5 ms), so that form keeps k_fprims.
+  carry = carry && mixed && !one_d && b.nz >= 2 * b.ng + 1 && (b.de || temp_floor || do_dt);
+  int const *cf = carry ? sc.status + 1 : nullptr;
   cudaError_t e;
   if (mixed) {
-    e = one_d ? launch_fast<float, 128, 1, 1>(b, recon, solver, U, sc, dt, dt_dev, s, marks)
-              : launch_fast<float, PTX, PTY, PTZ>(b, recon, solver, U, sc, dt, dt_dev, s, marks);
+    e = one_d ? launch_fast<float, 128, 1, 1>(b, recon, solver, U, sc, dt, dt_dev, s, marks, nullptr)
+              : launch_fast<float, PTX, PTY, PTZ>(b, recon, solver, U, sc, dt, dt_dev, s, marks, cf);
   } else {
-    e = one_d ? launch_fast<double, 128, 1, 1>(b, recon, solver, U, sc, dt, dt_dev, s, marks)
-              : launch_fast<double, PTX, PTY, PTZ>(b, recon, solver, U, sc, dt, dt_dev, s, marks);
+    e = one_d ? launch_fast<double, 128, 1, 1>(b, recon, solver, U, sc, dt, dt_dev, s, marks, nullptr)
+              : launch_fast<double, PTX, PTY, PTZ>(b, recon, solver, U, sc, dt, dt_dev, s, marks, cf);
   }
   if (e != cudaSuccess) return e;
   if (b.floor_on && !one_d) {
@@ -1230,12 +1382,13 @@ cudaError_t hydro_fast_step(const Box &box, int recon, int solver, int mixed, do
     long long const nreal =
         (long long)(b.nx - 2 * ng) * (one_d ? 1 : b.ny - 2 * ng) * (one_d ? 1 : b.nz - 2 * ng);
     unsigned const grid = (unsigned)((nreal + 255) / 256);
+    void *const wout = carry ? sc.W : nullptr;
     if (mixed) {
       k_ffinalize<true><<<grid, 256, 0, s>>>(b, U, sc.Epre, sc.dti, sc.status, U_floor, temp_floor, do_dt, b.idx,
-                                              b.idy, b.idz);
+                                              b.idy, b.idz, wout);
     } else {
       k_ffinalize<false><<<grid, 256, 0, s>>>(b, U, sc.Epre, sc.dti, sc.status, U_floor, temp_floor, do_dt, b.idx,
-                                               b.idy, b.idz);
+                                               b.idy, b.idz, wout);
     }
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
   }

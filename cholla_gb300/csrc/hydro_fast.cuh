@@ -409,6 +409,15 @@ __device__ __forceinline__ bool ratio_gt(T u, T e, T eta)
 {
   return e > T(0) ? u > eta * e : (e < T(0) ? u < eta * e : u > T(0));
 }
+// The FP64 form with every comparison on the integer pipe (ordered bit patterns, see ordered_key):
+// one FP64 multiply instead of a multiply and up to four FP64 compares.  It differs from the
+// quotient test only when u is +0 and eta * e is -0 (e negative and below 2e-305 in size).
+__device__ __forceinline__ bool ratio_gt(double u, double e, double eta)
+{
+  if (is_pos(e)) return ordered_key(u) > ordered_key(eta * e);
+  if (is_neg(e)) return ordered_key(u) < ordered_key(eta * e);
+  return is_pos(u);
+}
 
 // Pressure a Riemann solver uses for an interface state: with dual energy the reference
 // recomputes it from the interface's conserved E and GasEnergy with Get_Pressure_From_DE

@@ -23,9 +23,13 @@ cudaError_t hydro_2d_step(const Box &b, int recon, int solver, double *U, const 
 cudaError_t cfl_dt(const unsigned long long *dti, double *dt_t, double c_cfl, double t_end, cudaStream_t s);
 // Fast FP64 (mixed = 0) or mixed-precision (mixed = 1) step (hydro_fast.cu).  sc.W holds the
 // primitives of Uⁿ and of U½: 2 * (nf + 1) fields of 8 bytes cover both element types.
+// carry != 0 (3D boxes a caller steps repeatedly on the same state: the engine, batches): the
+// finalize also writes the next step's primitives of the real cells and sets sc.status[1], after
+// which a step forms only the ghost cells' primitives; the caller clears sc.status[1] whenever
+// the state may have changed outside the steps.
 cudaError_t hydro_fast_step(const Box &b, int recon, int solver, int mixed, double *U, const Scratch &sc, double dt,
                             const double *dt_dev, double U_floor, int temp_floor, int do_dt, cudaStream_t s,
-                            cudaEvent_t *marks = nullptr);
+                            cudaEvent_t *marks = nullptr, int carry = 0);
 // TMA staging of the fast forms' 3D corrector sweeps (on by default; off: plain loads, same results)
 void set_sweep_tma(int enable);
 int sweep_tma();
@@ -72,7 +76,7 @@ struct BatchJob {
   int flags[6];              // boundary flags (ghost fill)
 };
 // tile kinds: cells of the padded box (256 per tile), predictor tiles (8 x 8 x 4), corrector
-// sweep tiles (x: 64 x 2 x 2, y and z: 32 x 8 x 1), real cells (256 per tile)
+// sweep tiles of the chunk's tile set, real cells (256 per tile)
 enum BatchKind { BK_CELLS = 0, BK_PRED, BK_SWX, BK_SWY, BK_SWZ, BK_REAL, BK_NUM };
 struct BatchChunk {
   int njobs;
@@ -80,26 +84,27 @@ struct BatchChunk {
   int off[BK_NUM][BATCH_CHUNK + 1];   // first tile of each job per kind
   BatchJob jobs[BATCH_CHUNK];
 };
-static_assert(sizeof(BatchChunk) <= 4000, "a chunk must fit the 4 KB kernel parameter space");
-// tiles of a box per kind (the tiling the batched kernels decode)
-void batch_tiles(const Box &b, int tiles[BK_NUM]);
+// kernel parameters may take up to 32 764 bytes (CUDA 12.1 and later, Volta and later GPUs)
+static_assert(sizeof(BatchChunk) <= 32764, "a chunk must fit the kernel parameter space");
+// tiles of a box per kind (the tiling the batched kernels decode) with sweep tile set `set` (0 / 1)
+void batch_tiles(const Box &b, int tiles[BK_NUM], int set);
 // W bytes a job needs
 size_t batch_w_bytes(const Box &b);
 // Launch one step of every job of chunk C on stream s (all jobs share the scheme): ghost fill,
 // dt = c_cfl / max_dti (clamped to t_end), primitives, predictor, x/y/z sweeps, negative-density
 // repair, finalize with the CFL reduction for the next step; one block per tile.
 cudaError_t batch_chunk_step(const BatchChunk &C, int recon, int solver, int mixed, int de, int ns, double c_cfl,
-                             double U_floor, int temp_floor, cudaStream_t s);
+                             double U_floor, int temp_floor, int set, cudaStream_t s);
 
 // dispatch on the arithmetic: 0 = FP64 in the reference's order, 1 = mixed, 2 = fast FP64
 inline cudaError_t hydro_step(const Box &b, int recon, int solver, int precision, double *U, const Scratch &sc,
                               double dt, const double *dt_dev, double U_floor, int temp_floor, int do_dt,
-                              cudaStream_t s, cudaEvent_t *marks = nullptr)
+                              cudaStream_t s, cudaEvent_t *marks = nullptr, int carry = 0)
 {
   if (precision == 0)
     return hydro_exact_step(b, recon, solver, U, sc, dt, dt_dev, U_floor, temp_floor, do_dt, s, marks);
   return hydro_fast_step(b, recon, solver, precision == 1 ? 1 : 0, U, sc, dt, dt_dev, U_floor, temp_floor,
-                         do_dt, s, marks);
+                         do_dt, s, marks, carry);
 }
 
 // ghost-cell fill of all six faces in one launch (boundaries.cu)

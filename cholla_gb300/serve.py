@@ -212,7 +212,8 @@ class BatchedServer(_Base):
             t = tune_batch(torch, self.scheme, [n for n in SIZES for _ in range(2)])
             self.batch.set_chains(t["chains"])
             self.batch.set_solo_cells(t["solo_cells"])
-            self.extra["tuned"] = {"chains": t["chains"], "solo_cells": t["solo_cells"]}
+            self.batch.set_tiles(t.get("tiles", 0))
+            self.extra["tuned"] = {"chains": t["chains"], "solo_cells": t["solo_cells"], "tiles": t.get("tiles", 0)}
         else:
             self.batch.set_chains(chains or 2)
         self.policy = policy
@@ -346,3 +347,58 @@ def serve(torch, requests: list[Request], mode: str = "batched", **kw) -> dict:
         torch.cuda.synchronize()
         srv.close()
     return rep.summary()
+
+
+def sweep(torch, rates, counts, seeds, modes=MODES, steps: int = 100, **kw) -> dict:
+    """Every mode on the same seeded request streams: for each rate (with its request count) and
+    each seed, one run per mode; per rate the mean over seeds of throughput, p50 and p99 (and each
+    seed's [throughput, p50, p99]), and the batched server's ratios against each per-request mode
+    seed by seed as [min, mean, max] (throughput: batched / per-request; p99: per-request /
+    batched, so above 1 means the batched server is ahead on both)."""
+    out = {}
+    for mode in modes:  # module loading, first captures and allocator growth outside the runs
+        serve(torch, make_requests(rate=2000.0, count=6, seed=99, steps=5), mode=mode, **kw)
+    for rate, count in zip(rates, counts):
+        runs = {m: [] for m in modes}
+        for seed in seeds:
+            for mode in modes:
+                runs[mode].append(serve(torch, make_requests(rate=rate, count=count, seed=seed, steps=steps), mode=mode,
+                                        **kw))
+        row = {"requests": count, "seeds": list(seeds)}
+        for mode in modes:
+            rs = runs[mode]
+            row[mode] = {k: float(np.mean([r[k] for r in rs])) for k in ("cell_updates_per_s", "p50_ms", "p99_ms")}
+            row[mode]["per_seed"] = [[r["cell_updates_per_s"], r["p50_ms"], r["p99_ms"]] for r in rs]
+            if "tuned" in rs[0]:
+                row[mode]["tuned"] = rs[0]["tuned"]
+        for base in modes:
+            if base == "batched":
+                continue
+            tr = [b["cell_updates_per_s"] / p["cell_updates_per_s"] for b, p in zip(runs["batched"], runs[base])]
+            pr = [p["p99_ms"] / b["p99_ms"] for b, p in zip(runs["batched"], runs[base])]
+            row[f"vs_{base}"] = {"throughput_ratio": [min(tr), float(np.mean(tr)), max(tr)],
+                                 "p99_ratio": [min(pr), float(np.mean(pr)), max(pr)]}
+        out[f"{rate:g}"] = row
+    return out
+
+
+def main():
+    import argparse
+    import json
+
+    import torch
+
+    ap = argparse.ArgumentParser(description="serving sweep: batched server against per-request launches")
+    ap.add_argument("--rates", default="100,2000")
+    ap.add_argument("--counts", default="200", help="requests per rate (one per rate, or one for all)")
+    ap.add_argument("--seeds", default="17,18,19")
+    a = ap.parse_args()
+    rates = [float(r) for r in a.rates.split(",")]
+    counts = [int(c) for c in a.counts.split(",")]
+    counts = (counts * len(rates))[:len(rates)] if len(counts) < len(rates) else counts
+    seeds = [int(s) for s in a.seeds.split(",")]
+    print(json.dumps(sweep(torch, rates, counts, seeds)), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,10 +1,13 @@
 """Autotuner of the batch schedule.
 
-A batch step has two run-time schedule choices (`cgb_batch_set_chains`,
-`cgb_batch_set_solo_cells`): how many parallel chains of launches the shared jobs are spread
-over, and from what size a job runs the single-box kernels in a chain of its own.  Both give
-the same results bit for bit; which is fastest depends on the mix of job sizes and on the
-GPU.  `tune_batch` builds a representative batch of the given sizes (seeded blast and shock
+A batch step has three run-time schedule choices (`cgb_batch_set_chains`,
+`cgb_batch_set_solo_cells`, `cgb_batch_set_tiles`): how many parallel chains of launches the
+shared jobs are spread over, from what size a job runs the single-box kernels in a chain of its
+own, and which of the two compiled tile shapes the shared corrector sweeps use (x sweep / y and
+z sweeps: 30 x 2 x 4 / 30 x 8 x 1 cells, or 64 x 2 x 2 / 32 x 8 x 1).  Chains and the solo
+threshold give the same results bit for bit; the two tile shapes are two compiled instantiations
+of the same sweep, in which the compiler contracts a few products differently, so they agree to
+rounding.  Which is fastest depends on the mix of job sizes and on the GPU.  `tune_batch` builds a representative batch of the given sizes (seeded blast and shock
 tube states), times a few steps of every candidate with CUDA events on the batch stream, and
 returns the fastest.  Results are cached per (sizes, scheme) in memory and, when a path is
 given, in a JSON file, so a server tunes once per size mix.
@@ -18,6 +21,7 @@ from pathlib import Path
 
 CHAINS = (1, 2, 4)
 SOLO_CELLS = (1 << 20, 2 << 20, 4 << 20, 1 << 62)  # padded cells; the last: never solo
+TILES = (0, 1)
 
 _cache: dict = {}
 
@@ -28,8 +32,8 @@ def _key(sizes, scheme) -> str:
 
 
 def tune_batch(torch, scheme, sizes, steps: int = 6, warmup: int = 2, cache_path: str | Path | None = None) -> dict:
-    """Fastest (chains, solo_cells) for a batch holding one job per entry of `sizes` (real
-    cells per side).  Returns {"chains", "solo_cells", "ms_per_step", "table"}."""
+    """Fastest (chains, solo_cells, tiles) for a batch holding one job per entry of `sizes` (real
+    cells per side).  Returns {"chains", "solo_cells", "tiles", "ms_per_step", "table"}."""
     key = _key(sizes, scheme)
     if key in _cache:
         return _cache[key]
@@ -47,26 +51,29 @@ def tune_batch(torch, scheme, sizes, steps: int = 6, warmup: int = 2, cache_path
               for i, n in enumerate(sizes)]
     torch.cuda.synchronize()
     table = []
-    for chains in CHAINS:
-        for solo in SOLO_CELLS:
-            bt = Batch(scheme, stream, c_cfl=0.3)
-            bt.set_chains(chains)
-            bt.set_solo_cells(solo)
-            work = [(U.clone(), dx) for U, dx in states]
-            for U, dx in work:
-                bt.add(U, N_GHOST, dx, dx, dx)
-            bt.step(warmup)  # the job set is stable from here: the timed steps replay one graph
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            bt.step(steps)
-            b.record(stream)
-            b.synchronize()
-            table.append({"chains": chains, "solo_cells": solo, "ms_per_step": a.elapsed_time(b) / steps})
-            bt.close()
-            del work
+    for tiles in TILES:
+        for chains in CHAINS:
+            for solo in SOLO_CELLS:
+                bt = Batch(scheme, stream, c_cfl=0.3)
+                bt.set_chains(chains)
+                bt.set_solo_cells(solo)
+                bt.set_tiles(tiles)
+                work = [(U.clone(), dx) for U, dx in states]
+                for U, dx in work:
+                    bt.add(U, N_GHOST, dx, dx, dx)
+                bt.step(warmup)  # the job set is stable from here: the timed steps replay one graph
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                bt.step(steps)
+                b.record(stream)
+                b.synchronize()
+                table.append({"chains": chains, "solo_cells": solo, "tiles": tiles,
+                              "ms_per_step": a.elapsed_time(b) / steps})
+                bt.close()
+                del work
     best = min(table, key=lambda r: r["ms_per_step"])
-    out = {"chains": best["chains"], "solo_cells": best["solo_cells"], "ms_per_step": best["ms_per_step"],
-           "table": table}
+    out = {"chains": best["chains"], "solo_cells": best["solo_cells"], "tiles": best["tiles"],
+           "ms_per_step": best["ms_per_step"], "table": table}
     _cache[key] = out
     if path:
         stored = json.loads(path.read_text()) if path.exists() else {}

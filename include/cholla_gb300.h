@@ -241,6 +241,10 @@ int cgb_batch_set_solo_cells(cgb_batch *batch, long long cells);
 /* Spread the jobs over at least `chains` parallel chains of launches (default 1; a chain holds
  * at most 16 jobs), balanced by cells.  Same results bit for bit; takes effect at the next step. */
 int cgb_batch_set_chains(cgb_batch *batch, int chains);
+/* Sweep tile set (0 or 1) of the jobs that share the batched kernels: two compiled tile shapes of the
+ * corrector sweeps, for the autotuner to pick between per size mix; takes effect at the next step.
+ * The two agree to rounding (the compiler contracts a few products differently in each). */
+int cgb_batch_set_tiles(cgb_batch *batch, int set);
 /* Advance every job by n_steps on the batch stream (no host synchronisation). */
 int cgb_batch_step(cgb_batch *batch, int n_steps);
 /* Time and last dt of one job (synchronises the batch stream).  Returns CGB_ERR_NONFINITE, with t and

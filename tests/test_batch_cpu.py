@@ -48,6 +48,7 @@ def test_batch_calls_on_a_null_handle_fail_cleanly(lib):
     assert lib.cgb_batch_hold(null, 1, 1) == _lib.CGB_ERR_ARGS
     assert lib.cgb_batch_set_chains(null, 2) == _lib.CGB_ERR_ARGS
     assert lib.cgb_batch_set_solo_cells(null, 1 << 20) == _lib.CGB_ERR_ARGS
+    assert lib.cgb_batch_set_tiles(null, 1) == _lib.CGB_ERR_ARGS
     assert lib.cgb_batch_job_time(null, 1, C.byref(t), C.byref(dt)) == _lib.CGB_ERR_ARGS
     assert lib.cgb_batch_n_jobs(null) == -1
     assert lib.cgb_batch_destroy(null) == _lib.CGB_OK

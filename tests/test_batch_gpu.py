@@ -50,12 +50,13 @@ def _alone(cuda, U0, dx, scheme, steps):
     return U.cpu().numpy(), t
 
 
-def _in_batch(cuda, U0, dx, scheme, steps, solo_cells=None):
+def _in_batch(cuda, U0, dx, scheme, steps, solo_cells=None, tiles=0):
     from cholla_gb300.batch import Batch
 
     U = U0.clone()
     st = cuda.cuda.Stream()
     bt = Batch(scheme, st, c_cfl=0.3)
+    bt.set_tiles(tiles)
     if solo_cells is not None:
         bt.set_solo_cells(solo_cells)
     jid = bt.add(U, NG, dx, dx, dx)
@@ -220,8 +221,29 @@ def test_autotuner_picks_a_measured_candidate(cuda):
 
     s = _scheme("mixed")
     r = tune.tune_batch(cuda, s, [16, 24, 32, 40], steps=2, warmup=2)
-    assert len(r["table"]) == len(tune.CHAINS) * len(tune.SOLO_CELLS)
+    assert len(r["table"]) == len(tune.CHAINS) * len(tune.SOLO_CELLS) * len(tune.TILES)
     assert all(row["ms_per_step"] > 0 for row in r["table"])
     best = min(r["table"], key=lambda row: row["ms_per_step"])
-    assert (r["chains"], r["solo_cells"]) == (best["chains"], best["solo_cells"])
+    assert (r["chains"], r["solo_cells"], r["tiles"]) == (best["chains"], best["solo_cells"], best["tiles"])
     assert tune.tune_batch(cuda, s, [40, 32, 24, 16]) is r  # cached per size mix
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64_fast"])
+def test_tile_sets_agree_to_rounding(cuda, precision):
+    """The two compiled sweep tile shapes of the shared kernels (cgb_batch_set_tiles) compute the
+    same step; as for the engine's kernels, the compiler contracts a few products differently in
+    the two instantiations, so after one step a job agrees to rounding (relative L1 per field
+    1e-7 mixed, 1e-15 fast FP64), and each tile set is deterministic on its own.  The sizes leave
+    partial tiles in both shapes (20, 24, 36 real cells against 30- and 64-cell x pencils)."""
+    s = _scheme(precision)
+    rs = real_slice(NG)
+    for n, kind, sd in [(20, "blast", 11), (24, "tube", 12), (36, "blast", 13)]:
+        U, dx = _job_state(cuda, n, kind, sd, s)
+        a, ta = _in_batch(cuda, U, dx, s, 1, tiles=0)
+        b, tb = _in_batch(cuda, U, dx, s, 1, tiles=1)
+        err = _rel_l1(b[rs], a[rs])
+        assert np.all(err <= TOL[precision]), f"{n}^3 {kind}: {err}"
+        assert ta == tb
+        for tiles, ref in ((0, a), (1, b)):
+            again, _ = _in_batch(cuda, U, dx, s, 1, tiles=tiles)
+            assert _same(again[rs], ref[rs]).all()

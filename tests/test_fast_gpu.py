@@ -118,3 +118,39 @@ def test_engine_matches_dropin_sequence_bitwise(cuda):
         assert (a.view(np.int64) == b.view(np.int64)).all(), f"graph={graph}"
         assert t > 0 and dt_last > 0
         box.close()
+
+
+@pytest.mark.parametrize("precision,ns,flags", [("mixed", 0, (1,) * 6), ("fp64_fast", 0, (1,) * 6),
+                                                ("mixed", 1, (2, 3, 1, 1, 3, 2)), ("fp64_fast", 2, (3, 2, 2, 3, 1, 1))])
+def test_engine_carried_primitives_bitwise(cuda, precision, ns, flags):
+    """Within one advance call the mixed form's finalize writes the next step's primitives of the
+    real cells and the next step forms only the ghosts' (the state is the engine's between its
+    steps); every call starts from primitives of all cells.  Six steps in one call equal six
+    one-step calls bit for bit, with passive scalars and reflective / outflow faces, whose ghosts
+    are not copies (the fast FP64 form, which forms all primitives every step, runs the same check)."""
+    from cholla_gb300 import ics
+    from cholla_gb300 import integrator as I
+    from cholla_gb300.engine import Box
+
+    n, ng, gamma = 24, 4, 5 / 3
+    rng = np.random.default_rng(8)
+    U0 = ics.smooth_random_box((n, n, n), ng, rng, dual_energy=True, n_scalars=ns)
+    N = U0.shape[1]
+    dx = 1 / n
+    s = I.Scheme(reconstruction="PPMC", riemann_solver="HLLC", dual_energy=True, n_scalars=ns,
+                 temperature_floor=True, precision=precision)
+    stream = cuda.cuda.Stream()
+    out = []
+    for calls in (1, 6):
+        U = cuda.from_numpy(U0.copy()).cuda()
+        box = Box(N, N, N, ng, dx, dx, dx, s, flags=flags)
+        box.use_graph(True)
+        for _ in range(calls):
+            box.advance(U, 6 // calls, 0.3, stream)
+        stream.synchronize()
+        out.append((U.cpu().numpy(), box.time()))
+        box.close()
+    (a, ta), (b, tb) = out
+    rs = real_slice(ng)
+    assert np.array_equal(a[rs].view(np.int64), b[rs].view(np.int64))
+    assert ta == tb
