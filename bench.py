@@ -607,8 +607,9 @@ def run_serving(args, torch):
 
 
 def load_traffic(n, precision):
-    """DRAM bytes per corrector launch from the committed ncu summary (profiles/traffic.json),
-    scaled from the captured box to n^3 real cells (traffic grows with the number of cells)."""
+    """DRAM bytes of the corrector stage (its three sweep launches) in one step, from the committed ncu
+    summary (profiles/traffic.json, bytes per real cell at 160^3), scaled to n^3 real cells (traffic
+    grows with the number of cells)."""
     f = ROOT / "profiles" / "traffic.json"
     try:
         d = json.loads(f.read_text())

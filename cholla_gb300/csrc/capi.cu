@@ -28,7 +28,13 @@ struct ScratchSlot {
   bool live = false;
 };
 ScratchSlot g_slot;
-unsigned long long *g_dti_host = nullptr;  // pinned result of the CFL reduction
+// Reductions the drop-in calls return (max inverse dt, max |div B|) come back through one word of
+// mapped pinned memory that a one-thread kernel writes, not through a device-to-host copy: a copy
+// waits on the copy engine behind every large transfer queued before it, so a caller that overlaps
+// its state uploads and downloads with the steps would stall for them at every dt readback.
+unsigned long long *g_word_host = nullptr;           // mapped pinned word (host address)
+unsigned long long *g_word_dev  = nullptr;           // its device address
+__global__ void k_put_word(const unsigned long long *__restrict__ src, unsigned long long *dst) { *dst = *src; }
 
 int fail(int code, const std::string &msg)
 {
@@ -38,6 +44,29 @@ int fail(int code, const std::string &msg)
 int cuda_fail(cudaError_t e, const char *where)
 {
   return fail(CGB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// the word at d_src, read on the host after the drop-in stream reaches it
+int read_word(const unsigned long long *d_src, unsigned long long *out, const char *where)
+{
+  if (!g_word_host) {
+    if (cudaHostAlloc((void **)&g_word_host, sizeof(unsigned long long), cudaHostAllocMapped | cudaHostAllocPortable) !=
+        cudaSuccess) {
+      g_word_host = nullptr;
+      return fail(CGB_ERR_NOMEM, "pinned result word");
+    }
+    if (cudaHostGetDevicePointer((void **)&g_word_dev, g_word_host, 0) != cudaSuccess) {
+      cudaFreeHost(g_word_host);
+      g_word_host = nullptr;
+      return fail(CGB_ERR_CUDA, "mapped result word");
+    }
+  }
+  k_put_word<<<1, 1, 0, g_stream>>>(d_src, g_word_dev);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g_stream);
+  if (e != cudaSuccess) return cuda_fail(e, where);
+  *out = *(volatile unsigned long long *)g_word_host;
+  return CGB_OK;
 }
 
 void free_slot(ScratchSlot &sl)
@@ -83,7 +112,7 @@ int ensure_slot(int nx, int ny, int nz, int nf, int mhd)
   bool ok = alloc((void **)&s.dti, sizeof(unsigned long long)) && alloc((void **)&s.status, sizeof(int));
   if (ok && mhd) {
     // U½ + 6 interface-state arrays + 3 flux arrays of nf - 1 fields + 3 EMF fields
-    ok = alloc((void **)&s.mhd, ((size_t)nf + 9 * (size_t)(nf - 1) + 3) * n * sizeof(double));
+    ok = alloc((void **)&s.mhd, cgb::mhd_scratch_fields(nf) * n * sizeof(double));
   } else if (ok) {
     ok = alloc((void **)&s.Uh, n * nf * sizeof(double)) && alloc((void **)&s.GEp, n * sizeof(double)) &&
          alloc((void **)&s.Epre, n * sizeof(double)) && alloc((void **)&s.W, 2 * (nf + 1) * n * sizeof(double));
@@ -399,15 +428,12 @@ int cgb_calc_dt_gpu(const double *d_conserved, int nx, int ny, int nz, int n_gho
   unsigned long long *d_dti = nullptr;
   int const rw               = device_word(0, &d_dti);
   if (rw != CGB_OK) return rw;
-  if (!g_dti_host && cudaMallocHost(&g_dti_host, sizeof(unsigned long long)) != cudaSuccess)
-    return fail(CGB_ERR_NOMEM, "pinned dt buffer");
   cudaError_t e = b.mhd ? cgb::mhd_calc_dt(b, d_conserved, d_dti, g_stream)
                         : cgb::hydro_calc_dt(b, d_conserved, d_dti, g_stream);
   if (e != cudaSuccess) return cuda_fail(e, "calc_dt");
-  e = cudaMemcpyAsync(g_dti_host, d_dti, sizeof(unsigned long long), cudaMemcpyDeviceToHost, g_stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(g_stream);
-  if (e != cudaSuccess) return cuda_fail(e, "calc_dt readback");
-  unsigned long long const bits = *g_dti_host;
+  unsigned long long bits = 0;
+  int const rr            = read_word(d_dti, &bits, "calc_dt readback");
+  if (rr != CGB_OK) return rr;
   double v;
   std::memcpy(&v, &bits, sizeof(v));
   *max_dti = bits == 0 ? 0.0 : v;
@@ -456,14 +482,11 @@ int cgb_max_magnetic_divergence(const double *d_conserved, int nx, int ny, int n
   unsigned long long *d_div = nullptr;
   int const rw               = device_word(1, &d_div);
   if (rw != CGB_OK) return rw;
-  if (!g_dti_host && cudaMallocHost(&g_dti_host, sizeof(unsigned long long)) != cudaSuccess)
-    return fail(CGB_ERR_NOMEM, "pinned result buffer");
   cudaError_t e = cgb::mhd_max_divb(b, d_conserved, d_div, g_stream);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(g_dti_host, d_div, sizeof(unsigned long long), cudaMemcpyDeviceToHost, g_stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(g_stream);
   if (e != cudaSuccess) return cuda_fail(e, "max_magnetic_divergence");
-  unsigned long long const bits = *g_dti_host;
+  unsigned long long bits = 0;
+  int const rr            = read_word(d_div, &bits, "max_magnetic_divergence readback");
+  if (rr != CGB_OK) return rr;
   std::memcpy(max_divb, &bits, sizeof(double));
   return CGB_OK;
 }

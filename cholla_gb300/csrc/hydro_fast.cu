@@ -31,6 +31,12 @@ constexpr int NSLOT = 6 + NS_MAX;
 // the mixed form and 2 % less in the fast FP64 form; 6 / 3 resident blocks target 1 % less than
 // 5 / 2 in the mixed form.
 constexpr int PTX = 8, PTY = 8, PTZ = 4;
+constexpr int PRED_SIDEQ = 6;  // direction-free Riemann side quantities per cell in the predictor tile
+template <typename T>
+constexpr bool pred_sideq()
+{
+  return sizeof(T) == 8;
+}
 // (compile-time tunables: the tile shapes and the resident blocks per SM the sweeps' register
 // budget targets, FP32 and FP64 compute)
 #ifndef CGB_SWEEP_XL  // x sweep: cells per pencil, pencils along y and along z
@@ -244,6 +250,18 @@ __device__ __forceinline__ hf::Prim<T> prim_at(const T *P, int stride, int i, co
   return s;
 }
 
+// the same with the sides' direction-free quantities formed beforehand (hf::side_q)
+template <typename T, int SOLVER>
+__device__ __forceinline__ void riemann_q(const hf::Prim<T> &L, const hf::Prim<T> &R, const hf::SideQ<T> &QL,
+                                          const hf::SideQ<T> &QR, T *f, const Box &b)
+{
+  if (SOLVER == SOLVER_ROE) {
+    hf::roe_q(L, R, QL, QR, f, b.ns, b.de, gamma_of<T>(b));
+  } else {
+    hf::hllc_q(L, R, QL, QR, f, b.ns, b.de, gamma_of<T>(b));
+  }
+}
+
 template <typename T, int SOLVER>
 __device__ __forceinline__ void riemann(const hf::Prim<T> &L, const hf::Prim<T> &R, T *f, const Box &b)
 {
@@ -326,8 +344,10 @@ __device__ __forceinline__ void fpred_tile(const Box &b, const double *__restric
   constexpr int NT  = TX * TY * TZ;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int const ns_ = nslot(b);
+  constexpr bool PRE = pred_sideq<T>();      // side quantities formed once per cell (FP64 only)
   T *Ps  = reinterpret_cast<T *>(smem_raw);  // [slot][NB] primitives of the box
-  T *Fxs = Ps + ns_ * NB;                    // [slot][faces] fluxes, conserved orientation
+  T *Qs  = Ps + ns_ * NB;                    // [PRED_SIDEQ][NB] the cells' Riemann side quantities
+  T *Fxs = Qs + (PRE ? PRED_SIDEQ * NB : 0); // [slot][faces] fluxes, conserved orientation
   T *Fys = Fxs + ns_ * NFX;
   T *Fzs = Fys + ns_ * NFY;
 
@@ -348,6 +368,22 @@ __device__ __forceinline__ void fpred_tile(const Box &b, const double *__restric
     for (int s = 0; s < ns_; s++) Ps[s * NB + t] = Wn[(long long)s * n + gid];
   }
   __syncthreads();
+  // The PCM interface states are the cells: each cell's direction-free side quantities (energy,
+  // used pressure, 1/d, sqrt(d), sound speed, enthalpy) are formed once here for the up to six
+  // faces that read them (edge and corner cells of the halo feed no face and are skipped).  This
+  // takes 30% of the fast FP64 predictor's FP64 work away; the mixed predictor, whose Riemann
+  // work is FP32 and whose time goes to its FP64 half update, measured slower with the extra pass
+  // (1.62 -> 1.94 ms at 256^3) and forms them per face.
+  for (int t = threadIdx.x; PRE && t < NB; t += NT) {
+    int const bx = t % BX, by = (t / BX) % BY, bz = t / (BX * BY);
+    int const halo = (bx == 0 || bx == BX - 1) + (HY && (by == 0 || by == BY - 1)) + (HZ && (bz == 0 || bz == BZ - 1));
+    if (halo > 1) continue;
+    hf::SideQ<T> const q =
+        hf::side_q<T, SOLVER != SOLVER_ROE>(prim_at(Ps, NB, t, b), b.de, gamma_of<T>(b), ig1_of<T>(b));
+    Qs[0 * NB + t] = q.E, Qs[1 * NB + t] = q.p, Qs[2 * NB + t] = q.id;
+    Qs[3 * NB + t] = q.sq, Qs[4 * NB + t] = q.c, Qs[5 * NB + t] = q.h;
+  }
+  if (PRE) __syncthreads();
 
   int const nfaces = NFX + NFY + NFZ;
   for (int t = threadIdx.x; t < nfaces; t += NT) {
@@ -374,8 +410,17 @@ __device__ __forceinline__ void fpred_tile(const Box &b, const double *__restric
     T const ua = L.vn, ub = L.vt1, uc = L.vt2, va = R.vn, vb = R.vt1, vc = R.vt2;
     L.vn = pick(ua, ub, uc, o1), L.vt1 = pick(ua, ub, uc, o2), L.vt2 = pick(ua, ub, uc, o3);
     R.vn = pick(va, vb, vc, o1), R.vt1 = pick(va, vb, vc, o2), R.vt2 = pick(va, vb, vc, o3);
+    auto sq = [&](int c) {
+      hf::SideQ<T> q;
+      q.E = Qs[0 * NB + c], q.p = Qs[1 * NB + c], q.id = Qs[2 * NB + c];
+      q.sq = Qs[3 * NB + c], q.c = Qs[4 * NB + c], q.h = Qs[5 * NB + c];
+      return q;
+    };
     T f[NSLOT];
-    riemann<T, SOLVER>(L, R, f, b);
+    if constexpr (PRE)
+      riemann_q<T, SOLVER>(L, R, sq(cl), sq(cr), f, b);
+    else
+      riemann<T, SOLVER>(L, R, f, b);
 #pragma unroll
     for (int q = 0; q < NSLOT; q++)
       if (live(q, b)) Fd[rot(q, o1, o2, o3) * nfd + fidx] = f[q];
@@ -1053,7 +1098,7 @@ size_t fpred_smem(const Box &b)
   constexpr int HY = TY > 1, HZ = TZ > 1;
   constexpr int NB = (TX + 2) * (TY + 2 * HY) * (TZ + 2 * HZ);
   constexpr int NF = (TX + 1) * TY * TZ + (HY ? TX * (TY + 1) * TZ : 0) + (HZ ? TX * TY * (TZ + 1) : 0);
-  return sizeof(T) * (size_t)nslot(b) * (NB + NF);
+  return sizeof(T) * ((size_t)nslot(b) * (NB + NF) + (pred_sideq<T>() ? (size_t)PRED_SIDEQ * NB : 0));
 }
 
 template <typename T, int TX, int TY, int TZ>
@@ -1279,7 +1324,7 @@ cudaError_t launch_core(const BatchChunk &C, int recon, int solver, int nsl, dou
   {
     constexpr int NB = (PTX + 2) * (PTY + 2) * (PTZ + 2);
     constexpr int NF = (PTX + 1) * PTY * PTZ + PTX * (PTY + 1) * PTZ + PTX * PTY * (PTZ + 1);
-    size_t const sm  = sizeof(T) * (size_t)nsl * (NB + NF);
+    size_t const sm  = sizeof(T) * ((size_t)nsl * (NB + NF) + (pred_sideq<T>() ? (size_t)PRED_SIDEQ * NB : 0));
     auto k = (solver == SOLVER_ROE) ? kb_pred<T, SOLVER_ROE> : kb_pred<T, SOLVER_HLLC>;
     if ((e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm)) != cudaSuccess) return e;
     k<<<C.total[BK_PRED], PTX * PTY * PTZ, sm, s>>>(C);

@@ -124,22 +124,26 @@ struct Eps<float> {
   static constexpr float roundoff = 1.0e-6f;  // same test scaled to single precision
 };
 
-// Reciprocal and square root.  FP64: an FP32 estimate refined by Newton steps (4 and 5 FP64
-// FMAs instead of a ~12-instruction divide or square-root sequence).  rcp: two Newton-Raphson
-// steps r <- r + r (1 - d r) on the reciprocal.  sqrtT: two Newton-Raphson steps on the inverse
-// square root y <- y (3/2 - x y^2 / 2), then the square root s = x y corrected once with its own
-// residual, s + (x - s^2) y / 2 (Karp and Markstein, "High-precision division and square root",
-// ACM TOMS 23(4), 1997).  Both stay within 1 ulp of the correctly rounded result, which
-// cgb_selftest_fast_math measures against CUDA's 1 / x and sqrt over the FP32 exponent range.
-// Outside |x| in (1e-30, 1e30) a true divide / square root is used.  FP32: the hardware
+// Reciprocal and square root.  FP64: an FP32 estimate refined in FP64 (3 and 7 FP64
+// instructions instead of a ~12-instruction divide or square-root sequence).  rcp: with the
+// estimate's relative error e = 1 - d r (one FMA, exact up to one rounding), the third-order
+// iteration r (1 + e + e^2) leaves a relative error of order e^3 ~ 2^-69 (the cubically convergent
+// reciprocal iteration; J.-M. Muller et al., "Handbook of Floating-Point Arithmetic", 2nd ed.,
+// Birkhauser 2018, ch. 4 on Newton-Raphson-based division).  sqrtT: one Newton-Raphson step on the
+// inverse square root, y <- y (3/2 - x y^2 / 2), takes the FP32 estimate from ~2^-22 to ~2^-42
+// relative error; the square root s = x y is then corrected once with its own residual,
+// s + (x - s^2) y / 2 (Karp and Markstein, "High-precision division and square root", ACM TOMS
+// 23(4), 1997), which squares that error.  Both stay within 1 ulp of the correctly rounded result,
+// which cgb_selftest_fast_math measures against CUDA's 1 / x and sqrt over the FP32 exponent
+// range.  Outside |x| in (1e-30, 1e30) a true divide / square root is used.  FP32: the hardware
 // approximations (about 1 ulp).
 __device__ __forceinline__ double rcp(double d)
 {
   float const f = to_f32(d);
   if (!(fabsf(f) > 1e-30f && fabsf(f) < 1e30f)) return 1.0 / d;
-  double r = to_f64(__frcp_rn(f));
-  r        = fma(r, fma(-d, r, 1.0), r);
-  return fma(r, fma(-d, r, 1.0), r);
+  double const r = to_f64(__frcp_rn(f));
+  double const e = fma(-d, r, 1.0);
+  return fma(r, fma(e, e, e), r);
 }
 __device__ __forceinline__ float rcp(float d) { return __frcp_rn(d); }
 
@@ -149,7 +153,6 @@ __device__ __forceinline__ double sqrtT(double x)
   if (!(f > 1e-30f && f < 1e30f)) return sqrt(x);
   double y       = to_f64(rsqrtf(f));
   double const h = 0.5 * x;
-  y              = y * fma(-h * y, y, 1.5);
   y              = y * fma(-h * y, y, 1.5);
   double const s = x * y;
   return fma(fma(-s, s, x), 0.5 * y, s);  // Karp-Markstein correction of the square root
@@ -432,31 +435,49 @@ __device__ __forceinline__ T pressure_used(const Prim<T> &s, T E, T ig1, T g1, i
   return max_pos(p, T(TINY));
 }
 
+// The quantities of one side of a Riemann problem that depend on that state alone and not on the
+// direction: total energy, the pressure the solver uses, 1/d, sqrt(d), the sound speed of the used
+// pressure (HLLC only) and the specific enthalpy (E + p) / d.  The predictor's PCM interface states
+// are the cells themselves, so it forms these once per cell for the six faces that use them.
+template <typename T>
+struct SideQ {
+  T E, p, id, sq, c, h;
+};
+template <typename T, bool SOUND>
+__device__ __forceinline__ SideQ<T> side_q(const Prim<T> &s, int de, T gamma, T ig1)
+{
+  SideQ<T> q;
+  q.E  = s.p * ig1 + T(0.5) * s.d * (s.vn * s.vn + s.vt1 * s.vt1 + s.vt2 * s.vt2);
+  q.p  = pressure_used(s, q.E, ig1, gamma - T(1), de);
+  q.id = rcp(s.d);
+  q.sq = sqrtT(s.d);
+  q.c  = SOUND ? sqrtT(gamma * q.p * q.id) : T(0);
+  q.h  = (q.E + q.p) * q.id;
+  return q;
+}
+
 // HLLC flux (hllc_cuda.cu:19-307) from primitive interface states; f in rotated order
 // in fixed slots: 0 d, 1 m_n, 2 m_t1, 3 m_t2, 4 E, 5 GasEnergy, 6.. scalars.  Fixed slots keep
 // every register-array index a compile-time constant (no local memory).
 template <typename T>
-__device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, int ns, int de, T gamma, T ig1)
+__device__ __forceinline__ void hllc_q(const Prim<T> &l, const Prim<T> &r, const SideQ<T> &Ql, const SideQ<T> &Qr,
+                                       T *f, int ns, int de, T gamma)
 {
   T const g1  = gamma - T(1);
   T const mxl = l.d * l.vn, myl = l.d * l.vt1, mzl = l.d * l.vt2;
   T const mxr = r.d * r.vn, myr = r.d * r.vt1, mzr = r.d * r.vt2;
-  T const El  = l.p * ig1 + T(0.5) * l.d * (l.vn * l.vn + l.vt1 * l.vt1 + l.vt2 * l.vt2);
-  T const Er  = r.p * ig1 + T(0.5) * r.d * (r.vn * r.vn + r.vt1 * r.vt1 + r.vt2 * r.vt2);
-  T const pl  = pressure_used(l, El, ig1, g1, de);
-  T const pr  = pressure_used(r, Er, ig1, g1, de);
-  T const idl = rcp(l.d), idr = rcp(r.d);
-  T const sqrtdl = sqrtT(l.d), sqrtdr = sqrtT(r.d);
+  T const El = Ql.E, Er = Qr.E, pl = Ql.p, pr = Qr.p;
+  T const sqrtdl = Ql.sq, sqrtdr = Qr.sq;
   T const isum   = rcp(sqrtdl + sqrtdr);
   T const wl = sqrtdl * isum, wr = sqrtdr * isum;
   T const vx  = wl * l.vn + wr * r.vn;
   T const vy  = wl * l.vt1 + wr * r.vt1;
   T const vz  = wl * l.vt2 + wr * r.vt2;
-  T const H   = wl * ((El + pl) * idl) + wr * ((Er + pr) * idr);
+  T const H   = wl * Ql.h + wr * Qr.h;
   T const asq = g1 * (H - T(0.5) * (vx * vx + vy * vy + vz * vz));
   T const a   = sqrtT(asq);
-  T const cfl = sqrtT(gamma * pl * idl);
-  T const cfr = sqrtT(gamma * pr * idr);
+  T const cfl = Ql.c;
+  T const cfr = Qr.c;
   // outer wave speeds relative to each side's own velocity, kept apart from the velocity so a
   // cold side's sound speed is not rounded away (FP32: cf ~1e-10 against v ~1)
   T dSl, dSr, Sl, Sr;
@@ -516,23 +537,26 @@ __device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, i
   }
 }
 
+template <typename T>
+__device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, int ns, int de, T gamma, T ig1)
+{
+  hllc_q(l, r, side_q<T, true>(l, de, gamma, ig1), side_q<T, true>(r, de, gamma, ig1), f, ns, de, gamma);
+}
+
 // Roe flux with the HLLE fallback (roe_cuda.cu:19-400) from primitive interface states.
 template <typename T>
-__device__ __forceinline__ void roe(const Prim<T> &l, const Prim<T> &r, T *f, int ns, int de, T gamma, T ig1)
+__device__ __forceinline__ void roe_q(const Prim<T> &l, const Prim<T> &r, const SideQ<T> &Ql, const SideQ<T> &Qr,
+                                      T *f, int ns, int de, T gamma)
 {
   T const g1  = gamma - T(1);
   T const dl = l.d, dr = r.d, vxl = l.vn, vyl = l.vt1, vzl = l.vt2, vxr = r.vn, vyr = r.vt1, vzr = r.vt2;
   T const mxl = dl * vxl, myl = dl * vyl, mzl = dl * vzl, mxr = dr * vxr, myr = dr * vyr, mzr = dr * vzr;
-  T const El  = l.p * ig1 + T(0.5) * dl * (vxl * vxl + vyl * vyl + vzl * vzl);
-  T const Er  = r.p * ig1 + T(0.5) * dr * (vxr * vxr + vyr * vyr + vzr * vzr);
-  T const pl  = pressure_used(l, El, ig1, g1, de);
-  T const pr  = pressure_used(r, Er, ig1, g1, de);
-  T const idl = rcp(dl), idr = rcp(dr);
-  T const sqrtdl = sqrtT(dl), sqrtdr = sqrtT(dr);
+  T const El = Ql.E, Er = Qr.E, pl = Ql.p, pr = Qr.p, idl = Ql.id, idr = Qr.id;
+  T const sqrtdl = Ql.sq, sqrtdr = Qr.sq;
   T const isum   = rcp(sqrtdl + sqrtdr);
   T const wl = sqrtdl * isum, wr = sqrtdr * isum;
   T const vx = wl * vxl + wr * vxr, vy = wl * vyl + wr * vyr, vz = wl * vzl + wr * vzr;
-  T const H   = wl * ((El + pl) * idl) + wr * ((Er + pr) * idr);
+  T const H   = wl * Ql.h + wr * Qr.h;
   T const vsq = vx * vx + vy * vy + vz * vz;
   T const asq = g1 * fmax(H - T(0.5) * vsq, T(TINY));
   T const a   = sqrtT(asq);
@@ -609,6 +633,11 @@ __device__ __forceinline__ void roe(const Prim<T> &l, const Prim<T> &r, T *f, in
   for (int k = 0; k < NS_MAX; k++)
     if (k < ns) f[6 + k] = f[0] * ((f[0] >= T(0)) ? l.sc[k] : r.sc[k]);
   if (de) f[5] = f[0] * ((f[0] >= T(0)) ? l.ge : r.ge);
+}
+template <typename T>
+__device__ __forceinline__ void roe(const Prim<T> &l, const Prim<T> &r, T *f, int ns, int de, T gamma, T ig1)
+{
+  roe_q(l, r, side_q<T, false>(l, de, gamma, ig1), side_q<T, false>(r, de, gamma, ig1), f, ns, de, gamma);
 }
 
 }  // namespace hf

@@ -41,6 +41,9 @@ cudaError_t hydro_temperature_floor(const Box &b, double *U, double U_floor, cud
 // MHD (mhd_exact.cu): the VL step with HLLD and constrained transport, FP64 in the reference's
 // operation order.  scratch holds mhd_scratch_doubles(b) doubles and must start zeroed.
 size_t mhd_scratch_doubles(const Box &b);
+// fields of that scratch: U½ (nf), 6 interface-state and 3 flux arrays (nf - 1 each), the 3 edge
+// EMFs and the 3 cell-centred electric fields of the CT slopes
+inline size_t mhd_scratch_fields(int nf) { return (size_t)nf + 9 * (size_t)(nf - 1) + 6; }
 // dt_dev != null: dt is read on the device (the box engine keeps it there)
 cudaError_t mhd_exact_step(const Box &b, int recon, double *U, double *scratch, double dt, const double *dt_dev,
                            cudaStream_t s);

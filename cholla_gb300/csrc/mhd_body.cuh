@@ -649,35 +649,57 @@ __global__ void k_hlld(Box b, const double *__restrict__ QL, const double *__res
 // ------------------------------------------------------------------------------------------
 // constrained transport
 // ------------------------------------------------------------------------------------------
-// ct_electric_fields.h:66-118 _ctSlope
-__device__ __forceinline__ double ct_slope(const Box &b, const double *flux, const double *U, double fluxSign,
+// The cell-centred electric field that _ctSlope (ct_electric_fields.h:66-118) subtracts from a face
+// flux: at cell i for CT direction d, (M3 B2c - M2 B3c) / density with (m1, m2) = (d + 1, d + 2)
+// mod 3 and B2c, B3c the cell's face fields averaged with the faces below it.  It depends on the
+// cell and d alone, and each cell's three values feed 24 slope evaluations of its neighbours' edges,
+// so k_ct_centred forms them once per cell (the same operations, so the same bits) into ec[d][i].
+// Cells whose lower neighbour along m1 or m2 lies before the array's first element get 0: only
+// edges of the outermost ghost layer would read them.
+__global__ void k_ct_centred(Box b, const double *__restrict__ U, double *__restrict__ ec)
+{
+  long long const n = b.n;
+  int const fB      = b.fB();
+  CGB_CELLS(t)
+  {
+    double const density = U[t];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      int const m1 = (d + 1) % 3, m2 = (d + 2) % 3;
+      long long const s1 = m1 == 0 ? 1 : m1 == 1 ? (long long)b.nx : (long long)b.nx * b.ny;
+      long long const s2 = m2 == 0 ? 1 : m2 == 1 ? (long long)b.nx : (long long)b.nx * b.ny;
+      if (t < s1 || t < s2) {
+        ec[d * n + t] = 0.0;
+        continue;
+      }
+      double const M2  = U[t + (long long)(m1 + 1) * n];
+      double const M3  = U[t + (long long)(m2 + 1) * n];
+      double const B2c = 0.5 * (U[t + (long long)(m1 + fB) * n] + U[t - s1 + (long long)(m1 + fB) * n]);
+      double const B3c = 0.5 * (U[t + (long long)(m2 + fB) * n] + U[t - s2 + (long long)(m2 + fB) * n]);
+      ec[d * n + t]    = mdiv(M3 * B2c - M2 * B3c, density);
+    }
+  }
+}
+
+// ct_electric_fields.h:66-118 _ctSlope, with the cell-centred field read from ec
+__device__ __forceinline__ double ct_slope(const Box &b, const double *flux, const double *ec, double fluxSign,
                                            int ctDir, int cq1, int cq2, int fq1, int fq2, int x, int y, int z)
 {
   long long const n = b.n;
-  int const m1 = (ctDir + 1) % 3;
-  int const m2 = (ctDir + 2) % 3;
   int const xc = x - int(cq1 == 0) - int(cq2 == 0);
   int const yc = y - int(cq1 == 1) - int(cq2 == 1);
   int const zc = z - int(cq1 == 2) - int(cq2 == 2);
   long long const ic    = b.id(xc, yc, zc);
   long long const iflux = b.id(x - int(fq1 == 0) - int(fq2 == 0), y - int(fq1 == 1) - int(fq2 == 1),
                                z - int(fq1 == 2) - int(fq2 == 2));
-  long long const iB2 = b.id(xc - int(m1 == 0), yc - int(m1 == 1), zc - int(m1 == 2));
-  long long const iB3 = b.id(xc - int(m2 == 0), yc - int(m2 == 1), zc - int(m2 == 2));
-  int const fB        = b.fB();
-  double const density = U[ic];
-  double const M2      = U[ic + (long long)(m1 + 1) * n];
-  double const M3      = U[ic + (long long)(m2 + 1) * n];
-  double const B2c     = 0.5 * (U[ic + (long long)(m1 + fB) * n] + U[iB2 + (long long)(m1 + fB) * n]);
-  double const B3c     = 0.5 * (U[ic + (long long)(m2 + fB) * n] + U[iB3 + (long long)(m2 + fB) * n]);
-  double const ec      = mdiv(M3 * B2c - M2 * B3c, density);
-  double const ef      = fluxSign * flux[iflux + (long long)(int(fluxSign == 1) + fB) * n];
-  return ef - ec;
+  int const fB    = b.fB();
+  double const ef = fluxSign * flux[iflux + (long long)(int(fluxSign == 1) + fB) * n];
+  return ef - ec[(long long)ctDir * n + ic];
 }
 
 // ct_electric_fields.cu:20-279 Calculate_CT_Electric_Fields
 __global__ void k_ct(Box b, const double *__restrict__ Fx, const double *__restrict__ Fy,
-                     const double *__restrict__ Fz, const double *__restrict__ U, double *__restrict__ emf)
+                     const double *__restrict__ Fz, const double *__restrict__ ec, double *__restrict__ emf)
 {
   long long const n = b.n;
   int const fB      = b.fB();
@@ -688,13 +710,14 @@ __global__ void k_ct(Box b, const double *__restrict__ Fx, const double *__restr
     int x, y, z;
     xyz(b, t, x, y, z);
     if (!(x > 0 and y > 0 and z > 0 and x < b.nx and y < b.ny and z < b.nz)) continue;
+    // the upwind slope: only the side the mass flux selects is evaluated (both when it is zero)
     auto S = [&](const double *fl, double sg, int cd, int a, int c, int cc, int d) {
-      return ct_slope(b, fl, U, sg, cd, a, c, cc, d, x, y, z);
+      return [=, &b] { return ct_slope(b, fl, ec, sg, cd, a, c, cc, d, x, y, z); };
     };
-    auto pick = [](double sgnUp, double pos, double neg) {
-      if (mgt0(sgnUp)) return pos;
-      if (mlt0(sgnUp)) return neg;
-      return 0.5 * (pos + neg);
+    auto pick = [](double sgnUp, auto pos, auto neg) {
+      if (mgt0(sgnUp)) return pos();
+      if (mlt0(sgnUp)) return neg();
+      return 0.5 * (pos() + neg());
     };
     double syp, syn, szp, szn, sxp, sxn, fyp, fyn, fzp, fzn, fxp, fxn;
     // X electric field
@@ -909,11 +932,7 @@ unsigned grid_for(long long n)
 }  // namespace CGB_MHD_NS
 
 #if CGB_MHD_REDUCTIONS
-size_t mhd_scratch_doubles(const Box &b)
-{
-  // U½ (nf) + 6 interface arrays and 3 flux arrays of nf - 1 fields + 3 EMF fields
-  return ((size_t)b.nf + 9 * (size_t)(b.nf - 1) + 3) * (size_t)b.n;
-}
+size_t mhd_scratch_doubles(const Box &b) { return mhd_scratch_fields(b.nf) * (size_t)b.n; }
 #endif
 
 cudaError_t CGB_MHD_STEP(const Box &b, int recon, double *U, double *scratch, double dt, const double *dt_dev,
@@ -922,7 +941,8 @@ cudaError_t CGB_MHD_STEP(const Box &b, int recon, double *U, double *scratch, do
   using namespace CGB_MHD_NS;
   size_t const n = (size_t)b.n, nif = (size_t)(b.nf - 1) * n;
   double *Uh = scratch, *QLx = Uh + (size_t)b.nf * n, *QRx = QLx + nif, *QLy = QRx + nif, *QRy = QLy + nif,
-         *QLz = QRy + nif, *QRz = QLz + nif, *Fx = QRz + nif, *Fy = Fx + nif, *Fz = Fy + nif, *emf = Fz + nif;
+         *QLz = QRy + nif, *QRz = QLz + nif, *Fx = QRz + nif, *Fy = Fx + nif, *Fz = Fy + nif, *emf = Fz + nif,
+         *ec = emf + 3 * n;
   unsigned const g = grid_for(b.n);
   long long const fB = b.fB();
   auto face = [&](const double *src, int d) { return src + (fB + d) * (long long)n; };
@@ -934,7 +954,8 @@ cudaError_t CGB_MHD_STEP(const Box &b, int recon, double *U, double *scratch, do
   // predictor: PCM, HLLD, CT, half updates with 0.5 dt
   k_pcm<<<g, 256, 0, s>>>(b, U, QLx, QRx, QLy, QRy, QLz, QRz);
   riemann(U);
-  k_ct<<<g, 256, 0, s>>>(b, Fx, Fy, Fz, U, emf);
+  k_ct_centred<<<g, 256, 0, s>>>(b, U, ec);
+  k_ct<<<g, 256, 0, s>>>(b, Fx, Fy, Fz, ec, emf);
   // the half step uses dt * 0.5 on the device (the same product as 0.5 * dt on the host)
   k_update_half<<<g, 256, 0, s>>>(b, U, Uh, Fx, Fy, Fz, dt, dt_dev, 0.5);
   k_bupdate<<<g, 256, 0, s>>>(b, U, Uh, emf, dt, dt_dev, 0.5);
@@ -949,7 +970,8 @@ cudaError_t CGB_MHD_STEP(const Box &b, int recon, double *U, double *scratch, do
     k_pcm<<<g, 256, 0, s>>>(b, Uh, QLx, QRx, QLy, QRy, QLz, QRz);
   }
   riemann(Uh);
-  k_ct<<<g, 256, 0, s>>>(b, Fx, Fy, Fz, Uh, emf);
+  k_ct_centred<<<g, 256, 0, s>>>(b, Uh, ec);
+  k_ct<<<g, 256, 0, s>>>(b, Fx, Fy, Fz, ec, emf);
   k_update_full<<<g, 256, 0, s>>>(b, U, Fx, Fy, Fz, dt, dt_dev);
   k_bupdate<<<g, 256, 0, s>>>(b, U, U, emf, dt, dt_dev, 1.0);
   cudaError_t e = cudaGetLastError();

@@ -1,6 +1,6 @@
 """Error of the fast FP64 form's reciprocal and square root (cholla_gb300/csrc/hydro_fast.cuh:
-rcp, an FP32 estimate and two Newton-Raphson steps; sqrtT, two Newton-Raphson steps on the
-inverse square root and the Karp-Markstein correction) against CUDA's correctly rounded 1 / x and
+rcp, an FP32 estimate and one third-order iteration r (1 + e + e^2); sqrtT, one Newton-Raphson
+step on the inverse square root and the Karp-Markstein correction) against CUDA's correctly rounded 1 / x and
 sqrt, measured in units in the last place over the FP32 exponent range and on both sides of the
 1e-30 / 1e30 guards, where the helpers switch to the true divide and square root."""
 import numpy as np
