@@ -179,7 +179,7 @@ int make_box(cgb::Box &b, int nx, int ny, int nz, int ng, int nf, double dx, dou
 }  // namespace
 
 // Static scratch of cgb_vl_algorithm_3d_static: a file-scope array in the module's static device
-// memory, which the driver provides when it loads the module; no call allocates it.  A box of n
+// memory, which the CUDA driver provides when it loads the module; no call allocates it.  A box of n
 // padded cells and f fields needs (f + 2) 8 n bytes in exact FP64 and (2 f + 4) 8 n in the fast
 // forms (each array rounded to 256 bytes) plus 512: with 6 fields, 24 MiB holds fewer than
 // 393,216 padded cells (73^3) in FP64 and fewer than 196,608 (58^3) in fast FP64 / mixed.

@@ -103,7 +103,7 @@ int cgb_vl_algorithm_3d(double *d_conserved, double *d_grav_potential, int nx, i
  * program that has handed the device's memory to its own pool before stepping, and one that
  * overlaps the step with work on other streams and cannot take the device-wide
  * synchronisation that a first-call cudaMalloc, or the cudaFree of a shape change, implies.
- * Scratch comes from a 24 MiB file-scope __device__ array of the library, which the driver
+ * Scratch comes from a 24 MiB file-scope __device__ array of the library, which the CUDA driver
  * maps with the module's static data (under lazy module loading: on first use, so the first
  * call on a device is when those 24 MiB leave the free pool).  Its address is looked up once
  * per device (cudaGetSymbolAddress, with that device current) on the first call there, so

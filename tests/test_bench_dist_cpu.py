@@ -1,6 +1,6 @@
 """The bench's multi-process host logic on CPU with gloo, world size 2: the barrier and the
-max-over-ranks reduction that bracket the timed region, and the reference arm launched the
-way the driver launches it for N > 1 (torchrun, rank 0 alone runs and prints one line)."""
+max-over-ranks reduction that bracket the timed region, and the reference arm launched as a
+multi-GPU run launches it for N > 1 (torchrun, rank 0 alone runs and prints one line)."""
 import json
 import os
 import socket
