@@ -9,10 +9,11 @@ reduction, predictor, corrector, finalize (DE select/sync, temperature floor, CF
     python bench.py [--steps K] [--warmup W] [--gpus N] [--n 256] [--impl ours|reference]
 
 Besides the headline line's own numbers it reports, on the same GPU: the other arithmetic forms;
-per-field accuracy against the exact FP64 form for the 256^3 box (20 steps), the 512^3 box in
-mixed precision (50 steps) and every job of a serving stream; the 512^3 box's speed in every form
-and of the reference's own CUDA build; the 256^3 ideal-MHD box; the serving sweep; the drop-in
-C ABI end to end with host copies; and the CPU baseline (the FP64 host oracle, 256^3 sample).
+per-field accuracy against the exact FP64 form for the 256^3 box (20 steps) and every job of a
+serving stream, and against the fast FP64 form for the 512^3 box in mixed precision (50 steps);
+the 512^3 box's speed in every form and of the reference's own CUDA build; the 256^3 ideal-MHD
+box; the serving sweep (100 and 2000 req/s, three seeds); the drop-in C ABI end to end with host
+copies; and the CPU baseline (the FP64 host oracle on the same 256^3 box).
 
 --impl reference times the reference's CPU path: the FP64 host restatement of the same scheme
 (oracle/, OpenMP over every host core) on the same 256^3 box, W warm-up and K timed steps.
@@ -468,9 +469,10 @@ def run_ours(args, world, rank, local):
 
 def run_512(args, dev, stream, torch):
     """The 512^3 box of the same workload: ms per step of every arithmetic form and of the
-    reference's build on the same GPU, and the mixed form's per-field accuracy against the exact
-    FP64 form after 50 steps on the same dt sequence (whose timing also gives the exact form's
-    speed through the drop-in calls, with the host dt round trip of every step)."""
+    reference's build on the same GPU, and the mixed form's per-field accuracy after 50 steps
+    against the fast FP64 form on the same dt sequence (the fast form is within 1e-15 relative
+    L1 per field of the exact one at this size; tests/test_config_scale_gpu.py checks the mixed
+    form against the exact form itself, which takes 100 s here)."""
     from cholla_gb300 import accuracy, ics
     from cholla_gb300.engine import Box
 
@@ -479,7 +481,7 @@ def run_512(args, dev, stream, torch):
     U0 = ics.turbulence_box(n, ng, gamma, seed=0)
     out = {"workload": "3D adiabatic hydro 512^3 periodic turbulence-like box (seed 0, rms Mach 2), PPMC+HLLC+VL, "
                        "dual energy, floors, CFL 0.3", "n": n}
-    for prec, k in (("fp64_fast", 3), ("mixed", 10)):
+    for prec, k in (("fp64_fast", 3), ("mixed", 10), ("fp64", 2)):
         U = torch.from_numpy(U0).to(dev)
         box = Box(N, N, N, ng, dx, dx, dx, scheme_of(prec))
         box.use_graph(True)
@@ -496,17 +498,12 @@ def run_512(args, dev, stream, torch):
             rms = time_reference_build(R, U0, n, ng, gamma, dev, stream, torch, 2)
             out["reference_gpu"] = {"ms_per_step": rms, "value": n ** 3 / (rms / 1e3), "steps": 2,
                                     "variant": "no_sync", "build": REF_BUILD_NOTE}
-            out["speedup_vs_reference_build"] = {p: rms / out[p]["ms_per_step"] for p in ("fp64_fast", "mixed")}
+            out["speedup_vs_reference_build"] = {p: rms / out[p]["ms_per_step"] for p in ("fp64_fast", "mixed", "fp64")}
     except Exception as ex:  # the reference build is a comparison, not part of the product
         out["reference_gpu"] = {"unavailable": str(ex)[:200]}
     if not args.no_accuracy:
-        acc = accuracy.run(torch, n=n, steps=50, seed=0, forms=("mixed",), U0=U0)
-        out["accuracy_mixed_vs_exact_50_steps"] = acc
-        out["fp64"] = {"ms_per_step_dropin": 1e3 * acc["seconds"]["fp64"] / 50,
-                       "note": "exact FP64 through the drop-in calls, host dt round trip every step"}
-        if "reference_gpu" in out and "ms_per_step" in out["reference_gpu"]:
-            out.setdefault("speedup_vs_reference_build", {})["fp64"] = (out["reference_gpu"]["ms_per_step"] /
-                                                                      out["fp64"]["ms_per_step_dropin"])
+        out["accuracy_mixed_vs_fp64_50_steps"] = accuracy.run(torch, n=n, steps=50, seed=0, forms=("mixed",), U0=U0,
+                                                              baseline="fp64_fast")
     return out
 
 
@@ -632,8 +629,8 @@ def main():
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-512", action="store_true")
-    ap.add_argument("--serve-rates", default="10,30,100,2000")
-    ap.add_argument("--serve-count", default="60,100,200,200", help="requests per rate (one per rate, or one for all)")
+    ap.add_argument("--serve-rates", default="100,2000")
+    ap.add_argument("--serve-count", default="200", help="requests per rate (one per rate, or one for all)")
     ap.add_argument("--serve-seeds", default="17,18,19", help="request-stream seeds of the rates from 100 req/s up")
     ap.add_argument("--serve-twins", type=int, default=12, help="served jobs checked against their FP64 twins")
     ap.add_argument("--precision", choices=["fp64_fast", "fp64", "mixed"], default="fp64_fast")

@@ -487,8 +487,11 @@ __device__ __forceinline__ void fpred_tile(const Box &b, const double *__restric
     if (live(s, b)) W[(long long)s * n + gid] = w[s];
 }
 
+#ifndef CGB_PRED_MINB_F32
+#define CGB_PRED_MINB_F32 2  // resident predictor blocks per SM the FP32 register budget targets
+#endif
 template <typename T, int TX, int TY, int TZ, int SOLVER>
-__global__ void __launch_bounds__(TX *TY *TZ, 2)
+__global__ void __launch_bounds__(TX *TY *TZ, sizeof(T) == 4 ? CGB_PRED_MINB_F32 : 2)
     k_fpred(Box b, const double *__restrict__ U, const T *__restrict__ Wn, T *__restrict__ W, double *__restrict__ GEp,
             double dt, const double *__restrict__ dtp)
 {
@@ -584,14 +587,16 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
 
 // the increment k * fl - k * fr of a cell from its two faces; each product is rounded once, as
 // the face's other cell rounds it
-__device__ __forceinline__ Acc<double> flux_diff(double k, double fl, double fr)
-{
-  return {__dsub_rn(__dmul_rn(k, fl), __dmul_rn(k, fr))};
-}
-__device__ __forceinline__ Acc<float> flux_diff(float k, float fl, float fr)
+// a face's flux times dt/dx, rounded once (no contraction into a later sum)
+__device__ __forceinline__ double scaled_flux(double k, double f) { return __dmul_rn(k, f); }
+__device__ __forceinline__ float scaled_flux(float k, float f) { return __fmul_rn(k, f); }
+// a cell's increment from its low and high faces' scaled fluxes: their difference, rounded once
+// in the fast FP64 form, kept error-free as an FP32 (hi, lo) pair in the mixed form
+__device__ __forceinline__ Acc<double> scaled_diff(double fl, double fr) { return {__dsub_rn(fl, fr)}; }
+__device__ __forceinline__ Acc<float> scaled_diff(float fl, float fr)
 {
   Acc<float> r;
-  two_sum(__fmul_rn(k, fl), -__fmul_rn(k, fr), r.hi, r.lo);
+  two_sum(fl, -fr, r.hi, r.lo);
   return r;
 }
 __device__ __forceinline__ Acc<double> acc_add(Acc<double> a, Acc<double> b) { return {__dadd_rn(a.v, b.v)}; }
@@ -782,6 +787,12 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
     }
     __syncthreads();
   }
+  // Conservation: each face's flux is scaled once, dtod * F rounded as one uncontracted product
+  // that both of its cells read, and a cell's increment is the difference of its two faces'
+  // scaled fluxes, summed over the three sweeps in an accumulator of at least 48 significant bits
+  // (W^n's space, 8 bytes per field): FP64 in the fast FP64 form, an FP32 (hi, lo) pair built
+  // with error-free sums in the mixed form.  So the updates telescope to accumulation roundoff.
+  T const dtod = narrow<T>(dt * (DIR == 0 ? b.idx : DIR == 1 ? b.idy : b.idz));
   for (int f = t; f < S::NF; f += NT) {
     int a, c;
     S::split(f, S::LF, a, c);  // face a lies between sweep positions a - 1 and a
@@ -799,7 +810,7 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
     riemann<T, SOLVER>(Lf, Rf, fl, b);
 #pragma unroll
     for (int q = 0; q < NSLOT; q++)
-      if (live(q, b)) Fs[q * S::NF + f] = fl[q];
+      if (live(q, b)) Fs[q * S::NF + f] = scaled_flux(dtod, fl[q]);
   }
   __syncthreads();
 
@@ -812,17 +823,11 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
   if (!real) return;
   long long const gid = b.id(gx, gy, gz);
   int const fm        = S::at(a, c, S::LF);
-  T const dtod        = narrow<T>(dt * (DIR == 0 ? b.idx : DIR == 1 ? b.idy : b.idz));
-  // Conservation: each face's scaled flux dtod * F is rounded the same way for both of its
-  // cells (an uncontracted product) and the cell's increment is their exact difference, summed
-  // over the three sweeps in an accumulator of at least 48 significant bits (W^n's space, 8
-  // bytes per field): FP64 in the fast FP64 form, an FP32 (hi, lo) pair built with error-free
-  // sums in the mixed form.  So the updates telescope to accumulation roundoff in both.
   Acc<T> acc[NSLOT];
 #pragma unroll
   for (int q = 0; q < NSLOT; q++) {
     int const qq = q == 1 ? o1 : q == 2 ? o2 : q == 3 ? o3 : q;  // rotated momenta back to x, y, z
-    if (live(q, b)) acc[qq] = flux_diff(dtod, Fs[q * S::NF + fm], Fs[q * S::NF + fm + S::STRIDE]);
+    if (live(q, b)) acc[qq] = scaled_diff(Fs[q * S::NF + fm], Fs[q * S::NF + fm + S::STRIDE]);
   }
   Acc<T> *__restrict__ dA = reinterpret_cast<Acc<T> *>(dU);
   if (!FIRST) {

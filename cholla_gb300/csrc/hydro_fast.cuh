@@ -95,6 +95,12 @@ __device__ __forceinline__ long long ordered_key(double a)
 }
 __device__ __forceinline__ double max_ord(double a, double b) { return ordered_key(a) < ordered_key(b) ? b : a; }
 __device__ __forceinline__ double min_ord(double a, double b) { return ordered_key(b) < ordered_key(a) ? b : a; }
+// min / max of the compute type: FP32 instructions for float; for double the ordered bit patterns
+// on the integer pipe (finite inputs), which the FP64-bound forms leave idle
+__device__ __forceinline__ float tmin(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ float tmax(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ double tmin(double a, double b) { return min_ord(a, b); }
+__device__ __forceinline__ double tmax(double a, double b) { return max_ord(a, b); }
 __device__ __forceinline__ bool is_pos(float x) { return x > 0.f; }
 __device__ __forceinline__ bool is_neg(float x) { return x < 0.f; }
 __device__ __forceinline__ bool mag_lt(float a, float b) { return fabsf(a) < fabsf(b); }
@@ -159,33 +165,41 @@ __device__ __forceinline__ double sqrtT(double x)
 }
 __device__ __forceinline__ float sqrtT(float x) { return __fsqrt_rn(x); }
 
-// PPM_Single_Variable (reconstruction.h:794-901), reciprocal-multiply form.
+// PPM_Single_Variable (reconstruction.h:794-901), reciprocal-multiply form, with the stencil's
+// one-sided differences formed once: the second differences are differences of neighbouring
+// slopes; the parabolic face value midpoint + (centred slope left - centred slope right) / 6 is
+// midpoint + (outer one-sided slope - inner one) / 12 (the centred slopes' shared term cancels);
+// the limiter's face midpoint and its curvature 3 (a_{k-1} + a_k - 2 face) = 6 (midpoint - face)
+// reuse that midpoint (algebraically the reference's expressions; they round differently only in
+// the last bits).
 template <typename T>
 __device__ __forceinline__ void ppm1(T im2, T im1, T i, T ip1, T ip2, T &L_iph, T &R_imh)
 {
-  T const C2    = T(1.25);
-  T const sixth = T(1.0 / 6.0);
-  auto limit    = [&](T ci, T cim1, T iface, T s2i, T s2im1) -> T {
-    T const s2c = T(3) * (cim1 + ci - T(2) * iface);
+  T const C2      = T(1.25);
+  T const sixth   = T(1.0 / 6.0);
+  T const twelfth = T(1.0 / 12.0);
+  auto limit      = [&](T ci, T cim1, T mid, T iface, T s2i, T s2im1) -> T {
+    T const s2c = T(6) * (mid - iface);
     T lim       = T(0);
     bool const n = is_neg(s2c);
     // sgn(s2c) min(C2 |s2im1|, C2 |s2i|, |s2c|); C2 * min(|a|, |b|) == min(C2 |a|, C2 |b|)
     if (n == is_neg(s2im1) && n == is_neg(s2i)) lim = copysign(mag_min(C2 * mag_min(s2im1, s2i), s2c), s2c);
     T const dl = iface - cim1, dr = ci - iface;
-    return prod_neg(dl, dr) ? T(0.5) * (cim1 + ci) - lim * sixth : iface;
+    return prod_neg(dl, dr) ? mid - lim * sixth : iface;
   };
+  T const sm    = im1 - im2;
   T const sl    = i - im1;
   T const sr    = ip1 - i;
-  T const sim1  = T(0.5) * (sl + (im1 - im2));
-  T const si    = T(0.5) * (sr + sl);
-  T const sip1  = T(0.5) * ((ip2 - ip1) + sr);
-  T R           = T(0.5) * (im1 + i) + (sim1 - si) * sixth;
-  T L           = T(0.5) * (i + ip1) + (si - sip1) * sixth;
-  T const d2im1 = im2 + i - T(2) * im1;
-  T const d2i   = im1 + ip1 - T(2) * i;
-  T const d2ip1 = i + ip2 - T(2) * ip1;
-  R             = limit(i, im1, R, d2i, d2im1);
-  L             = limit(ip1, i, L, d2ip1, d2i);
+  T const sp    = ip2 - ip1;
+  T const mR    = T(0.5) * (im1 + i);
+  T const mL    = T(0.5) * (i + ip1);
+  T R           = mR + (sm - sr) * twelfth;
+  T L           = mL + (sl - sp) * twelfth;
+  T const d2im1 = sl - sm;
+  T const d2i   = sr - sl;
+  T const d2ip1 = sp - sr;
+  R             = limit(i, im1, mR, R, d2i, d2im1);
+  L             = limit(ip1, i, mL, L, d2ip1, d2i);
   T const sfl   = i - R;
   T const sfr   = L - i;
   if (!prod_pos(sfl, sfr) || !prod_pos(ip1 - i, i - im1)) {
@@ -358,8 +372,8 @@ __device__ __forceinline__ void plmc_cell(LD ld, ST st, int ns, int de, T gamma)
 {
   // each interface value within the range of its two cells (Plm_Limit_Interfaces)
   auto lim = [](T &l, T &r, T vm, T vi, T vp) {
-    r = fmin(fmax(vi, vm), fmax(fmin(vi, vm), r));
-    l = fmin(fmax(vi, vp), fmax(fmin(vi, vp), l));
+    r = tmin(tmax(vi, vm), tmax(tmin(vi, vm), r));
+    l = tmin(tmax(vi, vp), tmax(tmin(vi, vp), l));
   };
   T const tiny = T(TINY);
   {
@@ -485,7 +499,7 @@ __device__ __forceinline__ void hllc_q(const Prim<T> &l, const Prim<T> &r, const
     dSl = fmin((vx - a) - l.vn, -cfl), dSr = fmax((vx + a) - r.vn, cfr);
     Sl = l.vn + dSl, Sr = r.vn + dSr;
   } else {
-    Sl = fmin(vx - a, l.vn - cfl), Sr = fmax(vx + a, r.vn + cfr);
+    Sl = tmin(vx - a, l.vn - cfl), Sr = tmax(vx + a, r.vn + cfr);
     dSl = Sl - l.vn, dSr = Sr - r.vn;
   }
   T const gel = l.ge, ger = r.ge;  // specific
@@ -522,7 +536,7 @@ __device__ __forceinline__ void hllc_q(const Prim<T> &l, const Prim<T> &r, const
     // SK - Sm from the separated parts; it is negative on the left and positive on the right,
     // and only rounding of a degenerate (both sides cold) interface can bring it to zero
     T const gap = (lft ? dSl : dSr) - (Sm - Kv);
-    T const den = lft ? fmin(gap, T(-1e-30)) : fmax(gap, T(1e-30));
+    T const den = lft ? tmin(gap, T(-1e-30)) : tmax(gap, T(1e-30));
     T const k   = SK * (Sm - Kv) * rcp(den);
     T const vk  = Kv + k;
     f[0] = Kd * vk;
@@ -558,7 +572,7 @@ __device__ __forceinline__ void roe_q(const Prim<T> &l, const Prim<T> &r, const 
   T const vx = wl * vxl + wr * vxr, vy = wl * vyl + wr * vyr, vz = wl * vzl + wr * vzr;
   T const H   = wl * Ql.h + wr * Qr.h;
   T const vsq = vx * vx + vy * vy + vz * vz;
-  T const asq = g1 * fmax(H - T(0.5) * vsq, T(TINY));
+  T const asq = g1 * max_pos(H - T(0.5) * vsq, T(TINY));
   T const a   = sqrtT(asq);
   T const lm = vx - a, l0 = vx, lp = vx + a;
   T fdl = mxl, fmxl = mxl * vxl + pl, fmyl = mxl * vyl, fmzl = mxl * vzl, fEl = (El + pl) * vxl;
@@ -610,7 +624,7 @@ __device__ __forceinline__ void roe_q(const Prim<T> &l, const Prim<T> &r, const 
   }
   if (hlle) {
     T const cfl = sqrtT(gamma * pl * idl), cfr = sqrtT(gamma * pr * idr);
-    T const bm = fmin(fmin(lm, vxl - cfl), T(0)), bp = fmax(fmax(lp, vxr + cfr), T(0));
+    T const bm = tmin(tmin(lm, vxl - cfl), T(0)), bp = tmax(tmax(lp, vxr + cfr), T(0));
     T const tmp = T(0.5) * (bp + bm) / (bp - bm);
     auto hl = [&](T fl, T fr) { return T(0.5) * (fl + fr) + (fl - fr) * tmp; };
     f[0] = hl(mxl - bm * dl, mxr - bp * dr);

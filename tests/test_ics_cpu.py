@@ -1,8 +1,10 @@
 """Initial conditions on the host: the random fields follow the stated shell spectrum, the
-turbulence box has the stated statistics, and the blast box deposits the stated energy."""
+turbulence box has the stated statistics, and the blast box deposits the stated energy; the
+accuracy report refuses an unknown FP64 baseline."""
 import math
 
 import numpy as np
+import pytest
 
 from cholla_gb300 import ics
 
@@ -44,3 +46,14 @@ def test_blast_box_deposits_the_energy():
     r = U[:, ng:-ng, ng:-ng, ng:-ng]
     excess = (r[4] - 1e-5 / (gamma - 1.0)).sum() / n ** 3
     assert abs(excess - 1.0) < 1e-12 and np.all(r[1:4] == 0) and np.all(r[0] == 1.0)
+
+
+def test_accuracy_run_rejects_an_unknown_baseline():
+    """The accuracy report's FP64 baseline is the exact or the fast FP64 form; anything else is
+    refused before any device work."""
+    import torch
+
+    from cholla_gb300 import accuracy
+
+    with pytest.raises(ValueError):
+        accuracy.run(torch, n=8, steps=1, baseline="mixed")
