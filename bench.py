@@ -453,6 +453,7 @@ def run_ours(args, world, rank, local):
                          "kernels_ms": kt, "algorithmic_bytes_per_step": corr_bytes,
                          "peak_source": f"{peak_kind} (MEASURED_PEAKS.json)",
                          "binding_ceiling": "FP64 pipe: GB300 FP64 FMA measured 1.19 TFLOP/s, divide 60 G/s"},
+            "fp64_pipe": fp64_pipe(args.precision, value / world),
             "variants": others,
             "accuracy": acc,
             "at_512": big,
@@ -601,6 +602,30 @@ def run_serving(args, torch):
                    "relative L1 over the real cells",
             "jobs": twins, "max_rel_l1": worst}
     return out
+
+
+def fp64_pipe(precision, cells_per_s):
+    """The step against the FP64-pipe ceiling: FP64-pipe instructions per real cell of one step
+    (ncu smsp__inst_executed_pipe_fp64 x 32 at 160^3, profiles/traffic.json) times the measured
+    cell updates per second, against this GPU's FP64 FMA rate measured here (cgb_selftest_fp64_rate:
+    every SM issuing independent FMA chains)."""
+    import ctypes
+
+    from cholla_gb300 import _lib as L
+
+    try:
+        per_cell = json.loads((ROOT / "profiles" / "traffic.json").read_text())["fp64_per_real_cell"][precision]
+    except Exception:
+        return None
+    rate = ctypes.c_double()
+    if L.lib().cgb_selftest_fp64_rate(12000, ctypes.byref(rate), None) != L.CGB_OK:
+        return None
+    achieved = per_cell * cells_per_s
+    return {"achieved_instr_per_s": achieved, "peak_fma_per_s": rate.value, "frac": achieved / rate.value,
+            "instructions_per_real_cell": per_cell,
+            "source": "ncu smsp__inst_executed_pipe_fp64 x 32 per real cell of one step at 160^3 "
+                      "(profiles/fast_kernels_160cube_ncu.txt) x cell updates/s; peak measured in this run "
+                      "by cgb_selftest_fp64_rate"}
 
 
 def load_traffic(n, precision):

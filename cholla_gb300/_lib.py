@@ -101,6 +101,7 @@ SIGNATURES = {
     "cgb_set_tma": (_I, [_I]),
     "cgb_batch_set_solo_cells": (_I, [_P, C.c_longlong]),
     "cgb_batch_set_tiles": (_I, [_P, _I]),
+    "cgb_selftest_fp64_rate": (_I, [_I, C.POINTER(C.c_double), _P]),
     "cgb_batch_step": (_I, [_P, _I]),
     "cgb_batch_job_time": (_I, [_P, _I, C.POINTER(_D), C.POINTER(_D)]),
     "cgb_batch_job_status": (_I, [_P, _I, C.POINTER(_I)]),

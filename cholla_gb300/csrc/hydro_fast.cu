@@ -664,7 +664,9 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
   constexpr int NT = S::NT;
   constexpr int PS = TMA ? TM::NPS : S::NP;  // P elements per slot
   constexpr int o1 = DIR + 1, o2 = (DIR + 1) % 3 + 1, o3 = (DIR + 2) % 3 + 1;
-  if (dtp) dt = *dtp;
+  // dt / dx of the sweep, formed once per block (an FP64 product) before the first barrier
+  __shared__ T sdtod;
+  if (threadIdx.x == 0) sdtod = narrow<T>((dtp ? *dtp : dt) * (DIR == 0 ? b.idx : DIR == 1 ? b.idy : b.idz));
   extern __shared__ __align__(16) unsigned char smem_raw[];
   int const ns_ = nslot(b);
   // a TMA tile copy writes to a 128-byte-aligned shared address: the P slots start at the first
@@ -792,7 +794,7 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
   // scaled fluxes, summed over the three sweeps in an accumulator of at least 48 significant bits
   // (W^n's space, 8 bytes per field): FP64 in the fast FP64 form, an FP32 (hi, lo) pair built
   // with error-free sums in the mixed form.  So the updates telescope to accumulation roundoff.
-  T const dtod = narrow<T>(dt * (DIR == 0 ? b.idx : DIR == 1 ? b.idy : b.idz));
+  T const dtod = sdtod;
   for (int f = t; f < S::NF; f += NT) {
     int a, c;
     S::split(f, S::LF, a, c);  // face a lies between sweep positions a - 1 and a

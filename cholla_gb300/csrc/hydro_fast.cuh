@@ -53,6 +53,32 @@ __device__ __forceinline__ float to_f32(double x)
   return (float)x;
 }
 
+// Seeds of the FP64 reciprocal and square root: the same conversions for operands already known
+// to lie well inside the binary32 normal range (the callers check the binary64 exponent first), so
+// with no fallback at all; narrowing truncates (the refinement that follows absorbs the extra half
+// ulp).  Measured at 256^3 in the fast FP64 form: the hardware fallback of the general conversions,
+// although never taken there, still cost 3% of the step, and a general all-integer conversion (with
+// zeros, subnormals, infinities and NaNs on the integer pipe) slowed the mixed form and the MHD
+// kernels.
+__device__ __forceinline__ float seed_f32(double x)
+{
+  unsigned const hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  unsigned const e  = (hi >> 20) & 0x7ffu;
+  return __uint_as_float((hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29));
+}
+__device__ __forceinline__ double seed_f64(float f)
+{
+  unsigned const u = __float_as_uint(f);
+  return __hiloint2double((int)((u & 0x80000000u) | ((((u >> 23) & 0xffu) + 896u) << 20) | ((u & 0x7fffffu) >> 3)),
+                          (int)(u << 29));
+}
+// |x| in [2^-99, 2^99): the range where the seeds and their refinements stay far from overflow
+// and underflow (an exponent test on the integer pipe)
+__device__ __forceinline__ bool seed_range(double x)
+{
+  return ((((unsigned)__double2hiint(x) >> 20) & 0x7ffu) - 924u) < 198u;
+}
+
 // Comparisons of the limiters.  For double they run on the integer pipes, on the IEEE bit
 // patterns: the step is bound by the FP64 pipe, where every compare and min/max is a full-rate
 // FP64 instruction (DSETP), while the integer pipes sit idle.  Results equal the FP64
@@ -141,13 +167,12 @@ struct Eps<float> {
 // s + (x - s^2) y / 2 (Karp and Markstein, "High-precision division and square root", ACM TOMS
 // 23(4), 1997), which squares that error.  Both stay within 1 ulp of the correctly rounded result,
 // which cgb_selftest_fast_math measures against CUDA's 1 / x and sqrt over the FP32 exponent
-// range.  Outside |x| in (1e-30, 1e30) a true divide / square root is used.  FP32: the hardware
-// approximations (about 1 ulp).
+// range.  Outside |x| in [2^-99, 2^99) (and for x <= 0 in the square root) a true divide / square
+// root is used.  FP32: the hardware approximations (about 1 ulp).
 __device__ __forceinline__ double rcp(double d)
 {
-  float const f = to_f32(d);
-  if (!(fabsf(f) > 1e-30f && fabsf(f) < 1e30f)) return 1.0 / d;
-  double const r = to_f64(__frcp_rn(f));
+  if (!seed_range(d)) return 1.0 / d;
+  double const r = seed_f64(__frcp_rn(seed_f32(d)));
   double const e = fma(-d, r, 1.0);
   return fma(r, fma(e, e, e), r);
 }
@@ -155,9 +180,8 @@ __device__ __forceinline__ float rcp(float d) { return __frcp_rn(d); }
 
 __device__ __forceinline__ double sqrtT(double x)
 {
-  float const f = to_f32(x);
-  if (!(f > 1e-30f && f < 1e30f)) return sqrt(x);
-  double y       = to_f64(rsqrtf(f));
+  if (!(seed_range(x) && is_pos(x))) return sqrt(x);
+  double y       = seed_f64(rsqrtf(seed_f32(x)));
   double const h = 0.5 * x;
   y              = y * fma(-h * y, y, 1.5);
   double const s = x * y;

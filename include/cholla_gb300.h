@@ -259,17 +259,22 @@ const char *cgb_batch_last_error(void);
  * the hardware conversions, on the n doubles at d_values (and the binary32 in each low word);
  * mismatches[0] (narrowing) and [1] (widening) receive the counts.  Synchronises `stream`. ---- */
 int cgb_selftest_conversions(const double *d_values, long long n, unsigned long long *mismatches, void *stream);
-/* ---- self-check: the fast FP64 form's reciprocal and square root (an FP32 estimate refined by Newton
- * steps) beside CUDA's correctly rounded ones, on the n doubles at d_values: d_out[0..n) the fast
+/* ---- self-check: the fast FP64 form's reciprocal and square root (an FP32 estimate refined in FP64)
+ * beside CUDA's correctly rounded ones, on the n doubles at d_values: d_out[0..n) the fast
  * 1/x, [n..2n) CUDA's 1/x, [2n..3n) the fast sqrt(|x|), [3n..4n) CUDA's sqrt(|x|).  Synchronises
  * `stream`. ---- */
 int cgb_selftest_fast_math(const double *d_values, long long n, double *d_out, void *stream);
+/* FP64 fused multiply-adds per second of the whole GPU (8 blocks per SM of 256 threads, each 8
+ * independent FMA chains of `iters` steps), timed with events on `stream`: the FP64-pipe ceiling
+ * that the FP64 forms' kernels are measured against. */
+int cgb_selftest_fp64_rate(int iters, double *fma_per_s, void *stream);
 /* ---- self-check of the bounded waits: a kernel whose mbarrier expects bytes that no copy delivers
  * waits `limit` polls, gives up, and writes CGB_STATUS_TIMEOUT to *d_status (device int); no copy is
  * ever issued, so nothing is left in flight.  Synchronises `stream`. ---- */
 int cgb_selftest_tma_timeout(int *d_status, unsigned limit, void *stream);
 /* ---- TMA staging of the fast forms' 3D corrector sweeps: on (1, default) or off (0: every thread
- * loads its share of the tile).  The results are the same bit for bit either way. ---- */
+ * loads its share of the tile).  The two are separate kernels of the same tile code and agree to
+ * rounding (the code generator contracts a few products differently in each). ---- */
 int cgb_set_tma(int enable);
 
 /* ---- fault injection for tests (no counterpart in the reference): the n-th device allocation the

@@ -2,7 +2,7 @@
 rcp, an FP32 estimate and one third-order iteration r (1 + e + e^2); sqrtT, one Newton-Raphson
 step on the inverse square root and the Karp-Markstein correction) against CUDA's correctly rounded 1 / x and
 sqrt, measured in units in the last place over the FP32 exponent range and on both sides of the
-1e-30 / 1e30 guards, where the helpers switch to the true divide and square root."""
+2^-99 / 2^99 guards, where the helpers switch to the true divide and square root."""
 import numpy as np
 import pytest
 
@@ -18,7 +18,8 @@ def _inputs():
     mag = 10.0 ** rng.uniform(-38, 38, 400_000)  # beyond the guards on both sides
     x = mag * np.where(rng.random(mag.size) < 0.5, -1.0, 1.0)
     edges = []
-    for e in (1e-30, 1e30, 1.0, 2.0, 0.5, np.float64(np.float32(1e-30)), np.float64(np.float32(1e30))):
+    for e in (1e-30, 1e30, 1.0, 2.0, 0.5, np.float64(np.float32(1e-30)), np.float64(np.float32(1e30)),
+              np.ldexp(1.0, -99), np.ldexp(1.0, 99)):
         edges += list(np.nextafter(e, 0) * np.array([1.0, -1.0])) + [e, -e] + list(np.nextafter(e, np.inf) *
                                                                                 np.array([1.0, -1.0]))
         edges += list(e * (1 + np.arange(-40, 41) * 2.0 ** -30))
