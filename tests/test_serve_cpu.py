@@ -90,3 +90,36 @@ def test_fcfs_runs_the_earliest_jobs_up_to_the_saturation_cap():
     assert _sched("fcfs", 1).running(active) == [0]  # at least one job
     assert _sched("fcfs", 10 ** 12).running(active) == [0, 1, 2, 3, 4]
     assert _sched("all", 1).running(active) == [0, 1, 2, 3, 4]
+
+
+def test_sweep_aggregates_every_seed_and_ratio(monkeypatch):
+    """serve.sweep runs every mode on the same seeded streams and reports, per rate, the mean over
+    seeds and the batched server's per-seed ratios as [min, mean, max] (throughput batched /
+    per-request, p99 per-request / batched): checked with a fake `serve` whose numbers are known."""
+    table = {  # (mode, seed) -> (throughput, p50, p99)
+        ("batched", 1): (2.0, 10.0, 20.0), ("batched", 2): (3.0, 12.0, 30.0),
+        ("per_request", 1): (1.0, 20.0, 40.0), ("per_request", 2): (2.0, 30.0, 60.0),
+        ("per_request_graph", 1): (2.0, 15.0, 20.0), ("per_request_graph", 2): (1.5, 18.0, 45.0),
+    }
+    calls = []
+
+    def fake_serve(torch, reqs, mode="batched", **kw):
+        calls.append((mode, len(reqs)))
+        if len(reqs) == 6:  # the warm-up stream
+            return {"cell_updates_per_s": 1.0, "p50_ms": 1.0, "p99_ms": 1.0}
+        key = (mode, 1 if reqs[0].seed == serve.make_requests(5.0, 3, seed=1)[0].seed else 2)
+        t, p50, p99 = table[key]
+        return {"cell_updates_per_s": t, "p50_ms": p50, "p99_ms": p99, **({"tuned": {"chains": 1}} if mode == "batched" else {})}
+
+    monkeypatch.setattr(serve, "serve", fake_serve)
+    out = serve.sweep(None, [5.0], [3], [1, 2])
+    row = out["5"]
+    assert row["requests"] == 3 and row["seeds"] == [1, 2]
+    assert row["batched"]["cell_updates_per_s"] == 2.5 and row["per_request"]["p99_ms"] == 50.0
+    assert row["batched"]["per_seed"] == [[2.0, 10.0, 20.0], [3.0, 12.0, 30.0]]
+    assert row["batched"]["tuned"] == {"chains": 1}
+    assert row["vs_per_request"]["throughput_ratio"] == [1.5, 1.75, 2.0]
+    assert row["vs_per_request"]["p99_ratio"] == [2.0, 2.0, 2.0]
+    assert row["vs_per_request_graph"]["throughput_ratio"] == [1.0, 1.5, 2.0]
+    assert row["vs_per_request_graph"]["p99_ratio"] == [1.0, 1.25, 1.5]
+    assert sum(1 for m, n in calls if n == 3) == 6  # three modes x two seeds
