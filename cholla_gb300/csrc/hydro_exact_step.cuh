@@ -496,6 +496,18 @@ __global__ void __launch_bounds__(TX *TY *TZ, 2) k_corrector(Box b, const double
 // y sweep adds its own (acc + d), the z sweep adds its own and writes U + acc with the floor
 // and the pre-sync energy, exactly as the fused kernel's register accumulator does.
 // ------------------------------------------------------------------------------------------
+// exact sweeps' tiles (compile-time tunables): x sweep cells per pencil and pencils along y and
+// z, y and z sweeps cells per pencil and x-adjacent pencils
+#ifndef CGB_XSWEEP_XL
+#define CGB_XSWEEP_XL 64
+#define CGB_XSWEEP_XA 2
+#define CGB_XSWEEP_XB 2
+#define CGB_XSWEEP_YL 32
+#define CGB_XSWEEP_YA 8
+#endif
+constexpr int XSW_XL = CGB_XSWEEP_XL, XSW_XA = CGB_XSWEEP_XA, XSW_XB = CGB_XSWEEP_XB;
+constexpr int XSW_YL = CGB_XSWEEP_YL, XSW_YA = CGB_XSWEEP_YA;
+
 template <int DIR, int L, int WA, int WB, int RECON>
 struct XSweep {
   static constexpr int H  = Halo<RECON>::H;
@@ -734,9 +746,11 @@ template <int RECON, int SOLVER>
 cudaError_t launch_xsweeps(const Box &b, double *U, const Scratch &sc, double dt, const double *dtp, cudaStream_t s)
 {
   double *A     = static_cast<double *>(sc.W);
-  cudaError_t e = launch_xsweep<0, 64, 2, 2, RECON, SOLVER, true, false>(b, sc.Uh, A, U, sc, dt, dtp, s);
-  if (e == cudaSuccess) e = launch_xsweep<1, 32, 8, 1, RECON, SOLVER, false, false>(b, sc.Uh, A, U, sc, dt, dtp, s);
-  if (e == cudaSuccess) e = launch_xsweep<2, 32, 8, 1, RECON, SOLVER, false, true>(b, sc.Uh, A, U, sc, dt, dtp, s);
+  cudaError_t e = launch_xsweep<0, XSW_XL, XSW_XA, XSW_XB, RECON, SOLVER, true, false>(b, sc.Uh, A, U, sc, dt, dtp, s);
+  if (e == cudaSuccess)
+    e = launch_xsweep<1, XSW_YL, XSW_YA, 1, RECON, SOLVER, false, false>(b, sc.Uh, A, U, sc, dt, dtp, s);
+  if (e == cudaSuccess)
+    e = launch_xsweep<2, XSW_YL, XSW_YA, 1, RECON, SOLVER, false, true>(b, sc.Uh, A, U, sc, dt, dtp, s);
   return e;
 }
 

@@ -502,8 +502,6 @@ __device__ __forceinline__ void hllc_q(const Prim<T> &l, const Prim<T> &r, const
                                        T *f, int ns, int de, T gamma)
 {
   T const g1  = gamma - T(1);
-  T const mxl = l.d * l.vn, myl = l.d * l.vt1, mzl = l.d * l.vt2;
-  T const mxr = r.d * r.vn, myr = r.d * r.vt1, mzr = r.d * r.vt2;
   T const El = Ql.E, Er = Qr.E, pl = Ql.p, pr = Qr.p;
   T const sqrtdl = Ql.sq, sqrtdr = Qr.sq;
   T const isum   = rcp(sqrtdl + sqrtdr);
@@ -526,23 +524,6 @@ __device__ __forceinline__ void hllc_q(const Prim<T> &l, const Prim<T> &r, const
     Sl = tmin(vx - a, l.vn - cfl), Sr = tmax(vx + a, r.vn + cfr);
     dSl = Sl - l.vn, dSr = Sr - r.vn;
   }
-  T const gel = l.ge, ger = r.ge;  // specific
-  if (is_pos(Sl)) {
-    f[0] = mxl, f[1] = mxl * l.vn + pl, f[2] = myl * l.vn, f[3] = mzl * l.vn, f[4] = (El + pl) * l.vn;
-#pragma unroll
-    for (int k = 0; k < NS_MAX; k++)
-      if (k < ns) f[6 + k] = mxl * l.sc[k];
-    if (de) f[5] = mxl * gel;
-    return;
-  }
-  if (is_neg(Sr)) {
-    f[0] = mxr, f[1] = mxr * r.vn + pr, f[2] = myr * r.vn, f[3] = mzr * r.vn, f[4] = (Er + pr) * r.vn;
-#pragma unroll
-    for (int k = 0; k < NS_MAX; k++)
-      if (k < ns) f[6 + k] = mxr * r.sc[k];
-    if (de) f[5] = mxr * ger;
-    return;
-  }
   T const ql = l.d * dSl, qr = r.d * dSr;  // mass fluxes relative to the outer waves
   T const Sm  = (qr * r.vn - ql * l.vn + pl - pr) * rcp(qr - ql);
   {
@@ -552,14 +533,17 @@ __device__ __forceinline__ void hllc_q(const Prim<T> &l, const Prim<T> &r, const
     // k = SK (Sm - vK) / (SK - Sm).  Only the upwind star state is formed, and the symmetric
     // sum's subtraction of terms of the size of the wave speeds (~1e9 next to a near-vacuum
     // interface state, density floored at TINY) is avoided: in FP32 that cancellation costs
-    // every significant digit, in FP64 about nine.
-    bool const lft = !is_neg(Sm);  // Sm >= 0
+    // every significant digit, in FP64 about nine.  The supersonic cases (Sl > 0: FL; Sr < 0: FR)
+    // take the same instructions with SK = 0, which makes k = 0 and the flux FK, so the lanes of
+    // a warp do not split on the local Mach number.
+    bool const sup = is_pos(Sl) || is_neg(Sr);
+    bool const lft = is_pos(Sl) || (!is_neg(Sr) && !is_neg(Sm));
     // field-by-field selects (a reference to l or r would put both states in local memory)
     T const Kd = lft ? l.d : r.d, Kv = lft ? l.vn : r.vn, Kt1 = lft ? l.vt1 : r.vt1, Kt2 = lft ? l.vt2 : r.vt2;
-    T const SK = lft ? Sl : Sr, EK = lft ? El : Er, pK = lft ? pl : pr;
+    T const SK = sup ? T(0) : (lft ? Sl : Sr), EK = lft ? El : Er, pK = lft ? pl : pr;
     // SK - Sm from the separated parts; it is negative on the left and positive on the right,
     // and only rounding of a degenerate (both sides cold) interface can bring it to zero
-    T const gap = (lft ? dSl : dSr) - (Sm - Kv);
+    T const gap = (sup ? -Kv : (lft ? dSl : dSr)) - (Sm - Kv);
     T const den = lft ? tmin(gap, T(-1e-30)) : tmax(gap, T(1e-30));
     T const k   = SK * (Sm - Kv) * rcp(den);
     T const vk  = Kv + k;
