@@ -490,8 +490,11 @@ __device__ __forceinline__ void fpred_tile(const Box &b, const double *__restric
 #ifndef CGB_PRED_MINB_F32
 #define CGB_PRED_MINB_F32 2  // resident predictor blocks per SM the FP32 register budget targets
 #endif
+#ifndef CGB_PRED_MINB_F64
+#define CGB_PRED_MINB_F64 2  // the same for FP64 compute
+#endif
 template <typename T, int TX, int TY, int TZ, int SOLVER>
-__global__ void __launch_bounds__(TX *TY *TZ, sizeof(T) == 4 ? CGB_PRED_MINB_F32 : 2)
+__global__ void __launch_bounds__(TX *TY *TZ, sizeof(T) == 4 ? CGB_PRED_MINB_F32 : CGB_PRED_MINB_F64)
     k_fpred(Box b, const double *__restrict__ U, const T *__restrict__ Wn, T *__restrict__ W, double *__restrict__ GEp,
             double dt, const double *__restrict__ dtp)
 {
