@@ -90,6 +90,12 @@ def test_step_rejects_bad_arguments_before_device_work(lib):
     assert rc == I.CGB_ERR_ARGS
     arr = (C.c_int * 6)(1, 1, 1, 1, 9, 1)
     assert lib.cgb_set_boundaries(C.c_void_p(16), 8, 8, 8, 2, 6, arr) == I.CGB_ERR_ARGS
+    # self-tests refuse bad arguments before any CUDA call
+    rate = C.c_double()
+    assert lib.cgb_selftest_fp64_rate(0, C.byref(rate), None) == I.CGB_ERR_ARGS
+    assert lib.cgb_selftest_fp64_rate(100, None, None) == I.CGB_ERR_ARGS
+    assert lib.cgb_selftest_fast_math(None, 4, None, None) == I.CGB_ERR_ARGS
+    assert lib.cgb_selftest_tma_timeout(None, 10, None) == I.CGB_ERR_ARGS
 
 
 def test_product_has_no_oracle_dependency():
