@@ -1,6 +1,6 @@
 // hydro_fast.cuh -- the VL hydro arithmetic reformulated for GB300's ALU balance.
 //
-// Same scheme as hydro_math.cuh (PPMC / PLMC / PCM, HLLC / Roe, dual energy), same limiter
+// Same scheme as hydro_math.cuh (PPMC / PLMC / PCM, HLLC / Roe / HLL, dual energy), same limiter
 // decisions, but written for throughput: every quotient by a shared denominator becomes one
 // reciprocal and multiplies, primitives are computed once per cell instead of once per
 // stencil use, constant divisions are multiplications, the Riemann solvers take primitive
@@ -561,6 +561,55 @@ template <typename T>
 __device__ __forceinline__ void hllc(const Prim<T> &l, const Prim<T> &r, T *f, int ns, int de, T gamma, T ig1)
 {
   hllc_q(l, r, side_q<T, true>(l, de, gamma, ig1), side_q<T, true>(r, de, gamma, ig1), f, ns, de, gamma);
+}
+
+// HLL flux (hll_cuda.cu:19-268) from primitive interface states; f in the slots of hllc_q.  The
+// outer wave speeds are Davis's, Sl = min(vL - cL, vR - cR) and Sr = max(vL + cL, vR + cR), from
+// each side's velocity and sound speed of its used pressure (hll_cuda.cu:162-174).  The two-wave
+// flux F = (Sr FL - Sl FR + Sl Sr (UR - UL)) / (Sr - Sl) of a quantity X carried with the mass
+// (1, the velocities, GasEnergy and the scalars per unit mass: flux dK vK XK, state dK XK) is
+//   F = dL bL XL + dR bR XR,  bL = Sr (vL - Sl) / (Sr - Sl),  bR = Sl (Sr - vR) / (Sr - Sl),
+// plus wL pL + wR pR in the normal momentum and bL EL + bR ER + wL pL vL + wR pR vR in the energy,
+// with wL = Sr / (Sr - Sl) and wR = -Sl / (Sr - Sl) (expand the products to check).  vL - Sl >= cL
+// and Sr - vR >= cR come from the separated parts, as in hllc_q, so no difference of wave-speed
+// sized terms is formed.  Supersonic faces (Sl > 0: FL; Sr < 0: FR) take the same instructions
+// with the weights selected (wL = 1, bL = vL, wR = bR = 0, or the mirror image), so the lanes of
+// a warp do not split on the local Mach number.
+template <typename T>
+__device__ __forceinline__ void hll_q(const Prim<T> &l, const Prim<T> &r, const SideQ<T> &Ql, const SideQ<T> &Qr,
+                                      T *f, int ns, int de)
+{
+  T const cl = Ql.c, cr = Qr.c;
+  T Sl, Sr, dSl, dSr;  // dSl = Sl - vL <= -cL, dSr = Sr - vR >= cR
+  if constexpr (std::is_same<T, float>::value) {
+    dSl = tmin((r.vn - cr) - l.vn, -cl), dSr = tmax((l.vn + cl) - r.vn, cr);
+    Sl = l.vn + dSl, Sr = r.vn + dSr;
+  } else {
+    Sl = tmin(r.vn - cr, l.vn - cl), Sr = tmax(l.vn + cl, r.vn + cr);
+    dSl = Sl - l.vn, dSr = Sr - r.vn;
+  }
+  T const inv  = rcp(tmax(Sr - Sl, T(1e-30)));  // Sr - Sl >= cL + cR > 0 but for rounding
+  bool const upl = is_pos(Sl), upr = !upl && is_neg(Sr);
+  T const wl   = upl ? T(1) : (upr ? T(0) : Sr * inv);
+  T const wr   = upl ? T(0) : (upr ? T(1) : -Sl * inv);
+  T const bl   = upl ? l.vn : (upr ? T(0) : -(Sr * dSl) * inv);
+  T const br   = upl ? T(0) : (upr ? r.vn : (Sl * dSr) * inv);
+  T const al = l.d * bl, ar = r.d * br;
+  f[0] = al + ar;
+  f[1] = al * l.vn + ar * r.vn + (wl * Ql.p + wr * Qr.p);
+  f[2] = al * l.vt1 + ar * r.vt1;
+  f[3] = al * l.vt2 + ar * r.vt2;
+  f[4] = bl * Ql.E + br * Qr.E + (wl * Ql.p * l.vn + wr * Qr.p * r.vn);
+#pragma unroll
+  for (int q = 0; q < NS_MAX; q++)
+    if (q < ns) f[6 + q] = al * l.sc[q] + ar * r.sc[q];
+  if (de) f[5] = al * l.ge + ar * r.ge;
+}
+
+template <typename T>
+__device__ __forceinline__ void hll(const Prim<T> &l, const Prim<T> &r, T *f, int ns, int de, T gamma, T ig1)
+{
+  hll_q(l, r, side_q<T, true>(l, de, gamma, ig1), side_q<T, true>(r, de, gamma, ig1), f, ns, de);
 }
 
 // Roe flux with the HLLE fallback (roe_cuda.cu:19-400) from primitive interface states.

@@ -28,9 +28,9 @@ def _run_pair(cuda, oracle_lib, U0, ng, scheme, steps, dx):
     I.set_scheme(scheme)
     Ug = cuda.from_numpy(U0.copy()).cuda()
     Uo = U0.copy()
-    cfg = o.config(nx, ny, nz, ng, nf, de=scheme.dual_energy,
+    cfg = o.config(nx, ny, nz, ng, nf, de=scheme.dual_energy, n_scalars=scheme.n_scalars,
                    recon={"PCM": o.PCM, "PLMC": o.PLMC, "PPMC": o.PPMC}[scheme.reconstruction],
-                   solver={"HLLC": o.HLLC, "ROE": o.ROE}[scheme.riemann_solver], gamma=scheme.gamma,
+                   solver={"HLLC": o.HLLC, "ROE": o.ROE, "HLL": o.HLL}[scheme.riemann_solver], gamma=scheme.gamma,
                    dx=dx[0], dy=dx[1], dz=dx[2])
     for _ in range(steps):
         dt = 0.3 / o.calc_dt(cfg, Uo.reshape(-1))  # same dt sequence for both (the oracle's)
@@ -42,7 +42,7 @@ def _run_pair(cuda, oracle_lib, U0, ng, scheme, steps, dx):
 
 
 @pytest.mark.parametrize("recon", ["PCM", "PLMC", "PPMC"])
-@pytest.mark.parametrize("solver", ["HLLC", "ROE"])
+@pytest.mark.parametrize("solver", ["HLLC", "ROE", "HLL"])
 def test_fast_fp64_one_step(cuda, oracle_lib, recon, solver):
     from cholla_gb300 import ics
     from cholla_gb300 import integrator as I
@@ -53,6 +53,24 @@ def test_fast_fp64_one_step(cuda, oracle_lib, recon, solver):
     got, want = _run_pair(cuda, oracle_lib, U0, ng, s, 1, (1 / 19, 1 / 13, 1 / 11))
     err = rel_l1(got, want, ng)
     assert np.all(err <= 1e-12), dict(zip(FIELDS, err))
+
+
+@pytest.mark.parametrize("precision,tol", [("fp64_fast", 1e-12), ("mixed", 1e-5)])
+def test_hll_with_scalars_five_steps(cuda, oracle_lib, precision, tol):
+    """HLL in the throughput forms with two passive scalars and dual energy, 5 steps against the
+    oracle: every field within 1e-12 relative L1 (fast FP64), density within 1e-5 (mixed)."""
+    from cholla_gb300 import ics
+    from cholla_gb300 import integrator as I
+
+    ng = 4
+    U0 = ics.smooth_random_box((17, 14, 12), ng, np.random.default_rng(11), dual_energy=True, n_scalars=2)
+    s = I.Scheme(reconstruction="PPMC", riemann_solver="HLL", dual_energy=True, n_scalars=2, precision=precision)
+    got, want = _run_pair(cuda, oracle_lib, U0, ng, s, 5, (1 / 17, 1 / 14, 1 / 12))
+    err = rel_l1(got, want, ng)
+    names = FIELDS[:5] + ["scalar_0", "scalar_1", "GasEnergy"]
+    print(precision, {f: f"{e:.2e}" for f, e in zip(names, err)})
+    assert np.isfinite(got).all()
+    assert np.all(err <= tol) if precision == "fp64_fast" else err[0] <= tol, dict(zip(names, err))
 
 
 def test_fast_fp64_turbulence_20_steps(cuda, oracle_lib):
@@ -70,8 +88,8 @@ def test_fast_fp64_turbulence_20_steps(cuda, oracle_lib):
     assert np.all(err <= 1e-12), dict(zip(FIELDS, err))
 
 
-@pytest.mark.parametrize("seed,mach", [(4, 2.0), (6, 3.0)])
-def test_mixed_turbulence_20_steps(cuda, oracle_lib, seed, mach):
+@pytest.mark.parametrize("seed,mach,solver", [(4, 2.0, "HLLC"), (6, 3.0, "HLLC"), (4, 2.0, "HLL")])
+def test_mixed_turbulence_20_steps(cuda, oracle_lib, seed, mach, solver):
     """Mixed precision, 20 steps of rms-Mach-2 and -3 turbulence boxes: finite everywhere and
     relative L1 density error <= 1e-5 (the accuracy target of the mixed-precision form)."""
     from cholla_gb300 import ics
@@ -79,10 +97,10 @@ def test_mixed_turbulence_20_steps(cuda, oracle_lib, seed, mach):
 
     n, ng = 32, 4
     U0 = ics.turbulence_box(n, ng, 5 / 3, seed=seed, mach=mach)
-    s = I.Scheme(reconstruction="PPMC", riemann_solver="HLLC", dual_energy=True, precision="mixed")
+    s = I.Scheme(reconstruction="PPMC", riemann_solver=solver, dual_energy=True, precision="mixed")
     got, want = _run_pair(cuda, oracle_lib, U0, ng, s, 20, (1 / n,) * 3)
     err = rel_l1(got, want, ng)
-    print(f"mixed seed {seed} mach {mach}", {f: f"{e:.2e}" for f, e in zip(FIELDS, err)})
+    print(f"mixed {solver} seed {seed} mach {mach}", {f: f"{e:.2e}" for f, e in zip(FIELDS, err)})
     assert np.isfinite(got).all()
     assert err[0] <= 1e-5, dict(zip(FIELDS, err))
 
