@@ -181,9 +181,9 @@ int cgb_batch_create(cgb_batch **out, const cgb_scheme *scheme, double c_cfl, vo
   if (s.reconstruction < CGB_PCM || s.reconstruction > CGB_PPMP || s.riemann_solver < CGB_HLLC ||
       s.riemann_solver > CGB_EXACT)
     return bfail(CGB_ERR_ARGS, "bad reconstruction or riemann solver");
-  if (s.reconstruction >= CGB_PLMP || s.riemann_solver == CGB_EXACT)
-    return bfail(CGB_ERR_UNSUPPORTED, "batches run the fast forms, which do not build PLMP, PPMP or the exact "
-                                      "solver (the exact FP64 form does: cgb_box / cgb_vl_algorithm_3d)");
+  if (s.riemann_solver == CGB_EXACT)
+    return bfail(CGB_ERR_UNSUPPORTED, "batches run the fast forms, which do not build the exact Riemann solver (the "
+                                      "exact FP64 form does: cgb_box / cgb_vl_algorithm_3d)");
   if (s.mhd || s.riemann_solver == CGB_HLLD) return bfail(CGB_ERR_UNSUPPORTED, "batches are hydro only");
   if (s.precision != CGB_MIXED && s.precision != CGB_FP64_FAST)
     return bfail(CGB_ERR_UNSUPPORTED, "batches run the fast FP64 or the mixed-precision form");
@@ -249,7 +249,9 @@ int cgb_batch_add(cgb_batch *bt, double *d_conserved, int nx, int ny, int nz, in
   std::lock_guard<std::mutex> lk(bt->mu);
   if ((int)bt->jobs.size() >= cgb::BATCH_MAX_JOBS) return bfail(CGB_ERR_ARGS, "batch is full");
   cgb_scheme const &s = bt->scheme;
-  int const H = s.reconstruction == CGB_PPMC ? 4 : s.reconstruction == CGB_PLMC ? 3 : 2;
+  int const H = (s.reconstruction == CGB_PPMC || s.reconstruction == CGB_PPMP)   ? 4
+                : (s.reconstruction == CGB_PLMC || s.reconstruction == CGB_PLMP) ? 3
+                                                                                 : 2;
   if (ny < 2 || nz < 2) return bfail(CGB_ERR_ARGS, "batches hold 3D boxes");
   if (n_ghost < H || nx < 2 * n_ghost + 1 || ny < 2 * n_ghost + 1 || nz < 2 * n_ghost + 1)
     return bfail(CGB_ERR_ARGS, "box too small for the reconstruction stencil");

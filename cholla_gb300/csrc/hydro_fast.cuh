@@ -127,6 +127,10 @@ __device__ __forceinline__ float tmin(float a, float b) { return fminf(a, b); }
 __device__ __forceinline__ float tmax(float a, float b) { return fmaxf(a, b); }
 __device__ __forceinline__ double tmin(double a, double b) { return min_ord(a, b); }
 __device__ __forceinline__ double tmax(double a, double b) { return max_ord(a, b); }
+// a > b of the compute type (for double on the integer pipe, finite inputs; -0 orders below +0,
+// which changes no comparison below, whose sides are never a -0 / +0 pair of opposite meaning)
+__device__ __forceinline__ bool tgt(double a, double b) { return ordered_key(a) > ordered_key(b); }
+__device__ __forceinline__ bool tgt(float a, float b) { return a > b; }
 __device__ __forceinline__ bool is_pos(float x) { return x > 0.f; }
 __device__ __forceinline__ bool is_neg(float x) { return x < 0.f; }
 __device__ __forceinline__ bool mag_lt(float a, float b) { return fabsf(a) < fabsf(b); }
@@ -438,6 +442,80 @@ __device__ __forceinline__ void plmc_cell(LD ld, ST st, int ns, int de, T gamma)
 #pragma unroll
   for (int k = 0; k < NS_MAX; k++)
     if (k < ns) plain(6 + k);
+}
+
+// Van Leer-limited slope of a three-point stencil (plmp_cuda.cu:330-365 Interface_Values_PLM,
+// ppmp_cuda.cu:687-720 Calculate_Slope): sgn(centred) min(2 min(|dl|, |dr|), |centred|, |harmonic|),
+// the harmonic mean 2 dl dr / (dl + dr) taken where dl and dr have one sign.
+template <typename T>
+__device__ __forceinline__ T prim_slope(T qm, T q, T qp)
+{
+  T const dl = q - qm, dr = qp - q, dc = T(0.5) * (qp - qm);
+  T const dg = prod_pos(dl, dr) ? T(2) * dl * dr * rcp(dl + dr) : T(0);
+  T const m  = mag_min(T(2) * mag_min(dl, dr), mag_min(dc, dg));
+  return is_neg(dc) ? -m : m;
+}
+
+// PLMP_cuda for one cell under VL (plmp_cuda.cu, no half-step evolution): every primitive on its
+// own, faces at the centre value plus and minus half its limited slope, density and pressure
+// floored at TINY.  Streamed as plmc_cell: ld(j, s) for j = -1 .. 1, st(s, high face, low face).
+template <typename T, typename LD, typename ST>
+__device__ __forceinline__ void plmp_cell(LD ld, ST st, int ns, int de)
+{
+  auto one = [&](int s, bool floor) {
+    T const c = ld(0, s);
+    T const h = T(0.5) * prim_slope(ld(-1, s), c, ld(1, s));
+    T L = c + h, R = c - h;
+    if (floor) L = max_pos(L, T(TINY)), R = max_pos(R, T(TINY));
+    st(s, L, R);
+  };
+  one(0, true);
+  one(1, false);
+  one(2, false);
+  one(3, false);
+  one(4, true);
+  if (de) one(5, false);
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++)
+    if (k < ns) one(6 + k, false);
+}
+
+// PPMP_cuda for one cell under VL (ppmp_cuda.cu:727-752 Interface_Values_PPM, Fryxell et al. 2000,
+// without flattening or steepening, as the reference builds it): the parabola through the cell
+// from its neighbours' limited slopes, then its monotonicity constraints.  The two overshoot
+// corrections are selects on one evaluation of the test: the second cannot hold after the first
+// has moved the low face (then 6 (R - L)(q - (L + R)/2) = 9 (R - q)^2 >= 0 > -(R - L)^2).
+// Streamed as ppmc_cell: ld(j, s) for j = -2 .. 2, st(s, high face, low face).
+template <typename T, typename LD, typename ST>
+__device__ __forceinline__ void ppmp_cell(LD ld, ST st, int ns, int de)
+{
+  T const sixth = T(1.0 / 6.0);
+  auto one      = [&](int s, bool floor) {
+    T const q0 = ld(-2, s), qm = ld(-1, s), q = ld(0, s), qp = ld(1, s), q4 = ld(2, s);
+    T const sm = prim_slope(q0, qm, q), s0 = prim_slope(qm, q, qp), sp = prim_slope(q, qp, q4);
+    T L = T(0.5) * (q + qm) - sixth * (s0 - sm);
+    T R = T(0.5) * (qp + q) - sixth * (sp - s0);
+    bool const flat = !prod_pos(R - q, q - L);  // (R - q)(q - L) <= 0: a local extremum
+    L = flat ? q : L;
+    R = flat ? q : R;
+    T const dRL = R - L, lhs = T(6) * dRL * (q - T(0.5) * (L + R)), sq = dRL * dRL;
+    bool const lo = tgt(lhs, sq), hi = !lo && tgt(-sq, lhs);
+    T const Lc = lo ? T(3) * q - T(2) * R : L;
+    T const Rc = hi ? T(3) * q - T(2) * L : R;
+    L = tmin(tmax(q, qm), tmax(tmin(q, qm), Lc));
+    R = tmin(tmax(q, qp), tmax(tmin(q, qp), Rc));
+    if (floor) L = max_pos(L, T(TINY)), R = max_pos(R, T(TINY));
+    st(s, R, L);
+  };
+  one(0, true);
+  one(1, false);
+  one(2, false);
+  one(3, false);
+  one(4, true);
+  if (de) one(5, false);
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++)
+    if (k < ns) one(6 + k, false);
 }
 
 // u / e > eta without the division, keeping the quotient's sign behaviour: the total energy

@@ -527,7 +527,9 @@ __global__ void __launch_bounds__(TX *TY *TZ, sizeof(T) == 4 ? CGB_PRED_MINB_F32
 // ------------------------------------------------------------------------------------------
 template <int RECON>
 struct FHalo {
-  static constexpr int H = RECON == RECON_PPMC ? 3 : (RECON == RECON_PLMC ? 2 : 1);
+  static constexpr int H = (RECON == RECON_PPMC || RECON == RECON_PPMP)   ? 3
+                          : (RECON == RECON_PLMC || RECON == RECON_PLMP) ? 2
+                                                                         : 1;
 };
 
 // A sweep block: CS = WA * WB pencils of L cells along the sweep direction DIR.  Arrays in
@@ -805,11 +807,14 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
         QLs[q * S::NR + r] = l;
         QRs[q * S::NR + r] = rr;
       };
-      if (RECON == RECON_PPMC) {
+      if constexpr (RECON == RECON_PPMC)
         hf::ppmc_cell<T>(ld, out, b.ns, b.de, gamma_of<T>(b));
-      } else {
+      else if constexpr (RECON == RECON_PLMC)
         hf::plmc_cell<T>(ld, out, b.ns, b.de, gamma_of<T>(b));
-      }
+      else if constexpr (RECON == RECON_PPMP)
+        hf::ppmp_cell<T>(ld, out, b.ns, b.de);
+      else
+        hf::plmp_cell<T>(ld, out, b.ns, b.de);
     }
     __syncthreads();
   }
@@ -923,6 +928,10 @@ cudaError_t launch_sweep_tma(const Box &b, int recon, const T *Wh, T *dU, double
     CGB_PICK(RECON_PPMC)
   } else if (recon == RECON_PLMC) {
     CGB_PICK(RECON_PLMC)
+  } else if (recon == RECON_PPMP) {
+    CGB_PICK(RECON_PPMP)
+  } else if (recon == RECON_PLMP) {
+    CGB_PICK(RECON_PLMP)
   } else {
     CGB_PICK(RECON_PCM)
   }
@@ -963,6 +972,10 @@ cudaError_t launch_sweep(const Box &b, int recon, const T *Wh, T *dU, double *U,
     CGB_PICK(RECON_PPMC)
   } else if (recon == RECON_PLMC) {
     CGB_PICK(RECON_PLMC)
+  } else if (recon == RECON_PPMP) {
+    CGB_PICK(RECON_PPMP)
+  } else if (recon == RECON_PLMP) {
+    CGB_PICK(RECON_PLMP)
   } else {
     CGB_PICK(RECON_PCM)
   }
@@ -1141,6 +1154,10 @@ cudaError_t launch_batch_sweep(const BatchChunk &C, int recon, int nsl, cudaStre
     CGB_PICK(RECON_PPMC)
   } else if (recon == RECON_PLMC) {
     CGB_PICK(RECON_PLMC)
+  } else if (recon == RECON_PPMP) {
+    CGB_PICK(RECON_PPMP)
+  } else if (recon == RECON_PLMP) {
+    CGB_PICK(RECON_PLMP)
   } else {
     CGB_PICK(RECON_PCM)
   }

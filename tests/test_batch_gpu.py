@@ -20,10 +20,10 @@ pytestmark = pytest.mark.gpu
 NG = 4
 
 
-def _scheme(precision, solver="HLLC"):
+def _scheme(precision, solver="HLLC", recon="PPMC"):
     from cholla_gb300 import integrator as I
 
-    return I.Scheme(reconstruction="PPMC", riemann_solver=solver, dual_energy=True, density_floor=True,
+    return I.Scheme(reconstruction=recon, riemann_solver=solver, dual_energy=True, density_floor=True,
                     temperature_floor=True, gamma=5 / 3, precision=precision)
 
 
@@ -123,10 +123,10 @@ def test_each_job_same_alone_and_in_the_mix(cuda, precision, jobs, chains, solo)
     bt.close()
 
 
-@pytest.mark.parametrize("solver", ["HLLC", "HLL"])
+@pytest.mark.parametrize("solver,recon", [("HLLC", "PPMC"), ("HLL", "PPMC"), ("HLLC", "PPMP"), ("ROE", "PLMP")])
 @pytest.mark.parametrize("precision", ["mixed", "fp64_fast"])
-def test_batch_step_agrees_with_the_engine_to_rounding(cuda, precision, solver):
-    s = _scheme(precision, solver)
+def test_batch_step_agrees_with_the_engine_to_rounding(cuda, precision, solver, recon):
+    s = _scheme(precision, solver, recon)
     jobs = [(16, "blast", 1), (24, "tube", 2), (20, "blast", 3), (12, "tube", 4), (48, "blast", 7)]
     for n, kind, sd in jobs:
         U, dx = _job_state(cuda, n, kind, sd, s)

@@ -29,7 +29,7 @@ def _run_pair(cuda, oracle_lib, U0, ng, scheme, steps, dx):
     Ug = cuda.from_numpy(U0.copy()).cuda()
     Uo = U0.copy()
     cfg = o.config(nx, ny, nz, ng, nf, de=scheme.dual_energy, n_scalars=scheme.n_scalars,
-                   recon={"PCM": o.PCM, "PLMC": o.PLMC, "PPMC": o.PPMC}[scheme.reconstruction],
+                   recon=getattr(o, scheme.reconstruction),
                    solver={"HLLC": o.HLLC, "ROE": o.ROE, "HLL": o.HLL}[scheme.riemann_solver], gamma=scheme.gamma,
                    dx=dx[0], dy=dx[1], dz=dx[2])
     for _ in range(steps):
@@ -41,13 +41,13 @@ def _run_pair(cuda, oracle_lib, U0, ng, scheme, steps, dx):
     return Ug.cpu().numpy(), Uo
 
 
-@pytest.mark.parametrize("recon", ["PCM", "PLMC", "PPMC"])
+@pytest.mark.parametrize("recon", ["PCM", "PLMC", "PPMC", "PLMP", "PPMP"])
 @pytest.mark.parametrize("solver", ["HLLC", "ROE", "HLL"])
 def test_fast_fp64_one_step(cuda, oracle_lib, recon, solver):
     from cholla_gb300 import ics
     from cholla_gb300 import integrator as I
 
-    ng = {"PCM": 2, "PLMC": 3, "PPMC": 4}[recon]
+    ng = {"PCM": 2, "PLMC": 3, "PPMC": 4, "PLMP": 3, "PPMP": 4}[recon]
     U0 = ics.smooth_random_box((19, 13, 11), ng, np.random.default_rng(7), dual_energy=True)
     s = I.Scheme(reconstruction=recon, riemann_solver=solver, dual_energy=True, precision="fp64_fast")
     got, want = _run_pair(cuda, oracle_lib, U0, ng, s, 1, (1 / 19, 1 / 13, 1 / 11))
@@ -88,8 +88,10 @@ def test_fast_fp64_turbulence_20_steps(cuda, oracle_lib):
     assert np.all(err <= 1e-12), dict(zip(FIELDS, err))
 
 
-@pytest.mark.parametrize("seed,mach,solver", [(4, 2.0, "HLLC"), (6, 3.0, "HLLC"), (4, 2.0, "HLL")])
-def test_mixed_turbulence_20_steps(cuda, oracle_lib, seed, mach, solver):
+@pytest.mark.parametrize("seed,mach,solver,recon", [(4, 2.0, "HLLC", "PPMC"), (6, 3.0, "HLLC", "PPMC"),
+                                                    (4, 2.0, "HLL", "PPMC"), (4, 2.0, "HLLC", "PPMP"),
+                                                    (6, 3.0, "ROE", "PLMP")])
+def test_mixed_turbulence_20_steps(cuda, oracle_lib, seed, mach, solver, recon):
     """Mixed precision, 20 steps of rms-Mach-2 and -3 turbulence boxes: finite everywhere and
     relative L1 density error <= 1e-5 (the accuracy target of the mixed-precision form)."""
     from cholla_gb300 import ics
@@ -97,10 +99,10 @@ def test_mixed_turbulence_20_steps(cuda, oracle_lib, seed, mach, solver):
 
     n, ng = 32, 4
     U0 = ics.turbulence_box(n, ng, 5 / 3, seed=seed, mach=mach)
-    s = I.Scheme(reconstruction="PPMC", riemann_solver=solver, dual_energy=True, precision="mixed")
+    s = I.Scheme(reconstruction=recon, riemann_solver=solver, dual_energy=True, precision="mixed")
     got, want = _run_pair(cuda, oracle_lib, U0, ng, s, 20, (1 / n,) * 3)
     err = rel_l1(got, want, ng)
-    print(f"mixed {solver} seed {seed} mach {mach}", {f: f"{e:.2e}" for f, e in zip(FIELDS, err)})
+    print(f"mixed {recon} {solver} seed {seed} mach {mach}", {f: f"{e:.2e}" for f, e in zip(FIELDS, err)})
     assert np.isfinite(got).all()
     assert err[0] <= 1e-5, dict(zip(FIELDS, err))
 

@@ -8,7 +8,9 @@ solver evaluates its fractional powers with single-precision powf; CUDA's powf a
 glibc powf may round those differently (one binary32 ulp, 6e-8 relative, moves the star pressure
 by about as much), so with EXACT the bar is a relative L1 error per field of 1e-7 in 3D and 1e-6 for
 the 1D Sod tube to t = 0.2.  (Against the reference's own CUDA build, which calls the same CUDA powf, the
-exact solver is compared bit for bit in test_reference_gpu.py.)
+exact solver is compared bit for bit in test_reference_gpu.py.)  PLMP and PPMP also run in the throughput
+forms; test_fast_forms_sod_1d holds them to the fast FP64 and mixed bars on the 1D Sod tube (the 3D
+cases are in test_fast_gpu.py).
 """
 import numpy as np
 import pytest
@@ -138,6 +140,50 @@ def test_new_schemes_sod_1d(cuda, oracle_lib, recon, solver):
             assert np.all(err <= 1e-6), err
         else:
             assert np.array_equal(g.view(np.int64), w.view(np.int64))
+    finally:
+        I.set_scheme(I.Scheme())
+
+
+@pytest.mark.parametrize("recon,solver,precision", [("PPMP", "HLLC", "fp64_fast"), ("PLMP", "ROE", "fp64_fast"),
+                                                    ("PPMP", "HLLC", "mixed"), ("PLMP", "HLLC", "mixed")])
+def test_fast_forms_sod_1d(cuda, oracle_lib, recon, solver, precision):
+    """PLMP and PPMP in the throughput forms on the 1D Sod tube to t = 0.2 (145 steps through a
+    shock) against the oracle's exact FP64 step: relative L1 per field within 1e-11 (fast FP64; the
+    momentum, whose L1 norm is small, measured 1.2e-12 with PPMP, density and energy 3.5e-13 and
+    4.7e-13), density within 1e-5 (mixed)."""
+    from cholla_gb300 import ics
+    from cholla_gb300 import integrator as I
+
+    o = oracle_lib
+    ng, gamma = NG[recon], 1.4
+    U0, dx = ics.sod_1d(100, ng, gamma)
+    nf, N = U0.shape
+    I.set_scheme(I.Scheme(reconstruction=recon, riemann_solver=solver, dual_energy=False, density_floor=False,
+                          temperature_floor=False, gamma=gamma, precision=precision))
+    try:
+        Ug = _gpu(cuda, U0)
+        Uo = U0.copy()
+        cfg = o.config(N, 1, 1, ng, nf, recon=getattr(o, recon), solver=getattr(o, solver), gamma=gamma, dx=dx,
+                       dy=dx, dz=dx)
+        t = 0.0
+        while t < 0.2:
+            dti = I.Calc_dt_GPU(Ug, N, 1, 1, ng, nf, dx, dx, dx, gamma)
+            dt = min(0.3 / dti, 0.2 - t)
+            I.VL_Algorithm_1D_CUDA(Ug, N, 0, ng, dx, 0.0, dt, nf)
+            I.Set_Boundaries(Ug, N, 1, 1, ng, nf, (3, 3, 0, 0, 0, 0))
+            o.vl_step_1d(cfg, Uo.reshape(-1), dt)
+            o.set_boundaries(cfg, Uo.reshape(-1), (3, 3, 0, 0, 0, 0))
+            t += dt
+        cuda.cuda.synchronize()
+        g, w = Ug.cpu().numpy()[:, ng:-ng], Uo[:, ng:-ng]
+        diff, norm = np.abs(g - w).sum(axis=1), np.abs(w).sum(axis=1)
+        err = np.where(norm > 0, diff / np.where(norm > 0, norm, 1.0), diff)  # transverse momenta are 0
+        print(recon, solver, precision, err)
+        assert np.isfinite(g).all()
+        if precision == "fp64_fast":
+            assert np.all(err <= 1e-11), err
+        else:
+            assert err[0] <= 1e-5, err
     finally:
         I.set_scheme(I.Scheme())
 
