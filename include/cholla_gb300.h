@@ -43,8 +43,8 @@ extern "C" {
 #define CGB_MAX_DIVB 1.0e-9
 
 /* reconstruction (builds/make.type.*: -DPCM / -DPLMC / -DPPMC / -DPLMP / -DPPMP; PLMP and PPMP are
-   the primitive-limited forms of src/reconstruction/plmp_cuda.cu and ppmp_cuda.cu, built in the
-   exact FP64 form only: other precisions are rejected with CGB_ERR_UNSUPPORTED) */
+   the primitive-limited forms of src/reconstruction/plmp_cuda.cu and ppmp_cuda.cu; every
+   reconstruction is built in all three arithmetic forms) */
 #define CGB_PCM  0
 #define CGB_PLMC 1
 #define CGB_PPMC 2
