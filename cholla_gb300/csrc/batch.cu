@@ -181,9 +181,6 @@ int cgb_batch_create(cgb_batch **out, const cgb_scheme *scheme, double c_cfl, vo
   if (s.reconstruction < CGB_PCM || s.reconstruction > CGB_PPMP || s.riemann_solver < CGB_HLLC ||
       s.riemann_solver > CGB_EXACT)
     return bfail(CGB_ERR_ARGS, "bad reconstruction or riemann solver");
-  if (s.riemann_solver == CGB_EXACT)
-    return bfail(CGB_ERR_UNSUPPORTED, "batches run the fast forms, which do not build the exact Riemann solver (the "
-                                      "exact FP64 form does: cgb_box / cgb_vl_algorithm_3d)");
   if (s.mhd || s.riemann_solver == CGB_HLLD) return bfail(CGB_ERR_UNSUPPORTED, "batches are hydro only");
   if (s.precision != CGB_MIXED && s.precision != CGB_FP64_FAST)
     return bfail(CGB_ERR_UNSUPPORTED, "batches run the fast FP64 or the mixed-precision form");

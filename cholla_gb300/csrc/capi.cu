@@ -132,8 +132,6 @@ int check_scheme(const cgb_scheme &s)
 {
   if (s.reconstruction < CGB_PCM || s.reconstruction > CGB_PPMP) return fail(CGB_ERR_ARGS, "bad reconstruction");
   if (s.riemann_solver < CGB_HLLC || s.riemann_solver > CGB_EXACT) return fail(CGB_ERR_ARGS, "bad riemann solver");
-  if (s.riemann_solver == CGB_EXACT && s.precision != CGB_FP64)
-    return fail(CGB_ERR_UNSUPPORTED, "the exact Riemann solver is built in the exact FP64 form (CGB_FP64) only");
   if (s.n_scalars < 0 || s.n_scalars > cgb::NS_MAX) return fail(CGB_ERR_ARGS, "n_scalars must be 0..2");
   if (!(s.gamma > 1.0)) return fail(CGB_ERR_ARGS, "gamma must exceed 1");
   if (s.mhd && s.riemann_solver != CGB_HLLD) return fail(CGB_ERR_ARGS, "MHD needs the HLLD solver");

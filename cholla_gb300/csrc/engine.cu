@@ -135,8 +135,6 @@ int cgb_box_create(cgb_box **out, int nx, int ny, int nz, int n_ghost, double dx
   if (s.reconstruction < CGB_PCM || s.reconstruction > CGB_PPMP || s.riemann_solver < CGB_HLLC ||
       s.riemann_solver > CGB_EXACT)
     return box_fail(nullptr, CGB_ERR_ARGS, "bad reconstruction or riemann solver");
-  if (s.riemann_solver == CGB_EXACT && s.precision != CGB_FP64)
-    return box_fail(nullptr, CGB_ERR_UNSUPPORTED, "the exact Riemann solver is built in the exact FP64 form (CGB_FP64) only");
   if (s.precision < CGB_FP64 || s.precision > CGB_FP64_FAST) return box_fail(nullptr, CGB_ERR_ARGS, "bad precision");
   if (s.n_scalars < 0 || s.n_scalars > cgb::NS_MAX || !(s.gamma > 1.0) || (s.riemann_solver == CGB_HLLD) != (s.mhd != 0))
     return box_fail(nullptr, CGB_ERR_ARGS, "bad scheme (MHD goes with HLLD and only with it)");

@@ -1,7 +1,8 @@
 // hydro_fast.cu -- the fast forms' single-box and batch steps: primitives, the per-solver
-// predictor and corrector sweeps (hydro_fast_hllc.cu, hydro_fast_roe.cu, hydro_fast_hll.cu, one
-// translation unit per Riemann solver so that they compile in parallel), the negative-density
-// repair and the FP64 finalize (dual-energy select/sync, temperature floor, CFL reduction).
+// predictor and corrector sweeps (hydro_fast_hllc.cu, hydro_fast_roe.cu, hydro_fast_hll.cu,
+// hydro_fast_exact.cu: one translation unit per Riemann solver, so that they compile in
+// parallel), the negative-density repair and the FP64 finalize (dual-energy select/sync,
+// temperature floor, CFL reduction).
 #include "hydro_fast_body.cuh"
 
 namespace cgb
@@ -259,6 +260,7 @@ cudaError_t batch_chunk_step(const BatchChunk &C, int recon, int solver, int mix
   switch (solver) {
     case SOLVER_ROE: e = batch_solver_roe(C, recon, mixed, set, nsl, s); break;
     case SOLVER_HLL: e = batch_solver_hll(C, recon, mixed, set, nsl, s); break;
+    case SOLVER_EXACT: e = batch_solver_exact(C, recon, mixed, set, nsl, s); break;
     default: e = batch_solver_hllc(C, recon, mixed, set, nsl, s); break;
   }
   if (e != cudaSuccess) return e;
@@ -304,6 +306,7 @@ cudaError_t hydro_fast_step(const Box &box, int recon, int solver, int mixed, do
   switch (solver) {
     case SOLVER_ROE: e = fast_solver_roe(b, recon, mixed, U, sc, dt, dt_dev, s, marks); break;
     case SOLVER_HLL: e = fast_solver_hll(b, recon, mixed, U, sc, dt, dt_dev, s, marks); break;
+    case SOLVER_EXACT: e = fast_solver_exact(b, recon, mixed, U, sc, dt, dt_dev, s, marks); break;
     default: e = fast_solver_hllc(b, recon, mixed, U, sc, dt, dt_dev, s, marks); break;
   }
   if (e != cudaSuccess) return e;

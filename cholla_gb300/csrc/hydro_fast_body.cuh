@@ -14,14 +14,15 @@
 //
 // This header holds the kernels and launchers as templates.  hydro_fast.cu runs the steps around
 // the Riemann solver (primitives, negative-density repair, finalize); the predictor and the
-// sweeps are instantiated once per solver in hydro_fast_hllc.cu, hydro_fast_roe.cu and
-// hydro_fast_hll.cu, which compile in parallel.
+// sweeps are instantiated once per solver in hydro_fast_hllc.cu, hydro_fast_roe.cu,
+// hydro_fast_hll.cu and hydro_fast_exact.cu, which compile in parallel.
 #pragma once
 #include <type_traits>
 
 #include "common.cuh"
 #include "ghost.cuh"
 #include "hydro_fast.cuh"
+#include "hydro_math.cuh"
 #include "kernels.h"
 #include "tma.cuh"
 
@@ -39,6 +40,9 @@ cudaError_t fast_solver_hll(const Box &b, int recon, int mixed, double *U, const
 cudaError_t batch_solver_hllc(const BatchChunk &C, int recon, int mixed, int set, int nsl, cudaStream_t s);
 cudaError_t batch_solver_roe(const BatchChunk &C, int recon, int mixed, int set, int nsl, cudaStream_t s);
 cudaError_t batch_solver_hll(const BatchChunk &C, int recon, int mixed, int set, int nsl, cudaStream_t s);
+cudaError_t fast_solver_exact(const Box &b, int recon, int mixed, double *U, const Scratch &sc, double dt,
+                              const double *dtp, cudaStream_t s, cudaEvent_t *marks);
+cudaError_t batch_solver_exact(const BatchChunk &C, int recon, int mixed, int set, int nsl, cudaStream_t s);
 
 namespace
 {
@@ -270,6 +274,36 @@ __device__ __forceinline__ hf::Prim<T> prim_at(const T *P, int stride, int i, co
 }
 
 // the same with the sides' direction-free quantities formed beforehand (hf::side_q)
+// Exact Riemann solver (exact_cuda.cu:19-334) from primitive interface states, f in the slots of
+// hf::hllc_q.  The pressures are the ones the other solvers use (the DE selection, floored at TINY);
+// the star state (Newton iteration on the pressure, at most 21 passes) and its sample at x/t = 0 run
+// in FP64 in both forms, with the single-precision powf of the reference, and the flux follows
+// exact_cuda.cu: mass flux ds vs, transverse velocities and passive quantities upwind by vs.
+template <typename T>
+__device__ __forceinline__ void exact_q(const hf::Prim<T> &l, const hf::Prim<T> &r, const hf::SideQ<T> &Ql,
+                                        const hf::SideQ<T> &Qr, T *f, const Box &b)
+{
+  double const g  = b.gamma;
+  double const dl = widen(l.d), vl = widen(l.vn), pl = widen(Ql.p);
+  double const dr = widen(r.d), vr = widen(r.vn), pr = widen(Qr.p);
+  double const cl = hf::sqrtT(g * pl * hf::rcp(dl)), cr = hf::sqrtT(g * pr * hf::rcp(dr));
+  double pm = 0, vm = 0, ds = 0, vs = 0, ps = 0;
+  hx::exact_star(pm, vm, dl, vl, pl, cl, dr, vr, pr, cr, g);
+  hx::exact_sample(pm, vm, ds, vs, ps, dl, vl, pl, cl, dr, vr, pr, cr, g);
+  bool const left = vs >= 0;
+  double const vy = widen(left ? l.vt1 : r.vt1), vz = widen(left ? l.vt2 : r.vt2);
+  double const m  = ds * vs;
+  f[0] = narrow<T>(m);
+  f[1] = narrow<T>(m * vs + ps);
+  f[2] = narrow<T>(m * vy);
+  f[3] = narrow<T>(m * vz);
+  f[4] = narrow<T>((ps * b.ig1 + 0.5 * ds * (vs * vs + vy * vy + vz * vz) + ps) * vs);
+#pragma unroll
+  for (int k = 0; k < NS_MAX; k++)
+    if (k < b.ns) f[6 + k] = narrow<T>(m * widen(left ? l.sc[k] : r.sc[k]));
+  if (b.de) f[5] = narrow<T>(m * widen(left ? l.ge : r.ge));
+}
+
 template <typename T, int SOLVER>
 __device__ __forceinline__ void riemann_q(const hf::Prim<T> &L, const hf::Prim<T> &R, const hf::SideQ<T> &QL,
                                           const hf::SideQ<T> &QR, T *f, const Box &b)
@@ -278,6 +312,8 @@ __device__ __forceinline__ void riemann_q(const hf::Prim<T> &L, const hf::Prim<T
     hf::roe_q(L, R, QL, QR, f, b.ns, b.de, gamma_of<T>(b));
   else if constexpr (SOLVER == SOLVER_HLL)
     hf::hll_q(L, R, QL, QR, f, b.ns, b.de);
+  else if constexpr (SOLVER == SOLVER_EXACT)
+    exact_q(L, R, QL, QR, f, b);
   else
     hf::hllc_q(L, R, QL, QR, f, b.ns, b.de, gamma_of<T>(b));
 }
@@ -289,6 +325,9 @@ __device__ __forceinline__ void riemann(const hf::Prim<T> &L, const hf::Prim<T> 
     hf::roe(L, R, f, b.ns, b.de, gamma_of<T>(b), ig1_of<T>(b));
   else if constexpr (SOLVER == SOLVER_HLL)
     hf::hll(L, R, f, b.ns, b.de, gamma_of<T>(b), ig1_of<T>(b));
+  else if constexpr (SOLVER == SOLVER_EXACT)
+    exact_q(L, R, hf::side_q<T, false>(L, b.de, gamma_of<T>(b), ig1_of<T>(b)),
+            hf::side_q<T, false>(R, b.de, gamma_of<T>(b), ig1_of<T>(b)), f, b);
   else
     hf::hllc(L, R, f, b.ns, b.de, gamma_of<T>(b), ig1_of<T>(b));
 }
@@ -400,7 +439,8 @@ __device__ __forceinline__ void fpred_tile(const Box &b, const double *__restric
     int const halo = (bx == 0 || bx == BX - 1) + (HY && (by == 0 || by == BY - 1)) + (HZ && (bz == 0 || bz == BZ - 1));
     if (halo > 1) continue;
     hf::SideQ<T> const q =
-        hf::side_q<T, SOLVER != SOLVER_ROE>(prim_at(Ps, NB, t, b), b.de, gamma_of<T>(b), ig1_of<T>(b));
+        hf::side_q<T, SOLVER == SOLVER_HLLC || SOLVER == SOLVER_HLL>(prim_at(Ps, NB, t, b), b.de, gamma_of<T>(b),
+                                                                     ig1_of<T>(b));
     Qs[0 * NB + t] = q.E, Qs[1 * NB + t] = q.p, Qs[2 * NB + t] = q.id;
     Qs[3 * NB + t] = q.sq, Qs[4 * NB + t] = q.c, Qs[5 * NB + t] = q.h;
   }
@@ -579,6 +619,15 @@ struct Sweep {
     }
   }
 };
+
+// resident blocks per SM the sweeps' register budget targets: the tunables above, except for the
+// exact solver, whose FP64 Newton iteration needs more registers than 6 FP32 blocks leave (it
+// spilled about 1.5 KB a thread there) and targets 2
+template <typename T, int SOLVER>
+__host__ __device__ constexpr int sweep_min_blocks()
+{
+  return SOLVER == SOLVER_EXACT ? 2 : (sizeof(T) == 4 ? CGB_SWEEP_MINB_F32 : CGB_SWEEP_MINB_F64);
+}
 
 // W scratch of the fast forms: 2 * nslot * n * 8 bytes.  The first half holds Wⁿ (T) and then
 // the corrector's FP64 accumulator; W½ (T) starts at the second half.
@@ -881,8 +930,7 @@ __device__ __forceinline__ void fsweep_tile(const Box &b, const T *__restrict__ 
 // Mixed-precision sweeps are latency-bound (FP32 reconstruction chains): more resident blocks
 // per SM hide more of it (CGB_SWEEP_MINB_F32); the FP64 sweeps are FP64-pipe bound.
 template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
-__global__ void __launch_bounds__(sweep_threads(L, WA *WB, RECON), sizeof(T) == 4 ? CGB_SWEEP_MINB_F32
-                                                                                     : CGB_SWEEP_MINB_F64)
+__global__ void __launch_bounds__(sweep_threads(L, WA *WB, RECON), sweep_min_blocks<T, SOLVER>())
     k_fsweep(Box b, const T *__restrict__ W, T *__restrict__ dU, double *__restrict__ U,
              const double *__restrict__ GEp, double *__restrict__ Epre, int *__restrict__ status, double dt,
              const double *__restrict__ dtp)
@@ -893,8 +941,7 @@ __global__ void __launch_bounds__(sweep_threads(L, WA *WB, RECON), sizeof(T) == 
 
 // the same sweep with its P boxes staged by the TMA unit from the tensor map of W½
 template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
-__global__ void __launch_bounds__(sweep_threads(L, WA *WB, RECON), sizeof(T) == 4 ? CGB_SWEEP_MINB_F32
-                                                                                     : CGB_SWEEP_MINB_F64)
+__global__ void __launch_bounds__(sweep_threads(L, WA *WB, RECON), sweep_min_blocks<T, SOLVER>())
     k_fsweep_tma(Box b, const T *__restrict__ W, T *__restrict__ dU, double *__restrict__ U,
                  const double *__restrict__ GEp, double *__restrict__ Epre, int *__restrict__ status, double dt,
                  const double *__restrict__ dtp, const __grid_constant__ CUtensorMap map)
@@ -1122,8 +1169,7 @@ __global__ void __launch_bounds__(PTX *PTY *PTZ, sizeof(T) == 4 ? 4 : 2)
 }
 
 template <typename T, int DIR, int L, int WA, int WB, int RECON, int SOLVER, bool FIRST, bool FINAL>
-__global__ void __launch_bounds__(sweep_threads(L, WA *WB, RECON), sizeof(T) == 4 ? CGB_SWEEP_MINB_F32
-                                                                                     : CGB_SWEEP_MINB_F64)
+__global__ void __launch_bounds__(sweep_threads(L, WA *WB, RECON), sweep_min_blocks<T, SOLVER>())
     kb_sweep(const __grid_constant__ BatchChunk C)
 {
   int const kind    = BK_SWX + DIR;

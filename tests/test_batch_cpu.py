@@ -28,10 +28,6 @@ def test_batch_create_refuses_what_it_cannot_run(lib):
     cases = [
         (I.Scheme(riemann_solver="HLLD", mhd=True, dual_energy=False), 0.3, 0x10, _lib.CGB_ERR_UNSUPPORTED),
         (I.Scheme(precision="fp64"), 0.3, 0x10, _lib.CGB_ERR_UNSUPPORTED),  # exact form: single boxes only
-        # the exact solver is built in the exact FP64 form only (PLMP, PPMP and HLL are in all forms)
-        (I.Scheme(riemann_solver="EXACT", precision="mixed"), 0.3, 0x10, _lib.CGB_ERR_UNSUPPORTED),
-        (I.Scheme(reconstruction="PLMP", riemann_solver="EXACT", precision="fp64_fast"), 0.3, 0x10,
-         _lib.CGB_ERR_UNSUPPORTED),
         (mixed, 0.0, 0x10, _lib.CGB_ERR_ARGS),                               # CFL number must be positive
         (mixed, 0.3, 0, _lib.CGB_ERR_ARGS),                                  # a batch needs its own stream
     ]

@@ -72,6 +72,10 @@ def _rel_l1(a, b):
 
 
 TOL = {"mixed": 1e-7, "fp64_fast": 1e-15}
+# The exact solver's Newton iteration stops when the relative pressure change falls to 1e-6; a
+# last-bit difference can move that stop by one pass, which moves the star pressure by about the
+# square of the change (1e-12 relative) on such faces.
+TOL_EXACT = {"mixed": 1e-6, "fp64_fast": 1e-9}
 
 
 def _same(a, b):
@@ -123,10 +127,12 @@ def test_each_job_same_alone_and_in_the_mix(cuda, precision, jobs, chains, solo)
     bt.close()
 
 
-@pytest.mark.parametrize("solver,recon", [("HLLC", "PPMC"), ("HLL", "PPMC"), ("HLLC", "PPMP"), ("ROE", "PLMP")])
+@pytest.mark.parametrize("solver,recon", [("HLLC", "PPMC"), ("HLL", "PPMC"), ("HLLC", "PPMP"), ("ROE", "PLMP"),
+                                          ("EXACT", "PLMC")])
 @pytest.mark.parametrize("precision", ["mixed", "fp64_fast"])
 def test_batch_step_agrees_with_the_engine_to_rounding(cuda, precision, solver, recon):
     s = _scheme(precision, solver, recon)
+    tol = (TOL_EXACT if solver == "EXACT" else TOL)[precision]
     jobs = [(16, "blast", 1), (24, "tube", 2), (20, "blast", 3), (12, "tube", 4), (48, "blast", 7)]
     for n, kind, sd in jobs:
         U, dx = _job_state(cuda, n, kind, sd, s)
@@ -134,7 +140,7 @@ def test_batch_step_agrees_with_the_engine_to_rounding(cuda, precision, solver, 
         e, te = _alone(cuda, U, dx, s, 1)
         rs = real_slice(NG)
         err = _rel_l1(b[rs], e[rs])
-        assert np.all(err <= TOL[precision]), f"job {n}^3 {kind}: {err}"
+        assert np.all(err <= tol), f"job {n}^3 {kind}: {err}"
         assert tb == te
 
 

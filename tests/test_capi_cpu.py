@@ -55,15 +55,10 @@ def test_scheme_round_trip_and_validation(lib):
     assert e.value.code == _lib.CGB_ERR_UNSUPPORTED
     with pytest.raises(_lib.CgbError):
         I.set_scheme(I.Scheme(gamma=1.0))
-    for recon in ("PPMC", "PLMP"):
-        I.set_scheme(I.Scheme(reconstruction=recon, riemann_solver="EXACT"))  # built in the exact FP64 form
-        for prec in ("fp64_fast", "mixed"):  # not in the throughput forms
-            with pytest.raises(_lib.CgbError) as e:
-                I.set_scheme(I.Scheme(reconstruction=recon, riemann_solver="EXACT", precision=prec))
-            assert e.value.code == _lib.CGB_ERR_UNSUPPORTED
-    for prec in ("fp64", "fp64_fast", "mixed"):  # PLMP, PPMP and HLL are built in all three forms
-        for recon, solver in (("PPMC", "HLL"), ("PLMP", "HLLC"), ("PPMP", "ROE")):
-            I.set_scheme(I.Scheme(reconstruction=recon, riemann_solver=solver, precision=prec))
+    for prec in ("fp64", "fp64_fast", "mixed"):  # every hydro scheme is built in all three forms
+        for recon in ("PCM", "PLMC", "PPMC", "PLMP", "PPMP"):
+            for solver in ("HLLC", "ROE", "HLL", "EXACT"):
+                I.set_scheme(I.Scheme(reconstruction=recon, riemann_solver=solver, precision=prec))
     bad = I.Scheme().to_c()
     bad.reconstruction = 7
     assert _lib.lib().cgb_set_scheme(bad) == _lib.CGB_ERR_ARGS

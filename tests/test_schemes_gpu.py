@@ -145,12 +145,14 @@ def test_new_schemes_sod_1d(cuda, oracle_lib, recon, solver):
 
 
 @pytest.mark.parametrize("recon,solver,precision", [("PPMP", "HLLC", "fp64_fast"), ("PLMP", "ROE", "fp64_fast"),
-                                                    ("PPMP", "HLLC", "mixed"), ("PLMP", "HLLC", "mixed")])
+                                                    ("PPMP", "HLLC", "mixed"), ("PLMP", "HLLC", "mixed"),
+                                                    ("PPMC", "EXACT", "fp64_fast"), ("PLMP", "EXACT", "mixed")])
 def test_fast_forms_sod_1d(cuda, oracle_lib, recon, solver, precision):
-    """PLMP and PPMP in the throughput forms on the 1D Sod tube to t = 0.2 (145 steps through a
-    shock) against the oracle's exact FP64 step: relative L1 per field within 1e-11 (fast FP64; the
-    momentum, whose L1 norm is small, measured 1.2e-12 with PPMP, density and energy 3.5e-13 and
-    4.7e-13), density within 1e-5 (mixed)."""
+    """PLMP, PPMP and the exact solver in the throughput forms on the 1D Sod tube to t = 0.2 (145
+    steps through a shock) against the oracle's exact FP64 step: relative L1 per field within 1e-11
+    in fast FP64 (the momentum, whose L1 norm is small, measured 1.2e-12 with PPMP, density and energy
+    3.5e-13 and 4.7e-13), 1e-6 with the exact solver (its single-precision powf, as in the exact
+    form's Sod test), density within 1e-5 in mixed."""
     from cholla_gb300 import ics
     from cholla_gb300 import integrator as I
 
@@ -181,7 +183,7 @@ def test_fast_forms_sod_1d(cuda, oracle_lib, recon, solver, precision):
         print(recon, solver, precision, err)
         assert np.isfinite(g).all()
         if precision == "fp64_fast":
-            assert np.all(err <= 1e-11), err
+            assert np.all(err <= (1e-6 if solver == "EXACT" else 1e-11)), err
         else:
             assert err[0] <= 1e-5, err
     finally:
