@@ -50,9 +50,9 @@ extern "C" {
 #define CGB_PPMC 2
 #define CGB_PLMP 3
 #define CGB_PPMP 4
-/* Riemann solver (-DHLLC / -DROE / -DHLLD / -DHLL / -DEXACT; EXACT, src/riemann_solvers/exact_cuda.cu,
-   is built in the exact FP64 form only; HLL, hll_cuda.cu, in every form but not in 1D or 2D, where the
-   reference's VL_1D and VL_2D integrators have no HLL branch) */
+/* Riemann solver (-DHLLC / -DROE / -DHLLD / -DHLL / -DEXACT; the hydro solvers are built in every
+   arithmetic form; HLL, src/riemann_solvers/hll_cuda.cu, not in 1D or 2D, where the reference's
+   VL_1D and VL_2D integrators have no HLL branch) */
 #define CGB_HLLC  0
 #define CGB_ROE   1
 #define CGB_HLLD  2
