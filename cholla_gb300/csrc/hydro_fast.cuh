@@ -29,16 +29,21 @@ struct Prim {
 // the normal range widens exactly (exponent rebased by 1023 - 127, fraction shifted by 29
 // bits); a binary64 narrows by truncating the fraction to 23 bits and rounding to nearest,
 // ties to even (up when the 29 dropped bits exceed half an ulp, or equal it with an odd kept
-// fraction; a carry into the exponent is the correct result, up to infinity).  Zeros,
-// subnormals, infinities, NaNs and results outside the binary32 normal range take the
-// hardware conversion.
+// fraction; a carry into the exponent is the correct result, up to infinity).  Signed zeros
+// are formed on the integer pipe too.  Subnormals, infinities, NaNs and results outside the
+// binary32 normal range take the hardware conversion, out of line: inline, its predicated
+// conversion took an FP64-pipe issue slot in every thread although no thread needed it, while
+// a call is made only by the threads whose value does.
+static __device__ __noinline__ double to_f64_hw(float f) { return (double)f; }
+static __device__ __noinline__ float to_f32_hw(double x) { return (float)x; }
 __device__ __forceinline__ double to_f64(float f)
 {
   unsigned const u = __float_as_uint(f);
   unsigned const e = (u >> 23) & 0xffu;
   if (e - 1u < 254u)
     return __hiloint2double((int)((u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7fffffu) >> 3)), (int)(u << 29));
-  return (double)f;
+  if ((u & 0x7fffffffu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+  return to_f64_hw(f);
 }
 __device__ __forceinline__ float to_f32(double x)
 {
@@ -50,7 +55,8 @@ __device__ __forceinline__ float to_f32(double x)
     unsigned const r    = ((hi & 0x80000000u) | ((e - 896u) << 23)) + m;
     return __uint_as_float(r + ((rest > half) | ((rest == half) & (m & 1u))));
   }
-  return (float)x;
+  if (((hi & 0x7fffffffu) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+  return to_f32_hw(x);
 }
 
 // Seeds of the FP64 reciprocal and square root: the same conversions for operands already known
