@@ -1,6 +1,7 @@
 // hydro_fast.cuh -- the VL hydro arithmetic reformulated for GB300's ALU balance.
 //
-// Same scheme as hydro_math.cuh (PPMC / PLMC / PPMP / PLMP / PCM, HLLC / Roe / HLL, dual energy), same limiter
+// Same scheme as hydro_math.cuh (PPMC / PLMC / PPMP / PLMP / PCM, HLLC / Roe / HLL, dual
+// energy; the exact solver's fast form is in hydro_fast_body.cuh), same limiter
 // decisions, but written for throughput: every quotient by a shared denominator becomes one
 // reciprocal and multiplies, primitives are computed once per cell instead of once per
 // stencil use, constant divisions are multiplications, the Riemann solvers take primitive
