@@ -1,6 +1,6 @@
-"""The oracle's HLL and exact Riemann solvers (hll_cuda.cu, exact_cuda.cu), CPU only.  These
-two make.type options are not yet in libchollagb; their restatements are pinned here ahead of
-the GPU kernels:
+"""The oracle's HLL and exact Riemann solvers (hll_cuda.cu, exact_cuda.cu), CPU only.  The GPU
+kernels of these two make.type options are checked against these restatements in
+tests/test_schemes_gpu.py and tests/test_fast_gpu.py; the restatements themselves are pinned here:
 
 * HLL: the reference's HLLC known answer (a state against itself gives the pure pressure flux)
   under the reference's comparison rule; the upwind flux, bit for bit, when both wave speeds
@@ -10,6 +10,8 @@ the GPU kernels:
   reference's convergence tolerance (1e-6) and its single-precision fractional powers.
 * both: a Sod tube run to t = 0.2 through the oracle's 1D step stays within 1% mean density
   error of the exact solution, and a periodic 3D box conserves mass to rounding.
+* the weighted form in which the throughput kernels write the HLL flux: equal to the oracle's
+  two-wave flux to FP64 rounding on random subsonic and supersonic faces.
 """
 import json
 import math
@@ -127,3 +129,42 @@ def test_solver_conserves_on_periodic_box(oracle_lib, solver):
     tot = U[real_slice(4)][:5].sum(axis=(1, 2, 3))
     assert np.all(np.isfinite(U))
     assert np.allclose(tot, tot0, rtol=1e-12, atol=1e-12 * math.fsum(np.abs(tot0)))
+
+
+def _hll_weighted(left, right, g):
+    """The fast forms' HLL (hf::hll_q in cholla_gb300/csrc/hydro_fast.cuh) restated in numpy: the
+    two-wave flux as dL bL XL + dR bR XR plus the pressure terms, with selected weights on
+    supersonic faces."""
+    (dl, vl, t1l, t2l, pl), (dr, vr, t1r, t2r, pr) = left, right
+    El = pl / (g - 1) + 0.5 * dl * (vl * vl + t1l * t1l + t2l * t2l)
+    Er = pr / (g - 1) + 0.5 * dr * (vr * vr + t1r * t1r + t2r * t2r)
+    cl, cr = math.sqrt(g * pl / dl), math.sqrt(g * pr / dr)
+    Sl, Sr = min(vr - cr, vl - cl), max(vl + cl, vr + cr)
+    dSl, dSr = Sl - vl, Sr - vr
+    inv = 1.0 / max(Sr - Sl, 1e-30)
+    if Sl > 0:
+        wl, wr, bl, br = 1.0, 0.0, vl, 0.0
+    elif Sr < 0:
+        wl, wr, bl, br = 0.0, 1.0, 0.0, vr
+    else:
+        wl, wr, bl, br = Sr * inv, -Sl * inv, -(Sr * dSl) * inv, (Sl * dSr) * inv
+    al, ar = dl * bl, dr * br
+    return np.array([al + ar, al * vl + ar * vr + (wl * pl + wr * pr), al * t1l + ar * t1r, al * t2l + ar * t2r,
+                     bl * El + br * Er + (wl * pl * vl + wr * pr * vr)])
+
+
+def test_weighted_hll_form_equals_the_two_wave_flux(oracle_lib):
+    """The algebra of the fast forms' HLL: on random states (subsonic and supersonic, either
+    direction) the weighted form equals the oracle's (Sr FL - Sl FR + Sl Sr (UR - UL)) / (Sr - Sl)
+    to FP64 rounding (relative to the flux's scale)."""
+    o, g = oracle_lib, 1.4
+    rng = np.random.default_rng(5)
+    worst = 0.0
+    for _ in range(400):
+        left = (rng.uniform(0.1, 2), rng.normal(0, 3), rng.normal(0, 1), rng.normal(0, 1), rng.uniform(0.1, 2))
+        right = (rng.uniform(0.1, 2), rng.normal(0, 3), rng.normal(0, 1), rng.normal(0, 1), rng.uniform(0.1, 2))
+        want = _interface(o, left, right, g, o.HLL)
+        got = _hll_weighted(left, right, g)
+        scale = max(np.abs(want).max(), 1.0)
+        worst = max(worst, float(np.abs(got - want).max() / scale))
+    assert worst < 1e-13, worst
